@@ -1,0 +1,507 @@
+// abi.cu -- the extern "C" boundary declared in include/byo_gpu.h.
+// Argument checking, host<->device staging and object lifetime live here;
+// the work is in engine.cu, algos.cu, graph.cu and pma.cu.
+#include <cstring>
+#include <new>
+
+#include "engine.h"
+#include "internal.h"
+
+using namespace byo;
+
+#define BYO_VERSION_STR "byo_gpu 0.1 (sm_103a)"
+
+namespace {
+
+int need(byo_ctx *ctx, bool ok, const char *what) {
+  return ok ? BYO_OK : set_error(ctx, BYO_EINVAL, what);
+}
+
+// Device scratch for host-memory wrappers: one buffer per graph slot.
+template <typename T>
+int host_out_buffer(byo_graph *g, uint64_t count, T **d) {
+  return ws(g, WS_LABEL, count * sizeof(T) / sizeof(uint32_t) + 2, (uint32_t **)d);
+}
+
+int copy_to_host(byo_ctx *ctx, void *h, const void *d, size_t bytes) {
+  if (!bytes) return BYO_OK;
+  BYO_CU(ctx, cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  return BYO_OK;
+}
+
+}  // namespace
+
+struct byo_functor {
+  byo_graph *g = nullptr;
+  TravState st;
+  DevBuf lp, visited;
+};
+
+struct byo_vertex_subset {
+  byo_graph *g = nullptr;
+  Frontier f;
+  DevBuf list, bits;
+};
+
+extern "C" {
+
+const char *byo_version(void) { return BYO_VERSION_STR; }
+
+int byo_gpu_init(int device, byo_ctx **out) {
+  if (!out) return BYO_EINVAL;
+  *out = nullptr;
+  byo_ctx *ctx = new (std::nothrow) byo_ctx();
+  if (!ctx) return BYO_ENOMEM;
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  for (int i = 0; e == cudaSuccess && i < 64; i++) e = cudaEventCreate(&ctx->ev[i]);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return BYO_EDEVICE;
+  }
+  *out = ctx;
+  return BYO_OK;
+}
+
+void byo_gpu_shutdown(byo_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto &b : ctx->scratch) free_buf(b);
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  for (int i = 0; i < 64; i++)
+    if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *byo_last_error(const byo_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+void *byo_ctx_stream(byo_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+uint64_t byo_ctx_launches(const byo_ctx *ctx) { return ctx ? ctx->launches : 0; }
+int byo_ctx_synchronize(byo_ctx *ctx) {
+  if (!ctx) return BYO_EINVAL;
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  return BYO_OK;
+}
+
+// ---------------------------------------------------------------- containers
+
+int byo_graph_create_csr(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h_offsets,
+                         const uint32_t *h_nbrs, byo_graph **out) {
+  if (!ctx || !out) return BYO_EINVAL;
+  *out = nullptr;
+  return graph_from_host_csr(ctx, BYO_CONTAINER_CSR, n, m, h_offsets, h_nbrs, out);
+}
+
+int byo_graph_create_pma(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h_offsets,
+                         const uint32_t *h_nbrs, byo_graph **out) {
+  if (!ctx || !out) return BYO_EINVAL;
+  *out = nullptr;
+  return graph_from_host_csr(ctx, BYO_CONTAINER_PMA, n, m, h_offsets, h_nbrs, out);
+}
+
+int byo_graph_generate(byo_ctx *ctx, int container, const byo_gen_spec *spec, byo_graph **out) {
+  if (!ctx || !out) return BYO_EINVAL;
+  *out = nullptr;
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+    return set_error(ctx, BYO_EINVAL, "unknown container");
+  return graph_generate(ctx, container, spec, out);
+}
+
+void byo_graph_destroy(byo_graph *g) {
+  if (!g) return;
+  if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+  for (auto &b : g->ws) free_buf(b);
+  if (g->pma) pma_destroy(g->pma);
+  else if (g->d_slots) cudaFree(g->d_slots);
+  if (g->d_off) cudaFree(g->d_off);
+  if (g->d_deg) cudaFree(g->d_deg);
+  delete g;
+}
+
+int byo_graph_container(const byo_graph *g) { return g ? g->container : BYO_EINVAL; }
+uint64_t byo_graph_num_vertices(const byo_graph *g) { return g ? g->n : 0; }
+uint64_t byo_graph_num_edges(const byo_graph *g) { return g ? g->m : 0; }
+
+int byo_graph_degrees(byo_graph *g, uint32_t *h_out) {
+  if (!g || !h_out) return BYO_EINVAL;
+  return copy_to_host(g->ctx, h_out, g->d_deg, g->n * 4);
+}
+
+__global__ void k_compact_slots(const uint64_t *__restrict__ off, const uint32_t *__restrict__ slots,
+                                const uint64_t *__restrict__ out_off, uint64_t n, uint32_t *out) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const unsigned lane = threadIdx.x & 31;
+  for (uint64_t v = gw; v < n; v += nw) {
+    uint64_t w = out_off[v];
+    for (uint64_t base = off[v]; base < off[v + 1]; base += 32) {
+      uint64_t j = base + lane;
+      uint32_t u = j < off[v + 1] ? slots[j] : kSentinel;
+      bool keep = u != kSentinel;
+      unsigned m = __ballot_sync(0xFFFFFFFFu, keep);
+      if (keep) out[w + __popc(m & ((1u << lane) - 1))] = u;
+      w += __popc(m);
+    }
+  }
+}
+
+int byo_graph_export_csr(byo_graph *g, uint64_t *h_offsets, uint32_t *h_nbrs) {
+  if (!g || !h_offsets || (g->m && !h_nbrs)) return BYO_EINVAL;
+  byo_ctx *ctx = g->ctx;
+  uint64_t *d_off2 = nullptr;
+  uint32_t *d_n2 = nullptr;
+  BYO_TRY(ws(g, WS_SCAN, g->n + 1, &d_off2));
+  BYO_TRY(ws(g, WS_TC_NBR, g->m + 1, &d_n2));
+  BYO_TRY(scan_u32_to_u64(ctx, g->d_deg, g->n, d_off2));
+  launch(ctx, k_compact_slots, dim3(grid_for(ctx, g->n * 32, 256, 16)), dim3(256), 0,
+         (const uint64_t *)g->d_off, (const uint32_t *)g->d_slots, (const uint64_t *)d_off2, g->n, d_n2);
+  BYO_TRY(check_launch(ctx, "export_csr"));
+  BYO_TRY(copy_to_host(ctx, h_offsets, d_off2, (g->n + 1) * 8));
+  if (h_offsets[g->n] != g->m) return set_error(ctx, BYO_EDEVICE, "export: degree sum != m");
+  return copy_to_host(ctx, h_nbrs, d_n2, g->m * 4);
+}
+
+int byo_graph_neighbors(byo_graph *g, uint32_t v, uint32_t *h_out, uint64_t cap, uint64_t *deg) {
+  if (!g || v >= g->n) return g ? set_error(g->ctx, BYO_EINVAL, "vertex out of range") : BYO_EINVAL;
+  byo_ctx *ctx = g->ctx;
+  uint64_t range[2];
+  uint32_t d = 0;
+  BYO_CU(ctx, cudaMemcpyAsync(range, g->d_off + v, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaMemcpyAsync(&d, g->d_deg + v, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  if (deg) *deg = d;
+  if (!h_out || cap == 0) return BYO_OK;
+  uint64_t len = range[1] - range[0];
+  uint32_t *tmp = new (std::nothrow) uint32_t[len ? len : 1];
+  if (!tmp) return set_error(ctx, BYO_ENOMEM, "host buffer");
+  int rc = copy_to_host(ctx, tmp, g->d_slots + range[0], len * 4);
+  uint64_t w = 0;
+  for (uint64_t i = 0; rc == BYO_OK && i < len && w < cap; i++)
+    if (tmp[i] != kSentinel) h_out[w++] = tmp[i];
+  delete[] tmp;
+  return rc;
+}
+
+static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int sorted, int insert,
+                         int host, uint64_t *changed) {
+  if (!g) return BYO_EINVAL;
+  byo_ctx *ctx = g->ctx;
+  if (changed) *changed = 0;
+  if (g->container != BYO_CONTAINER_PMA)
+    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA container");
+  if (count == 0) return BYO_OK;
+  if (!keys) return set_error(ctx, BYO_EINVAL, "null keys");
+  const uint64_t *d = keys;
+  if (host) {
+    uint64_t *buf = nullptr;
+    BYO_TRY(ws(g, WS_TC_OFF, count, &buf));
+    BYO_CU(ctx, cudaMemcpyAsync(buf, keys, count * 8, cudaMemcpyHostToDevice, ctx->stream));
+    d = buf;
+  }
+  return pma_update(g, d, count, sorted, insert, changed);
+}
+
+int byo_graph_insert_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
+                           uint64_t *changed) {
+  return update_common(g, h_keys, count, sorted, 1, 1, changed);
+}
+int byo_graph_remove_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
+                           uint64_t *changed) {
+  return update_common(g, h_keys, count, sorted, 0, 1, changed);
+}
+int byo_graph_insert_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted,
+                                  uint64_t *changed) {
+  return update_common(g, d_keys, count, sorted, 1, 0, changed);
+}
+int byo_graph_remove_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted,
+                                  uint64_t *changed) {
+  return update_common(g, d_keys, count, sorted, 0, 0, changed);
+}
+
+// ---------------------------------------------------------------- generators
+
+int byo_gen_rmat_pairs_device(byo_ctx *ctx, uint64_t seed, uint32_t lg_n, double a, double b, double c,
+                              uint64_t first, uint64_t count, uint32_t *d_src, uint32_t *d_dst) {
+  if (!ctx) return BYO_EINVAL;
+  return gen_rmat_pairs(ctx, seed, lg_n, a, b, c, first, count, d_src, d_dst);
+}
+int byo_gen_uniform_pairs_device(byo_ctx *ctx, uint64_t seed, uint64_t n, uint64_t first, uint64_t count,
+                                 uint32_t *d_src, uint32_t *d_dst) {
+  if (!ctx) return BYO_EINVAL;
+  return gen_uniform_pairs(ctx, seed, n, first, count, d_src, d_dst);
+}
+int byo_gen_uniform_keys_device(byo_ctx *ctx, uint64_t seed, uint64_t n, uint64_t count, uint64_t *d_keys) {
+  if (!ctx) return BYO_EINVAL;
+  return gen_uniform_keys(ctx, seed, n, count, d_keys);
+}
+
+// ---------------------------------------------------------------- algorithms
+
+int byo_bfs_device(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, int policy,
+                   uint32_t *rounds) {
+  if (!g) return BYO_EINVAL;
+  BYO_TRY(need(g->ctx, policy >= 0 && policy <= BYO_POLICY_M20_BLOCKED, "unknown policy"));
+  return bfs_run(g, src, d_parent, d_level, policy, rounds);
+}
+
+int byo_bfs(byo_graph *g, uint32_t src, uint32_t *h_parent, uint32_t *h_level, int policy,
+            uint32_t *rounds) {
+  if (!g) return BYO_EINVAL;
+  byo_ctx *ctx = g->ctx;
+  uint32_t *d = nullptr;
+  BYO_TRY(ws(g, WS_LABEL, 2 * g->n + 2, &d));
+  uint32_t *dp = h_parent ? d : nullptr, *dl = h_level ? d + g->n : nullptr;
+  BYO_TRY(byo_bfs_device(g, src, dp, dl, policy, rounds));
+  if (h_parent) BYO_TRY(copy_to_host(ctx, h_parent, dp, g->n * 4));
+  if (h_level) BYO_TRY(copy_to_host(ctx, h_level, dl, g->n * 4));
+  return BYO_OK;
+}
+
+int byo_cc_device(byo_graph *g, uint32_t *d_label) {
+  if (!g || !d_label) return BYO_EINVAL;
+  return cc_run(g, d_label);
+}
+
+int byo_cc(byo_graph *g, uint32_t *h_label) {
+  if (!g || !h_label) return BYO_EINVAL;
+  uint32_t *d = nullptr;
+  BYO_TRY(ws(g, WS_PR_A, g->n + 1, &d));
+  BYO_TRY(cc_run(g, d));
+  return copy_to_host(g->ctx, h_label, d, g->n * 4);
+}
+
+int byo_bfs_cc(byo_graph *g, uint32_t *h_label) {
+  if (!g || !h_label) return BYO_EINVAL;
+  uint32_t *d = nullptr;
+  BYO_TRY(ws(g, WS_PR_B, g->n + 1, &d));
+  BYO_TRY(bfs_cc_run(g, d));
+  return copy_to_host(g->ctx, h_label, d, g->n * 4);
+}
+
+int byo_pagerank_device(byo_graph *g, double eps, uint32_t max_iters, int precision, double *d_p,
+                        uint32_t *iters, double *l1) {
+  if (!g || !d_p) return BYO_EINVAL;
+  return pagerank_run(g, eps, max_iters, precision, d_p, iters, l1);
+}
+
+int byo_pagerank(byo_graph *g, double eps, uint32_t max_iters, int precision, double *h_p, uint32_t *iters,
+                 double *l1) {
+  if (!g || !h_p) return BYO_EINVAL;
+  double *d = nullptr;
+  BYO_TRY(ws(g, WS_TC_CNT, 2 * g->n + 2, (uint32_t **)&d));
+  BYO_TRY(pagerank_run(g, eps, max_iters, precision, d, iters, l1));
+  return copy_to_host(g->ctx, h_p, d, g->n * 8);
+}
+
+int byo_triangle_count(byo_graph *g, uint64_t *count) {
+  if (!g || !count) return BYO_EINVAL;
+  return tc_run(g, count);
+}
+
+// ---------------------------------------------------------------- edgeMap API
+
+int byo_functor_bfs_create(byo_graph *g, uint32_t src, byo_functor **out) {
+  if (!g || !out) return BYO_EINVAL;
+  *out = nullptr;
+  if (src >= g->n) return set_error(g->ctx, BYO_EINVAL, "src >= n");
+  byo_functor *f = new (std::nothrow) byo_functor();
+  if (!f) return BYO_ENOMEM;
+  f->g = g;
+  const uint64_t W = (g->n + 31) / 32;
+  int rc = ensure(g->ctx, f->lp, g->n * 8);
+  if (rc == BYO_OK) rc = ensure(g->ctx, f->visited, W * 4);
+  if (rc == BYO_OK) {
+    f->st.lp = (uint64_t *)f->lp.p;
+    f->st.visited = (uint32_t *)f->visited.p;
+    rc = trav_init(g, f->st, src);
+  }
+  if (rc != BYO_OK) {
+    byo_functor_destroy(f);
+    return rc;
+  }
+  *out = f;
+  return BYO_OK;
+}
+
+int byo_functor_bfs_parents(byo_functor *f, uint32_t *h_parents) {
+  if (!f || !h_parents) return BYO_EINVAL;
+  byo_graph *g = f->g;
+  uint32_t *d = nullptr;
+  BYO_TRY(ws(g, WS_LABEL, g->n + 1, &d));
+  BYO_TRY(trav_extract(g, f->st, d, nullptr));
+  return copy_to_host(g->ctx, h_parents, d, g->n * 4);
+}
+
+void byo_functor_destroy(byo_functor *f) {
+  if (!f) return;
+  if (f->g && f->g->ctx) cudaStreamSynchronize(f->g->ctx->stream);
+  free_buf(f->lp);
+  free_buf(f->visited);
+  delete f;
+}
+
+static int vs_alloc(byo_graph *g, byo_vertex_subset **out) {
+  byo_vertex_subset *vs = new (std::nothrow) byo_vertex_subset();
+  if (!vs) return BYO_ENOMEM;
+  vs->g = g;
+  const uint64_t W = (g->n + 31) / 32;
+  int rc = ensure(g->ctx, vs->list, g->n * 4);
+  if (rc == BYO_OK) rc = ensure(g->ctx, vs->bits, W * 4);
+  if (rc != BYO_OK) {
+    byo_vs_destroy(vs);
+    return rc;
+  }
+  vs->f.list = (uint32_t *)vs->list.p;
+  vs->f.bits = (uint32_t *)vs->bits.p;
+  *out = vs;
+  return BYO_OK;
+}
+
+__global__ void k_sum_deg(const uint32_t *__restrict__ list, uint64_t cnt, const uint32_t *__restrict__ deg,
+                          unsigned long long *out) {
+  unsigned long long s = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    s += deg[list[i]];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
+}
+
+int byo_vs_create_list(byo_graph *g, const uint32_t *h_ids, uint64_t count, byo_vertex_subset **out) {
+  if (!g || !out || (count && !h_ids)) return BYO_EINVAL;
+  *out = nullptr;
+  byo_ctx *ctx = g->ctx;
+  if (count > g->n) return set_error(ctx, BYO_EINVAL, "subset larger than n");
+  for (uint64_t i = 0; i < count; i++)
+    if (h_ids[i] >= g->n) return set_error(ctx, BYO_EINVAL, "vertex id >= n");
+  byo_vertex_subset *vs = nullptr;
+  BYO_TRY(vs_alloc(g, &vs));
+  int rc = BYO_OK;
+  if (count) {
+    cudaError_t e = cudaMemcpyAsync(vs->f.list, h_ids, count * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) rc = set_error(ctx, BYO_EDEVICE, "upload subset", e);
+  }
+  unsigned long long *d_sum = nullptr;
+  if (rc == BYO_OK) rc = ws(g, WS_MISC, 4, (uint32_t **)&d_sum);
+  if (rc == BYO_OK) {
+    cudaMemsetAsync(d_sum, 0, 8, ctx->stream);
+    if (count)
+      launch(ctx, k_sum_deg, dim3(grid_for(ctx, count, 256)), dim3(256), 0, (const uint32_t *)vs->f.list, count,
+             (const uint32_t *)g->d_deg, d_sum);
+    unsigned long long h = 0;
+    cudaMemcpyAsync(&h, d_sum, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = set_error(ctx, BYO_EDEVICE, "subset degrees", e);
+    vs->f.outdeg = h;
+  }
+  if (rc != BYO_OK) {
+    byo_vs_destroy(vs);
+    return rc;
+  }
+  vs->f.size = count;
+  vs->f.has_list = true;
+  vs->f.has_bits = false;
+  vs->f.dense = false;
+  *out = vs;
+  return BYO_OK;
+}
+
+int byo_vs_create_single(byo_graph *g, uint32_t v, byo_vertex_subset **out) {
+  return byo_vs_create_list(g, &v, 1, out);
+}
+
+void byo_vs_destroy(byo_vertex_subset *vs) {
+  if (!vs) return;
+  if (vs->g && vs->g->ctx) cudaStreamSynchronize(vs->g->ctx->stream);
+  free_buf(vs->list);
+  free_buf(vs->bits);
+  delete vs;
+}
+
+uint64_t byo_vs_size(const byo_vertex_subset *vs) { return vs ? vs->f.size : 0; }
+int byo_vs_is_dense(const byo_vertex_subset *vs) { return vs ? (vs->f.dense ? 1 : 0) : BYO_EINVAL; }
+
+int byo_vs_to_list(byo_vertex_subset *vs, uint32_t *h_out, uint64_t cap) {
+  if (!vs || (vs->f.size && !h_out)) return BYO_EINVAL;
+  byo_ctx *ctx = vs->g->ctx;
+  if (cap < vs->f.size) return set_error(ctx, BYO_EINVAL, "output smaller than the subset");
+  if (!vs->f.size) return BYO_OK;
+  // toSparse order: increasing ids
+  uint64_t *keys = nullptr, *tmp = nullptr, *sorted = nullptr;
+  BYO_TRY(ws(vs->g, WS_TC_OFF, 2 * vs->f.size + 2, &keys));
+  tmp = keys + vs->f.size + 1;
+  std::vector<uint32_t> h(vs->f.size);
+  BYO_TRY(copy_to_host(ctx, h.data(), vs->f.list, vs->f.size * 4));
+  std::vector<uint64_t> k(h.begin(), h.end());
+  BYO_CU(ctx, cudaMemcpyAsync(keys, k.data(), k.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  BYO_TRY(sort_u64(ctx, keys, tmp, vs->f.size, sig_mask_for(vs->g->n) & 0xFFFFFFFFull, &sorted));
+  BYO_TRY(copy_to_host(ctx, k.data(), sorted, k.size() * 8));
+  for (uint64_t i = 0; i < vs->f.size; i++) h_out[i] = (uint32_t)k[i];
+  return BYO_OK;
+}
+
+int byo_edge_map(byo_graph *g, byo_vertex_subset *vs, byo_functor *f, int64_t threshold, uint32_t flags,
+                 byo_vertex_subset **out) {
+  if (!g || !vs || !f || !out) return BYO_EINVAL;
+  *out = nullptr;
+  byo_ctx *ctx = g->ctx;
+  if (vs->g != g || f->g != g) return set_error(ctx, BYO_EINVAL, "subset / functor of another graph");
+  byo_vertex_subset *o = nullptr;
+  BYO_TRY(vs_alloc(g, &o));
+  const uint64_t W = (g->n + 31) / 32;
+  int rc = memset_async(ctx, o->f.bits, 0, W * 4);
+  // edgeMapData, edge_map_data.h:254-307
+  int mode = MODE_PUSH;
+  bool empty = vs->f.size == 0;
+  if (!empty) {
+    if ((flags & BYO_FL_DENSE_ONLY) || (vs->f.dense && vs->f.size > g->n / 10)) {
+      mode = MODE_PULL;
+    } else if (vs->f.outdeg == 0) {
+      empty = true;
+    } else {
+      const int sparse = (flags & BYO_FL_SPARSE_BLOCKED) ? MODE_BLOCKED : MODE_PUSH;
+      mode = m20_mode(g, vs->f, threshold, sparse);
+      if (mode == MODE_PULL && (flags & BYO_FL_NO_DENSE)) mode = sparse;
+    }
+  }
+  if (rc == BYO_OK && !empty) {
+    EngineTuning tune = default_tuning(g);
+    rc = edge_map_round(g, f->st, vs->f, o->f, mode, tune);
+  } else if (rc == BYO_OK) {
+    o->f.size = 0;
+    o->f.has_list = o->f.has_bits = true;
+  }
+  if (rc == BYO_OK) rc = check_launch(ctx, "edge_map");
+  if (rc != BYO_OK) {
+    byo_vs_destroy(o);
+    return rc;
+  }
+  if (flags & BYO_FL_NO_OUTPUT) {
+    o->f.size = 0;
+    o->f.outdeg = 0;
+  }
+  *out = o;
+  return BYO_OK;
+}
+
+int byo_last_rounds(byo_ctx *ctx, byo_round_log *out, uint64_t cap, uint64_t *count) {
+  if (!ctx) return BYO_EINVAL;
+  uint64_t n = ctx->rounds.size();
+  if (count) *count = n;
+  if (out)
+    for (uint64_t i = 0; i < n && i < cap; i++) out[i] = ctx->rounds[i];
+  return BYO_OK;
+}
+
+int byo_ctx_set_round_timing(byo_ctx *ctx, int on) {
+  if (!ctx) return BYO_EINVAL;
+  ctx->time_rounds = on != 0;
+  return BYO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,572 @@
+// engine.cu -- edgeMap rounds (push / blocked / pull) and the BFS driver.
+// See engine.h for the design.  Algorithmic bytes of one BFS traversal:
+// 4 B per adjacency entry of every reached vertex + 8 B offsets per vertex
+// + 8 B lp written per reached vertex (parent/level split is 8 B more).
+#include "device.cuh"
+#include "engine.h"
+#include "internal.h"
+#include "scan.cuh"
+
+namespace byo {
+
+__device__ __forceinline__ int log4_bin(uint32_t d) {
+  int b = d ? (31 - __clz(d)) / 2 : 0;  // 0:[0,4) 1:[4,16) ...
+  return b > 7 ? 7 : b;
+}
+
+// Emits v (if `emit`) to the next frontier list and bitmap; accumulates its
+// degree for the round statistics.  Warp-collective.
+__device__ __forceinline__ void emit_next(bool emit, uint32_t v, uint32_t *out_list,
+                                          uint32_t *out_bits, RoundStats *st,
+                                          const uint32_t *__restrict__ deg, uint64_t &dsum,
+                                          bool set_bits) {
+  uint64_t slot = warp_append(emit, &st->count);
+  if (emit) {
+    out_list[slot] = v;
+    if (set_bits) atomicOr(out_bits + (v >> 5), 1u << (v & 31));
+    uint32_t d = deg[v];
+    dsum += d;
+    atomicAdd(&st->hist[log4_bin(d)], 1ull);
+  }
+}
+
+__device__ __forceinline__ void flush_dsum(uint64_t dsum, RoundStats *st) {
+  dsum = warp_sum(dsum);
+  if (lane_id() == 0 && dsum) atomicAdd(&st->outdeg, (unsigned long long)dsum);
+}
+
+// Visits edge u->v for BFS_F: cond(v) = not visited before this round;
+// updateAtomic keeps the smallest (level, parent); the first writer emits.
+__device__ __forceinline__ bool visit(uint32_t u, uint32_t v, uint64_t lvl, uint64_t *lp,
+                                      const uint32_t *__restrict__ visited) {
+  if (v == kSentinel) return false;
+  if (test_bit_cg(visited, v)) return false;
+  unsigned long long old = atomicMin((unsigned long long *)(lp + v), (unsigned long long)(lvl | u));
+  return old == kNone64;
+}
+
+// ---------------------------------------------------------------- push
+template <int GS>
+__global__ void __launch_bounds__(256) k_push(const uint64_t *__restrict__ off,
+                                              const uint32_t *__restrict__ slots,
+                                              const uint32_t *__restrict__ deg,
+                                              const uint32_t *__restrict__ F, uint64_t fsize,
+                                              uint64_t *lp, const uint32_t *__restrict__ visited,
+                                              uint32_t *out_list, uint32_t *out_bits,
+                                              RoundStats *st, uint64_t lvl, uint32_t *hubs,
+                                              uint32_t hub_min) {
+  constexpr int PER_WARP = 32 / GS;
+  const unsigned lane = lane_id(), g = lane / GS, gl = lane % GS;
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint64_t dsum = 0;
+  for (uint64_t i0 = gw * PER_WARP; i0 < fsize; i0 += nw * PER_WARP) {
+    uint64_t i = i0 + g;
+    uint32_t u = 0;
+    uint64_t b = 0, e = 0;
+    if (i < fsize) {
+      u = F[i];
+      b = off[u];
+      e = off[u + 1];
+      if (e - b >= hub_min) {
+        if (gl == 0) hubs[atomicAdd(&st->ndefer, 1ull)] = u;
+        e = b;
+      }
+    }
+    uint64_t chunks = (e - b + GS - 1) / GS;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      uint64_t t = __shfl_xor_sync(kFull, chunks, o);
+      chunks = t > chunks ? t : chunks;
+    }
+    for (uint64_t c = 0; c < chunks; c++) {
+      uint64_t j = b + c * GS + gl;
+      bool em = false;
+      uint32_t v = kSentinel;
+      if (j < e) {
+        v = slots[j];
+        em = visit(u, v, lvl, lp, visited);
+      }
+      emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+    }
+  }
+  flush_dsum(dsum, st);
+}
+
+// One CTA per hub vertex (degree >= hub_min).
+__global__ void __launch_bounds__(256) k_push_hubs(const uint64_t *__restrict__ off,
+                                                   const uint32_t *__restrict__ slots,
+                                                   const uint32_t *__restrict__ deg,
+                                                   const uint32_t *__restrict__ hubs,
+                                                   uint64_t *lp, const uint32_t *__restrict__ visited,
+                                                   uint32_t *out_list, uint32_t *out_bits,
+                                                   RoundStats *st, uint64_t lvl) {
+  const uint64_t nh = *(volatile unsigned long long *)&st->ndefer;
+  uint64_t dsum = 0;
+  for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
+    const uint32_t u = hubs[h];
+    const uint64_t b = off[u], e = off[u + 1];
+    for (uint64_t base = b; base < e; base += blockDim.x) {
+      uint64_t j = base + threadIdx.x;
+      bool em = false;
+      uint32_t v = kSentinel;
+      if (j < e) {
+        v = slots[j];
+        em = visit(u, v, lvl, lp, visited);
+      }
+      emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+    }
+  }
+  flush_dsum(dsum, st);
+}
+
+// ---------------------------------------------------------------- blocked
+// Edge-balanced: tile t covers frontier-edge ranks [t*TILE, (t+1)*TILE) of
+// the exclusive degree prefix `pre`; each rank is mapped to its frontier
+// vertex by binary search (the merge-path split of rank space).
+__global__ void __launch_bounds__(256) k_push_blocked(const uint64_t *__restrict__ off,
+                                                      const uint32_t *__restrict__ slots,
+                                                      const uint32_t *__restrict__ deg,
+                                                      const uint32_t *__restrict__ F, uint64_t fsize,
+                                                      const uint64_t *__restrict__ pre,
+                                                      uint64_t *lp,
+                                                      const uint32_t *__restrict__ visited,
+                                                      uint32_t *out_list, uint32_t *out_bits,
+                                                      RoundStats *st, uint64_t lvl, int tile) {
+  const uint64_t total = pre[fsize];
+  const uint64_t ntiles = (total + tile - 1) / tile;
+  __shared__ uint64_t s_lo, s_hi;
+  uint64_t dsum = 0;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint64_t e0 = t * tile;
+    const uint64_t e1 = e0 + tile < total ? e0 + tile : total;
+    if (threadIdx.x == 0) {
+      // last index with pre[i] <= e0, and with pre[i] <= e1-1
+      uint64_t lo = 0, hi = fsize;  // search in [0, fsize)
+      while (hi - lo > 1) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (pre[mid] <= e0) lo = mid; else hi = mid;
+      }
+      s_lo = lo;
+      uint64_t lo2 = lo, hi2 = fsize;
+      while (hi2 - lo2 > 1) {
+        uint64_t mid = (lo2 + hi2) >> 1;
+        if (pre[mid] <= e1 - 1) lo2 = mid; else hi2 = mid;
+      }
+      s_hi = lo2;
+    }
+    __syncthreads();
+    const uint64_t vlo = s_lo, vhi = s_hi;
+    for (uint64_t base = e0; base < e1; base += blockDim.x) {
+      const uint64_t e = base + threadIdx.x;
+      bool em = false;
+      uint32_t v = kSentinel;
+      if (e < e1) {
+        uint64_t lo = vlo, hi = vhi + 1;
+        while (hi - lo > 1) {
+          uint64_t mid = (lo + hi) >> 1;
+          if (pre[mid] <= e) lo = mid; else hi = mid;
+        }
+        const uint32_t u = F[lo];
+        v = slots[off[u] + (e - pre[lo])];
+        em = visit(u, v, lvl, lp, visited);
+      }
+      emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+    }
+    __syncthreads();
+  }
+  flush_dsum(dsum, st);
+}
+
+// ---------------------------------------------------------------- pull
+__device__ __forceinline__ bool in_frontier(const uint32_t *s_bits, int stage_words,
+                                            const uint32_t *__restrict__ Fbits, uint32_t u) {
+  uint32_t w = u >> 5;
+  uint32_t word = (w < (uint32_t)stage_words) ? s_bits[w] : __ldg(Fbits + w);
+  return (word >> (u & 31)) & 1u;
+}
+
+__global__ void __launch_bounds__(1024) k_pull(const uint64_t *__restrict__ off,
+                                               const uint32_t *__restrict__ slots,
+                                               const uint32_t *__restrict__ deg,
+                                               const uint32_t *__restrict__ Fbits, uint64_t n,
+                                               uint64_t *__restrict__ lp, uint32_t *visited,
+                                               uint32_t *out_list, uint32_t *out_bits,
+                                               RoundStats *st, uint64_t lvl, uint32_t *defer,
+                                               int cap, int stage_words) {
+  extern __shared__ uint32_t s_bits[];
+  for (int i = threadIdx.x; i < stage_words; i += blockDim.x) s_bits[i] = Fbits[i];
+  __syncthreads();
+  const uint64_t W = (n + 31) >> 5;
+  const unsigned lane = lane_id();
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint64_t dsum = 0;
+  for (uint64_t w = gw; w < W; w += nw) {
+    const uint32_t vword = visited[w];
+    if (vword == kFull) continue;
+    const uint64_t v = w * 32 + lane;
+    bool active = v < n && !((vword >> lane) & 1u);
+    bool found = false, deferred = false;
+    uint32_t parent = 0;
+    if (active) {
+      const uint64_t b = off[v], e = off[v + 1];
+      const uint64_t lim = (e - b > (uint64_t)cap) ? b + cap : e;
+      for (uint64_t j = b; j < lim; j++) {
+        uint32_t u = slots[j];
+        if (u == kSentinel) continue;
+        if (in_frontier(s_bits, stage_words, Fbits, u)) {
+          found = true;
+          parent = u;
+          break;
+        }
+      }
+      deferred = !found && lim < e;
+    }
+    if (found) lp[v] = lvl | parent;
+    const unsigned fb = __ballot_sync(kFull, found);
+    if (lane == 0 && fb) {
+      out_bits[w] = fb;
+      visited[w] = vword | fb;
+    }
+    uint64_t slot = warp_append(found, &st->count);
+    if (found) {
+      out_list[slot] = (uint32_t)v;
+      uint32_t d = deg[v];
+      dsum += d;
+      atomicAdd(&st->hist[log4_bin(d)], 1ull);
+    }
+    uint64_t ds = warp_append(deferred, &st->ndefer);
+    if (deferred) defer[ds] = (uint32_t)v;
+  }
+  flush_dsum(dsum, st);
+}
+
+// Warp per deferred vertex: 32 neighbours per step, ballot, lowest lane wins.
+__global__ void __launch_bounds__(256) k_pull_long(const uint64_t *__restrict__ off,
+                                                   const uint32_t *__restrict__ slots,
+                                                   const uint32_t *__restrict__ deg,
+                                                   const uint32_t *__restrict__ Fbits,
+                                                   uint64_t *__restrict__ lp, uint32_t *visited,
+                                                   uint32_t *out_list, uint32_t *out_bits,
+                                                   RoundStats *st, uint64_t lvl,
+                                                   const uint32_t *__restrict__ defer, int cap) {
+  const uint64_t nd = *(volatile unsigned long long *)&st->ndefer;
+  const unsigned lane = lane_id();
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t i = gw; i < nd; i += nw) {
+    const uint32_t v = defer[i];
+    const uint64_t b = off[v] + cap, e = off[v + 1];
+    bool found = false;
+    uint32_t parent = 0;
+    for (uint64_t base = b; base < e && !found; base += 32) {
+      uint64_t j = base + lane;
+      uint32_t u = j < e ? slots[j] : kSentinel;
+      bool hit = u != kSentinel && ((__ldg(Fbits + (u >> 5)) >> (u & 31)) & 1u);
+      unsigned m = __ballot_sync(kFull, hit);
+      if (m) {
+        found = true;
+        parent = __shfl_sync(kFull, u, __ffs(m) - 1);
+      }
+    }
+    if (found && lane == 0) {
+      lp[v] = lvl | parent;
+      atomicOr(out_bits + (v >> 5), 1u << (v & 31));
+      atomicOr(visited + (v >> 5), 1u << (v & 31));
+      unsigned long long slot = atomicAdd(&st->count, 1ull);
+      out_list[slot] = v;
+      uint32_t d = deg[v];
+      atomicAdd(&st->outdeg, (unsigned long long)d);
+      atomicAdd(&st->hist[log4_bin(d)], 1ull);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- bookkeeping
+__global__ void k_mark_visited(const uint32_t *__restrict__ list, const RoundStats *st,
+                               uint32_t *visited) {
+  const uint64_t cnt = st->count;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t v = list[i];
+    atomicOr(visited + (v >> 5), 1u << (v & 31));
+  }
+}
+
+__global__ void k_clear_words_from_list(const uint32_t *__restrict__ list, uint64_t cnt,
+                                        uint32_t *bits) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    bits[list[i] >> 5] = 0;  // every set bit of `bits` belongs to some list entry
+}
+
+__global__ void k_set_bits_from_list(const uint32_t *__restrict__ list, uint64_t cnt, uint32_t *bits) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t v = list[i];
+    atomicOr(bits + (v >> 5), 1u << (v & 31));
+  }
+}
+
+__global__ void k_trav_init(uint64_t *lp, uint32_t *visited, uint64_t n, uint32_t src) {
+  const uint64_t W = (n + 31) >> 5;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    lp[i] = (i == src) ? (uint64_t)src : kNone64;
+    if (i < W) visited[i] = (i == (src >> 5)) ? (1u << (src & 31)) : 0u;
+  }
+}
+
+__global__ void k_trav_extract(const uint64_t *__restrict__ lp, uint64_t n, uint32_t *parent,
+                               uint32_t *level) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t x = lp[i];
+    if (parent) parent[i] = x == kNone64 ? kSentinel : (uint32_t)x;
+    if (level) level[i] = x == kNone64 ? kSentinel : (uint32_t)(x >> 32);
+  }
+}
+
+// ---------------------------------------------------------------- host side
+
+EngineTuning default_tuning(const byo_graph *g) {
+  EngineTuning t;
+  const uint64_t W = (g->n + 31) / 32;
+  t.pull_stage_words = (int)(W < 32768 ? W : 32768);
+  double avg = g->n ? (double)g->m / (double)g->n : 0.0;
+  t.push_group = avg >= 24 ? 32 : avg >= 12 ? 16 : avg >= 6 ? 8 : 4;
+  return t;
+}
+
+int m20_mode(const byo_graph *g, const Frontier &f, int64_t threshold, int sparse_mode) {
+  const uint64_t n = g->n, M = g->m;
+  const uint64_t dense_threshold = threshold < 0 ? M / 20 : (uint64_t)threshold;
+  if (f.dense && f.size > n / 10) return MODE_PULL;
+  if (f.size + f.outdeg > dense_threshold) return MODE_PULL;
+  return sparse_mode;
+}
+
+int trav_init(byo_graph *g, TravState &st, uint32_t src) {
+  byo_ctx *ctx = g->ctx;
+  launch(ctx, k_trav_init, dim3(grid_for(ctx, g->n, 256)), dim3(256), 0, st.lp, st.visited, g->n, src);
+  st.round = 1;
+  st.reached = 1;
+  return check_launch(ctx, "trav_init");
+}
+
+int trav_extract(byo_graph *g, const TravState &st, uint32_t *d_parent, uint32_t *d_level) {
+  byo_ctx *ctx = g->ctx;
+  launch(ctx, k_trav_extract, dim3(grid_for(ctx, g->n, 256)), dim3(256), 0, (const uint64_t *)st.lp,
+         g->n, d_parent, d_level);
+  return check_launch(ctx, "trav_extract");
+}
+
+int clear_frontier_bits(byo_graph *g, Frontier &f) {
+  byo_ctx *ctx = g->ctx;
+  const uint64_t W = (g->n + 31) / 32;
+  if (f.has_list && f.size < W / 8) {
+    if (f.size)
+      launch(ctx, k_clear_words_from_list, dim3(grid_for(ctx, f.size, 256)), dim3(256), 0,
+             (const uint32_t *)f.list, f.size, f.bits);
+  } else {
+    BYO_TRY(memset_async(ctx, f.bits, 0, W * sizeof(uint32_t)));
+  }
+  return check_launch(ctx, "clear_frontier_bits");
+}
+
+int ensure_bits(byo_graph *g, Frontier &f) {
+  if (f.has_bits) return BYO_OK;
+  byo_ctx *ctx = g->ctx;
+  const uint64_t W = (g->n + 31) / 32;
+  BYO_TRY(memset_async(ctx, f.bits, 0, W * sizeof(uint32_t)));
+  if (f.size)
+    launch(ctx, k_set_bits_from_list, dim3(grid_for(ctx, f.size, 256)), dim3(256), 0,
+           (const uint32_t *)f.list, f.size, f.bits);
+  f.has_bits = true;
+  return check_launch(ctx, "ensure_bits");
+}
+
+static int pull_smem_ok(int bytes) {
+  static int configured = 0;
+  if (bytes > 48 * 1024 && configured < bytes) {
+    if (cudaFuncSetAttribute(k_pull, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+      return 0;
+    configured = bytes;
+  }
+  return 1;
+}
+
+int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int mode,
+                   const EngineTuning &tune) {
+  byo_ctx *ctx = g->ctx;
+  RoundStats *d_st = nullptr;
+  BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 1, (uint64_t **)&d_st));
+  BYO_CU(ctx, cudaMemsetAsync(d_st, 0, sizeof(RoundStats), ctx->stream));
+  uint32_t *defer = nullptr;
+  BYO_TRY(ws(g, WS_DEFER, g->n + 1, &defer));
+  const uint64_t lvl = (uint64_t)st.round << 32;
+  if (mode == MODE_PULL) {
+    BYO_TRY(ensure_bits(g, in));
+    int stage = tune.pull_stage_words;
+    int smem = stage * 4;
+    if (!pull_smem_ok(smem)) {
+      if (stage > 12 * 1024) stage = 12 * 1024;
+      smem = stage * 4;
+    }
+    const uint64_t W = (g->n + 31) / 32;
+    int block = 1024;
+    int grid = (int)((W + 31) / 32);
+    int maxg = ctx->num_sms * (smem > 100 * 1024 ? 1 : 2);
+    if (grid > maxg) grid = maxg;
+    if (grid < 1) grid = 1;
+    launch(ctx, k_pull, dim3(grid), dim3(block), (size_t)smem, (const uint64_t *)g->d_off,
+           (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.bits, g->n,
+           st.lp, st.visited, out.list, out.bits, d_st, lvl, defer, tune.pull_cap, stage);
+    launch(ctx, k_pull_long, dim3(ctx->num_sms * 4), dim3(256), 0, (const uint64_t *)g->d_off,
+           (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.bits, st.lp,
+           st.visited, out.list, out.bits, d_st, lvl, (const uint32_t *)defer, tune.pull_cap);
+  } else {
+    if (!in.has_list) return set_error(ctx, BYO_EINVAL, "sparse round needs a frontier list");
+    if (mode == MODE_PUSH) {
+      const int grid = grid_for(ctx, (in.size * (uint64_t)tune.push_group + 255) / 256 * 256, 256, 16);
+      switch (tune.push_group) {
+#define PUSH_CASE(GS)                                                                            \
+  case GS:                                                                                       \
+    launch(ctx, k_push<GS>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,                \
+           (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.list,  \
+           in.size, st.lp, (const uint32_t *)st.visited, out.list, out.bits, d_st, lvl, defer,   \
+           tune.hub_min);                                                                        \
+    break;
+        PUSH_CASE(4)
+        PUSH_CASE(8)
+        PUSH_CASE(16)
+        PUSH_CASE(32)
+#undef PUSH_CASE
+        default:
+          return set_error(ctx, BYO_EINVAL, "push group must be 4, 8, 16 or 32");
+      }
+      launch(ctx, k_push_hubs, dim3(ctx->num_sms * 2), dim3(256), 0, (const uint64_t *)g->d_off,
+             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)defer, st.lp,
+             (const uint32_t *)st.visited, out.list, out.bits, d_st, lvl);
+    } else {
+      uint64_t *pre = nullptr;
+      BYO_TRY(ws(g, WS_SCAN, in.size + 1, &pre));
+      // prefix over slot-range lengths (= degrees for a CSR; gaps included
+      // for the PMA so ranks map to slots)
+      BYO_TRY(scan_gather_range(ctx, g->d_off, in.list, in.size, pre));
+      const uint64_t est_tiles = (in.outdeg + tune.blocked_tile - 1) / tune.blocked_tile;
+      const int grid = grid_for(ctx, est_tiles ? est_tiles : 1, 1, 16);
+      launch(ctx, k_push_blocked, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
+             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.list,
+             in.size, (const uint64_t *)pre, st.lp, (const uint32_t *)st.visited, out.list, out.bits,
+             d_st, lvl, tune.blocked_tile);
+    }
+    launch(ctx, k_mark_visited, dim3(grid_for(ctx, in.outdeg + 1, 256)), dim3(256), 0,
+           (const uint32_t *)out.list, (const RoundStats *)d_st, st.visited);
+  }
+  BYO_TRY(check_launch(ctx, "edge_map_round"));
+  RoundStats *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, d_st, sizeof(RoundStats), cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  out.size = h->count;
+  out.outdeg = h->outdeg;
+  for (int i = 0; i < 8; i++) out.hist[i] = h->hist[i];
+  out.dense = (mode == MODE_PULL);
+  out.has_list = true;
+  out.has_bits = true;
+  st.round++;
+  st.reached += out.size;
+  return BYO_OK;
+}
+
+// ---------------------------------------------------------------- BFS driver
+
+int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, int policy,
+            uint32_t *rounds) {
+  byo_ctx *ctx = g->ctx;
+  if (src >= g->n) return set_error(ctx, BYO_EINVAL, "bfs: src >= n");
+  const uint64_t n = g->n, W = (n + 31) / 32;
+  TravState st;
+  Frontier fa, fb;
+  BYO_TRY(ws(g, WS_LP, n, &st.lp));
+  BYO_TRY(ws(g, WS_VISITED, W, &st.visited));
+  BYO_TRY(ws(g, WS_FRONT_LIST_A, n, &fa.list));
+  BYO_TRY(ws(g, WS_FRONT_LIST_B, n, &fb.list));
+  BYO_TRY(ws(g, WS_FRONT_BITS_A, W, &fa.bits));
+  BYO_TRY(ws(g, WS_FRONT_BITS_B, W, &fb.bits));
+  BYO_TRY(trav_init(g, st, src));
+  BYO_CU(ctx, cudaMemcpyAsync(fa.list, &src, sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+  BYO_TRY(memset_async(ctx, fa.bits, 0, W * 4));
+  BYO_TRY(memset_async(ctx, fb.bits, 0, W * 4));
+  uint32_t word = 1u << (src & 31);
+  BYO_CU(ctx, cudaMemcpyAsync(fa.bits + (src >> 5), &word, 4, cudaMemcpyHostToDevice, ctx->stream));
+  uint32_t dsrc = 0;
+  BYO_CU(ctx, cudaMemcpyAsync(&dsrc, g->d_deg + src, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  fa.size = 1;
+  fa.outdeg = dsrc;
+  fa.has_list = fa.has_bits = true;
+  fb.size = 0;
+  fb.has_list = true;  // empty list: its bitmap is all zero
+  const EngineTuning tune = default_tuning(g);
+  ctx->rounds.clear();
+  Frontier *cur = &fa, *nxt = &fb;
+  uint32_t nr = 0;
+  while (cur->size > 0) {
+    int mode;
+    switch (policy) {
+      case BYO_POLICY_PUSH: mode = MODE_PUSH; break;
+      case BYO_POLICY_PULL: mode = MODE_PULL; break;
+      case BYO_POLICY_BLOCKED: mode = MODE_BLOCKED; break;
+      case BYO_POLICY_M20_BLOCKED: mode = m20_mode(g, *cur, -1, MODE_BLOCKED); break;
+      case BYO_POLICY_LEARNED: {
+        mode = m20_mode(g, *cur, -1, MODE_PUSH);
+        float feat[16];
+        const double lg = 1.0 / 32.0;
+        feat[0] = (float)(log2((double)cur->size + 1) * lg);
+        feat[1] = (float)(log2((double)cur->outdeg + 1) * lg);
+        feat[2] = (float)(log2((double)(n - st.reached) + 1) * lg);
+        feat[3] = (float)(log2((double)n + 1) * lg);
+        feat[4] = (float)(log2((double)g->m + 1) * lg);
+        feat[5] = cur->dense ? 1.f : 0.f;
+        double tot = 0;
+        for (int i = 0; i < 8; i++) tot += (double)cur->hist[i];
+        for (int i = 0; i < 8; i++) feat[6 + i] = tot > 0 ? (float)(cur->hist[i] / tot) : 0.f;
+        feat[14] = (float)((double)(cur->size + cur->outdeg) / ((double)g->m / 20.0 + 1.0));
+        feat[15] = 0.f;
+        int m2 = mode;
+        if (policy_choose(ctx, feat, 16, &m2) == BYO_OK) mode = m2;
+        break;
+      }
+      default: mode = m20_mode(g, *cur, -1, MODE_PUSH); break;
+    }
+    if (mode != MODE_PULL && cur->outdeg == 0) break;  // edge_map_data.h:290
+    // next's bitmap still holds the frontier before `cur`: clear it
+    BYO_TRY(clear_frontier_bits(g, *nxt));
+    byo_round_log lg{};
+    lg.round = st.round;
+    lg.mode = (uint32_t)mode;
+    lg.frontier = cur->size;
+    lg.frontier_deg = cur->outdeg;
+    lg.unvisited = n - st.reached;
+    if (ctx->time_rounds) BYO_CU(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+    nxt->size = 0;
+    BYO_TRY(edge_map_round(g, st, *cur, *nxt, mode, tune));
+    if (ctx->time_rounds) {
+      BYO_CU(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+      BYO_CU(ctx, cudaEventSynchronize(ctx->ev[1]));
+      cudaEventElapsedTime(&lg.ms, ctx->ev[0], ctx->ev[1]);
+    }
+    ctx->rounds.push_back(lg);
+    nr++;
+    Frontier *t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  if (rounds) *rounds = nr;
+  return trav_extract(g, st, d_parent, d_level);
+}
+
+}  // namespace byo

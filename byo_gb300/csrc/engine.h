@@ -1,0 +1,75 @@
+// engine.h -- the edgeMap / vertexSubset engine shared by BFS, BFS-CC and the
+// public edgeMap API.
+//
+// One traversal state (the BFS_F functor of BFS.h:30-45 with its Parents
+// array) is a packed word per vertex, lp[v] = level << 32 | parent, plus a
+// "visited before this round" bitmap (cond(v) of the functor).  A round reads
+// frontier F (list and/or bitmap) and writes the next frontier as both a list
+// and a bitmap, so no sparse<->dense conversion pass is ever needed.
+//
+//   push     (edgeMapSparse, edge_map_blocked.h:18-92): groups of lanes per
+//            frontier vertex, coalesced neighbour loads, atomicMin on lp so the
+//            smallest-id parent of this level wins; hubs go to one CTA each.
+//   blocked  (edgeMapBlocked, edge_map_blocked.h:130-246): edge-balanced tiles
+//            over the exclusive scan of frontier degrees (merge-path split).
+//   pull     (edgeMapDense, edge_map_data.h:47-175): one thread per unvisited
+//            vertex, warp per 32-vertex bitmap word, early exit at the first
+//            frontier neighbour (= smallest id, adjacency is sorted), frontier
+//            bitmap prefix staged in shared memory; long scans deferred to a
+//            warp-cooperative pass.
+#pragma once
+
+#include "internal.h"
+
+namespace byo {
+
+enum Mode { MODE_PUSH = 0, MODE_PULL = 1, MODE_BLOCKED = 2 };
+
+struct RoundStats {
+  unsigned long long count;   // |next frontier|
+  unsigned long long outdeg;  // sum of degrees of the next frontier
+  unsigned long long ndefer;  // pull: deferred long scans; push: hubs
+  unsigned long long edges;   // edges examined (diagnostic)
+  unsigned long long hist[8]; // degree sketch of the next frontier (log4 bins)
+};
+
+struct Frontier {
+  uint32_t *list = nullptr;  // uint32[n]
+  uint32_t *bits = nullptr;  // uint32[W]
+  uint64_t size = 0;
+  uint64_t outdeg = 0;
+  bool dense = false;        // produced by a dense round
+  bool has_list = false, has_bits = false;
+  unsigned long long hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+struct TravState {
+  uint64_t *lp = nullptr;        // level<<32 | parent
+  uint32_t *visited = nullptr;   // uint32[W]
+  uint32_t round = 0;            // level being discovered next
+  uint64_t reached = 0;          // vertices with a level so far
+};
+
+struct EngineTuning {
+  int push_group = 8;        // lanes per frontier vertex in push
+  uint32_t hub_min = 4096;   // degree at which push hands a vertex to a CTA
+  int pull_cap = 32;         // neighbours a pull thread scans before deferring
+  int pull_stage_words = 32768;  // frontier bitmap words staged in shared memory
+  int blocked_tile = 2048;   // edges per blocked tile
+};
+
+// Decision of the GBBS rule for the next round (edge_map_data.h:254-307).
+int m20_mode(const byo_graph *g, const Frontier &f, int64_t threshold, int sparse_mode);
+
+// Runs one edgeMap round over BFS_F semantics: reads `in`, writes `out`
+// (out.bits must be all zero; out.list capacity n).  Updates st.
+int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int mode,
+                   const EngineTuning &tune);
+// Zeroes a frontier bitmap using its list when that is cheaper.
+int clear_frontier_bits(byo_graph *g, Frontier &f);
+int ensure_bits(byo_graph *g, Frontier &f);
+int trav_init(byo_graph *g, TravState &st, uint32_t src);
+int trav_extract(byo_graph *g, const TravState &st, uint32_t *d_parent, uint32_t *d_level);
+EngineTuning default_tuning(const byo_graph *g);
+
+}  // namespace byo

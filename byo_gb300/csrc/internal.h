@@ -1,0 +1,191 @@
+// internal.h -- shared host-side declarations of the byo_gpu library.
+//
+// Layout in HBM of a graph (both containers):
+//   d_off   uint64[n+1]  slot range [d_off[v], d_off[v+1]) of vertex v
+//   d_slots uint32[nslots] neighbour ids; the PMA leaves gaps marked kSentinel
+//                        inside that range, a CSR has none
+//   d_deg   uint32[n]    degree (non-gap entries) of every vertex
+// so one family of traversal kernels serves the static CSR and the packed
+// memory array alike.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/byo_gpu.h"
+
+namespace byo {
+
+constexpr uint32_t kSentinel = 0xFFFFFFFFu;
+constexpr uint64_t kNone64 = ~0ull;
+
+// A device buffer that only grows; freed with its owner.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Pma;  // pma.cu
+struct Mlp;  // mlp.cu
+
+}  // namespace byo
+
+struct byo_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  uint64_t launches = 0;
+  void *pinned = nullptr;  // small pinned host staging area
+  size_t pinned_bytes = 0;
+  cudaEvent_t ev[64];      // per-round timing events
+  bool time_rounds = false;
+  std::vector<byo_round_log> rounds;
+  byo::DevBuf scratch[8];  // context-wide temporaries (sort, scan)
+  byo::Mlp *policy = nullptr;
+};
+
+struct byo_graph {
+  byo_ctx *ctx = nullptr;
+  int container = BYO_CONTAINER_CSR;
+  uint64_t n = 0, m = 0;
+  uint64_t *d_off = nullptr;
+  uint32_t *d_slots = nullptr;
+  uint64_t nslots = 0;
+  uint32_t *d_deg = nullptr;
+  byo::Pma *pma = nullptr;
+  byo::DevBuf ws[24];  // per-graph workspaces, indexed by the Ws enum
+};
+
+namespace byo {
+
+enum Ws {
+  WS_LP = 0,        // uint64[n]   BFS level<<32 | parent
+  WS_VISITED,       // uint32[W]
+  WS_FRONT_LIST_A,  // uint32[n]
+  WS_FRONT_LIST_B,
+  WS_FRONT_BITS_A,  // uint32[W]
+  WS_FRONT_BITS_B,
+  WS_DEFER,         // uint32[n]   pull long-list / hub list
+  WS_SCAN,          // uint64[n+1] frontier degree prefix (blocked push)
+  WS_STATS,         // small device stats block
+  WS_LABEL,         // uint32[n]   CC
+  WS_PR_A,          // PageRank state
+  WS_PR_B,
+  WS_PR_C,
+  WS_PR_D,
+  WS_TC_RANK,
+  WS_TC_OFF,
+  WS_TC_NBR,
+  WS_TC_CNT,
+  WS_BUCKETS,
+  WS_MISC,
+  WS_COUNT
+};
+
+// ---------------------------------------------------------------- errors
+int set_error(byo_ctx *ctx, int code, const char *what, cudaError_t e = cudaSuccess);
+#define BYO_CU(ctx, call)                                             \
+  do {                                                                \
+    cudaError_t e_ = (call);                                          \
+    if (e_ != cudaSuccess) return byo::set_error(ctx, BYO_EDEVICE, #call, e_); \
+  } while (0)
+#define BYO_TRY(call)            \
+  do {                           \
+    int rc_ = (call);            \
+    if (rc_ != BYO_OK) return rc_; \
+  } while (0)
+int check_launch(byo_ctx *ctx, const char *what);
+
+// Launch on the context's stream and count it.
+template <typename Kern, typename... Args>
+inline void launch(byo_ctx *ctx, Kern kernel, dim3 grid, dim3 block, size_t smem, Args... args) {
+  kernel<<<grid, block, smem, ctx->stream>>>(args...);
+  ctx->launches++;
+}
+
+// ---------------------------------------------------------------- memory
+int ensure(byo_ctx *ctx, DevBuf &b, size_t bytes);
+template <typename T>
+int ws(byo_graph *g, int slot, size_t count, T **out) {
+  BYO_TRY(ensure(g->ctx, g->ws[slot], count * sizeof(T)));
+  *out = static_cast<T *>(g->ws[slot].p);
+  return BYO_OK;
+}
+template <typename T>
+int scratch(byo_ctx *ctx, int slot, size_t count, T **out) {
+  BYO_TRY(ensure(ctx, ctx->scratch[slot], count * sizeof(T)));
+  *out = static_cast<T *>(ctx->scratch[slot].p);
+  return BYO_OK;
+}
+void free_buf(DevBuf &b);
+int pinned(byo_ctx *ctx, size_t bytes, void **out);
+int grid_for(byo_ctx *ctx, uint64_t work, int block, int per_sm = 8);
+
+// ---------------------------------------------------------------- primitives (primitives.cu)
+// Exclusive scan of uint32 or uint64 items into uint64 out[count+1]
+// (out[count] = total).  Uses scratch slots 6,7.
+int scan_u32_to_u64(byo_ctx *ctx, const uint32_t *in, uint64_t count, uint64_t *out);
+int scan_u64(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t *out);
+// Exclusive scan of deg[list[i]] (frontier degree prefix) into out[count+1].
+int scan_gather_deg(byo_ctx *ctx, const uint32_t *deg, const uint32_t *list, uint64_t count,
+                    uint64_t *out);
+// Exclusive scan of off[list[i]+1] - off[list[i]] (slot-range lengths).
+int scan_gather_range(byo_ctx *ctx, const uint64_t *off, const uint32_t *list, uint64_t count,
+                      uint64_t *out);
+// LSD radix sort of uint64 keys restricted to the bytes set in sig_mask;
+// returns the buffer that holds the result (keys or tmp).  Scratch slots 4,5.
+int sort_u64(byo_ctx *ctx, uint64_t *keys, uint64_t *tmp, uint64_t count, uint64_t sig_mask,
+             uint64_t **sorted);
+// Removes adjacent duplicates of a sorted array (and src==dst keys if
+// drop_loops) into out; *out_count on the host.  Scratch slots 3.
+int unique_u64(byo_ctx *ctx, const uint64_t *in, uint64_t count, int drop_loops, uint64_t *out,
+               uint64_t *out_count);
+// offsets[v] = first index of keys with src >= v (keys sorted), v in [0,n].
+int offsets_from_keys(byo_ctx *ctx, const uint64_t *keys, uint64_t count, uint64_t n,
+                      uint64_t *offsets);
+int dst_from_keys(byo_ctx *ctx, const uint64_t *keys, uint64_t count, uint32_t *dst);
+int degrees_from_offsets(byo_ctx *ctx, const uint64_t *off, uint64_t n, uint32_t *deg);
+int reduce_max_u64(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t *out_host);
+uint64_t sig_mask_for(uint64_t n);
+int memset_async(byo_ctx *ctx, void *p, int v, size_t bytes);
+
+// ---------------------------------------------------------------- graph construction (graph.cu)
+int graph_from_sorted_keys(byo_ctx *ctx, int container, uint64_t n, const uint64_t *d_keys,
+                           uint64_t m, byo_graph **out);
+int graph_from_host_csr(byo_ctx *ctx, int container, uint64_t n, uint64_t m, const uint64_t *h_off,
+                        const uint32_t *h_nbrs, byo_graph **out);
+int graph_generate(byo_ctx *ctx, int container, const byo_gen_spec *sp, byo_graph **out);
+int graph_alloc_view(byo_graph *g);
+int gen_rmat_pairs(byo_ctx *ctx, uint64_t seed, uint32_t lg_n, double a, double b, double c,
+                   uint64_t first, uint64_t count, uint32_t *src, uint32_t *dst);
+int gen_uniform_pairs(byo_ctx *ctx, uint64_t seed, uint64_t n, uint64_t first, uint64_t count,
+                      uint32_t *src, uint32_t *dst);
+int gen_uniform_keys(byo_ctx *ctx, uint64_t seed, uint64_t n, uint64_t count, uint64_t *keys);
+
+// ---------------------------------------------------------------- traversal (engine.cu)
+int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, int policy,
+            uint32_t *rounds);
+
+// ---------------------------------------------------------------- algorithms (algos.cu)
+int cc_run(byo_graph *g, uint32_t *d_label);
+int bfs_cc_run(byo_graph *g, uint32_t *d_label);
+int pagerank_run(byo_graph *g, double eps, uint32_t max_iters, int precision, double *d_p,
+                 uint32_t *iters, double *l1);
+int tc_run(byo_graph *g, uint64_t *count);
+
+// ---------------------------------------------------------------- PMA (pma.cu)
+int pma_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);
+int pma_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert,
+               uint64_t *changed);
+int pma_export_keys(byo_graph *g, uint64_t *d_keys_out);
+void pma_destroy(Pma *p);
+
+// ---------------------------------------------------------------- policy (mlp.cu)
+int policy_choose(byo_ctx *ctx, const float *features, int nfeat, int *mode);
+
+}  // namespace byo

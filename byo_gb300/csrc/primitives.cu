@@ -1,0 +1,343 @@
+// primitives.cu -- device replacements for the parlaylib primitives on the
+// path (gbbs/bridge.h:208-313): scan, radix sort, unique, CSR offsets.
+//
+// Radix sort: LSD, 8-bit digits, only over the key bytes that can differ
+// (sig_mask), three launches per pass:
+//   histogram  per SORT_TILE-key tile, 256 bins in shared memory;
+//   scan       digit-major tile histograms -> global output offsets;
+//   scatter    stable ranking inside the tile with __match_any_sync, one
+//              256-key sub-round at a time, then one store per key.
+// Algorithmic bytes per pass: 8 (histogram read) + 8 + 8 (scatter read/write)
+// per key.
+#include "device.cuh"
+#include "internal.h"
+#include "scan.cuh"
+
+namespace byo {
+
+// ---------------------------------------------------------------- host utilities
+
+int set_error(byo_ctx *ctx, int code, const char *what, cudaError_t e) {
+  if (ctx) {
+    ctx->err = what ? what : "";
+    if (e != cudaSuccess) {
+      ctx->err += ": ";
+      ctx->err += cudaGetErrorString(e);
+    }
+  }
+  return code;
+}
+
+int check_launch(byo_ctx *ctx, const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(ctx, BYO_EDEVICE, what, e);
+  return BYO_OK;
+}
+
+void free_buf(DevBuf &b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+int ensure(byo_ctx *ctx, DevBuf &b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) return BYO_OK;
+  // The old contents are not preserved; buffers grow only between uses.
+  if (b.p) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return set_error(ctx, BYO_EDEVICE, "sync before realloc", e);
+    cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  size_t want = bytes + bytes / 8;  // headroom against repeated small growth
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    return set_error(ctx, BYO_ENOMEM, "cudaMalloc", e);
+  }
+  b.bytes = want;
+  return BYO_OK;
+}
+
+int pinned(byo_ctx *ctx, size_t bytes, void **out) {
+  if (ctx->pinned_bytes < bytes) {
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    ctx->pinned = nullptr;
+    ctx->pinned_bytes = 0;
+    cudaError_t e = cudaMallocHost(&ctx->pinned, bytes);
+    if (e != cudaSuccess) return set_error(ctx, BYO_ENOMEM, "cudaMallocHost", e);
+    ctx->pinned_bytes = bytes;
+  }
+  *out = ctx->pinned;
+  return BYO_OK;
+}
+
+int grid_for(byo_ctx *ctx, uint64_t work, int block, int per_sm) {
+  uint64_t want = (work + block - 1) / block;
+  uint64_t cap = (uint64_t)ctx->num_sms * per_sm;
+  if (want > cap) want = cap;
+  if (want < 1) want = 1;
+  return (int)want;
+}
+
+int memset_async(byo_ctx *ctx, void *p, int v, size_t bytes) {
+  if (bytes == 0) return BYO_OK;
+  BYO_CU(ctx, cudaMemsetAsync(p, v, bytes, ctx->stream));
+  return BYO_OK;
+}
+
+uint64_t sig_mask_for(uint64_t n) {
+  // keys are src<<32 | dst with src, dst < n
+  uint64_t lo = 0;
+  if (n > 1) {
+    uint64_t top = n - 1;
+    lo = 1;
+    while (lo <= top && lo != 0) lo <<= 1;
+    lo = lo - 1;
+    if (lo > 0xFFFFFFFFull) lo = 0xFFFFFFFFull;
+  }
+  return lo | (lo << 32);
+}
+
+// ---------------------------------------------------------------- scans
+
+int scan_u32_to_u64(byo_ctx *ctx, const uint32_t *in, uint64_t count, uint64_t *out) {
+  const uint64_t *tot = nullptr;
+  BYO_TRY(scan_apply(ctx, count, InU32{in}, OutPrefix{out}, &tot));
+  BYO_CU(ctx, cudaMemcpyAsync(out + count, tot, sizeof(uint64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+  return BYO_OK;
+}
+
+int scan_u64(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t *out) {
+  const uint64_t *tot = nullptr;
+  BYO_TRY(scan_apply(ctx, count, InU64{in}, OutPrefix{out}, &tot));
+  BYO_CU(ctx, cudaMemcpyAsync(out + count, tot, sizeof(uint64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+  return BYO_OK;
+}
+
+int scan_gather_deg(byo_ctx *ctx, const uint32_t *deg, const uint32_t *list, uint64_t count,
+                    uint64_t *out) {
+  const uint64_t *tot = nullptr;
+  BYO_TRY(scan_apply(ctx, count, InDegOfList{deg, list}, OutPrefix{out}, &tot));
+  BYO_CU(ctx, cudaMemcpyAsync(out + count, tot, sizeof(uint64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+  return BYO_OK;
+}
+
+int scan_gather_range(byo_ctx *ctx, const uint64_t *off, const uint32_t *list, uint64_t count,
+                      uint64_t *out) {
+  const uint64_t *tot = nullptr;
+  BYO_TRY(scan_apply(ctx, count, InRangeOfList{off, list}, OutPrefix{out}, &tot));
+  BYO_CU(ctx, cudaMemcpyAsync(out + count, tot, sizeof(uint64_t), cudaMemcpyDeviceToDevice, ctx->stream));
+  return BYO_OK;
+}
+
+// ---------------------------------------------------------------- radix sort
+
+constexpr int SORT_BLOCK = 256;
+constexpr int SORT_SUB = 16;  // sub-rounds of SORT_BLOCK keys per tile
+constexpr int SORT_TILE = SORT_BLOCK * SORT_SUB;
+constexpr int SORT_WARPS = SORT_BLOCK / 32;
+
+__global__ void __launch_bounds__(SORT_BLOCK) k_radix_hist(const uint64_t *__restrict__ keys,
+                                                           uint64_t count, int shift,
+                                                           uint32_t *__restrict__ hist,
+                                                           uint32_t ntiles) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t base = (uint64_t)blockIdx.x * SORT_TILE;
+#pragma unroll 4
+  for (int k = 0; k < SORT_SUB; k++) {
+    uint64_t i = base + (uint64_t)k * SORT_BLOCK + threadIdx.x;
+    if (i < count) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[(uint64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(SORT_BLOCK) k_radix_scatter(const uint64_t *__restrict__ in,
+                                                              uint64_t *__restrict__ out,
+                                                              uint64_t count, int shift,
+                                                              const uint64_t *__restrict__ offs,
+                                                              uint32_t ntiles) {
+  __shared__ uint64_t run[256];
+  __shared__ uint64_t wh[SORT_WARPS][256];
+  const unsigned t = threadIdx.x, w = t >> 5;
+  run[t] = offs[(uint64_t)t * ntiles + blockIdx.x];
+#pragma unroll
+  for (int q = 0; q < SORT_WARPS; q++) wh[q][t] = 0;
+  __syncthreads();
+  const uint64_t base = (uint64_t)blockIdx.x * SORT_TILE;
+  for (int k = 0; k < SORT_SUB; k++) {
+    uint64_t i = base + (uint64_t)k * SORT_BLOCK + t;
+    bool valid = i < count;
+    uint64_t key = valid ? in[i] : 0;
+    unsigned d = valid ? (unsigned)((key >> shift) & 255u) : 256u;
+    unsigned peers = __match_any_sync(kFull, d);
+    unsigned rank = __popc(peers & lanemask_lt());
+    if (valid && rank == 0) wh[w][d] = __popc(peers);
+    __syncthreads();
+    {
+      uint64_t r = run[t];
+#pragma unroll
+      for (int q = 0; q < SORT_WARPS; q++) {
+        uint64_t c = wh[q][t];
+        wh[q][t] = r;
+        r += c;
+      }
+      run[t] = r;
+    }
+    __syncthreads();
+    if (valid) out[wh[w][d] + rank] = key;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < SORT_WARPS; q++) wh[q][t] = 0;
+    __syncthreads();
+  }
+}
+
+int sort_u64(byo_ctx *ctx, uint64_t *keys, uint64_t *tmp, uint64_t count, uint64_t sig_mask,
+             uint64_t **sorted) {
+  uint64_t *a = keys, *b = tmp;
+  if (count > 1) {
+    const uint64_t ntiles = (count + SORT_TILE - 1) / SORT_TILE;
+    uint32_t *hist = nullptr;
+    uint64_t *offs = nullptr;
+    BYO_TRY(scratch(ctx, 4, 256 * ntiles, &hist));
+    BYO_TRY(scratch(ctx, 5, 256 * ntiles + 1, &offs));
+    for (int shift = 0; shift < 64; shift += 8) {
+      if (((sig_mask >> shift) & 0xFF) == 0) continue;
+      launch(ctx, k_radix_hist, dim3((unsigned)ntiles), dim3(SORT_BLOCK), 0, (const uint64_t *)a,
+             count, shift, hist, (uint32_t)ntiles);
+      BYO_TRY(scan_u32_to_u64(ctx, hist, 256 * ntiles, offs));
+      launch(ctx, k_radix_scatter, dim3((unsigned)ntiles), dim3(SORT_BLOCK), 0, (const uint64_t *)a,
+             b, count, shift, (const uint64_t *)offs, (uint32_t)ntiles);
+      uint64_t *s = a;
+      a = b;
+      b = s;
+    }
+  }
+  *sorted = a;
+  return check_launch(ctx, "sort_u64");
+}
+
+// ---------------------------------------------------------------- unique / compaction
+
+struct InKeep {
+  const uint64_t *k;
+  int drop_loops;
+  __device__ uint64_t operator()(uint64_t i) const {
+    uint64_t x = k[i];
+    bool keep = (i == 0) || (x != k[i - 1]);
+    if (drop_loops && (uint32_t)(x >> 32) == (uint32_t)x) keep = false;
+    return keep ? 1 : 0;
+  }
+};
+struct OutCompact {
+  const uint64_t *k;
+  uint64_t *out;
+  __device__ void operator()(uint64_t i, uint64_t pre, uint64_t v) const {
+    if (v) out[pre] = k[i];
+  }
+};
+
+int unique_u64(byo_ctx *ctx, const uint64_t *in, uint64_t count, int drop_loops, uint64_t *out,
+               uint64_t *out_count) {
+  const uint64_t *tot = nullptr;
+  BYO_TRY(scan_apply(ctx, count, InKeep{in, drop_loops}, OutCompact{in, out}, &tot));
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, tot, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  *out_count = h[0];
+  return BYO_OK;
+}
+
+// ---------------------------------------------------------------- CSR helpers
+
+__global__ void k_offsets_from_keys(const uint64_t *__restrict__ keys, uint64_t count, uint64_t n,
+                                    uint64_t *__restrict__ off) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t s = keys[i] >> 32;
+    uint64_t sp1 = (i == 0) ? 0 : (keys[i - 1] >> 32) + 1;
+    for (uint64_t v = sp1; v <= s && v <= n; v++) off[v] = i;
+    if (i == count - 1)
+      for (uint64_t v = s + 1; v <= n; v++) off[v] = count;
+  }
+}
+
+__global__ void k_fill_u64(uint64_t *p, uint64_t count, uint64_t val) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    p[i] = val;
+}
+
+int offsets_from_keys(byo_ctx *ctx, const uint64_t *keys, uint64_t count, uint64_t n,
+                      uint64_t *offsets) {
+  if (count == 0) {
+    launch(ctx, k_fill_u64, dim3(grid_for(ctx, n + 1, 256)), dim3(256), 0, offsets, n + 1, (uint64_t)0);
+  } else {
+    launch(ctx, k_offsets_from_keys, dim3(grid_for(ctx, count, 256)), dim3(256), 0, keys, count, n,
+           offsets);
+  }
+  return check_launch(ctx, "offsets_from_keys");
+}
+
+__global__ void k_dst_from_keys(const uint64_t *__restrict__ keys, uint64_t count,
+                                uint32_t *__restrict__ dst) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    dst[i] = (uint32_t)keys[i];
+}
+
+int dst_from_keys(byo_ctx *ctx, const uint64_t *keys, uint64_t count, uint32_t *dst) {
+  if (count == 0) return BYO_OK;
+  launch(ctx, k_dst_from_keys, dim3(grid_for(ctx, count, 256)), dim3(256), 0, keys, count, dst);
+  return check_launch(ctx, "dst_from_keys");
+}
+
+__global__ void k_degrees_from_offsets(const uint64_t *__restrict__ off, uint64_t n,
+                                       uint32_t *__restrict__ deg) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    deg[v] = (uint32_t)(off[v + 1] - off[v]);
+}
+
+int degrees_from_offsets(byo_ctx *ctx, const uint64_t *off, uint64_t n, uint32_t *deg) {
+  if (n == 0) return BYO_OK;
+  launch(ctx, k_degrees_from_offsets, dim3(grid_for(ctx, n, 256)), dim3(256), 0, off, n, deg);
+  return check_launch(ctx, "degrees_from_offsets");
+}
+
+__global__ void k_reduce_max_u64(const uint64_t *__restrict__ in, uint64_t count,
+                                 unsigned long long *out) {
+  uint64_t m = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    m = in[i] > m ? in[i] : m;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    uint64_t t = __shfl_xor_sync(kFull, m, o);
+    m = t > m ? t : m;
+  }
+  if (lane_id() == 0) atomicMax(out, (unsigned long long)m);
+}
+
+int reduce_max_u64(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t *out_host) {
+  unsigned long long *d = nullptr;
+  BYO_TRY(scratch(ctx, 3, 1, &d));
+  BYO_CU(ctx, cudaMemsetAsync(d, 0, sizeof(uint64_t), ctx->stream));
+  if (count) launch(ctx, k_reduce_max_u64, dim3(grid_for(ctx, count, 256)), dim3(256), 0, in, count, d);
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, d, sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  *out_host = h[0];
+  return check_launch(ctx, "reduce_max");
+}
+
+}  // namespace byo

@@ -1,0 +1,295 @@
+"""Host-side mirror of the reference's container / edgeMap interface over the
+C ABI, so code written against BYO's names reads the same.
+
+Reference names kept (paths in the wheatman/BYO tree):
+  Graph.N / M / num_vertices / num_edges / degree / out_degree /
+  map_neighbors / map_neighbors_early_exit / insert_batch / remove_batch /
+  write_adj                 gbbs/graph.h:2154-3150, run_csr.cc:28-175,
+                            run_single_pma.cc:39-141
+  vertexSubset, edgeMap     gbbs/vertex_subset.h:202-371,
+                            gbbs/edge_map_data.h:254-315
+  BFS_F, BFS                benchmarks/BFS/NonDeterministicBFS/BFS.h:30-64
+  SimpleUnionAsync          benchmarks/Connectivity/SimpleUnionAsync/Connectivity.h:122-136
+  bfs_cc                    benchmarks/Connectivity/BFSCC/Connectivity.h:79-88
+  PageRank                  benchmarks/PageRank/PageRank.h:125-193
+  Triangle_degree_ordering  benchmarks/TriangleCounting/ShunTangwongsan15/Triangle.h:167-204
+Errors surface as ByoError carrying the library's status code.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import ByoError, check, lib  # noqa: F401
+
+UINT_E_MAX = _abi.NONE
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
+
+
+class Context:
+    """One device, one stream (byo_gpu_init)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        rc = lib().byo_gpu_init(device, ctypes.byref(h))
+        if rc != _abi.BYO_OK:
+            raise ByoError(rc, "byo_gpu_init(%d) failed" % device)
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().byo_gpu_shutdown(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    @property
+    def stream(self):
+        return lib().byo_ctx_stream(self.h)
+
+    @property
+    def launches(self):
+        return int(lib().byo_ctx_launches(self.h))
+
+    def synchronize(self):
+        check(lib().byo_ctx_synchronize(self.h), self.h)
+
+    def set_round_timing(self, on):
+        check(lib().byo_ctx_set_round_timing(self.h, int(bool(on))), self.h)
+
+    def last_rounds(self):
+        n = ctypes.c_uint64(0)
+        check(lib().byo_last_rounds(self.h, None, 0, ctypes.byref(n)), self.h)
+        arr = (_abi.RoundLog * max(n.value, 1))()
+        check(lib().byo_last_rounds(self.h, arr, n.value, ctypes.byref(n)), self.h)
+        return [dict(round=r.round, mode=r.mode, frontier=r.frontier, frontier_deg=r.frontier_deg,
+                     unvisited=r.unvisited, ms=r.ms) for r in arr[:n.value]]
+
+
+class Graph:
+    """gbbs::Graph<Rep, symmetric=true, full_api> over a device container."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.h = handle
+
+    # ------------------------------------------------------------ construction
+    @classmethod
+    def from_csr(cls, ctx, offsets, nbrs, container="csr"):
+        off = np.ascontiguousarray(offsets, np.uint64)
+        nb = np.ascontiguousarray(nbrs, np.uint32)
+        n = len(off) - 1
+        h = ctypes.c_void_p()
+        fn = lib().byo_graph_create_pma if container == "pma" else lib().byo_graph_create_csr
+        check(fn(ctx.h, n, len(nb), _ptr(off), _ptr(nb), ctypes.byref(h)), ctx.h)
+        return cls(ctx, h)
+
+    @classmethod
+    def generate(cls, ctx, kind, seed=1, lg_n=0, n=0, draws=0, a=0.57, b=0.19, c=0.19,
+                 exponent=2.1, container="csr"):
+        kinds = {"rmat": _abi.GEN_RMAT, "er": _abi.GEN_ER, "grid": _abi.GEN_GRID,
+                 "chung_lu": _abi.GEN_CHUNG_LU}
+        spec = _abi.GenSpec(kinds[kind], seed, lg_n, n, draws, a, b, c, exponent)
+        h = ctypes.c_void_p()
+        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        check(lib().byo_graph_generate(ctx.h, cont, ctypes.byref(spec), ctypes.byref(h)), ctx.h)
+        return cls(ctx, h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().byo_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    # ------------------------------------------------------------ container interface
+    def N(self):
+        return int(lib().byo_graph_num_vertices(self.h))
+
+    num_vertices = N
+    n = property(N)
+
+    def M(self):
+        return int(lib().byo_graph_num_edges(self.h))
+
+    num_edges = M
+
+    @property
+    def container(self):
+        return "pma" if lib().byo_graph_container(self.h) == _abi.CONTAINER_PMA else "csr"
+
+    def degrees(self):
+        out = np.empty(self.N(), np.uint32)
+        check(lib().byo_graph_degrees(self.h, _ptr(out)), self.ctx.h)
+        return out
+
+    def degree(self, i):
+        d = ctypes.c_uint64(0)
+        check(lib().byo_graph_neighbors(self.h, i, None, 0, ctypes.byref(d)), self.ctx.h)
+        return int(d.value)
+
+    out_degree = degree
+
+    def neighbors(self, i):
+        d = self.degree(i)
+        out = np.empty(max(d, 1), np.uint32)
+        dd = ctypes.c_uint64(0)
+        check(lib().byo_graph_neighbors(self.h, i, _ptr(out), d, ctypes.byref(dd)), self.ctx.h)
+        return out[:d]
+
+    def map_neighbors(self, i, f):
+        for u in self.neighbors(i):
+            f(i, int(u), None)
+
+    def map_neighbors_early_exit(self, i, f):
+        for u in self.neighbors(i):
+            if f(i, int(u), None):
+                break
+
+    def export_csr(self):
+        off = np.empty(self.N() + 1, np.uint64)
+        nb = np.empty(max(self.M(), 1), np.uint32)
+        check(lib().byo_graph_export_csr(self.h, _ptr(off), _ptr(nb)), self.ctx.h)
+        return off, nb[:self.M()]
+
+    def write_adj(self, path):
+        """AdjacencyGraph text of the current contents (graph.h:3018-3044)."""
+        off, nb = self.export_csr()
+        with open(path, "w") as f:
+            f.write("AdjacencyGraph\n%d\n%d\n" % (self.N(), self.M()))
+            f.write("".join("%d\n" % x for x in off[:-1]))
+            f.write("".join("%d\n" % x for x in nb))
+
+    @staticmethod
+    def _keys(batch):
+        a = np.asarray(batch)
+        if a.ndim == 2:  # (src, dst) pairs as std::tuple<uintE,uintE>
+            a = (a[:, 0].astype(np.uint64) << np.uint64(32)) | a[:, 1].astype(np.uint64)
+        return np.ascontiguousarray(a, np.uint64)
+
+    def insert_batch(self, batch, sorted=False):
+        k = self._keys(batch)
+        ch = ctypes.c_uint64(0)
+        check(lib().byo_graph_insert_batch(self.h, _ptr(k), len(k), int(sorted), ctypes.byref(ch)),
+              self.ctx.h)
+        return int(ch.value)
+
+    def remove_batch(self, batch, sorted=False):
+        k = self._keys(batch)
+        ch = ctypes.c_uint64(0)
+        check(lib().byo_graph_remove_batch(self.h, _ptr(k), len(k), int(sorted), ctypes.byref(ch)),
+              self.ctx.h)
+        return int(ch.value)
+
+    insert_sorted_batch = insert_batch
+    remove_sorted_batch = remove_batch
+
+
+# ------------------------------------------------------------ vertexSubset / edgeMap
+
+class vertexSubset:
+    """vertexSubset(n, v) / vertexSubset(n, list) (vertex_subset.h:240-262)."""
+
+    def __init__(self, G, vertices=None, _handle=None):
+        self.G = G
+        if _handle is not None:
+            self.h = _handle
+            return
+        h = ctypes.c_void_p()
+        if isinstance(vertices, (int, np.integer)):
+            check(lib().byo_vs_create_single(G.h, int(vertices), ctypes.byref(h)), G.ctx.h)
+        else:
+            ids = np.ascontiguousarray(vertices if vertices is not None else [], np.uint32)
+            check(lib().byo_vs_create_list(G.h, _ptr(ids), len(ids), ctypes.byref(h)), G.ctx.h)
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().byo_vs_destroy(self.h)
+            self.h = None
+
+    def size(self):
+        return int(lib().byo_vs_size(self.h))
+
+    def isEmpty(self):
+        return self.size() == 0
+
+    @property
+    def isDense(self):
+        return bool(lib().byo_vs_is_dense(self.h))
+
+    def to_list(self):
+        s = self.size()
+        out = np.empty(max(s, 1), np.uint32)
+        check(lib().byo_vs_to_list(self.h, _ptr(out), s), self.G.ctx.h)
+        return out[:s]
+
+
+class BFS_F:
+    """BFS_F (BFS.h:30-45) over a device Parents array."""
+
+    def __init__(self, G, src):
+        self.G = G
+        h = ctypes.c_void_p()
+        check(lib().byo_functor_bfs_create(G.h, src, ctypes.byref(h)), G.ctx.h)
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().byo_functor_destroy(self.h)
+            self.h = None
+
+    def parents(self):
+        out = np.empty(self.G.N(), np.uint32)
+        check(lib().byo_functor_bfs_parents(self.h, _ptr(out)), self.G.ctx.h)
+        return out
+
+
+def edgeMap(G, vs, F, threshold=-1, flags=0):
+    h = ctypes.c_void_p()
+    check(lib().byo_edge_map(G.h, vs.h, F.h, threshold, flags, ctypes.byref(h)), G.ctx.h)
+    return vertexSubset(G, _handle=h)
+
+
+# ------------------------------------------------------------ algorithms
+
+def BFS(G, src, policy=_abi.POLICY_M20, levels=False):
+    n = G.N()
+    par = np.empty(n, np.uint32)
+    lev = np.empty(n, np.uint32) if levels else None
+    r = ctypes.c_uint32(0)
+    check(lib().byo_bfs(G.h, src, _ptr(par), _ptr(lev), policy, ctypes.byref(r)), G.ctx.h)
+    return (par, lev) if levels else par
+
+
+def SimpleUnionAsync(G):
+    out = np.empty(G.N(), np.uint32)
+    check(lib().byo_cc(G.h, _ptr(out)), G.ctx.h)
+    return out
+
+
+def bfs_cc(G):
+    out = np.empty(G.N(), np.uint32)
+    check(lib().byo_bfs_cc(G.h, _ptr(out)), G.ctx.h)
+    return out
+
+
+def PageRank(G, eps=1e-6, max_iters=100, precision=_abi.PR_FP32_KAHAN, info=False):
+    p = np.empty(G.N(), np.float64)
+    it = ctypes.c_uint32(0)
+    l1 = ctypes.c_double(0)
+    check(lib().byo_pagerank(G.h, eps, max_iters, precision, _ptr(p), ctypes.byref(it),
+                             ctypes.byref(l1)), G.ctx.h)
+    return (p, it.value, l1.value) if info else p
+
+
+def Triangle_degree_ordering(G):
+    c = ctypes.c_uint64(0)
+    check(lib().byo_triangle_count(G.h, ctypes.byref(c)), G.ctx.h)
+    return int(c.value)

@@ -1,0 +1,235 @@
+/*
+ * byo_gpu.h -- C ABI of the GB300 (sm_103a) graph-container engine.
+ *
+ * This is the drop-in boundary for BYO's data-parallel hot path: the GBBS
+ * edgeMap / vertexSubset traversal engine, the algorithms that BYO's run_all
+ * drives through it, and the batched insert/delete of a packed-memory-array
+ * graph container.  Everything is plain pointers and sizes; no C++ or torch
+ * type crosses it.  Reference interfaces are cited as path:line of the
+ * wheatman/BYO tree.
+ *
+ * Conventions
+ *  - vertex ids uint32 (gbbs uintE), edge offsets uint64 (uintT),
+ *    BYO_NONE (0xFFFFFFFF) = "unreached / no parent" (UINT_E_MAX).
+ *  - update keys are uint64 (src << 32) | dst, the bit pattern of the
+ *    std::tuple<uintE,uintE> that PMA_graph bit_casts
+ *    (benchmarks/run_structures/run_single_pma.cc:63-70).
+ *  - functions return BYO_OK (0) or a negative BYO_E* code; the message of the
+ *    last failure is byo_last_error(ctx).  No function aborts the process.
+ *  - Arguments named h_* are host memory; d_* are device memory of the
+ *    context's device.  Host-memory variants copy through the context's
+ *    stream and return when the result is on the host.
+ *  - A context owns one CUDA stream; calls on one context are not thread safe
+ *    (the reference is likewise driven from one host thread, its parallelism
+ *    is internal).
+ */
+#ifndef BYO_GPU_H
+#define BYO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BYO_NONE 0xFFFFFFFFu
+
+enum byo_status {
+  BYO_OK = 0,
+  BYO_EINVAL = -1,    /* bad argument (null pointer, id >= n, bad size) */
+  BYO_ENOMEM = -2,    /* device allocation failed */
+  BYO_EDEVICE = -3,   /* CUDA error; see byo_last_error */
+  BYO_ETIMEDOUT = -4, /* a bounded device-side wait gave up */
+  BYO_ENOTSUP = -5    /* operation not supported by this container */
+};
+
+typedef struct byo_ctx byo_ctx;
+typedef struct byo_graph byo_graph;
+typedef struct byo_vertex_subset byo_vertex_subset;
+
+/* ------------------------------------------------------------------ context */
+
+/* Opens a context on CUDA device `device`; creates its stream. */
+int byo_gpu_init(int device, byo_ctx **out);
+void byo_gpu_shutdown(byo_ctx *ctx);
+const char *byo_last_error(const byo_ctx *ctx);
+/* The context's cudaStream_t, for callers that time or order work around it. */
+void *byo_ctx_stream(byo_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+uint64_t byo_ctx_launches(const byo_ctx *ctx);
+int byo_ctx_synchronize(byo_ctx *ctx);
+/* Library version string. */
+const char *byo_version(void);
+
+/* ------------------------------------------------------------------ containers
+ * Replaces the container adapters of benchmarks/run_structures: CSR
+ * (run_csr.cc:28-175, static) and PMA_graph (run_single_pma.cc:39-141, a
+ * packed memory array of (src,dst) keys).  Both constructors take the loader's
+ * CSR (graph_io.h:117-123 builds it; run_csr.cc:87-106 and
+ * run_single_pma.cc:75-89 consume it): offsets[n+1] and nbrs[m], sorted and
+ * duplicate-free per vertex.  The arrays are copied; the caller keeps them. */
+enum byo_container { BYO_CONTAINER_CSR = 0, BYO_CONTAINER_PMA = 1 };
+
+int byo_graph_create_csr(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h_offsets,
+                         const uint32_t *h_nbrs, byo_graph **out);
+int byo_graph_create_pma(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h_offsets,
+                         const uint32_t *h_nbrs, byo_graph **out);
+void byo_graph_destroy(byo_graph *g);
+int byo_graph_container(const byo_graph *g);
+/* G.N() / num_vertices() (graph.h:2627; run_csr.cc:31) */
+uint64_t byo_graph_num_vertices(const byo_graph *g);
+/* G.M() / num_edges(): directed entries currently stored (run_csr.cc:32) */
+uint64_t byo_graph_num_edges(const byo_graph *g);
+/* degree(i) for every vertex (run_csr.cc:34-36; Graph::finilize
+ * graph.h:2559-2588 for containers without a native degree). */
+int byo_graph_degrees(byo_graph *g, uint32_t *h_out);
+/* Sorted adjacency of every vertex, the content Graph::write_adj dumps
+ * (graph.h:3018-3044); the parity view of a container after updates. */
+int byo_graph_export_csr(byo_graph *g, uint64_t *h_offsets, uint32_t *h_nbrs);
+/* Neighbours of one vertex, sorted (map_neighbors, run_csr.cc:38-43). Writes
+ * at most cap ids and the degree to *deg. */
+int byo_graph_neighbors(byo_graph *g, uint32_t v, uint32_t *h_out, uint64_t cap, uint64_t *deg);
+
+/* Batched updates: Graph::insert_batch / remove_batch (graph.h:3071-3124) ->
+ * PMA_graph::insert_sorted_batch / remove_sorted_batch (run_single_pma.cc:63-70).
+ * keys may be unsorted and contain duplicates unless `sorted` is 1 (then they
+ * must be strictly increasing).  Inserting a present key and removing an
+ * absent key are no-ops.  Keys with src or dst >= n are rejected (BYO_EINVAL).
+ * *changed (may be NULL) receives the number of keys actually inserted or
+ * removed.  Only BYO_CONTAINER_PMA supports updates (CSR: BYO_ENOTSUP). */
+int byo_graph_insert_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
+                           uint64_t *changed);
+int byo_graph_remove_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
+                           uint64_t *changed);
+int byo_graph_insert_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted,
+                                  uint64_t *changed);
+int byo_graph_remove_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted,
+                                  uint64_t *changed);
+
+/* ------------------------------------------------------------------ generators
+ * Synthetic graphs built on the device (counter-based streams; a slice of any
+ * stream is reproducible on the host bit for bit).  Pairs are symmetrised,
+ * sorted, deduplicated and self loops dropped, as the workloads specify. */
+enum byo_gen_kind { BYO_GEN_RMAT = 0, BYO_GEN_ER = 1, BYO_GEN_GRID = 2, BYO_GEN_CHUNG_LU = 3 };
+typedef struct byo_gen_spec {
+  int kind;          /* byo_gen_kind */
+  uint64_t seed;
+  uint32_t lg_n;     /* RMAT: n = 2^lg_n */
+  uint64_t n;        /* ER / Chung-Lu: vertices; GRID: rows */
+  uint64_t draws;    /* RMAT / ER / Chung-Lu: pairs drawn; GRID: columns */
+  double a, b, c;    /* RMAT quadrant probabilities */
+  double exponent;   /* Chung-Lu power-law exponent */
+} byo_gen_spec;
+int byo_graph_generate(byo_ctx *ctx, int container, const byo_gen_spec *spec, byo_graph **out);
+/* Raw pair streams into device buffers (RMAT thresholds as in the oracle). */
+int byo_gen_rmat_pairs_device(byo_ctx *ctx, uint64_t seed, uint32_t lg_n, double a, double b,
+                              double c, uint64_t first, uint64_t count, uint32_t *d_src,
+                              uint32_t *d_dst);
+int byo_gen_uniform_pairs_device(byo_ctx *ctx, uint64_t seed, uint64_t n, uint64_t first,
+                                 uint64_t count, uint32_t *d_src, uint32_t *d_dst);
+/* Symmetrised update keys for a uniform batch: 2*count keys (u<<32|v, v<<32|u). */
+int byo_gen_uniform_keys_device(byo_ctx *ctx, uint64_t seed, uint64_t n, uint64_t count,
+                                uint64_t *d_keys);
+
+/* ------------------------------------------------------------------ traversal
+ * Direction policy for edgeMap rounds (the choice never changes a result). */
+enum byo_policy {
+  BYO_POLICY_M20 = 0,          /* GBBS rule, edge_map_data.h:254-307 (sparse = push) */
+  BYO_POLICY_LEARNED = 1,      /* MLP over frontier statistics, falls back to M20 */
+  BYO_POLICY_PUSH = 2,         /* force sparse push every round */
+  BYO_POLICY_PULL = 3,         /* force dense pull every round */
+  BYO_POLICY_BLOCKED = 4,      /* force edge-balanced blocked push every round */
+  BYO_POLICY_M20_BLOCKED = 5   /* GBBS rule with blocked push for sparse rounds */
+};
+
+/* BFS (benchmarks/BFS/NonDeterministicBFS/BFS.h:47-64).  parent[v]: the
+ * smallest-id neighbour of v one level closer to src (a valid outcome of the
+ * reference's nondeterministic CAS, and exactly what its dense pull produces on
+ * sorted adjacency); parent[src] = src; BYO_NONE if unreached.  level may be
+ * NULL.  *rounds (may be NULL) = edgeMap rounds run. */
+int byo_bfs(byo_graph *g, uint32_t src, uint32_t *h_parent, uint32_t *h_level, int policy,
+            uint32_t *rounds);
+int byo_bfs_device(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, int policy,
+                   uint32_t *rounds);
+
+/* Connectivity, SimpleUnionAsync semantics
+ * (benchmarks/Connectivity/SimpleUnionAsync/Connectivity.h:122-136): label[v]
+ * = smallest vertex id in v's component. */
+int byo_cc(byo_graph *g, uint32_t *h_label);
+int byo_cc_device(byo_graph *g, uint32_t *d_label);
+/* BFS-based connectivity (benchmarks/Connectivity/BFSCC/Connectivity.h:33-88);
+ * same labels as byo_cc. */
+int byo_bfs_cc(byo_graph *g, uint32_t *h_label);
+
+/* PageRank (benchmarks/PageRank/PageRank.h:125-193): damping 0.85, p0 = 1/n,
+ * stop when the L1 change < eps or after max_iters; no dangling
+ * redistribution.  Output p_out in FP64. */
+enum byo_precision {
+  BYO_PR_FP32_KAHAN = 0, /* FP32 state, compensated per-vertex sums, FP64 residual */
+  BYO_PR_FP64 = 1,       /* FP64 throughout */
+  BYO_PR_FP32 = 2        /* FP32, uncompensated (for the error comparison) */
+};
+int byo_pagerank(byo_graph *g, double eps, uint32_t max_iters, int precision, double *h_p,
+                 uint32_t *iters, double *l1);
+int byo_pagerank_device(byo_graph *g, double eps, uint32_t max_iters, int precision, double *d_p,
+                        uint32_t *iters, double *l1);
+
+/* Triangle counting, degree ordering
+ * (benchmarks/TriangleCounting/ShunTangwongsan15/Triangle.h:167-204). */
+int byo_triangle_count(byo_graph *g, uint64_t *count);
+
+/* ------------------------------------------------------------------ edgeMap API
+ * vertexSubset (gbbs/vertex_subset.h:202-371) and edgeMap
+ * (gbbs/edge_map_data.h:254-315) over device functors.  The functor set is
+ * closed (a device kernel cannot call a host lambda); each mirrors a GBBS
+ * functor struct {update, updateAtomic, cond}. */
+enum byo_functor_kind {
+  BYO_F_BFS = 0 /* BFS_F, BFS.h:30-45, over a parents array owned by the functor */
+};
+/* edgeMap flags, values as gbbs/flags.h:8-19 */
+enum byo_edge_map_flags {
+  BYO_FL_NO_OUTPUT = 1,
+  BYO_FL_SPARSE_BLOCKED = 4,
+  BYO_FL_DENSE_FORWARD = 8,
+  BYO_FL_DENSE_PARALLEL = 16,
+  BYO_FL_NO_DENSE = 64,
+  BYO_FL_DENSE_ONLY = 1024
+};
+typedef struct byo_functor byo_functor;
+/* BFS_F over a fresh Parents array (all BYO_NONE but Parents[src] = src). */
+int byo_functor_bfs_create(byo_graph *g, uint32_t src, byo_functor **out);
+int byo_functor_bfs_parents(byo_functor *f, uint32_t *h_parents);
+void byo_functor_destroy(byo_functor *f);
+
+/* vertexSubset(n, v) and vertexSubset(n, list) (vertex_subset.h:240-262). */
+int byo_vs_create_single(byo_graph *g, uint32_t v, byo_vertex_subset **out);
+int byo_vs_create_list(byo_graph *g, const uint32_t *h_ids, uint64_t count,
+                       byo_vertex_subset **out);
+void byo_vs_destroy(byo_vertex_subset *vs);
+uint64_t byo_vs_size(const byo_vertex_subset *vs);
+int byo_vs_is_dense(const byo_vertex_subset *vs);
+/* Members in increasing id order (toSparse + sort). */
+int byo_vs_to_list(byo_vertex_subset *vs, uint32_t *h_out, uint64_t cap);
+/* edgeMap(G, vs, F, threshold, flags): threshold -1 => M/20. */
+int byo_edge_map(byo_graph *g, byo_vertex_subset *vs, byo_functor *f, int64_t threshold,
+                 uint32_t flags, byo_vertex_subset **out);
+
+/* ------------------------------------------------------------------ statistics
+ * Per-round log of the last traversal (the learned policy's training data). */
+typedef struct byo_round_log {
+  uint32_t round;
+  uint32_t mode;          /* 0 push, 1 pull, 2 blocked */
+  uint64_t frontier;      /* |F| */
+  uint64_t frontier_deg;  /* sum of out-degrees of F */
+  uint64_t unvisited;     /* vertices not yet reached before the round */
+  float ms;               /* device time of the round */
+} byo_round_log;
+int byo_last_rounds(byo_ctx *ctx, byo_round_log *out, uint64_t cap, uint64_t *count);
+/* Times every round with CUDA events (adds one host wait per round). */
+int byo_ctx_set_round_timing(byo_ctx *ctx, int on);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,173 @@
+"""CUDA path (through the C ABI) against the oracle: bit-exact BFS levels and
+min-id parents, CC labels, triangle counts, generated graphs; PageRank within
+1e-6 L1 of the FP64 oracle."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+POLICIES = [0, 2, 3, 4, 5]  # m/20, push, pull, blocked, m/20+blocked
+PR_TOL = 1e-6               # L1 vs the FP64 oracle
+
+
+def _csr(g):
+    return np.array(g["offsets"], np.uint64), np.array(g["nbrs"], np.uint32)
+
+
+def _check_all(byo, O, G, off, nb, srcs, policies=POLICIES, pr_iters=(100,)):
+    n = len(off) - 1
+    for s in srcs:
+        opar, olev = O.bfs(off, nb, s)
+        for pol in policies:
+            par, lev = byo.BFS(G, s, policy=pol, levels=True)
+            assert np.array_equal(lev, olev), ("level", s, pol)
+            assert np.array_equal(par, opar), ("parent", s, pol)
+    olab = O.cc(off, nb)
+    assert np.array_equal(byo.SimpleUnionAsync(G), olab)
+    assert np.array_equal(byo.bfs_cc(G), olab)
+    assert byo.Triangle_degree_ordering(G) == O.triangle_count(off, nb)
+    for iters in pr_iters:
+        op, oit, _ = O.pagerank(off, nb, 1e-6, iters)
+        p, it, _ = byo.PageRank(G, 1e-6, iters, info=True)
+        assert abs(it - oit) <= 1
+        if it == oit:
+            assert float(np.abs(p - op).sum()) <= PR_TOL
+        p64, it64, _ = byo.PageRank(G, 1e-6, iters, precision=1, info=True)
+        assert it64 == oit
+        assert float(np.abs(p64 - op).sum()) <= 1e-12
+
+
+def test_golden_graphs(ctx, golden, oracle_mod):
+    import byo_gb300 as byo
+    for g in golden["graphs"]:
+        off, nb = _csr(g)
+        G = byo.Graph.from_csr(ctx, off, nb)
+        assert G.N() == g["n"] and G.M() == len(g["nbrs"])
+        for src, exp in g["bfs"].items():
+            for pol in POLICIES:
+                par, lev = byo.BFS(G, int(src), policy=pol, levels=True)
+                assert lev.tolist() == exp["level"], (g["name"], src, pol)
+                assert par.tolist() == exp["parent"], (g["name"], src, pol)
+            if "reference_bfs" in g:
+                par = byo.BFS(G, int(src))
+                for v, choices in enumerate(g["reference_bfs"][src]):
+                    assert int(par[v]) in choices
+        assert byo.SimpleUnionAsync(G).tolist() == g["cc"]
+        assert byo.bfs_cc(G).tolist() == g["cc"]
+        assert byo.Triangle_degree_ordering(G) == g["triangles"]
+        for pr in g["pagerank"].values():
+            p, it, _ = byo.PageRank(G, pr["eps"], pr["max_iters"], info=True)
+            assert it == pr["iters"]
+            assert float(np.abs(p - np.array(pr["p"])).sum()) <= PR_TOL
+        o2, n2 = G.export_csr()
+        assert np.array_equal(o2, off) and np.array_equal(n2, nb)
+        G.close()
+
+
+@pytest.mark.parametrize("lg,draws,seed", [(10, 1 << 13, 1), (14, 1 << 17, 2), (16, 1 << 20, 3)])
+def test_rmat_generated(ctx, oracle_mod, lg, draws, seed):
+    import byo_gb300 as byo
+    O = oracle_mod
+    G = byo.Graph.generate(ctx, "rmat", seed=seed, lg_n=lg, draws=draws)
+    s, d = O.rmat_edges(seed, lg, draws)
+    off, nb = O.build_csr(1 << lg, s, d)
+    go, gn = G.export_csr()
+    assert np.array_equal(go, off) and np.array_equal(gn, nb)
+    assert np.array_equal(G.degrees(), np.diff(off).astype(np.uint32))
+    hub = int(np.argmax(np.diff(off.astype(np.int64))))
+    _check_all(byo, O, G, off, nb, [10 % (1 << lg), hub], pr_iters=(20, 100))
+
+
+def test_er_grid_chung_lu(ctx, oracle_mod):
+    import byo_gb300 as byo
+    O = oracle_mod
+    cases = []
+    G = byo.Graph.generate(ctx, "er", seed=5, n=5000, draws=40000)
+    s, d = O.uniform_pairs(5, 5000, 40000)
+    cases.append((G, *O.build_csr(5000, s, d)))
+    G = byo.Graph.generate(ctx, "grid", n=37, draws=53)
+    s, d = O.grid_pairs(37, 53)
+    cases.append((G, *O.build_csr(37 * 53, s, d)))
+    G = byo.Graph.generate(ctx, "chung_lu", seed=7, n=20000, draws=80000, exponent=2.1)
+    s, d = O.chung_lu_pairs(7, 20000, 80000, exponent=2.1)
+    cases.append((G, *O.build_csr(20000, s, d)))
+    for G, off, nb in cases:
+        go, gn = G.export_csr()
+        assert np.array_equal(go, off) and np.array_equal(gn, nb)
+        _check_all(byo, O, G, off, nb, [0, len(off) // 2 - 1])
+        G.close()
+
+
+def test_device_pair_streams(ctx, oracle_mod):
+    import torch
+    from byo_gb300 import _abi
+    L = _abi.lib()
+    cnt, first = 4096, 777
+    s = torch.empty(cnt, dtype=torch.int32, device="cuda")
+    d = torch.empty(cnt, dtype=torch.int32, device="cuda")
+    _abi.check(L.byo_gen_rmat_pairs_device(ctx.h, 9, 18, 0.57, 0.19, 0.19, first, cnt, s.data_ptr(),
+                                           d.data_ptr()), ctx.h)
+    ctx.synchronize()
+    os_, od = oracle_mod.rmat_edges(9, 18, cnt, first=first)
+    assert np.array_equal(s.cpu().numpy().view(np.uint32), os_)
+    assert np.array_equal(d.cpu().numpy().view(np.uint32), od)
+    _abi.check(L.byo_gen_uniform_pairs_device(ctx.h, 4, 123457, first, cnt, s.data_ptr(), d.data_ptr()),
+               ctx.h)
+    ctx.synchronize()
+    us, ud = oracle_mod.uniform_pairs(4, 123457, cnt, first=first)
+    assert np.array_equal(s.cpu().numpy().view(np.uint32), us)
+    assert np.array_equal(d.cpu().numpy().view(np.uint32), ud)
+
+
+def test_edge_map_api_matches_bfs(ctx, oracle_mod):
+    """BFS written as the reference's loop over edgeMap (BFS.h:47-64)."""
+    import byo_gb300 as byo
+    G = byo.Graph.generate(ctx, "rmat", seed=11, lg_n=13, draws=1 << 16)
+    off, nb = G.export_csr()
+    for flags in (byo._abi.FL_DENSE_PARALLEL | byo._abi.FL_SPARSE_BLOCKED, byo._abi.FL_NO_DENSE,
+                  byo._abi.FL_DENSE_ONLY):
+        F = byo.BFS_F(G, 10)
+        frontier = byo.vertexSubset(G, 10)
+        sizes = []
+        while not frontier.isEmpty():
+            sizes.append(frontier.size())
+            frontier = byo.edgeMap(G, frontier, F, -1, flags)
+        opar, olev = oracle_mod.bfs(off, nb, 10)
+        assert np.array_equal(F.parents(), opar)
+        assert sizes == [int((olev == l).sum()) for l in range(len(sizes))]
+    vs = byo.vertexSubset(G, [5, 3, 9])
+    assert vs.to_list().tolist() == [3, 5, 9]
+
+
+def test_error_paths(ctx):
+    import byo_gb300 as byo
+    off = np.array([0, 1, 2], np.uint64)
+    with pytest.raises(byo.ByoError) as e:
+        byo.Graph.from_csr(ctx, off, np.array([1, 5], np.uint32))  # id >= n
+    assert e.value.code == byo._abi.BYO_EINVAL
+    with pytest.raises(byo.ByoError) as e:  # adjacency of vertex 0 not increasing
+        byo.Graph.from_csr(ctx, np.array([0, 2, 2], np.uint64), np.array([1, 1], np.uint32))
+    assert e.value.code == byo._abi.BYO_EINVAL
+    G = byo.Graph.from_csr(ctx, off, np.array([1, 0], np.uint32))
+    with pytest.raises(byo.ByoError) as e:
+        byo.BFS(G, 7)
+    assert e.value.code == byo._abi.BYO_EINVAL
+    with pytest.raises(byo.ByoError) as e:
+        G.insert_batch(np.array([1], np.uint64))
+    assert e.value.code == byo._abi.BYO_ENOTSUP
+    # the context stays usable after errors
+    assert byo.BFS(G, 0).tolist() == [0, 0]
+
+
+def test_empty_and_isolated(ctx, oracle_mod):
+    import byo_gb300 as byo
+    off = np.zeros(5, np.uint64)
+    G = byo.Graph.from_csr(ctx, off, np.zeros(0, np.uint32))
+    for pol in POLICIES:
+        assert byo.BFS(G, 2, policy=pol).tolist() == [byo.UINT_E_MAX] * 2 + [2] + [byo.UINT_E_MAX]
+    assert byo.SimpleUnionAsync(G).tolist() == [0, 1, 2, 3]
+    assert byo.Triangle_degree_ordering(G) == 0
+    p = byo.PageRank(G, 1e-6, 10)
+    assert np.allclose(p, 0.15 / 4)

@@ -1,0 +1,115 @@
+"""Oracle properties: generator slices, CSR build invariants, and the
+algorithms against networkx on seeded random graphs."""
+import networkx as nx
+import numpy as np
+import pytest
+
+NONE = 0xFFFFFFFF
+
+
+def _nx(off, nb):
+    g = nx.Graph()
+    n = len(off) - 1
+    g.add_nodes_from(range(n))
+    for v in range(n):
+        for j in range(int(off[v]), int(off[v + 1])):
+            g.add_edge(v, int(nb[j]))
+    return g
+
+
+def test_generator_slices(oracle_mod):
+    s, d = oracle_mod.rmat_edges(7, 14, 5000)
+    s2, d2 = oracle_mod.rmat_edges(7, 14, 1000, first=2000)
+    assert np.array_equal(s[2000:3000], s2) and np.array_equal(d[2000:3000], d2)
+    u, v = oracle_mod.uniform_pairs(3, 1000, 4000)
+    u2, v2 = oracle_mod.uniform_pairs(3, 1000, 100, first=3900)
+    assert np.array_equal(u[3900:], u2) and np.array_equal(v[3900:], v2)
+    assert u.max() < 1000 and v.max() < 1000
+    assert s.max() < (1 << 14)
+
+
+def test_rmat_skew(oracle_mod):
+    # quadrant a=0.57 biases both endpoints toward low ids
+    s, d = oracle_mod.rmat_edges(1, 16, 200000)
+    top = (s < (1 << 15)).mean()
+    assert 0.74 < top < 0.78  # P(first src bit 0) = a + b = 0.76
+
+
+def test_build_csr_invariants(oracle_mod):
+    s, d = oracle_mod.rmat_edges(2, 10, 6000)
+    off, nb = oracle_mod.build_csr(1024, s, d)
+    n = 1024
+    keys = set()
+    for v in range(n):
+        run = nb[off[v]:off[v + 1]]
+        assert np.all(np.diff(run.astype(np.int64)) > 0)
+        assert v not in run
+        keys |= {(v, int(x)) for x in run}
+    assert all((b, a) in keys for a, b in keys)
+
+
+@pytest.mark.parametrize("seed,lg,draws", [(1, 9, 3000), (5, 11, 20000), (9, 8, 100)])
+def test_against_networkx(oracle_mod, seed, lg, draws):
+    s, d = oracle_mod.rmat_edges(seed, lg, draws)
+    n = 1 << lg
+    off, nb = oracle_mod.build_csr(n, s, d)
+    g = _nx(off, nb)
+    src = int(np.argmax(np.diff(off.astype(np.int64))))
+    par, lev = oracle_mod.bfs(off, nb, src)
+    dist = nx.single_source_shortest_path_length(g, src)
+    for v in range(n):
+        if v in dist:
+            assert lev[v] == dist[v]
+            if v != src:
+                assert par[v] == min(u for u in g[v] if dist.get(u) == dist[v] - 1)
+        else:
+            assert lev[v] == NONE and par[v] == NONE
+    lab = oracle_mod.cc(off, nb)
+    for comp in nx.connected_components(g):
+        m = min(comp)
+        assert all(lab[v] == m for v in comp)
+    assert oracle_mod.triangle_count(off, nb) == sum(nx.triangles(g).values()) // 3
+
+
+def test_grid_and_chung_lu(oracle_mod):
+    s, d = oracle_mod.grid_pairs(5, 7)
+    off, nb = oracle_mod.build_csr(35, s, d)
+    assert len(nb) == 2 * (2 * 35 - 5 - 7)
+    par, lev = oracle_mod.bfs(off, nb, 0)
+    assert lev[34] == 4 + 6
+    cdf = oracle_mod.chung_lu_cdf(1000, 2.1)
+    assert cdf[-1] == 1 << 63 and np.all(np.diff(cdf.astype(np.float64)) >= 0)
+    cs, cd = oracle_mod.chung_lu_pairs(4, 1000, 50000, cdf=cdf)
+    deg = np.bincount(np.concatenate([cs, cd]), minlength=1000)
+    assert deg[0] > deg[10] > deg[500]
+
+
+def test_pagerank_semantics(oracle_mod):
+    # isolated vertex keeps (1-d)/n; no dangling redistribution (PageRank.h:125-193)
+    off = np.array([0, 1, 2, 2], np.uint64)
+    nb = np.array([1, 0], np.uint32)
+    p, it, l1 = oracle_mod.pagerank(off, nb, 1e-12, 100)
+    assert abs(p[2] - 0.15 / 3) < 1e-15
+    assert abs(p[0] - p[1]) < 1e-15
+    assert abs(p.sum() - (2 * (1 / 3) + 0.15 / 3)) < 1e-12
+
+
+def test_store_model_random(oracle_mod):
+    rng = np.random.default_rng(3)
+    s, d = oracle_mod.rmat_edges(4, 9, 2000)
+    off, nb = oracle_mod.build_csr(512, s, d)
+    st = oracle_mod.Store(off, nb)
+    cur = {(v, int(x)) for v in range(512) for x in nb[off[v]:off[v + 1]]}
+    for it in range(6):
+        pairs = rng.integers(0, 512, size=(300, 2))
+        keys = (pairs[:, 0].astype(np.uint64) << np.uint64(32)) | pairs[:, 1].astype(np.uint64)
+        ps = {(int(a), int(b)) for a, b in pairs}
+        if it % 2 == 0:
+            assert st.insert_batch(keys) == len(ps - cur)
+            cur |= ps
+        else:
+            assert st.remove_batch(keys) == len(ps & cur)
+            cur -= ps
+        o2, n2 = st.export_csr()
+        got = {(v, int(x)) for v in range(512) for x in n2[o2[v]:o2[v + 1]]}
+        assert got == cur
