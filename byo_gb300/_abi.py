@@ -73,6 +73,8 @@ SIGNATURES = {
     "byo_ctx_launches": (_u64, [_vp]),
     "byo_ctx_synchronize": (_int, [_vp]),
     "byo_ctx_set_round_timing": (_int, [_vp, _int]),
+    "byo_ctx_kernel_timing": (_int, [_vp, ctypes.c_char_p]),
+    "byo_ctx_kernel_time": (_int, [_vp, ctypes.c_char_p, _P(_u64), _P(_dbl)]),
     "byo_graph_create_csr": (_int, [_vp, _u64, _u64, _vp, _vp, _P(_vp)]),
     "byo_graph_create_pma": (_int, [_vp, _u64, _u64, _vp, _vp, _P(_vp)]),
     "byo_graph_generate": (_int, [_vp, _int, _P(GenSpec), _P(_vp)]),
@@ -80,6 +82,7 @@ SIGNATURES = {
     "byo_graph_container": (_int, [_vp]),
     "byo_graph_num_vertices": (_u64, [_vp]),
     "byo_graph_num_edges": (_u64, [_vp]),
+    "byo_graph_num_slots": (_u64, [_vp]),
     "byo_graph_degrees": (_int, [_vp, _vp]),
     "byo_graph_export_csr": (_int, [_vp, _vp, _vp]),
     "byo_graph_neighbors": (_int, [_vp, _u32, _vp, _u64, _P(_u64)]),

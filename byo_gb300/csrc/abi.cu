@@ -75,6 +75,7 @@ void byo_gpu_shutdown(byo_ctx *ctx) {
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   for (int i = 0; i < 64; i++)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -126,6 +127,7 @@ void byo_graph_destroy(byo_graph *g) {
 int byo_graph_container(const byo_graph *g) { return g ? g->container : BYO_EINVAL; }
 uint64_t byo_graph_num_vertices(const byo_graph *g) { return g ? g->n : 0; }
 uint64_t byo_graph_num_edges(const byo_graph *g) { return g ? g->m : 0; }
+uint64_t byo_graph_num_slots(const byo_graph *g) { return g ? g->nslots : 0; }
 
 int byo_graph_degrees(byo_graph *g, uint32_t *h_out) {
   if (!g || !h_out) return BYO_EINVAL;
@@ -495,6 +497,32 @@ int byo_last_rounds(byo_ctx *ctx, byo_round_log *out, uint64_t cap, uint64_t *co
   if (count) *count = n;
   if (out)
     for (uint64_t i = 0; i < n && i < cap; i++) out[i] = ctx->rounds[i];
+  return BYO_OK;
+}
+
+int byo_ctx_kernel_timing(byo_ctx *ctx, const char *tag) {
+  if (!ctx) return BYO_EINVAL;
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->ktag = tag ? tag : "";
+  ctx->kev_used = 0;
+  ctx->ktags.clear();
+  return BYO_OK;
+}
+
+int byo_ctx_kernel_time(byo_ctx *ctx, const char *tag, uint64_t *launches, double *ms) {
+  if (!ctx) return BYO_EINVAL;
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  double tot = 0.0;
+  uint64_t cnt = 0;
+  for (size_t i = 0; i + 1 < ctx->kev_used; i += 2) {
+    if (tag && std::strcmp(tag, ctx->ktags[i / 2]) != 0) continue;
+    float t = 0.f;
+    BYO_CU(ctx, cudaEventElapsedTime(&t, ctx->kev[i], ctx->kev[i + 1]));
+    tot += t;
+    cnt++;
+  }
+  if (launches) *launches = cnt;
+  if (ms) *ms = tot;
   return BYO_OK;
 }
 

@@ -159,13 +159,13 @@ int cc_run(byo_graph *g, uint32_t *d_label) {
   const int GS = avg >= 24 ? 16 : avg >= 8 ? 8 : 4;
   const int grid = grid_for(ctx, n * GS, 256, 16);
   if (GS == 16)
-    launch(ctx, k_cc_finish<16>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
+    launch_t(ctx, "cc_finish", k_cc_finish<16>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
            (const uint32_t *)g->d_slots, p, n, giant);
   else if (GS == 8)
-    launch(ctx, k_cc_finish<8>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
+    launch_t(ctx, "cc_finish", k_cc_finish<8>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
            (const uint32_t *)g->d_slots, p, n, giant);
   else
-    launch(ctx, k_cc_finish<4>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
+    launch_t(ctx, "cc_finish", k_cc_finish<4>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
            (const uint32_t *)g->d_slots, p, n, giant);
   launch(ctx, k_cc_compress, dim3(grid_for(ctx, n, 256)), dim3(256), 0, p, n);
   return check_launch(ctx, "cc");
@@ -314,84 +314,188 @@ __device__ __forceinline__ T group_total(T s, T c) {
   return kComp ? s + c : s;
 }
 
-// p_next[v] = damping * sum + added; pdiv_out[v] = p_next[v] / deg[v];
-// l1 += |p_curr[v] - p_next[v]| (FP64).  Vertices with degree >= hub_min are
-// skipped here and handled by k_pr_hubs.
-template <bool kComp, typename T, int GS>
-__global__ void __launch_bounds__(256) k_pr_pull(const uint64_t *__restrict__ off,
-                                                 const uint32_t *__restrict__ slots,
-                                                 const uint32_t *__restrict__ deg,
-                                                 const T *__restrict__ pdiv_in,
-                                                 const T *__restrict__ p_curr, T *__restrict__ p_next,
-                                                 T *__restrict__ pdiv_out, uint64_t n, T damping,
-                                                 T added, uint32_t hub_min, double *l1) {
-  __shared__ double sm[9];
-  const unsigned gl = threadIdx.x % GS;
-  const uint64_t gid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / GS;
-  const uint64_t ng = ((uint64_t)gridDim.x * blockDim.x) / GS;
+// ---------------------------------------------------------------- PageRank plan
+// Vertices are split by slot-range length: light (<= kPrLightMax) vertices are
+// packed into tiles of consecutive ids whose ranges total about kPrTile slots;
+// medium vertices get a warp each, hubs (> kPrHubMin) a CTA each.  A tile
+// never spans a heavier vertex, so its slots are one contiguous run.
+constexpr int kPrTile = 4096;
+constexpr uint32_t kPrLightMax = 512;
+constexpr uint32_t kPrHubMin = 16384;
+constexpr int kPrBlock = 256;
+
+struct InLightLen {
+  const uint64_t *off;
+  __device__ uint64_t operator()(uint64_t v) const {
+    uint64_t len = off[v + 1] - off[v];
+    return len <= kPrLightMax ? len : 0;
+  }
+};
+
+// tile starts: v == 0, v heavy, v-1 heavy, or the light prefix crossed a
+// multiple of kPrTile between v-1 and v
+struct InTileStart {
+  const uint64_t *off;
+  const uint64_t *pre;
+  __device__ uint64_t operator()(uint64_t v) const {
+    if (v == 0) return 1;
+    bool heavy = off[v + 1] - off[v] > kPrLightMax;
+    bool prev_heavy = off[v] - off[v - 1] > kPrLightMax;
+    return (heavy || prev_heavy || (pre[v] / kPrTile) != (pre[v - 1] / kPrTile)) ? 1 : 0;
+  }
+};
+struct OutTileStart {
+  uint32_t *starts;
+  __device__ void operator()(uint64_t v, uint64_t pre, uint64_t f) const {
+    if (f) starts[pre] = (uint32_t)v;
+  }
+};
+
+__global__ void k_pr_heavy_lists(const uint64_t *__restrict__ off, uint64_t n, uint32_t *med,
+                                 unsigned long long *nmed, uint32_t *hubs, unsigned long long *nhub) {
+  // warp-uniform trip count: every lane reaches warp_append
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n; base += stride) {
+    const uint64_t v = base + lane_id();
+    uint64_t len = v < n ? off[v + 1] - off[v] : 0;
+    bool m = len > kPrLightMax && len <= kPrHubMin, h = len > kPrHubMin;
+    uint64_t sm = warp_append(m, nmed);
+    if (m) med[sm] = (uint32_t)v;
+    uint64_t sh = warp_append(h, nhub);
+    if (h) hubs[sh] = (uint32_t)v;
+  }
+}
+
+template <bool kComp, typename T>
+__device__ __forceinline__ void pr_finish(uint64_t v, T tot, const uint32_t *__restrict__ deg,
+                                          const T *__restrict__ p_curr, T *__restrict__ p_next,
+                                          T *__restrict__ pdiv_out, T damping, T added, double &l1loc) {
+  T p = damping * tot + added;
+  p_next[v] = p;
+  pdiv_out[v] = p / (T)deg[v];
+  l1loc += fabs((double)p_curr[v] - (double)p);
+}
+
+// One CTA per light tile: stage p_div[u] of the tile's slots in shared memory
+// (coalesced id loads, four independent gathers per thread in flight), then
+// one thread per vertex sums its run left to right.
+template <bool kComp, typename T>
+__global__ void __launch_bounds__(kPrBlock) k_pr_tiles(const uint64_t *__restrict__ off,
+                                                       const uint32_t *__restrict__ slots,
+                                                       const uint32_t *__restrict__ deg,
+                                                       const uint32_t *__restrict__ tstart, uint64_t ntiles,
+                                                       const T *__restrict__ pdiv_in,
+                                                       const T *__restrict__ p_curr, T *__restrict__ p_next,
+                                                       T *__restrict__ pdiv_out, T damping, T added, double *l1) {
+  __shared__ T vals[kPrTile + kPrLightMax];
+  __shared__ double sm[kPrBlock / 32 + 1];
   double l1loc = 0.0;
-  const uint64_t nround = (n + ng - 1) / ng;
-  for (uint64_t r = 0; r < nround; r++) {
-    const uint64_t v = gid + r * ng;
-    T s = T(0), c = T(0);
-    bool mine = v < n;
-    uint32_t d = 0;
-    if (mine) {
-      d = deg[v];
-      if (d >= hub_min) mine = false;
-    }
-    if (mine) {
-      const uint64_t b = off[v], e = off[v + 1];
-      for (uint64_t j = b + gl; j < e; j += GS) {
-        uint32_t u = slots[j];
-        if (u != kSentinel) acc_add<kComp>(s, c, pdiv_in[u]);
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t v0 = tstart[t], v1 = tstart[t + 1];
+    const uint64_t s0 = off[v0], s1 = off[v1];
+    if (v1 - v0 == 1 && s1 - s0 > kPrLightMax) continue;  // a heavy vertex: its own kernel
+    const uint32_t len = (uint32_t)(s1 - s0);
+    for (uint32_t i = threadIdx.x; i < len; i += 4 * kPrBlock) {
+      uint32_t u[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        uint32_t idx = i + k * kPrBlock;
+        u[k] = idx < len ? __ldcs(slots + s0 + idx) : kSentinel;
+      }
+      T g[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) g[k] = u[k] != kSentinel ? pdiv_in[u[k]] : T(0);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        uint32_t idx = i + k * kPrBlock;
+        if (idx < len) vals[idx] = g[k];
       }
     }
-    T tot = group_total<kComp, T, GS>(s, c);
-    if (mine && gl == 0) {
-      T p = damping * tot + added;
-      p_next[v] = p;
-      pdiv_out[v] = p / (T)d;
-      l1loc += fabs((double)p_curr[v] - (double)p);
+    __syncthreads();
+    for (uint32_t v = v0 + threadIdx.x; v < v1; v += kPrBlock) {
+      const uint32_t r0 = (uint32_t)(off[v] - s0), r1 = (uint32_t)(off[v + 1] - s0);
+      T s = T(0), c = T(0);
+      for (uint32_t r = r0; r < r1; r++) acc_add<kComp>(s, c, vals[r]);
+      pr_finish<kComp, T>(v, kComp ? s + c : s, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
     }
+    __syncthreads();
   }
   l1loc = block_sum(l1loc, sm);
   if (threadIdx.x == 0 && l1loc != 0.0) atomicAdd(l1, l1loc);
 }
 
+// One warp per medium vertex; four independent loads per lane in flight.
+template <bool kComp, typename T>
+__global__ void __launch_bounds__(256) k_pr_medium(const uint64_t *__restrict__ off,
+                                                   const uint32_t *__restrict__ slots,
+                                                   const uint32_t *__restrict__ deg,
+                                                   const uint32_t *__restrict__ med,
+                                                   const unsigned long long *__restrict__ nmed,
+                                                   const T *__restrict__ pdiv_in,
+                                                   const T *__restrict__ p_curr, T *__restrict__ p_next,
+                                                   T *__restrict__ pdiv_out, T damping, T added, double *l1) {
+  __shared__ double sm[9];
+  const uint64_t nm = *nmed;
+  const unsigned lane = lane_id();
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  double l1loc = 0.0;
+  for (uint64_t h = gw; h < nm; h += nw) {
+    const uint32_t v = med[h];
+    const uint64_t b = off[v], e = off[v + 1];
+    T s = T(0), c = T(0);
+    for (uint64_t j = b + lane; j < e; j += 128) {
+      uint32_t u[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) u[k] = j + 32 * k < e ? __ldcs(slots + j + 32 * k) : kSentinel;
+      T g[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) g[k] = u[k] != kSentinel ? pdiv_in[u[k]] : T(0);
+#pragma unroll
+      for (int k = 0; k < 4; k++) acc_add<kComp>(s, c, g[k]);
+    }
+    T tot = group_total<kComp, T, 32>(s, c);
+    if (lane == 0) pr_finish<kComp, T>(v, tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+  }
+  l1loc = block_sum(l1loc, sm);
+  if (threadIdx.x == 0 && l1loc != 0.0) atomicAdd(l1, l1loc);
+}
+
+// One CTA per hub; warp partials combined in warp order.
 template <bool kComp, typename T>
 __global__ void __launch_bounds__(256) k_pr_hubs(const uint64_t *__restrict__ off,
                                                  const uint32_t *__restrict__ slots,
                                                  const uint32_t *__restrict__ deg,
-                                                 const uint32_t *__restrict__ hubs, uint64_t nh,
+                                                 const uint32_t *__restrict__ hubs,
+                                                 const unsigned long long *__restrict__ nhub,
                                                  const T *__restrict__ pdiv_in,
                                                  const T *__restrict__ p_curr, T *__restrict__ p_next,
-                                                 T *__restrict__ pdiv_out, T damping, T added,
-                                                 double *l1) {
-  __shared__ T ss[8], sc[8];
+                                                 T *__restrict__ pdiv_out, T damping, T added, double *l1) {
+  __shared__ T ss[8];
+  const uint64_t nh = *nhub;
   for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
     const uint32_t v = hubs[h];
     const uint64_t b = off[v], e = off[v + 1];
     T s = T(0), c = T(0);
-    for (uint64_t j = b + threadIdx.x; j < e; j += blockDim.x) {
-      uint32_t u = slots[j];
-      if (u != kSentinel) acc_add<kComp>(s, c, pdiv_in[u]);
+    for (uint64_t j = b + threadIdx.x; j < e; j += 4 * blockDim.x) {
+      uint32_t u[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) u[k] = j + blockDim.x * k < e ? __ldcs(slots + j + blockDim.x * k) : kSentinel;
+      T g[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) g[k] = u[k] != kSentinel ? pdiv_in[u[k]] : T(0);
+#pragma unroll
+      for (int k = 0; k < 4; k++) acc_add<kComp>(s, c, g[k]);
     }
     T tot = group_total<kComp, T, 32>(s, c);
-    // group_total leaves the warp total in every lane; combine warps in order
-    if (lane_id() == 0) {
-      ss[threadIdx.x >> 5] = tot;
-      sc[threadIdx.x >> 5] = T(0);
-    }
+    if (lane_id() == 0) ss[threadIdx.x >> 5] = tot;
     __syncthreads();
     if (threadIdx.x == 0) {
       T S = T(0), C = T(0);
       for (int w = 0; w < (int)(blockDim.x >> 5); w++) acc_add<kComp>(S, C, ss[w]);
-      T t = kComp ? S + C : S;
-      T p = damping * t + added;
-      p_next[v] = p;
-      pdiv_out[v] = p / (T)deg[v];
-      atomicAdd(l1, fabs((double)p_curr[v] - (double)p));
+      double l1loc = 0.0;
+      pr_finish<kComp, T>(v, kComp ? S + C : S, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+      atomicAdd(l1, l1loc);
     }
     __syncthreads();
   }
@@ -413,16 +517,6 @@ __global__ void k_to_f64(const T *__restrict__ in, uint64_t n, double *out) {
     out[v] = (double)in[v];
 }
 
-__global__ void k_collect_hubs(const uint32_t *__restrict__ deg, uint64_t n, uint32_t hub_min,
-                               uint32_t *hubs, unsigned long long *cnt) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    bool h = deg[v] >= hub_min;
-    uint64_t s = warp_append(h, cnt);
-    if (h) hubs[s] = (uint32_t)v;
-  }
-}
-
 template <bool kComp, typename T>
 static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d_p, uint32_t *iters_out,
                          double *l1_out) {
@@ -433,53 +527,55 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   BYO_TRY(ws(g, WS_PR_B, n, &pb));
   BYO_TRY(ws(g, WS_PR_C, n, &da));
   BYO_TRY(ws(g, WS_PR_D, n, &db));
-  // hub list: vertices of degree >= hub_min, one CTA each
-  const uint32_t hub_min = 4096;
-  uint32_t *hubs = nullptr;
-  BYO_TRY(ws(g, WS_BUCKETS, n + 4, &hubs));
-  // counter in the trailing 8-byte-aligned word
-  unsigned long long *d_cnt = (unsigned long long *)(hubs + ((n + 1) & ~1ull));
+  // plan: light prefix, tile starts, medium and hub lists
+  uint64_t *pre = nullptr;
+  uint32_t *lists = nullptr;
+  BYO_TRY(ws(g, WS_SCAN, n + 1, &pre));
+  BYO_TRY(ws(g, WS_BUCKETS, 3 * n + 16, &lists));
+  uint32_t *tstart = lists, *med = lists + (n + 2), *hubs = lists + 2 * (n + 2);
+  unsigned long long *cnt = (unsigned long long *)(lists + 3 * n + 8 - ((3 * n + 8) & 1));
   double *d_l1 = nullptr;
   BYO_TRY(ws(g, WS_MISC, 4, (uint32_t **)&d_l1));
-  BYO_CU(ctx, cudaMemsetAsync(d_cnt, 0, 8, ctx->stream));
-  launch(ctx, k_collect_hubs, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint32_t *)g->d_deg, n,
-         hub_min, hubs, d_cnt);
-  double *h = nullptr;
+  const uint64_t *tot = nullptr;
+  BYO_TRY(scan_apply(ctx, n, InLightLen{g->d_off}, OutPrefix{pre}, &tot));
+  BYO_TRY(scan_apply(ctx, n, InTileStart{g->d_off, pre}, OutTileStart{tstart}, &tot));
+  uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
-  BYO_CU(ctx, cudaMemcpyAsync(h, d_cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  launch(ctx, k_pr_init<T>, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint32_t *)g->d_deg, n, pa,
-         da, (T)(1.0 / (double)n));
+  BYO_CU(ctx, cudaMemcpyAsync(h, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaMemsetAsync(cnt, 0, 16, ctx->stream));
+  launch(ctx, k_pr_heavy_lists, dim3(grid_for(ctx, n + 31, 256)), dim3(256), 0, (const uint64_t *)g->d_off, n,
+         med, cnt, hubs, cnt + 1);
+  launch(ctx, k_pr_init<T>, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint32_t *)g->d_deg, n, pa, da,
+         (T)(1.0 / (double)n));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const uint64_t nh = ((uint64_t *)h)[0];
+  const uint64_t ntiles = h[0];
+  uint32_t nn = (uint32_t)n;
+  BYO_CU(ctx, cudaMemcpyAsync(tstart + ntiles, &nn, 4, cudaMemcpyHostToDevice, ctx->stream));
   const T damping = (T)0.85;
   const T added = (T)((1 - 0.85) * (1 / (double)n));
-  const double avg = (double)g->m / (double)n;
-  const int GS = avg >= 24 ? 16 : avg >= 8 ? 8 : 4;
-  const int grid = grid_for(ctx, n * GS, 256, 8);
+  const int grid_t = grid_for(ctx, ntiles, 1, 8);
+  const int grid_m = ctx->num_sms * 8;
+  const int grid_h = ctx->num_sms * 2;
   uint32_t it = 0;
   double L1 = 0.0;
   T *p_curr = pa, *p_next = pb, *pdiv = da, *pdiv_next = db, *last = nullptr;
+  double *hl = (double *)h;
   while (it++ < max_iters) {
     BYO_CU(ctx, cudaMemsetAsync(d_l1, 0, 8, ctx->stream));
-#define PR_CASE(G)                                                                                   \
-  launch(ctx, k_pr_pull<kComp, T, G>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,          \
-         (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const T *)pdiv, (const T *)p_curr, \
-         p_next, pdiv_next, n, damping, added, hub_min, d_l1)
-    if (GS == 16)
-      PR_CASE(16);
-    else if (GS == 8)
-      PR_CASE(8);
-    else
-      PR_CASE(4);
-#undef PR_CASE
-    if (nh)
-      launch(ctx, k_pr_hubs<kComp, T>, dim3((unsigned)std::min<uint64_t>(nh, ctx->num_sms * 4)), dim3(256),
-             0, (const uint64_t *)g->d_off, (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg,
-             (const uint32_t *)hubs, nh, (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next, damping,
+    launch_t(ctx, "pr_pull", k_pr_tiles<kComp, T>, dim3(grid_t), dim3(kPrBlock), 0, (const uint64_t *)g->d_off,
+             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)tstart, ntiles,
+             (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next, damping, added, d_l1);
+    launch_t(ctx, "pr_pull", k_pr_medium<kComp, T>, dim3(grid_m), dim3(256), 0, (const uint64_t *)g->d_off,
+             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)med,
+             (const unsigned long long *)cnt, (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next, damping,
              added, d_l1);
-    BYO_CU(ctx, cudaMemcpyAsync(h, d_l1, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    launch_t(ctx, "pr_pull", k_pr_hubs<kComp, T>, dim3(grid_h), dim3(256), 0, (const uint64_t *)g->d_off,
+             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)hubs,
+             (const unsigned long long *)(cnt + 1), (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next,
+             damping, added, d_l1);
+    BYO_CU(ctx, cudaMemcpyAsync(hl, d_l1, 8, cudaMemcpyDeviceToHost, ctx->stream));
     BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-    L1 = h[0];
+    L1 = hl[0];
     std::swap(pdiv, pdiv_next);
     last = p_next;
     if (L1 < eps) break;
@@ -630,7 +726,7 @@ int tc_run(byo_graph *g, uint64_t *count) {
   unsigned long long *d_total = nullptr;
   BYO_TRY(ws(g, WS_MISC, 4, (uint32_t **)&d_total));
   BYO_CU(ctx, cudaMemsetAsync(d_total, 0, 8, ctx->stream));
-  launch(ctx, k_tc_intersect<8>, dim3(grid_for(ctx, n * 8, 256, 16)), dim3(256), 0, (const uint64_t *)doff,
+  launch_t(ctx, "tc_intersect", k_tc_intersect<8>, dim3(grid_for(ctx, n * 8, 256, 16)), dim3(256), 0, (const uint64_t *)doff,
          (const uint32_t *)dn, n, d_total);
   BYO_CU(ctx, cudaMemcpyAsync(h, d_total, 8, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));

@@ -420,7 +420,7 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
     int maxg = ctx->num_sms * (smem > 100 * 1024 ? 1 : 2);
     if (grid > maxg) grid = maxg;
     if (grid < 1) grid = 1;
-    launch(ctx, k_pull, dim3(grid), dim3(block), (size_t)smem, (const uint64_t *)g->d_off,
+    launch_t(ctx, "bfs_pull", k_pull, dim3(grid), dim3(block), (size_t)smem, (const uint64_t *)g->d_off,
            (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.bits, g->n,
            st.lp, st.visited, out.list, out.bits, d_st, lvl, defer, tune.pull_cap, stage);
     launch(ctx, k_pull_long, dim3(ctx->num_sms * 4), dim3(256), 0, (const uint64_t *)g->d_off,
@@ -433,7 +433,7 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
       switch (tune.push_group) {
 #define PUSH_CASE(GS)                                                                            \
   case GS:                                                                                       \
-    launch(ctx, k_push<GS>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,                \
+    launch_t(ctx, "bfs_push", k_push<GS>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,                \
            (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.list,  \
            in.size, st.lp, (const uint32_t *)st.visited, out.list, out.bits, d_st, lvl, defer,   \
            tune.hub_min);                                                                        \
@@ -457,7 +457,7 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
       BYO_TRY(scan_gather_range(ctx, g->d_off, in.list, in.size, pre));
       const uint64_t est_tiles = (in.outdeg + tune.blocked_tile - 1) / tune.blocked_tile;
       const int grid = grid_for(ctx, est_tiles ? est_tiles : 1, 1, 16);
-      launch(ctx, k_push_blocked, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
+      launch_t(ctx, "bfs_blocked", k_push_blocked, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
              (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.list,
              in.size, (const uint64_t *)pre, st.lp, (const uint32_t *)st.visited, out.list, out.bits,
              d_st, lvl, tune.blocked_tile);

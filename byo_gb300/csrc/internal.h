@@ -47,6 +47,12 @@ struct byo_ctx {
   std::vector<byo_round_log> rounds;
   byo::DevBuf scratch[8];  // context-wide temporaries (sort, scan)
   byo::Mlp *policy = nullptr;
+  // per-kernel timing: tagged launches matching `ktag` ("*" = every tag) are
+  // bracketed by event pairs; ktags[i] names the pair i
+  std::string ktag;
+  std::vector<cudaEvent_t> kev;
+  std::vector<const char *> ktags;
+  size_t kev_used = 0;
 };
 
 struct byo_graph {
@@ -106,6 +112,19 @@ template <typename Kern, typename... Args>
 inline void launch(byo_ctx *ctx, Kern kernel, dim3 grid, dim3 block, size_t smem, Args... args) {
   kernel<<<grid, block, smem, ctx->stream>>>(args...);
   ctx->launches++;
+}
+
+// As launch(), and when `tag` is the context's timed tag, brackets the launch
+// with a pair of CUDA events on the same stream.
+bool ktimer_begin(byo_ctx *ctx, const char *tag);
+void ktimer_end(byo_ctx *ctx);
+template <typename Kern, typename... Args>
+inline void launch_t(byo_ctx *ctx, const char *tag, Kern kernel, dim3 grid, dim3 block, size_t smem,
+                     Args... args) {
+  bool timed = !ctx->ktag.empty() && ktimer_begin(ctx, tag);
+  kernel<<<grid, block, smem, ctx->stream>>>(args...);
+  ctx->launches++;
+  if (timed) ktimer_end(ctx);
 }
 
 // ---------------------------------------------------------------- memory

@@ -1,17 +1,641 @@
-// pma.cu -- packed-memory-array container (placeholder until the device PMA
-// lands; every entry point reports BYO_ENOTSUP).
+// pma.cu -- packed-memory-array graph container on the device, the GB300
+// counterpart of PMA_graph / CPMA (benchmarks/run_structures/run_single_pma.cc:
+// 39-141; the CPMA itself lives in the un-vendored Packed-Memory-Array
+// submodule).  Its observable contract is the sorted set of (src,dst) keys
+// with insert = union and remove = difference after sort+unique of the batch
+// (Graph::insert_batch / remove_batch, gbbs/graph.h:3071-3124).
+//
+// Layout in HBM (structure of arrays, leaves of kLeaf slots):
+//   dst[NL*kLeaf], src[NL*kLeaf]  the keys (src<<32|dst) of leaf i sorted and
+//                                 left-packed in [i*kLeaf, i*kLeaf+cnt[i]);
+//                                 the rest of the leaf holds kSentinel
+//   cnt[NL]                       elements per leaf
+//   sep[NL]                       routing separators: leaf i holds keys in
+//                                 [sep[i], sep[i+1]); sep[0] = 0
+// `dst` is the graph's traversal slot array: vertex v's slot range
+// [off[v], off[v+1]) holds its neighbours in order plus the gaps at the ends of
+// the leaves it spans, so BFS / CC / PageRank run on the PMA unchanged.
+//
+// A batch update (keys already sorted and unique):
+//   route     batch segment of every leaf (binary search of sep[i])
+//   count     per leaf, how many batch keys are new (insert) / present (remove)
+//   windows   an overflowing leaf takes the smallest aligned window of 2^h
+//             leaves whose density after the update is within the bound for
+//             height h (1.0 at a leaf down to kRootMax at the root); nested
+//             windows resolve to the outermost; none fits -> grow
+//   merge     one CTA per leaf with work: the leaf is staged in shared memory,
+//             every output element's position is computed by rank (binary
+//             searches, no serial merge), and written in place or, for a leaf
+//             inside a window, to a staging buffer
+//   spread    one CTA per windowed leaf copies its even share of the window's
+//             elements back and resets its separator
+//   view      off[v] / deg[v] for every vertex by binary search
+// Bytes per update: 16 per batch key (sort passes excluded) + 16 per slot of
+// every leaf touched (read + write of src and dst), twice for windowed leaves.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "device.cuh"
 #include "internal.h"
+#include "scan.cuh"
 
 namespace byo {
-struct Pma {};
-int pma_build(byo_graph *g, const uint64_t *, uint64_t) {
-  return set_error(g->ctx, BYO_ENOTSUP, "pma container not available");
+
+constexpr uint32_t kLeafLg = 9;
+constexpr uint32_t kLeaf = 1u << kLeafLg;
+constexpr int kPmaBlock = 256;
+constexpr double kBuildDensity = 0.70;
+constexpr double kRootMax = 0.90;
+constexpr double kRootMin = 0.25;  // below this after a remove: rebuild smaller
+
+struct Pma {
+  uint64_t NL = 0;        // leaves
+  int H = 0;              // ceil(log2 NL)
+  uint32_t *src = nullptr, *dst = nullptr, *cnt = nullptr;
+  uint64_t *sep = nullptr;
+  // update scratch
+  DevBuf keys_a, keys_b;  // batch copies for sort / unique
+  DevBuf bstart;          // uint64[NL+1]
+  DevBuf rcount;          // uint32[NL] elements after the update
+  DevBuf rpre;            // uint64[NL+1]
+  DevBuf win;             // uint32[NL]   window code per leaf (or kNoWin)
+  DevBuf marks;           // uint8[2*NL]  marked windows per (level,index)
+  DevBuf staging;         // uint64[...]  windowed elements
+  DevBuf misc;            // flags / counters
+  DevBuf epre;            // uint64[NL+1] element prefix for the view
+  uint64_t rebuilds = 0, windows = 0;
+};
+
+constexpr uint32_t kNoWin = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint64_t slot_key(const uint32_t *src, const uint32_t *dst, uint64_t s) {
+  return ((uint64_t)src[s] << 32) | dst[s];
 }
-int pma_update(byo_graph *g, const uint64_t *, uint64_t, int, int, uint64_t *) {
-  return set_error(g->ctx, BYO_ENOTSUP, "pma container not available");
+
+__host__ __device__ __forceinline__ double upper_bound_density(int h, int H) {
+  return H == 0 ? kRootMax : 1.0 - (1.0 - kRootMax) * (double)h / (double)H;
 }
-int pma_export_keys(byo_graph *g, uint64_t *) {
-  return set_error(g->ctx, BYO_ENOTSUP, "pma container not available");
+
+// last leaf i with sep[i] <= key
+__device__ __forceinline__ uint64_t route(const uint64_t *sep, uint64_t NL, uint64_t key) {
+  uint64_t lo = 0, hi = NL;
+  while (hi - lo > 1) {
+    uint64_t mid = (lo + hi) >> 1;
+    if (sep[mid] <= key) lo = mid; else hi = mid;
+  }
+  return lo;
 }
-void pma_destroy(Pma *p) { delete p; }
+
+// ---------------------------------------------------------------- batch preparation
+
+__global__ void k_key_bounds(const uint64_t *__restrict__ keys, uint64_t cnt, unsigned long long *out) {
+  uint64_t ms = 0, md = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t k = keys[i];
+    ms = ms > (k >> 32) ? ms : (k >> 32);
+    md = md > (k & 0xFFFFFFFFull) ? md : (k & 0xFFFFFFFFull);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    uint64_t a = __shfl_xor_sync(kFull, ms, o), b = __shfl_xor_sync(kFull, md, o);
+    ms = ms > a ? ms : a;
+    md = md > b ? md : b;
+  }
+  if (lane_id() == 0) {
+    atomicMax(out, (unsigned long long)ms);
+    atomicMax(out + 1, (unsigned long long)md);
+  }
+}
+
+// strictly increasing check for callers that pass sorted = 1
+__global__ void k_check_sorted(const uint64_t *__restrict__ keys, uint64_t cnt, unsigned int *bad) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x + 1; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    if (keys[i] <= keys[i - 1]) atomicOr(bad, 1u);
+}
+
+// ---------------------------------------------------------------- routing / counting
+
+__global__ void k_pma_route(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
+                            uint64_t b, uint64_t *bstart) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= NL;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    if (i == NL) {
+      bstart[NL] = b;
+      continue;
+    }
+    const uint64_t s = sep[i];
+    uint64_t lo = 0, hi = b;  // first index with keys >= s
+    while (lo < hi) {
+      uint64_t mid = (lo + hi) >> 1;
+      if (keys[mid] < s) lo = mid + 1; else hi = mid;
+    }
+    bstart[i] = i == 0 ? 0 : lo;
+  }
+}
+
+__device__ __forceinline__ bool leaf_contains(const uint32_t *src, const uint32_t *dst, uint64_t base, uint32_t c,
+                                              uint64_t key) {
+  uint32_t lo = 0, hi = c;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (slot_key(src, dst, base + mid) < key) lo = mid + 1; else hi = mid;
+  }
+  return lo < c && slot_key(src, dst, base + lo) == key;
+}
+
+// rcount[i] = elements of leaf i after the update; one warp per leaf
+__global__ void k_pma_count(const uint32_t *__restrict__ src, const uint32_t *__restrict__ dst,
+                            const uint32_t *__restrict__ cnt, uint64_t NL, const uint64_t *__restrict__ keys,
+                            const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t i = gw; i < NL; i += nw) {
+    const uint64_t b0 = bstart[i], b1 = bstart[i + 1];
+    const uint32_t c = cnt[i];
+    uint64_t present = 0;
+    for (uint64_t k = b0 + lane_id(); k < b1; k += 32)
+      present += leaf_contains(src, dst, i * kLeaf, c, keys[k]);
+    present = warp_sum(present);
+    if (lane_id() == 0) {
+      uint64_t r = insert ? (uint64_t)c + (b1 - b0) - present : (uint64_t)c - present;
+      rcount[i] = (uint32_t)(r > 0xFFFFFFFFull ? 0xFFFFFFFFull : r);
+    }
+  }
+}
+
+struct InCount32 {
+  const uint32_t *p;
+  __device__ uint64_t operator()(uint64_t i) const { return p[i]; }
+};
+
+// ---------------------------------------------------------------- windows
+
+// For each overflowing leaf: the smallest aligned window whose density after
+// the update is within bound; marks[(h, idx)] = 1.  Sets *grow when even the
+// root is too dense.
+__global__ void k_pma_windows(const uint32_t *__restrict__ rcount, const uint64_t *__restrict__ rpre,
+                              uint64_t NL, int H, uint8_t *marks, unsigned int *grow, unsigned int *any) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < NL;
+       j += (uint64_t)gridDim.x * blockDim.x) {
+    if (rcount[j] <= kLeaf) continue;
+    atomicOr(any, 1u);
+    bool found = false;
+    for (int h = 1; h <= H; h++) {
+      uint64_t a = (j >> h) << h, e = a + (1ull << h);
+      if (e > NL) e = NL;
+      double tot = (double)(rpre[e] - rpre[a]);
+      if (tot <= upper_bound_density(h, H) * (double)(e - a) * kLeaf) {
+        // level h occupies marks[(2^h-ish) offset]: index by level base = h*NL
+        marks[(uint64_t)h * NL + (j >> h)] = 1;
+        found = true;
+        break;
+      }
+    }
+    if (!found) atomicOr(grow, 1u);
+  }
+}
+
+// Window of every leaf: the highest marked ancestor; code = h << 27 | start
+// leaf index is recovered from j and h.
+__global__ void k_pma_cover(const uint8_t *__restrict__ marks, uint64_t NL, int H, uint32_t *win) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < NL;
+       j += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t code = kNoWin;
+    for (int h = H; h >= 1; h--)
+      if (marks[(uint64_t)h * NL + (j >> h)]) {
+        code = (uint32_t)h;
+        break;
+      }
+    win[j] = code;
+  }
+}
+
+// ---------------------------------------------------------------- merge
+
+// One CTA per leaf with work.  Leaf A (<= kLeaf keys) is staged in shared
+// memory; batch segment B streams from global memory.
+//   insert: pos(A[i]) = i + lb_B(A[i]) - PA[i]
+//           pos(B[k]) = k - PA[lb_A(B[k])] + lb_A(B[k])   for B[k] not in A
+//           (PA[i] = number of A[0..i) also present in B)
+//   remove: pos(A[i]) = i - PA[i] for A[i] not in B
+// Output goes in place (leaf not in a window) or to staging[rpre[leaf]...].
+__global__ void __launch_bounds__(kPmaBlock) k_pma_merge(uint32_t *src, uint32_t *dst, uint32_t *cnt,
+                                                        uint64_t NL, const uint64_t *__restrict__ keys,
+                                                        const uint64_t *__restrict__ bstart,
+                                                        const uint32_t *__restrict__ win,
+                                                        const uint64_t *__restrict__ rpre, uint64_t *staging,
+                                                        int insert, int all_windowed) {
+  __shared__ uint64_t A[kLeaf];
+  __shared__ uint32_t PA[kLeaf + 1];
+  __shared__ uint32_t wsum[kPmaBlock / 32 + 1];
+  for (uint64_t j = blockIdx.x; j < NL; j += gridDim.x) {
+    const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
+    const bool windowed = all_windowed || win[j] != kNoWin;
+    if (b0 == b1 && !windowed) continue;
+    const uint32_t c = cnt[j];
+    const uint64_t base = j * kLeaf;
+    for (uint32_t i = threadIdx.x; i < c; i += kPmaBlock) A[i] = slot_key(src, dst, base + i);
+    __syncthreads();
+    // presence of A[i] in B, then exclusive prefix PA (kLeaf <= 2 * block)
+    uint32_t f[kLeaf / kPmaBlock];
+#pragma unroll
+    for (int q = 0; q < (int)(kLeaf / kPmaBlock); q++) {
+      uint32_t i = threadIdx.x * (kLeaf / kPmaBlock) + q;
+      uint32_t hit = 0;
+      if (i < c && b1 > b0) {
+        uint64_t lo = b0, hi = b1, x = A[i];
+        while (lo < hi) {
+          uint64_t mid = (lo + hi) >> 1;
+          if (keys[mid] < x) lo = mid + 1; else hi = mid;
+        }
+        hit = (lo < b1 && keys[lo] == x) ? 1u : 0u;
+      }
+      f[q] = hit;
+    }
+    uint32_t ts = 0;
+#pragma unroll
+    for (int q = 0; q < (int)(kLeaf / kPmaBlock); q++) ts += f[q];
+    uint32_t tot;
+    uint32_t pre = block_exclusive_scan(ts, wsum, &tot);
+#pragma unroll
+    for (int q = 0; q < (int)(kLeaf / kPmaBlock); q++) {
+      PA[threadIdx.x * (kLeaf / kPmaBlock) + q] = pre;
+      pre += f[q];
+    }
+    if (threadIdx.x == 0) PA[kLeaf] = tot;
+    __syncthreads();
+    // PA entries beyond c are tot (all q with i >= c have f = 0): PA[c] valid
+    const uint64_t r = insert ? (uint64_t)c + (b1 - b0) - tot : (uint64_t)c - tot;
+    uint32_t *osrc = src, *odst = dst;
+    uint64_t obase = base;
+    uint64_t *ostage = nullptr;
+    if (windowed) {
+      ostage = staging + rpre[j];
+    }
+    auto put = [&](uint64_t pos, uint64_t key) {
+      if (ostage) {
+        ostage[pos] = key;
+      } else {
+        osrc[obase + pos] = (uint32_t)(key >> 32);
+        odst[obase + pos] = (uint32_t)key;
+      }
+    };
+    // A elements
+    for (uint32_t i = threadIdx.x; i < c; i += kPmaBlock) {
+      const uint64_t x = A[i];
+      if (insert) {
+        uint64_t lo = b0, hi = b1;  // lb_B(x)
+        while (lo < hi) {
+          uint64_t mid = (lo + hi) >> 1;
+          if (keys[mid] < x) lo = mid + 1; else hi = mid;
+        }
+        put(i + (lo - b0) - PA[i], x);
+      } else {
+        const bool gone = PA[i + 1] != PA[i];
+        if (!gone) put(i - PA[i], x);
+      }
+    }
+    // B elements (insert only)
+    if (insert) {
+      for (uint64_t k = b0 + threadIdx.x; k < b1; k += kPmaBlock) {
+        const uint64_t x = keys[k];
+        uint32_t lo = 0, hi = c;  // lb_A(x)
+        while (lo < hi) {
+          uint32_t mid = (lo + hi) >> 1;
+          if (A[mid] < x) lo = mid + 1; else hi = mid;
+        }
+        if (lo < c && A[lo] == x) continue;  // already present
+        put((k - b0) - PA[lo] + lo, x);
+      }
+    }
+    if (!windowed) {
+      // pad what the leaf no longer holds (remove) and publish the count
+      for (uint64_t p = r + threadIdx.x; p < c; p += kPmaBlock) {
+        src[base + p] = kSentinel;
+        dst[base + p] = kSentinel;
+      }
+      if (threadIdx.x == 0) cnt[j] = (uint32_t)r;
+    }
+    __syncthreads();
+  }
+}
+
+// One CTA per leaf of a window: its even share of the window's staged
+// elements.  The window of leaf j starts at a = (j >> h) << h (or 0 for the
+// whole-array rebuild); elements [rpre[a], rpre[e]) are in staging at the same
+// offsets.  Destination arrays may be new ones (grow / shrink).
+__global__ void __launch_bounds__(kPmaBlock) k_pma_spread(const uint64_t *__restrict__ staging,
+                                                         const uint64_t *__restrict__ rpre,
+                                                         const uint32_t *__restrict__ win, uint64_t NL_src,
+                                                         uint32_t *dsrc, uint32_t *ddst, uint32_t *dcnt,
+                                                         uint64_t *dsep, uint64_t NL_dst, int all,
+                                                         const uint64_t *__restrict__ old_sep) {
+  for (uint64_t j = blockIdx.x; j < NL_dst; j += gridDim.x) {
+    uint64_t a, e, s0, T, k, width;
+    if (all) {
+      a = 0;
+      e = NL_dst;
+      s0 = 0;
+      T = rpre[NL_src];
+    } else {
+      const uint32_t h = win[j];
+      if (h == kNoWin) continue;
+      a = (j >> h) << h;
+      e = a + (1ull << h);
+      if (e > NL_dst) e = NL_dst;
+      s0 = rpre[a];
+      T = rpre[e] - s0;
+    }
+    width = e - a;
+    k = j - a;
+    const uint64_t lo = (T * k) / width, hi = (T * (k + 1)) / width;
+    const uint64_t base = j * kLeaf;
+    for (uint64_t p = threadIdx.x; p < kLeaf; p += kPmaBlock) {
+      if (lo + p < hi) {
+        const uint64_t key = staging[s0 + lo + p];
+        dsrc[base + p] = (uint32_t)(key >> 32);
+        ddst[base + p] = (uint32_t)key;
+      } else {
+        dsrc[base + p] = kSentinel;
+        ddst[base + p] = kSentinel;
+      }
+    }
+    if (threadIdx.x == 0) {
+      dcnt[j] = (uint32_t)(hi - lo);
+      if (k == 0) {
+        if (all) dsep[j] = 0;  // window start keeps its separator otherwise
+      } else if (hi > lo) {
+        dsep[j] = staging[s0 + lo];
+      } else {
+        // empty leaf: route nothing here; take the next separator
+        uint64_t nxt = ~0ull;
+        if (hi < T) nxt = staging[s0 + hi];
+        else if (!all && e < NL_src) nxt = old_sep[e];
+        dsep[j] = nxt;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- graph view
+
+// off[v] = slot of the first key >= (v,0); elem[v] = number of keys < (v,0);
+// for v in [0, n]
+__global__ void k_pma_view(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
+                           const uint64_t *__restrict__ sep, const uint64_t *__restrict__ epre, uint64_t NL,
+                           uint64_t n, uint64_t *off, uint64_t *elem) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v <= n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t key = v << 32;
+    const uint64_t i = route(sep, NL, key);
+    const uint32_t c = cnt[i];
+    uint32_t lo = 0, hi = c;
+    while (lo < hi) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (src[i * kLeaf + mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
+    }
+    // every key of leaf i is >= sep[i]; keys < (v,0) in leaf i are a prefix
+    off[v] = i * kLeaf + lo;
+    elem[v] = epre[i] + lo;
+  }
+}
+
+__global__ void k_pma_deg(const uint64_t *__restrict__ elem, uint64_t n, uint32_t *deg) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    deg[v] = (uint32_t)(elem[v + 1] - elem[v]);
+}
+
+// export: element e of leaf i -> out[epre[i] + e]
+__global__ void k_pma_export(const uint32_t *__restrict__ src, const uint32_t *__restrict__ dst,
+                             const uint32_t *__restrict__ cnt, const uint64_t *__restrict__ epre, uint64_t NL,
+                             uint64_t *out) {
+  for (uint64_t i = blockIdx.x; i < NL; i += gridDim.x) {
+    const uint32_t c = cnt[i];
+    for (uint32_t e = threadIdx.x; e < c; e += blockDim.x) out[epre[i] + e] = slot_key(src, dst, i * kLeaf + e);
+  }
+}
+
+// ---------------------------------------------------------------- host side
+
+static int pma_alloc(byo_ctx *ctx, uint64_t NL, uint32_t **src, uint32_t **dst, uint32_t **cnt, uint64_t **sep) {
+  cudaError_t e;
+  *src = *dst = *cnt = nullptr;
+  *sep = nullptr;
+  if ((e = cudaMalloc(src, NL * kLeaf * 4)) != cudaSuccess ||
+      (e = cudaMalloc(dst, NL * kLeaf * 4)) != cudaSuccess || (e = cudaMalloc(cnt, NL * 4)) != cudaSuccess ||
+      (e = cudaMalloc(sep, NL * 8)) != cudaSuccess) {
+    cudaGetLastError();
+    if (*src) cudaFree(*src);
+    if (*dst) cudaFree(*dst);
+    if (*cnt) cudaFree(*cnt);
+    if (*sep) cudaFree(*sep);
+    *src = *dst = *cnt = nullptr;
+    *sep = nullptr;
+    return set_error(ctx, BYO_ENOMEM, "pma arrays", e);
+  }
+  return BYO_OK;
+}
+
+static void pma_free_arrays(Pma *p) {
+  if (p->src) cudaFree(p->src);
+  if (p->dst) cudaFree(p->dst);
+  if (p->cnt) cudaFree(p->cnt);
+  if (p->sep) cudaFree(p->sep);
+  p->src = p->dst = p->cnt = nullptr;
+  p->sep = nullptr;
+}
+
+static int ceil_log2(uint64_t x) {
+  int h = 0;
+  while ((1ull << h) < x) h++;
+  return h;
+}
+
+static uint64_t leaves_for(uint64_t m) {
+  uint64_t NL = (uint64_t)std::ceil((double)m / (kBuildDensity * kLeaf));
+  return NL < 1 ? 1 : NL;
+}
+
+// Recomputes the traversal view (off, deg, nslots, m) from the leaves.
+static int pma_view(byo_graph *g) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  uint64_t *epre = nullptr, *elem = nullptr;
+  BYO_TRY(ensure(ctx, p->epre, (p->NL + 1) * 8));
+  epre = (uint64_t *)p->epre.p;
+  BYO_TRY(scan_u32_to_u64(ctx, p->cnt, p->NL, epre));
+  BYO_TRY(ws(g, WS_SCAN, g->n + 2, &elem));
+  launch(ctx, k_pma_view, dim3(grid_for(ctx, g->n + 1, 256)), dim3(256), 0, (const uint32_t *)p->src,
+         (const uint32_t *)p->cnt, (const uint64_t *)p->sep, (const uint64_t *)epre, p->NL, g->n, g->d_off, elem);
+  launch(ctx, k_pma_deg, dim3(grid_for(ctx, g->n, 256)), dim3(256), 0, (const uint64_t *)elem, g->n, g->d_deg);
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, epre + p->NL, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  g->m = h[0];
+  g->d_slots = p->dst;
+  g->nslots = p->NL * kLeaf;
+  return check_launch(ctx, "pma_view");
+}
+
+// Lays `m` sorted unique keys (device) evenly over NL new leaves.
+static int pma_layout(byo_graph *g, const uint64_t *d_keys, uint64_t m, uint64_t NL) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  uint32_t *s, *d, *c;
+  uint64_t *sp;
+  BYO_TRY(pma_alloc(ctx, NL, &s, &d, &c, &sp));
+  // rpre for the "all" spread: only rpre[NL_src] = m is read
+  uint64_t *rp = nullptr;
+  BYO_TRY(ensure(ctx, p->rpre, 16));
+  rp = (uint64_t *)p->rpre.p;
+  BYO_CU(ctx, cudaMemcpyAsync(rp, &m, 8, cudaMemcpyHostToDevice, ctx->stream));
+  launch(ctx, k_pma_spread, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0, d_keys, (const uint64_t *)rp,
+         (const uint32_t *)nullptr, (uint64_t)0, s, d, c, sp, NL, 1, (const uint64_t *)nullptr);
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  pma_free_arrays(p);
+  p->src = s;
+  p->dst = d;
+  p->cnt = c;
+  p->sep = sp;
+  p->NL = NL;
+  p->H = ceil_log2(NL);
+  return pma_view(g);
+}
+
+int pma_build(byo_graph *g, const uint64_t *d_keys, uint64_t m) {
+  Pma *p = new Pma();
+  g->pma = p;
+  return pma_layout(g, d_keys, m, leaves_for(m));
+}
+
+void pma_destroy(Pma *p) {
+  if (!p) return;
+  pma_free_arrays(p);
+  for (DevBuf *b : {&p->keys_a, &p->keys_b, &p->bstart, &p->rcount, &p->rpre, &p->win, &p->marks, &p->staging,
+                    &p->misc, &p->epre})
+    free_buf(*b);
+  delete p;
+}
+
+int pma_export_keys(byo_graph *g, uint64_t *d_keys_out) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  BYO_TRY(ensure(ctx, p->epre, (p->NL + 1) * 8));
+  BYO_TRY(scan_u32_to_u64(ctx, p->cnt, p->NL, (uint64_t *)p->epre.p));
+  launch(ctx, k_pma_export, dim3(grid_for(ctx, p->NL, 1, 16)), dim3(256), 0, (const uint32_t *)p->src,
+         (const uint32_t *)p->dst, (const uint32_t *)p->cnt, (const uint64_t *)p->epre.p, p->NL, d_keys_out);
+  return check_launch(ctx, "pma_export");
+}
+
+// Full rebuild: every leaf merged into staging, then laid out over NL_new
+// leaves (grow, shrink, or the "rebuild" update strategy).
+static int pma_rebuild(byo_graph *g, const uint64_t *keys, const uint64_t *bstart, const uint64_t *rpre,
+                       uint64_t total, int insert) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  BYO_TRY(ensure(ctx, p->staging, (total ? total : 1) * 8));
+  uint64_t *stg = (uint64_t *)p->staging.p;
+  launch_t(ctx, "pma_merge", k_pma_merge, dim3(grid_for(ctx, p->NL, 1, 16)), dim3(kPmaBlock), 0, p->src, p->dst,
+           p->cnt, p->NL, keys, bstart, (const uint32_t *)nullptr, rpre, stg, insert, 1);
+  BYO_TRY(check_launch(ctx, "pma_rebuild merge"));
+  p->rebuilds++;
+  return pma_layout(g, stg, total, leaves_for(total));
+}
+
+int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sorted, int insert,
+               uint64_t *changed) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PMA container");
+  const uint64_t m_before = g->m;
+  // 1. validate, copy, sort, unique
+  BYO_TRY(ensure(ctx, p->keys_a, count * 8));
+  BYO_TRY(ensure(ctx, p->keys_b, count * 8));
+  BYO_TRY(ensure(ctx, p->misc, 64));
+  uint64_t *ka = (uint64_t *)p->keys_a.p, *kb = (uint64_t *)p->keys_b.p;
+  unsigned long long *bounds = (unsigned long long *)p->misc.p;
+  unsigned int *flags = (unsigned int *)(bounds + 2);  // [0] unsorted, [1] grow, [2] any overflow
+  BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 64, ctx->stream));
+  launch(ctx, k_key_bounds, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, bounds);
+  if (sorted)
+    launch(ctx, k_check_sorted, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, flags);
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h[0] >= g->n || h[1] >= g->n) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+  if (sorted && (((unsigned int *)(h + 2))[0])) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  uint64_t *batch = nullptr;
+  uint64_t b = count;
+  if (sorted) {
+    batch = const_cast<uint64_t *>(d_keys_in);
+  } else {
+    BYO_CU(ctx, cudaMemcpyAsync(ka, d_keys_in, count * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    uint64_t *s = nullptr;
+    BYO_TRY(sort_u64(ctx, ka, kb, count, sig_mask_for(g->n), &s));
+    uint64_t *u = s == ka ? kb : ka;
+    BYO_TRY(unique_u64(ctx, s, count, 0, u, &b));
+    batch = u;
+  }
+  // 2. route and count
+  const uint64_t NL = p->NL;
+  BYO_TRY(ensure(ctx, p->bstart, (NL + 1) * 8));
+  BYO_TRY(ensure(ctx, p->rcount, NL * 4));
+  BYO_TRY(ensure(ctx, p->rpre, (NL + 1) * 8));
+  uint64_t *bstart = (uint64_t *)p->bstart.p, *rpre = (uint64_t *)p->rpre.p;
+  uint32_t *rcount = (uint32_t *)p->rcount.p;
+  launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
+         (const uint64_t *)batch, b, bstart);
+  launch(ctx, k_pma_count, dim3(grid_for(ctx, NL * 32, 256, 16)), dim3(256), 0, (const uint32_t *)p->src,
+         (const uint32_t *)p->dst, (const uint32_t *)p->cnt, NL, (const uint64_t *)batch,
+         (const uint64_t *)bstart, insert, rcount);
+  BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
+  BYO_CU(ctx, cudaMemcpyAsync(h, rpre + NL, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const uint64_t total = h[0];
+  if (changed) *changed = insert ? total - m_before : m_before - total;
+  if (total == m_before) return BYO_OK;  // nothing new / nothing present
+  // 3. capacity: grow or shrink by full rebuild
+  const double cap = (double)NL * kLeaf;
+  if ((double)total > kRootMax * cap || (!insert && (double)total < kRootMin * cap && NL > 1))
+    return pma_rebuild(g, batch, bstart, rpre, total, insert);
+  // 4. windows for overflowing leaves
+  BYO_TRY(ensure(ctx, p->marks, (uint64_t)(p->H + 1) * NL));
+  BYO_TRY(ensure(ctx, p->win, NL * 4));
+  uint8_t *marks = (uint8_t *)p->marks.p;
+  uint32_t *win = (uint32_t *)p->win.p;
+  BYO_CU(ctx, cudaMemsetAsync(marks, 0, (uint64_t)(p->H + 1) * NL, ctx->stream));
+  launch(ctx, k_pma_windows, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint32_t *)rcount,
+         (const uint64_t *)rpre, NL, p->H, marks, flags + 1, flags + 2);
+  BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned int *hf = (const unsigned int *)h;
+  if (hf[1]) return pma_rebuild(g, batch, bstart, rpre, total, insert);
+  const bool any = hf[2] != 0;
+  uint64_t *stg = nullptr;
+  if (any) {
+    launch(ctx, k_pma_cover, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint8_t *)marks, NL, p->H, win);
+    BYO_TRY(ensure(ctx, p->staging, total * 8));
+    stg = (uint64_t *)p->staging.p;
+    p->windows++;
+  } else {
+    BYO_CU(ctx, cudaMemsetAsync(win, 0xFF, NL * 4, ctx->stream));
+  }
+  // 5. merge (in place, or into staging for windowed leaves), then spread
+  launch_t(ctx, "pma_merge", k_pma_merge, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0, p->src, p->dst,
+           p->cnt, NL, (const uint64_t *)batch, (const uint64_t *)bstart, (const uint32_t *)win,
+           (const uint64_t *)rpre, stg, insert, 0);
+  if (any)
+    launch_t(ctx, "pma_redistribute", k_pma_spread, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0,
+             (const uint64_t *)stg, (const uint64_t *)rpre, (const uint32_t *)win, NL, p->src, p->dst, p->cnt,
+             p->sep, NL, 0, (const uint64_t *)p->sep);
+  BYO_TRY(check_launch(ctx, "pma_update"));
+  return pma_view(g);
+}
+
 }  // namespace byo

@@ -28,6 +28,23 @@ int set_error(byo_ctx *ctx, int code, const char *what, cudaError_t e) {
   return code;
 }
 
+bool ktimer_begin(byo_ctx *ctx, const char *tag) {
+  if (ctx->ktag != "*" && ctx->ktag != tag) return false;
+  while (ctx->kev.size() < ctx->kev_used + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return false;
+    ctx->kev.push_back(e);
+  }
+  cudaEventRecord(ctx->kev[ctx->kev_used], ctx->stream);
+  ctx->ktags.push_back(tag);
+  return true;
+}
+
+void ktimer_end(byo_ctx *ctx) {
+  cudaEventRecord(ctx->kev[ctx->kev_used + 1], ctx->stream);
+  ctx->kev_used += 2;
+}
+
 int check_launch(byo_ctx *ctx, const char *what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(ctx, BYO_EDEVICE, what, e);
@@ -213,7 +230,7 @@ int sort_u64(byo_ctx *ctx, uint64_t *keys, uint64_t *tmp, uint64_t count, uint64
       launch(ctx, k_radix_hist, dim3((unsigned)ntiles), dim3(SORT_BLOCK), 0, (const uint64_t *)a,
              count, shift, hist, (uint32_t)ntiles);
       BYO_TRY(scan_u32_to_u64(ctx, hist, 256 * ntiles, offs));
-      launch(ctx, k_radix_scatter, dim3((unsigned)ntiles), dim3(SORT_BLOCK), 0, (const uint64_t *)a,
+      launch_t(ctx, "sort_scatter", k_radix_scatter, dim3((unsigned)ntiles), dim3(SORT_BLOCK), 0, (const uint64_t *)a,
              b, count, shift, (const uint64_t *)offs, (uint32_t)ntiles);
       uint64_t *s = a;
       a = b;

@@ -15,7 +15,9 @@ Reference names kept (paths in the wheatman/BYO tree):
   Triangle_degree_ordering  benchmarks/TriangleCounting/ShunTangwongsan15/Triangle.h:167-204
 Errors surface as ByoError carrying the library's status code.
 """
+import atexit
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -29,8 +31,19 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None and a.size else None
 
 
+_live_contexts = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    # native objects must go before the CUDA runtime tears itself down
+    for c in list(_live_contexts):
+        c.close()
+
+
 class Context:
-    """One device, one stream (byo_gpu_init)."""
+    """One device, one stream (byo_gpu_init).  Closing a context first closes
+    every graph, vertexSubset and functor created on it."""
 
     def __init__(self, device=0):
         h = ctypes.c_void_p()
@@ -39,9 +52,19 @@ class Context:
             raise ByoError(rc, "byo_gpu_init(%d) failed" % device)
         self.h = h
         self.device = device
+        self._children = weakref.WeakSet()
+        _live_contexts.add(self)
+
+    def _adopt(self, obj):
+        self._children.add(obj)
+        return obj
 
     def close(self):
         if getattr(self, "h", None):
+            kids = list(self._children)
+            # subsets and functors before the graphs they belong to
+            for k in sorted(kids, key=lambda o: 0 if not isinstance(o, Graph) else 1):
+                k.close()
             lib().byo_gpu_shutdown(self.h)
             self.h = None
 
@@ -58,6 +81,17 @@ class Context:
 
     def synchronize(self):
         check(lib().byo_ctx_synchronize(self.h), self.h)
+
+    def kernel_timing(self, tag):
+        check(lib().byo_ctx_kernel_timing(self.h, tag.encode() if tag else None), self.h)
+
+    def kernel_time(self, tag=None):
+        """(launches, total ms) of the timed launches of `tag` (None: all)."""
+        n = ctypes.c_uint64(0)
+        ms = ctypes.c_double(0)
+        check(lib().byo_ctx_kernel_time(self.h, tag.encode() if tag else None, ctypes.byref(n),
+                                        ctypes.byref(ms)), self.h)
+        return int(n.value), float(ms.value)
 
     def set_round_timing(self, on):
         check(lib().byo_ctx_set_round_timing(self.h, int(bool(on))), self.h)
@@ -77,6 +111,7 @@ class Graph:
     def __init__(self, ctx, handle):
         self.ctx = ctx
         self.h = handle
+        ctx._adopt(self)
 
     # ------------------------------------------------------------ construction
     @classmethod
@@ -119,6 +154,10 @@ class Graph:
         return int(lib().byo_graph_num_edges(self.h))
 
     num_edges = M
+
+    def nslots(self):
+        """Slots of the traversal view (edges plus the PMA's gaps)."""
+        return int(lib().byo_graph_num_slots(self.h))
 
     @property
     def container(self):
@@ -200,6 +239,7 @@ class vertexSubset:
         self.G = G
         if _handle is not None:
             self.h = _handle
+            G.ctx._adopt(self)
             return
         h = ctypes.c_void_p()
         if isinstance(vertices, (int, np.integer)):
@@ -208,11 +248,15 @@ class vertexSubset:
             ids = np.ascontiguousarray(vertices if vertices is not None else [], np.uint32)
             check(lib().byo_vs_create_list(G.h, _ptr(ids), len(ids), ctypes.byref(h)), G.ctx.h)
         self.h = h
+        G.ctx._adopt(self)
 
-    def __del__(self):
+    def close(self):
         if getattr(self, "h", None):
             lib().byo_vs_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        self.close()
 
     def size(self):
         return int(lib().byo_vs_size(self.h))
@@ -239,11 +283,15 @@ class BFS_F:
         h = ctypes.c_void_p()
         check(lib().byo_functor_bfs_create(G.h, src, ctypes.byref(h)), G.ctx.h)
         self.h = h
+        G.ctx._adopt(self)
 
-    def __del__(self):
+    def close(self):
         if getattr(self, "h", None):
             lib().byo_functor_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        self.close()
 
     def parents(self):
         out = np.empty(self.G.N(), np.uint32)
@@ -259,17 +307,18 @@ def edgeMap(G, vs, F, threshold=-1, flags=0):
 
 # ------------------------------------------------------------ algorithms
 
-def BFS(G, src, policy=_abi.POLICY_M20, levels=False):
+def BFS(G, src, policy=_abi.POLICY_M20, levels=False, out=None):
+    """Parents (and levels); `out` may supply the parents array (e.g. pinned)."""
     n = G.N()
-    par = np.empty(n, np.uint32)
+    par = out if out is not None else np.empty(n, np.uint32)
     lev = np.empty(n, np.uint32) if levels else None
     r = ctypes.c_uint32(0)
     check(lib().byo_bfs(G.h, src, _ptr(par), _ptr(lev), policy, ctypes.byref(r)), G.ctx.h)
     return (par, lev) if levels else par
 
 
-def SimpleUnionAsync(G):
-    out = np.empty(G.N(), np.uint32)
+def SimpleUnionAsync(G, out=None):
+    out = out if out is not None else np.empty(G.N(), np.uint32)
     check(lib().byo_cc(G.h, _ptr(out)), G.ctx.h)
     return out
 
@@ -280,8 +329,8 @@ def bfs_cc(G):
     return out
 
 
-def PageRank(G, eps=1e-6, max_iters=100, precision=_abi.PR_FP32_KAHAN, info=False):
-    p = np.empty(G.N(), np.float64)
+def PageRank(G, eps=1e-6, max_iters=100, precision=_abi.PR_FP32_KAHAN, info=False, out=None):
+    p = out if out is not None else np.empty(G.N(), np.float64)
     it = ctypes.c_uint32(0)
     l1 = ctypes.c_double(0)
     check(lib().byo_pagerank(G.h, eps, max_iters, precision, _ptr(p), ctypes.byref(it),

@@ -81,6 +81,8 @@ int byo_graph_container(const byo_graph *g);
 uint64_t byo_graph_num_vertices(const byo_graph *g);
 /* G.M() / num_edges(): directed entries currently stored (run_csr.cc:32) */
 uint64_t byo_graph_num_edges(const byo_graph *g);
+/* Slots of the traversal view (= num_edges for a CSR; the PMA counts gaps). */
+uint64_t byo_graph_num_slots(const byo_graph *g);
 /* degree(i) for every vertex (run_csr.cc:34-36; Graph::finilize
  * graph.h:2559-2588 for containers without a native degree). */
 int byo_graph_degrees(byo_graph *g, uint32_t *h_out);
@@ -228,6 +230,13 @@ typedef struct byo_round_log {
 int byo_last_rounds(byo_ctx *ctx, byo_round_log *out, uint64_t cap, uint64_t *count);
 /* Times every round with CUDA events (adds one host wait per round). */
 int byo_ctx_set_round_timing(byo_ctx *ctx, int on);
+/* Brackets every launch of the kernels tagged `tag` ("*": all tags, NULL: off)
+ * with CUDA events on the context's stream; byo_ctx_kernel_time sums the
+ * launches of one tag (NULL: all) since the last byo_ctx_kernel_timing call.
+ * Tags: "bfs_push", "bfs_pull", "bfs_blocked", "cc_finish", "pr_pull",
+ * "tc_intersect", "sort_scatter", "pma_merge", "pma_redistribute". */
+int byo_ctx_kernel_timing(byo_ctx *ctx, const char *tag);
+int byo_ctx_kernel_time(byo_ctx *ctx, const char *tag, uint64_t *launches, double *ms);
 
 #ifdef __cplusplus
 }

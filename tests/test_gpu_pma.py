@@ -1,0 +1,122 @@
+"""Packed-memory-array container on the GPU against the oracle's container
+model: contents after every batch (sorted adjacency, bit-exact), the number of
+keys changed, and BFS / CC / PageRank / TC run directly on the PMA."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_view(byo, O, G, ref_off, ref_nb, bfs_src=(0,)):
+    off, nb = G.export_csr()
+    assert np.array_equal(off, ref_off) and np.array_equal(nb, ref_nb)
+    assert G.M() == len(ref_nb)
+    assert np.array_equal(G.degrees(), np.diff(ref_off).astype(np.uint32))
+    for s in bfs_src:
+        opar, olev = O.bfs(ref_off, ref_nb, s)
+        for pol in (0, 2, 3, 4):
+            par, lev = byo.BFS(G, s, policy=pol, levels=True)
+            assert np.array_equal(lev, olev) and np.array_equal(par, opar), (s, pol)
+    assert np.array_equal(byo.SimpleUnionAsync(G), O.cc(ref_off, ref_nb))
+
+
+def test_golden_update_sequence(ctx, golden, oracle_mod):
+    import byo_gb300 as byo
+    u = golden["updates"]
+    G = byo.Graph.from_csr(ctx, np.array(u["offsets"], np.uint64), np.array(u["nbrs"], np.uint32),
+                           container="pma")
+    assert G.container == "pma"
+    for b in u["batches"]:
+        keys = np.array(b["keys"], np.uint64)
+        ch = G.insert_batch(keys) if b["op"] == "insert" else G.remove_batch(keys)
+        assert ch == b["changed"]
+        off, nb = G.export_csr()
+        assert off.tolist() == b["offsets"] and nb.tolist() == b["nbrs"]
+
+
+@pytest.mark.parametrize("lg,draws,batch", [(10, 6000, 500), (13, 1 << 16, 20000), (15, 1 << 18, 300000)])
+def test_random_batches(ctx, oracle_mod, lg, draws, batch):
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 1 << lg
+    G = byo.Graph.generate(ctx, "rmat", seed=lg, lg_n=lg, draws=draws, container="pma")
+    s, d = O.rmat_edges(lg, lg, draws)
+    off, nb = O.build_csr(n, s, d)
+    _check_view(byo, O, G, off, nb, (10,))
+    st = O.Store(off, nb)
+    batches = []
+    for k in range(4):
+        us, ud = O.uniform_pairs(100 + k, n, batch)
+        keys = O.keys_from_pairs(us, ud)            # symmetrised, unsorted, duplicates
+        batches.append(keys)
+        assert G.insert_batch(keys) == st.insert_batch(keys)
+        ro, rn = st.export_csr()
+        _check_view(byo, O, G, ro, rn, (10,))
+    for keys in batches[:3]:
+        assert G.remove_batch(keys) == st.remove_batch(keys)
+        ro, rn = st.export_csr()
+        _check_view(byo, O, G, ro, rn, (10,))
+    ro, rn = st.export_csr()
+    p = byo.PageRank(G, 1e-6, 30)
+    op, _, _ = O.pagerank(ro, rn, 1e-6, 30)
+    assert float(np.abs(p - op).sum()) <= 1e-6
+    assert byo.Triangle_degree_ordering(G) == O.triangle_count(ro, rn)
+
+
+def test_skewed_batch_grows_and_shrinks(ctx, oracle_mod):
+    """One hub receives a batch far larger than a leaf (windows / growth),
+    then everything is removed again (shrink)."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 1 << 14
+    G = byo.Graph.generate(ctx, "rmat", seed=3, lg_n=14, draws=1 << 15, container="pma")
+    s, d = O.rmat_edges(3, 14, 1 << 15)
+    off, nb = O.build_csr(n, s, d)
+    st = O.Store(off, nb)
+    hub = 12345
+    others = np.arange(n, dtype=np.uint64)
+    keys = np.concatenate([(np.uint64(hub) << np.uint64(32)) | others, (others << np.uint64(32)) | np.uint64(hub)])
+    assert G.insert_batch(keys) == st.insert_batch(keys)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (hub, 0))
+    sk = np.sort(np.unique(keys))
+    assert G.remove_batch(sk, sorted=True) == st.remove_batch(sk)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (0,))
+    # remove everything, then re-insert everything
+    all_keys = O.keys_from_pairs(s, d)
+    assert G.remove_batch(all_keys) == st.remove_batch(all_keys)
+    assert G.M() == st.num_edges
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (0,))
+    assert G.insert_batch(all_keys) == st.insert_batch(all_keys)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (10,))
+
+
+def test_small_batches_and_errors(ctx, oracle_mod):
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 1 << 12
+    G = byo.Graph.generate(ctx, "rmat", seed=9, lg_n=12, draws=1 << 14, container="pma")
+    s, d = O.rmat_edges(9, 12, 1 << 14)
+    off, nb = O.build_csr(n, s, d)
+    st = O.Store(off, nb)
+    rng = np.random.default_rng(5)
+    for size in (1, 2, 10, 100, 1000):
+        pairs = rng.integers(0, n, size=(size, 2))
+        keys = (pairs[:, 0].astype(np.uint64) << np.uint64(32)) | pairs[:, 1].astype(np.uint64)
+        assert G.insert_batch(keys) == st.insert_batch(keys)
+        assert G.remove_batch(keys[: size // 2 + 1]) == st.remove_batch(keys[: size // 2 + 1])
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (1,))
+    assert G.insert_batch(np.zeros(0, np.uint64)) == 0
+    with pytest.raises(byo.ByoError) as e:
+        G.insert_batch(np.array([(5 << 32) | n], np.uint64))
+    assert e.value.code == byo._abi.BYO_EINVAL
+    with pytest.raises(byo.ByoError) as e:
+        G.insert_batch(np.array([(5 << 32) | 7, (5 << 32) | 3], np.uint64), sorted=True)
+    assert e.value.code == byo._abi.BYO_EINVAL
+    # the container is unchanged by rejected batches
+    o2, n2 = G.export_csr()
+    assert np.array_equal(o2, ro) and np.array_equal(n2, rn)
