@@ -315,14 +315,20 @@ __device__ __forceinline__ T group_total(T s, T c) {
 }
 
 // ---------------------------------------------------------------- PageRank plan
-// Vertices are split by slot-range length: light (<= kPrLightMax) vertices are
-// packed into tiles of consecutive ids whose ranges total about kPrTile slots;
-// medium vertices get a warp each, hubs (> kPrHubMin) a CTA each.  A tile
-// never spans a heavier vertex, so its slots are one contiguous run.
-constexpr int kPrTile = 4096;
-constexpr uint32_t kPrLightMax = 512;
-constexpr uint32_t kPrHubMin = 16384;
+// Work units of at most kPrTile + kPrLightMax slots, all processed by one
+// kernel so every CTA streams the same amount:
+//   light tile   consecutive vertices with runs <= kPrLightMax; one run of
+//                slots; per-vertex sums written directly
+//   heavy chunk  kPrTile consecutive slots of one heavier vertex; its
+//                compensated partial goes to part[chunk] and k_pr_combine sums
+//                a vertex's chunks in order
+// A unit's p_div values are gathered into shared memory with 4/8-byte
+// cp.async copies (no registers held per gather), double-buffered so the next
+// unit's gathers are in flight while this one is reduced.
+constexpr int kPrTile = 512;            // slots per warp tile / heavy chunk
+constexpr uint32_t kPrLightMax = 128;   // longest run of a light vertex
 constexpr int kPrBlock = 256;
+constexpr int kPrStage = kPrTile + kPrLightMax;  // staged values per warp
 
 struct InLightLen {
   const uint64_t *off;
@@ -350,19 +356,120 @@ struct OutTileStart {
     if (f) starts[pre] = (uint32_t)v;
   }
 };
+// heavy vertices and their chunk counts
+struct InHeavy {
+  const uint64_t *off;
+  __device__ uint64_t operator()(uint64_t v) const { return off[v + 1] - off[v] > kPrLightMax ? 1 : 0; }
+};
+struct OutHeavy {
+  uint32_t *heavy;
+  __device__ void operator()(uint64_t v, uint64_t pre, uint64_t f) const {
+    if (f) heavy[pre] = (uint32_t)v;
+  }
+};
+struct InChunks {
+  const uint64_t *off;
+  const uint32_t *heavy;
+  __device__ uint64_t operator()(uint64_t h) const {
+    uint32_t v = heavy[h];
+    return (off[v + 1] - off[v] + kPrTile - 1) / kPrTile;
+  }
+};
 
-__global__ void k_pr_heavy_lists(const uint64_t *__restrict__ off, uint64_t n, uint32_t *med,
-                                 unsigned long long *nmed, uint32_t *hubs, unsigned long long *nhub) {
-  // warp-uniform trip count: every lane reaches warp_append
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n; base += stride) {
-    const uint64_t v = base + lane_id();
-    uint64_t len = v < n ? off[v + 1] - off[v] : 0;
-    bool m = len > kPrLightMax && len <= kPrHubMin, h = len > kPrHubMin;
-    uint64_t sm = warp_append(m, nmed);
-    if (m) med[sm] = (uint32_t)v;
-    uint64_t sh = warp_append(h, nhub);
-    if (h) hubs[sh] = (uint32_t)v;
+template <typename T>
+__device__ __forceinline__ void cp_async_gather(T *dst_smem, const T *src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst_smem);
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// ---- TMA bulk copy of a unit's slot ids into shared memory (mbarrier
+// completion); waits are bounded and report through *err.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)));
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+}
+__device__ __forceinline__ void tma_ids(uint32_t *dst, const uint32_t *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes));
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// true when the phase completed within the spin budget
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
+  const unsigned a = smem_u32(bar);
+  for (uint32_t it = 0; it < (1u << 24); it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Unit descriptor (built once per PageRank call): slot range and either a
+// light tile's vertices [v0, v1) or a heavy chunk (v1 == kNoVertex).
+struct PrDesc {
+  uint64_t s0, s1;
+  uint32_t v0, v1;
+  uint32_t chunk, pad;
+};
+constexpr uint32_t kNoVertex = 0xFFFFFFFFu;
+
+// light tiles that are not a lone heavy vertex
+struct InLightTile {
+  const uint64_t *off;
+  const uint32_t *tstart;
+  __device__ uint64_t operator()(uint64_t t) const {
+    uint32_t v0 = tstart[t], v1 = tstart[t + 1];
+    return (v1 - v0 == 1 && off[v1] - off[v0] > kPrLightMax) ? 0 : 1;
+  }
+};
+struct OutLightTile {
+  const uint64_t *off;
+  const uint32_t *tstart;
+  PrDesc *desc;
+  __device__ void operator()(uint64_t t, uint64_t pre, uint64_t f) const {
+    if (!f) return;
+    PrDesc d;
+    d.v0 = tstart[t];
+    d.v1 = tstart[t + 1];
+    d.s0 = off[d.v0];
+    d.s1 = off[d.v1];
+    d.chunk = 0;
+    d.pad = 0;
+    desc[pre] = d;
+  }
+};
+
+__global__ void k_pr_desc_chunks(const uint64_t *__restrict__ off, const uint32_t *__restrict__ heavy,
+                                 const uint64_t *__restrict__ cbase, uint64_t nheavy, uint64_t base, PrDesc *desc) {
+  for (uint64_t h = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; h < nheavy;
+       h += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = heavy[h];
+    const uint64_t b = off[v], e = off[v + 1];
+    for (uint64_t k = 0; k < cbase[h + 1] - cbase[h]; k++) {
+      PrDesc d;
+      d.s0 = b + k * kPrTile;
+      d.s1 = d.s0 + kPrTile < e ? d.s0 + kPrTile : e;
+      d.v0 = v;
+      d.v1 = kNoVertex;
+      d.chunk = (uint32_t)(cbase[h] + k);
+      d.pad = 0;
+      desc[base + cbase[h] + k] = d;
+    }
   }
 }
 
@@ -376,129 +483,102 @@ __device__ __forceinline__ void pr_finish(uint64_t v, T tot, const uint32_t *__r
   l1loc += fabs((double)p_curr[v] - (double)p);
 }
 
-// One CTA per light tile: stage p_div[u] of the tile's slots in shared memory
-// (coalesced id loads, four independent gathers per thread in flight), then
-// one thread per vertex sums its run left to right.
+// One warp per unit, no block-wide barriers: the warp gathers p_div of the
+// unit's slots (16 independent loads per lane in flight) into its own stage in
+// shared memory, then reduces.  Light tile: runs of <= 32 one lane each, longer
+// runs (found by ballot) one warp each.  Heavy chunk: warp partial to part[].
 template <bool kComp, typename T>
-__global__ void __launch_bounds__(kPrBlock) k_pr_tiles(const uint64_t *__restrict__ off,
+__global__ void __launch_bounds__(kPrBlock) k_pr_units(const uint64_t *__restrict__ off,
                                                        const uint32_t *__restrict__ slots,
                                                        const uint32_t *__restrict__ deg,
-                                                       const uint32_t *__restrict__ tstart, uint64_t ntiles,
-                                                       const T *__restrict__ pdiv_in,
-                                                       const T *__restrict__ p_curr, T *__restrict__ p_next,
-                                                       T *__restrict__ pdiv_out, T damping, T added, double *l1) {
-  __shared__ T vals[kPrTile + kPrLightMax];
+                                                       const PrDesc *__restrict__ desc, uint64_t nunits,
+                                                       const T *__restrict__ pdiv_in, const T *__restrict__ p_curr,
+                                                       T *__restrict__ p_next, T *__restrict__ pdiv_out,
+                                                       T *__restrict__ part, T damping, T added, double *l1) {
+  __shared__ T stage[kPrBlock / 32][kPrStage];
   __shared__ double sm[kPrBlock / 32 + 1];
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  T *buf = stage[warp];
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   double l1loc = 0.0;
-  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const uint32_t v0 = tstart[t], v1 = tstart[t + 1];
-    const uint64_t s0 = off[v0], s1 = off[v1];
-    if (v1 - v0 == 1 && s1 - s0 > kPrLightMax) continue;  // a heavy vertex: its own kernel
-    const uint32_t len = (uint32_t)(s1 - s0);
-    for (uint32_t i = threadIdx.x; i < len; i += 4 * kPrBlock) {
-      uint32_t u[4];
+  for (uint64_t t = gw; t < nunits; t += nw) {
+    const PrDesc d = desc[t];
+    const uint32_t len = (uint32_t)(d.s1 - d.s0);
+    const uint32_t *id = slots + d.s0;
+    for (uint32_t i = lane; i < len; i += 32 * 16) {
+      uint32_t u[16];
 #pragma unroll
-      for (int k = 0; k < 4; k++) {
-        uint32_t idx = i + k * kPrBlock;
-        u[k] = idx < len ? __ldcs(slots + s0 + idx) : kSentinel;
-      }
-      T g[4];
+      for (int q = 0; q < 16; q++) u[q] = i + 32 * q < len ? __ldcs(id + i + 32 * q) : kSentinel;
 #pragma unroll
-      for (int k = 0; k < 4; k++) g[k] = u[k] != kSentinel ? pdiv_in[u[k]] : T(0);
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        uint32_t idx = i + k * kPrBlock;
-        if (idx < len) vals[idx] = g[k];
-      }
+      for (int q = 0; q < 16; q++)
+        if (i + 32 * q < len) buf[i + 32 * q] = u[q] != kSentinel ? __ldg(pdiv_in + u[q]) : T(0);
     }
-    __syncthreads();
-    for (uint32_t v = v0 + threadIdx.x; v < v1; v += kPrBlock) {
-      const uint32_t r0 = (uint32_t)(off[v] - s0), r1 = (uint32_t)(off[v + 1] - s0);
+    __syncwarp();
+    if (d.v1 != kNoVertex) {
+      for (uint32_t x0 = d.v0; x0 < d.v1; x0 += 32) {
+        const uint32_t x = x0 + lane;
+        uint32_t r0 = 0, r1 = 0;
+        if (x < d.v1) {
+          r0 = (uint32_t)(off[x] - d.s0);
+          r1 = (uint32_t)(off[x + 1] - d.s0);
+        }
+        const bool lng = r1 - r0 > 32;
+        if (x < d.v1 && !lng) {
+          T s = T(0), c = T(0);
+          for (uint32_t r = r0; r < r1; r++) acc_add<kComp>(s, c, buf[r]);
+          pr_finish<kComp, T>(x, kComp ? s + c : s, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+        }
+        unsigned m = __ballot_sync(kFull, lng);
+        while (m) {
+          const int src = __ffs(m) - 1;
+          m &= m - 1;
+          const uint32_t q0 = __shfl_sync(kFull, r0, src), q1 = __shfl_sync(kFull, r1, src);
+          T s = T(0), c = T(0);
+          for (uint32_t r = q0 + lane; r < q1; r += 32) acc_add<kComp>(s, c, buf[r]);
+          T tot = group_total<kComp, T, 32>(s, c);
+          if (lane == 0) pr_finish<kComp, T>(x0 + src, tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+        }
+      }
+    } else {
       T s = T(0), c = T(0);
-      for (uint32_t r = r0; r < r1; r++) acc_add<kComp>(s, c, vals[r]);
-      pr_finish<kComp, T>(v, kComp ? s + c : s, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+      for (uint32_t r = lane; r < len; r += 32) acc_add<kComp>(s, c, buf[r]);
+      T tot = group_total<kComp, T, 32>(s, c);
+      if (lane == 0) {
+        part[2 * (uint64_t)d.chunk] = tot;
+        part[2 * (uint64_t)d.chunk + 1] = T(0);
+      }
     }
-    __syncthreads();
+    __syncwarp();
   }
   l1loc = block_sum(l1loc, sm);
   if (threadIdx.x == 0 && l1loc != 0.0) atomicAdd(l1, l1loc);
 }
 
-// One warp per medium vertex; four independent loads per lane in flight.
+// One warp per heavy vertex: its chunk partials in chunk order.
 template <bool kComp, typename T>
-__global__ void __launch_bounds__(256) k_pr_medium(const uint64_t *__restrict__ off,
-                                                   const uint32_t *__restrict__ slots,
-                                                   const uint32_t *__restrict__ deg,
-                                                   const uint32_t *__restrict__ med,
-                                                   const unsigned long long *__restrict__ nmed,
-                                                   const T *__restrict__ pdiv_in,
-                                                   const T *__restrict__ p_curr, T *__restrict__ p_next,
-                                                   T *__restrict__ pdiv_out, T damping, T added, double *l1) {
+__global__ void __launch_bounds__(256) k_pr_combine(const uint32_t *__restrict__ heavy,
+                                                    const uint64_t *__restrict__ cbase, uint64_t nheavy,
+                                                    const T *__restrict__ part, const uint32_t *__restrict__ deg,
+                                                    const T *__restrict__ p_curr, T *__restrict__ p_next,
+                                                    T *__restrict__ pdiv_out, T damping, T added, double *l1) {
   __shared__ double sm[9];
-  const uint64_t nm = *nmed;
   const unsigned lane = lane_id();
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   double l1loc = 0.0;
-  for (uint64_t h = gw; h < nm; h += nw) {
-    const uint32_t v = med[h];
-    const uint64_t b = off[v], e = off[v + 1];
+  for (uint64_t h = gw; h < nheavy; h += nw) {
+    const uint64_t c0 = cbase[h], c1 = cbase[h + 1];
     T s = T(0), c = T(0);
-    for (uint64_t j = b + lane; j < e; j += 128) {
-      uint32_t u[4];
-#pragma unroll
-      for (int k = 0; k < 4; k++) u[k] = j + 32 * k < e ? __ldcs(slots + j + 32 * k) : kSentinel;
-      T g[4];
-#pragma unroll
-      for (int k = 0; k < 4; k++) g[k] = u[k] != kSentinel ? pdiv_in[u[k]] : T(0);
-#pragma unroll
-      for (int k = 0; k < 4; k++) acc_add<kComp>(s, c, g[k]);
+    for (uint64_t k = c0 + lane; k < c1; k += 32) {
+      acc_add<kComp>(s, c, part[2 * k]);
+      if (kComp) c += part[2 * k + 1];
     }
     T tot = group_total<kComp, T, 32>(s, c);
-    if (lane == 0) pr_finish<kComp, T>(v, tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+    if (lane == 0) pr_finish<kComp, T>(heavy[h], tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
   }
   l1loc = block_sum(l1loc, sm);
   if (threadIdx.x == 0 && l1loc != 0.0) atomicAdd(l1, l1loc);
-}
-
-// One CTA per hub; warp partials combined in warp order.
-template <bool kComp, typename T>
-__global__ void __launch_bounds__(256) k_pr_hubs(const uint64_t *__restrict__ off,
-                                                 const uint32_t *__restrict__ slots,
-                                                 const uint32_t *__restrict__ deg,
-                                                 const uint32_t *__restrict__ hubs,
-                                                 const unsigned long long *__restrict__ nhub,
-                                                 const T *__restrict__ pdiv_in,
-                                                 const T *__restrict__ p_curr, T *__restrict__ p_next,
-                                                 T *__restrict__ pdiv_out, T damping, T added, double *l1) {
-  __shared__ T ss[8];
-  const uint64_t nh = *nhub;
-  for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
-    const uint32_t v = hubs[h];
-    const uint64_t b = off[v], e = off[v + 1];
-    T s = T(0), c = T(0);
-    for (uint64_t j = b + threadIdx.x; j < e; j += 4 * blockDim.x) {
-      uint32_t u[4];
-#pragma unroll
-      for (int k = 0; k < 4; k++) u[k] = j + blockDim.x * k < e ? __ldcs(slots + j + blockDim.x * k) : kSentinel;
-      T g[4];
-#pragma unroll
-      for (int k = 0; k < 4; k++) g[k] = u[k] != kSentinel ? pdiv_in[u[k]] : T(0);
-#pragma unroll
-      for (int k = 0; k < 4; k++) acc_add<kComp>(s, c, g[k]);
-    }
-    T tot = group_total<kComp, T, 32>(s, c);
-    if (lane_id() == 0) ss[threadIdx.x >> 5] = tot;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      T S = T(0), C = T(0);
-      for (int w = 0; w < (int)(blockDim.x >> 5); w++) acc_add<kComp>(S, C, ss[w]);
-      double l1loc = 0.0;
-      pr_finish<kComp, T>(v, kComp ? S + C : S, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
-      atomicAdd(l1, l1loc);
-    }
-    __syncthreads();
-  }
 }
 
 template <typename T>
@@ -523,57 +603,69 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   byo_ctx *ctx = g->ctx;
   const uint64_t n = g->n;
   T *pa, *pb, *da, *db;
-  BYO_TRY(ws(g, WS_PR_A, n, &pa));
+  BYO_TRY(ws(g, WS_PR_A, n + 2, &pa));
   BYO_TRY(ws(g, WS_PR_B, n, &pb));
   BYO_TRY(ws(g, WS_PR_C, n, &da));
   BYO_TRY(ws(g, WS_PR_D, n, &db));
-  // plan: light prefix, tile starts, medium and hub lists
+  // plan
   uint64_t *pre = nullptr;
   uint32_t *lists = nullptr;
-  BYO_TRY(ws(g, WS_SCAN, n + 1, &pre));
-  BYO_TRY(ws(g, WS_BUCKETS, 3 * n + 16, &lists));
-  uint32_t *tstart = lists, *med = lists + (n + 2), *hubs = lists + 2 * (n + 2);
-  unsigned long long *cnt = (unsigned long long *)(lists + 3 * n + 8 - ((3 * n + 8) & 1));
+  BYO_TRY(ws(g, WS_SCAN, 2 * n + 4, &pre));
+  uint64_t *cbase = pre + n + 2;
+  BYO_TRY(ws(g, WS_BUCKETS, 2 * n + 8, &lists));
+  uint32_t *tstart = lists, *heavy = lists + (n + 4);
   double *d_l1 = nullptr;
   BYO_TRY(ws(g, WS_MISC, 4, (uint32_t **)&d_l1));
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
   const uint64_t *tot = nullptr;
   BYO_TRY(scan_apply(ctx, n, InLightLen{g->d_off}, OutPrefix{pre}, &tot));
   BYO_TRY(scan_apply(ctx, n, InTileStart{g->d_off, pre}, OutTileStart{tstart}, &tot));
-  uint64_t *h = nullptr;
-  BYO_TRY(pinned(ctx, 4096, (void **)&h));
   BYO_CU(ctx, cudaMemcpyAsync(h, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaMemsetAsync(cnt, 0, 16, ctx->stream));
-  launch(ctx, k_pr_heavy_lists, dim3(grid_for(ctx, n + 31, 256)), dim3(256), 0, (const uint64_t *)g->d_off, n,
-         med, cnt, hubs, cnt + 1);
+  BYO_TRY(scan_apply(ctx, n, InHeavy{g->d_off}, OutHeavy{heavy}, &tot));
+  BYO_CU(ctx, cudaMemcpyAsync(h + 1, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const uint64_t ntiles = h[0], nheavy = h[1];
+  BYO_TRY(scan_apply(ctx, nheavy, InChunks{g->d_off, heavy}, OutPrefix{cbase}, &tot));
+  BYO_CU(ctx, cudaMemcpyAsync(cbase + nheavy, tot, 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  BYO_CU(ctx, cudaMemcpyAsync(h + 2, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  h[3] = n;
+  BYO_CU(ctx, cudaMemcpyAsync(tstart + ntiles, h + 3, 4, cudaMemcpyHostToDevice, ctx->stream));
   launch(ctx, k_pr_init<T>, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint32_t *)g->d_deg, n, pa, da,
          (T)(1.0 / (double)n));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const uint64_t ntiles = h[0];
-  uint32_t nn = (uint32_t)n;
-  BYO_CU(ctx, cudaMemcpyAsync(tstart + ntiles, &nn, 4, cudaMemcpyHostToDevice, ctx->stream));
+  const uint64_t nchunks = h[2];
+  // descriptors: compacted light tiles, then heavy chunks
+  PrDesc *desc = nullptr;
+  BYO_TRY(ws(g, WS_TC_NBR, (ntiles + nchunks + 1) * sizeof(PrDesc) / 4, (uint32_t **)&desc));
+  BYO_TRY(scan_apply(ctx, ntiles, InLightTile{g->d_off, tstart}, OutLightTile{g->d_off, tstart, desc}, &tot));
+  BYO_CU(ctx, cudaMemcpyAsync(h + 4, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const uint64_t nlight = h[4];
+  if (nheavy)
+    launch(ctx, k_pr_desc_chunks, dim3(grid_for(ctx, nheavy, 256)), dim3(256), 0, (const uint64_t *)g->d_off,
+           (const uint32_t *)heavy, (const uint64_t *)cbase, nheavy, nlight, desc);
+  const uint64_t nunits = nlight + nchunks;
+  T *part = nullptr;
+  BYO_TRY(ws(g, WS_TC_CNT, 2 * nchunks + 2, &part));
   const T damping = (T)0.85;
   const T added = (T)((1 - 0.85) * (1 / (double)n));
-  const int grid_t = grid_for(ctx, ntiles, 1, 8);
-  const int grid_m = ctx->num_sms * 8;
-  const int grid_h = ctx->num_sms * 2;
+  const int grid_c = grid_for(ctx, nheavy * 32, 256, 8);
+  const int grid_u = grid_for(ctx, nunits * 32, kPrBlock, sizeof(T) == 4 ? 5 : 3);
   uint32_t it = 0;
   double L1 = 0.0;
   T *p_curr = pa, *p_next = pb, *pdiv = da, *pdiv_next = db, *last = nullptr;
   double *hl = (double *)h;
   while (it++ < max_iters) {
-    BYO_CU(ctx, cudaMemsetAsync(d_l1, 0, 8, ctx->stream));
-    launch_t(ctx, "pr_pull", k_pr_tiles<kComp, T>, dim3(grid_t), dim3(kPrBlock), 0, (const uint64_t *)g->d_off,
-             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)tstart, ntiles,
-             (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next, damping, added, d_l1);
-    launch_t(ctx, "pr_pull", k_pr_medium<kComp, T>, dim3(grid_m), dim3(256), 0, (const uint64_t *)g->d_off,
-             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)med,
-             (const unsigned long long *)cnt, (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next, damping,
-             added, d_l1);
-    launch_t(ctx, "pr_pull", k_pr_hubs<kComp, T>, dim3(grid_h), dim3(256), 0, (const uint64_t *)g->d_off,
-             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)hubs,
-             (const unsigned long long *)(cnt + 1), (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next,
-             damping, added, d_l1);
-    BYO_CU(ctx, cudaMemcpyAsync(hl, d_l1, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaMemsetAsync(d_l1, 0, 16, ctx->stream));
+    launch_t(ctx, "pr_pull", k_pr_units<kComp, T>, dim3(grid_u), dim3(kPrBlock), 0, (const uint64_t *)g->d_off,
+             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const PrDesc *)desc, nunits,
+             (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next, part, damping, added, d_l1);
+    if (nheavy)
+      launch_t(ctx, "pr_pull", k_pr_combine<kComp, T>, dim3(grid_c), dim3(256), 0, (const uint32_t *)heavy,
+               (const uint64_t *)cbase, nheavy, (const T *)part, (const uint32_t *)g->d_deg, (const T *)p_curr,
+               p_next, pdiv_next, damping, added, d_l1);
+    BYO_CU(ctx, cudaMemcpyAsync(hl, d_l1, 16, cudaMemcpyDeviceToHost, ctx->stream));
     BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
     L1 = hl[0];
     std::swap(pdiv, pdiv_next);

@@ -212,7 +212,8 @@ int graph_from_sorted_keys(byo_ctx *ctx, int container, uint64_t n, const uint64
     if (container == BYO_CONTAINER_PMA) {
       rc = pma_build(g, d_keys, m);
     } else {
-      cudaError_t e = cudaMalloc(&g->d_slots, (m ? m : 1) * sizeof(uint32_t));
+      // 16 ids of padding: bulk copies of a slot run round its end up to 16 bytes
+      cudaError_t e = cudaMalloc(&g->d_slots, (m + 16) * sizeof(uint32_t));
       if (e != cudaSuccess) rc = set_error(ctx, BYO_ENOMEM, "cudaMalloc slots", e);
       g->nslots = m;
       if (rc == BYO_OK) rc = offsets_from_keys(ctx, d_keys, m, n, g->d_off);
