@@ -1,0 +1,239 @@
+// byo_gpu_graph.hpp -- C++ container adapters over the byo_gpu C ABI, in the
+// shape BYO's gbbs::Graph<Rep, symmetric, API> consumes
+// (gbbs/graph.h:2154-2421), so that a benchmarks/run_structures target can
+// put a GB300-resident graph where run_csr.cc / run_single_pma.cc put theirs.
+//
+//   GPU_CSR            replaces CSR<node_t, edge_t>   (run_csr.cc:28-175)
+//   GPU_PMA_graph<W>   replaces PMA_graph<W>          (run_single_pma.cc:39-141)
+//
+// Both expose the container concept: num_vertices()/N(), num_edges(),
+// degree(i), map_neighbors(i, f), map_neighbors_early_exit(i, f),
+// parallel_map_neighbors(i, f), parallel_map_neighbors_early_exit(i, f), the
+// loader constructor Rep(v_data, n, m, deleter, edges) and, for the PMA,
+// insert_sorted_batch / remove_sorted_batch(std::tuple<uint32_t,uint32_t>*, n).
+// Neighbour maps run on the host over a mirror of the device adjacency that is
+// refreshed after every update, so any GBBS algorithm still works; the hot
+// algorithms run on the GPU through the free functions gpu_bfs, gpu_cc,
+// gpu_pagerank and gpu_triangle_count.
+//
+// Errors from the C ABI throw byo::Error (the reference aborts instead).
+#pragma once
+
+#include <cstdint>
+#include <functional>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "byo_gpu.h"
+
+namespace byo {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+// One process-wide context per device (the reference drives its graph from
+// one host thread as well).
+class Context {
+ public:
+  static Context &get(int device = 0) {
+    static Context c(device);
+    return c;
+  }
+  byo_ctx *h() const { return ctx_; }
+  void check(int rc, const char *what) const {
+    if (rc != BYO_OK) throw Error(rc, std::string(what) + ": " + byo_last_error(ctx_));
+  }
+  ~Context() {
+    if (ctx_) byo_gpu_shutdown(ctx_);
+  }
+
+ private:
+  explicit Context(int device) {
+    int rc = byo_gpu_init(device, &ctx_);
+    if (rc != BYO_OK) throw Error(rc, "byo_gpu_init failed");
+  }
+  byo_ctx *ctx_ = nullptr;
+};
+
+namespace detail {
+
+// Shared body of both adapters: the device graph plus a host mirror.
+class DeviceGraph {
+ public:
+  using weight_type = struct empty_w {};
+
+  DeviceGraph() = default;
+  DeviceGraph(int container, const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m) {
+    Context &c = Context::get();
+    int rc = container == BYO_CONTAINER_PMA ? byo_graph_create_pma(c.h(), n, m, off, nbrs, &g_)
+                                            : byo_graph_create_csr(c.h(), n, m, off, nbrs, &g_);
+    c.check(rc, "create graph");
+    refresh();
+  }
+  DeviceGraph(const DeviceGraph &) = delete;
+  DeviceGraph &operator=(const DeviceGraph &) = delete;
+  DeviceGraph(DeviceGraph &&o) noexcept { *this = std::move(o); }
+  DeviceGraph &operator=(DeviceGraph &&o) noexcept {
+    std::swap(g_, o.g_);
+    off_.swap(o.off_);
+    nbrs_.swap(o.nbrs_);
+    return *this;
+  }
+  ~DeviceGraph() {
+    if (g_) byo_graph_destroy(g_);
+  }
+
+  byo_graph *handle() const { return g_; }
+  size_t num_vertices() const { return byo_graph_num_vertices(g_); }
+  size_t N() const { return num_vertices(); }
+  size_t num_edges() const { return byo_graph_num_edges(g_); }
+  size_t degree(size_t i) const { return off_[i + 1] - off_[i]; }
+
+  template <class F>
+  void map_neighbors(size_t i, F f) const {
+    weight_type w{};
+    for (uint64_t j = off_[i]; j < off_[i + 1]; j++) f(i, nbrs_[j], w);
+  }
+  template <class F>
+  void map_neighbors_early_exit(size_t i, F f) const {
+    weight_type w{};
+    for (uint64_t j = off_[i]; j < off_[i + 1]; j++)
+      if (f(i, nbrs_[j], w)) break;
+  }
+  template <class F>
+  void parallel_map_neighbors(size_t i, F f) const {
+    map_neighbors(i, f);
+  }
+  template <class F, typename Block_F = std::nullptr_t>
+  void parallel_map_neighbors_early_exit(size_t i, F f, Block_F = {}) const {
+    map_neighbors_early_exit(i, f);
+  }
+
+  // device-side views of the mirror refresh
+  void refresh() {
+    off_.assign(num_vertices() + 1, 0);
+    nbrs_.assign(num_edges() ? num_edges() : 1, 0);
+    Context::get().check(byo_graph_export_csr(g_, off_.data(), nbrs_.data()), "export adjacency");
+  }
+  const std::vector<uint64_t> &offsets() const { return off_; }
+  const std::vector<uint32_t> &edges() const { return nbrs_; }
+
+ protected:
+  byo_graph *g_ = nullptr;
+  std::vector<uint64_t> off_;
+  std::vector<uint32_t> nbrs_;
+};
+
+template <class VData, class Edge>
+void loader_csr(const VData *v_data, size_t n, const Edge *e0, std::vector<uint64_t> &off,
+                std::vector<uint32_t> &nbrs) {
+  off.assign(n + 1, 0);
+  for (size_t i = 0; i < n; i++) off[i + 1] = off[i] + v_data[i].degree;
+  nbrs.resize(off[n]);
+  for (size_t i = 0; i < n; i++)
+    for (size_t j = 0; j < v_data[i].degree; j++) nbrs[off[i] + j] = std::get<0>(e0[v_data[i].offset + j]);
+}
+
+}  // namespace detail
+
+// Static CSR on the GPU (run_csr.cc:28-175).
+class GPU_CSR : public detail::DeviceGraph {
+ public:
+  using vertex_weight_type = double;
+  GPU_CSR() = default;
+  GPU_CSR(const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m)
+      : DeviceGraph(BYO_CONTAINER_CSR, off, nbrs, n, m) {}
+  // the loader constructor of run_csr.cc:87-106
+  template <class VData, class Edge>
+  GPU_CSR(VData *v_data, size_t n, size_t, std::function<void()> deletion_fn, Edge *e0,
+          vertex_weight_type * = nullptr) {
+    std::vector<uint64_t> off;
+    std::vector<uint32_t> nbrs;
+    detail::loader_csr(v_data, n, e0, off, nbrs);
+    static_cast<DeviceGraph &>(*this) = DeviceGraph(BYO_CONTAINER_CSR, off.data(), nbrs.data(), n, nbrs.size());
+    if (deletion_fn) deletion_fn();
+  }
+};
+
+// Packed-memory-array graph on the GPU (run_single_pma.cc:39-141).
+template <class W>
+class GPU_PMA_graph : public detail::DeviceGraph {
+ public:
+  using vertex_weight_type = double;
+  using edge_type = std::tuple<uint32_t, W>;
+  GPU_PMA_graph() = default;
+  GPU_PMA_graph(const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m)
+      : DeviceGraph(BYO_CONTAINER_PMA, off, nbrs, n, m) {}
+  template <class VData, class Edge>
+  GPU_PMA_graph(VData *v_data, size_t n, size_t, std::function<void()> deletion_fn, Edge *e0,
+                vertex_weight_type * = nullptr) {
+    std::vector<uint64_t> off;
+    std::vector<uint32_t> nbrs;
+    detail::loader_csr(v_data, n, e0, off, nbrs);
+    static_cast<DeviceGraph &>(*this) = DeviceGraph(BYO_CONTAINER_PMA, off.data(), nbrs.data(), n, nbrs.size());
+    if (deletion_fn) deletion_fn();
+  }
+
+  // PMA_graph::insert_sorted_batch / remove_sorted_batch: the tuple array is
+  // read as uint64 (src << 32 | dst) keys, as the reference bit_casts it.
+  void insert_sorted_batch(std::tuple<uint32_t, uint32_t> *es, size_t n) { update(es, n, true); }
+  void remove_sorted_batch(std::tuple<uint32_t, uint32_t> *es, size_t n) { update(es, n, false); }
+  // Graph::insert_batch / remove_batch with unsorted, duplicated input
+  void insert_batch(std::tuple<uint32_t, uint32_t> *es, size_t n) { update_unsorted(es, n, true); }
+  void remove_batch(std::tuple<uint32_t, uint32_t> *es, size_t n) { update_unsorted(es, n, false); }
+
+ private:
+  static std::vector<uint64_t> keys_of(const std::tuple<uint32_t, uint32_t> *es, size_t n) {
+    std::vector<uint64_t> k(n);
+    for (size_t i = 0; i < n; i++) k[i] = ((uint64_t)std::get<0>(es[i]) << 32) | std::get<1>(es[i]);
+    return k;
+  }
+  void update(const std::tuple<uint32_t, uint32_t> *es, size_t n, bool ins) {
+    std::vector<uint64_t> k = keys_of(es, n);
+    int rc = ins ? byo_graph_insert_batch(g_, k.data(), n, 1, nullptr)
+                 : byo_graph_remove_batch(g_, k.data(), n, 1, nullptr);
+    Context::get().check(rc, ins ? "insert_sorted_batch" : "remove_sorted_batch");
+    refresh();
+  }
+  void update_unsorted(const std::tuple<uint32_t, uint32_t> *es, size_t n, bool ins) {
+    std::vector<uint64_t> k = keys_of(es, n);
+    int rc = ins ? byo_graph_insert_batch(g_, k.data(), n, 0, nullptr)
+                 : byo_graph_remove_batch(g_, k.data(), n, 0, nullptr);
+    Context::get().check(rc, ins ? "insert_batch" : "remove_batch");
+    refresh();
+  }
+};
+
+// ---------------------------------------------------------------- GPU algorithms
+// BFS (BFS.h:47-64): Parents with UINT_E_MAX for unreached, parent[src] = src.
+inline std::vector<uint32_t> gpu_bfs(const detail::DeviceGraph &G, uint32_t src, int policy = BYO_POLICY_M20) {
+  std::vector<uint32_t> parents(G.num_vertices());
+  Context::get().check(byo_bfs(G.handle(), src, parents.data(), nullptr, policy, nullptr), "bfs");
+  return parents;
+}
+// SimpleUnionAsync (Connectivity.h:122-136): minimum vertex id per component.
+inline std::vector<uint32_t> gpu_cc(const detail::DeviceGraph &G) {
+  std::vector<uint32_t> label(G.num_vertices());
+  Context::get().check(byo_cc(G.handle(), label.data()), "cc");
+  return label;
+}
+// PageRank (PageRank.h:125-193).
+inline std::vector<double> gpu_pagerank(const detail::DeviceGraph &G, double eps = 1e-6, uint32_t iters = 100,
+                                        int precision = BYO_PR_FP32_KAHAN) {
+  std::vector<double> p(G.num_vertices());
+  Context::get().check(byo_pagerank(G.handle(), eps, iters, precision, p.data(), nullptr, nullptr), "pagerank");
+  return p;
+}
+// Triangle_degree_ordering (Triangle.h:167-204).
+inline uint64_t gpu_triangle_count(const detail::DeviceGraph &G) {
+  uint64_t c = 0;
+  Context::get().check(byo_triangle_count(G.handle(), &c), "triangle_count");
+  return c;
+}
+
+}  // namespace byo

@@ -1,0 +1,72 @@
+// Exercises include/byo_gpu_graph.hpp the way a benchmarks/run_structures
+// target would: the loader's (vertex_data, edges) arrays into GPU_CSR and
+// GPU_PMA_graph, the container concept, batch updates and the GPU algorithms.
+// Graph: test_bfs.cc:26-50 (0-1, 2-3, 3-4, 3-5, 4-5, 5-6).
+#include <cstdio>
+#include <cstdlib>
+#include <tuple>
+#include <vector>
+
+#include "byo_gpu_graph.hpp"
+
+struct vertex_data {
+  uint64_t offset;
+  uint64_t degree;
+};
+
+#define CHECK(c)                                              \
+  do {                                                        \
+    if (!(c)) {                                               \
+      std::fprintf(stderr, "check failed line %d: %s\n", __LINE__, #c); \
+      return 1;                                               \
+    }                                                         \
+  } while (0)
+
+int main() {
+  const size_t n = 7;
+  std::vector<std::vector<uint32_t>> adj = {{1}, {0}, {3}, {2, 4, 5}, {3, 5}, {3, 4, 6}, {5}};
+  std::vector<vertex_data> vd(n);
+  std::vector<std::tuple<uint32_t, int>> edges;
+  for (size_t v = 0; v < n; v++) {
+    vd[v] = {edges.size(), adj[v].size()};
+    for (uint32_t u : adj[v]) edges.emplace_back(u, 0);
+  }
+  bool deleted = false;
+  byo::GPU_CSR csr(vd.data(), n, edges.size(), [&] { deleted = true; }, edges.data());
+  CHECK(deleted);
+  CHECK(csr.num_vertices() == 7 && csr.num_edges() == 12);
+  CHECK(csr.degree(3) == 3 && csr.degree(6) == 1);
+  std::vector<uint32_t> seen;
+  csr.map_neighbors(5, [&](size_t, uint32_t u, auto) { seen.push_back(u); });
+  CHECK((seen == std::vector<uint32_t>{3, 4, 6}));
+  int visits = 0;
+  csr.map_neighbors_early_exit(3, [&](size_t, uint32_t u, auto) { visits++; return u == 4; });
+  CHECK(visits == 2);
+  // BFS(2): parents {NONE, NONE, 2, 2, 3, 3, 5} (canonical min-id parents)
+  auto par = byo::gpu_bfs(csr, 2);
+  const uint32_t X = BYO_NONE;
+  CHECK((par == std::vector<uint32_t>{X, X, 2, 2, 3, 3, 5}));
+  auto lab = byo::gpu_cc(csr);
+  CHECK((lab == std::vector<uint32_t>{0, 0, 2, 2, 2, 2, 2}));
+  CHECK(byo::gpu_triangle_count(csr) == 1);
+  auto pr = byo::gpu_pagerank(csr, 1e-9, 200, BYO_PR_FP64);
+  double sum = 0;
+  for (double x : pr) sum += x;
+  CHECK(sum > 0.5 && sum < 1.01);
+
+  byo::GPU_PMA_graph<int> pma(vd.data(), n, edges.size(), nullptr, edges.data());
+  CHECK(pma.num_edges() == 12);
+  std::vector<std::tuple<uint32_t, uint32_t>> batch = {{1, 2}, {2, 1}, {0, 6}, {6, 0}, {1, 2}};
+  pma.insert_batch(batch.data(), batch.size());
+  CHECK(pma.num_edges() == 16);
+  CHECK(pma.degree(1) == 2 && pma.degree(6) == 2);
+  par = byo::gpu_bfs(pma, 0);
+  CHECK((par == std::vector<uint32_t>{0, 0, 1, 2, 5, 6, 0}));
+  std::vector<std::tuple<uint32_t, uint32_t>> sorted = {{0, 6}, {6, 0}};
+  pma.remove_sorted_batch(sorted.data(), sorted.size());
+  CHECK(pma.num_edges() == 14 && pma.degree(6) == 1);
+  lab = byo::gpu_cc(pma);
+  CHECK((lab == std::vector<uint32_t>{0, 0, 0, 0, 0, 0, 0}));
+  std::printf("adapter ok\n");
+  return 0;
+}
