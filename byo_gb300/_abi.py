@@ -112,7 +112,9 @@ SIGNATURES = {
     "byo_vs_to_list": (_int, [_vp, _vp, _u64]),
     "byo_edge_map": (_int, [_vp, _vp, _vp, _i64, _u32, _P(_vp)]),
     "byo_last_rounds": (_int, [_vp, _P(RoundLog), _u64, _P(_u64)]),
+    "byo_bfs_csr_noalloc": (_int, [_vp, _vp, _u64, _u64, _u32, _vp, _vp, _vp, _P(_u32)]),
 }
+NOALLOC_MAX_VERTICES = 1 << 20
 
 _lib = None
 

@@ -238,6 +238,26 @@ int byo_ctx_set_round_timing(byo_ctx *ctx, int on);
 int byo_ctx_kernel_timing(byo_ctx *ctx, const char *tag);
 int byo_ctx_kernel_time(byo_ctx *ctx, const char *tag, uint64_t *launches, double *ms);
 
+/* ------------------------------------------------------------------ allocation-free BFS
+ * No counterpart in the reference.  For callers that cannot let a library
+ * allocate device memory: hosts whose memory manager owns the whole GPU and
+ * hands out sub-ranges itself, and code issuing work while a CUDA stream is
+ * being captured, where cudaMalloc is not allowed.  BFS from src over the
+ * caller's device CSR (d_offsets[n+1], d_nbrs[m], symmetric, sorted), on the
+ * caller's stream (cudaStream_t, NULL = default) of the current device,
+ * writing the same parents and levels as byo_bfs into the caller's device
+ * arrays (either may be NULL, not both).  Calls no cudaMalloc / cudaFree:
+ * the traversal state lives in one static device array sized for
+ * BYO_NOALLOC_MAX_VERTICES vertices (16.4 MiB per GPU, held until exit);
+ * n above that returns BYO_EINVAL.  The array is shared by all calls: calls
+ * that overlap on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks the array up and should come before any
+ * stream capture starts.  Returns when the result is in the output arrays. */
+#define BYO_NOALLOC_MAX_VERTICES (1u << 20)
+int byo_bfs_csr_noalloc(const uint64_t *d_offsets, const uint32_t *d_nbrs, uint64_t n, uint64_t m,
+                        uint32_t src, uint32_t *d_parent, uint32_t *d_level, void *stream,
+                        uint32_t *rounds);
+
 #ifdef __cplusplus
 }
 #endif
