@@ -60,7 +60,7 @@ class GenSpec(ctypes.Structure):
 
 class RoundLog(ctypes.Structure):
     _fields_ = [("round", _u32), ("mode", _u32), ("frontier", _u64), ("frontier_deg", _u64),
-                ("unvisited", _u64), ("ms", ctypes.c_float)]
+                ("unvisited", _u64), ("ms", ctypes.c_float), ("features", ctypes.c_float * 16)]
 
 
 # name -> (restype, argtypes)
@@ -113,7 +113,19 @@ SIGNATURES = {
     "byo_edge_map": (_int, [_vp, _vp, _vp, _i64, _u32, _P(_vp)]),
     "byo_last_rounds": (_int, [_vp, _P(RoundLog), _u64, _P(_u64)]),
     "byo_bfs_csr_noalloc": (_int, [_vp, _vp, _u64, _u64, _u32, _vp, _vp, _vp, _P(_u32)]),
+    "byo_ctx_set_update_policy": (_int, [_vp, _int]),
+    "byo_ctx_last_update_strategy": (_int, [_vp]),
+    "byo_policy_init_params": (_int, [_u64, _vp]),
+    "byo_policy_set_params": (_int, [_vp, _vp]),
+    "byo_policy_get_params": (_int, [_vp, _vp]),
+    "byo_policy_clear": (_int, [_vp]),
+    "byo_policy_forward": (_int, [_vp, _vp, _vp, _u64, _vp]),
+    "byo_policy_loss_grad": (_int, [_vp, _vp, _vp, _vp, _vp, _u64, _P(ctypes.c_float), _vp]),
+    "byo_policy_train": (_int, [_vp, _vp, _vp, _vp, _vp, _u64, _u32, ctypes.c_float, _u64, _vp]),
+    "byo_update_sample": (_int, [_vp, _vp, _u64, _vp, _vp, _vp]),
 }
+POLICY_NFEATURES, POLICY_NOUTPUTS, POLICY_NPARAMS = 16, 5, 1765
+UPDATE_MERGE, UPDATE_LEARNED, UPDATE_REBUILD = 0, 1, 2
 NOALLOC_MAX_VERTICES = 1 << 20
 
 _lib = None

@@ -1,6 +1,7 @@
 // abi.cu -- the extern "C" boundary declared in include/byo_gpu.h.
 // Argument checking, host<->device staging and object lifetime live here;
 // the work is in engine.cu, algos.cu, graph.cu and pma.cu.
+#include <cmath>
 #include <cstring>
 #include <new>
 
@@ -76,6 +77,7 @@ void byo_gpu_shutdown(byo_ctx *ctx) {
   for (int i = 0; i < 64; i++)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   for (cudaEvent_t e : ctx->kev) cudaEventDestroy(e);
+  policy_destroy(ctx->policy);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -525,6 +527,49 @@ int byo_ctx_kernel_time(byo_ctx *ctx, const char *tag, uint64_t *launches, doubl
   if (ms) *ms = tot;
   return BYO_OK;
 }
+
+int byo_ctx_set_update_policy(byo_ctx *ctx, int policy) {
+  if (!ctx) return BYO_EINVAL;
+  if (policy != BYO_UPDATE_MERGE && policy != BYO_UPDATE_LEARNED && policy != BYO_UPDATE_REBUILD)
+    return set_error(ctx, BYO_EINVAL, "unknown update policy");
+  ctx->update_policy = policy;
+  return BYO_OK;
+}
+
+// Times one batch both ways (in-place merge and rebuild), as insert and as
+// remove, restoring the contents in between; two samples for the policy.
+int byo_update_sample(byo_graph *g, const uint64_t *h_keys, uint64_t count, float *h_x, float *h_y,
+                      uint8_t *h_mask) {
+  if (!g || !h_keys || !count || !h_x || !h_y || !h_mask) return BYO_EINVAL;
+  byo_ctx *ctx = g->ctx;
+  if (g->container != BYO_CONTAINER_PMA) return set_error(ctx, BYO_ENOTSUP, "needs the PMA container");
+  const int saved = ctx->update_policy;
+  float t[4] = {0, 0, 0, 0};
+  uint64_t m0 = g->m, slots0 = g->nslots;
+  int rc = BYO_OK;
+  for (int k = 0; k < 4 && rc == BYO_OK; k++) {
+    const int insert = (k % 2) == 0;
+    ctx->update_policy = k < 2 ? BYO_UPDATE_MERGE : BYO_UPDATE_REBUILD;
+    cudaEventRecord(ctx->ev[2], ctx->stream);
+    rc = update_common(g, h_keys, count, 0, insert, 1, nullptr);
+    cudaEventRecord(ctx->ev[3], ctx->stream);
+    cudaEventSynchronize(ctx->ev[3]);
+    cudaEventElapsedTime(&t[k], ctx->ev[2], ctx->ev[3]);
+  }
+  ctx->update_policy = saved;
+  if (rc != BYO_OK) return rc;
+  for (int s2 = 0; s2 < 2; s2++) {
+    update_features(count, m0, slots0, 0, s2 == 0, h_x + 16 * s2);
+    for (int o = 0; o < 5; o++) h_y[5 * s2 + o] = 0.f;
+    const float merge_ms = t[s2], rebuild_ms = t[2 + s2];
+    h_y[5 * s2 + 3] = std::log2(1.f + merge_ms * 1000.f) / 16.f;
+    h_y[5 * s2 + 4] = std::log2(1.f + rebuild_ms * 1000.f) / 16.f;
+    h_mask[s2] = (uint8_t)((1u << 3) | (1u << 4));
+  }
+  return BYO_OK;
+}
+
+int byo_ctx_last_update_strategy(const byo_ctx *ctx) { return ctx ? ctx->last_update_strategy : BYO_EINVAL; }
 
 int byo_ctx_set_round_timing(byo_ctx *ctx, int on) {
   if (!ctx) return BYO_EINVAL;

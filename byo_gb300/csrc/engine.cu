@@ -2,6 +2,8 @@
 // See engine.h for the design.  Algorithmic bytes of one BFS traversal:
 // 4 B per adjacency entry of every reached vertex + 8 B offsets per vertex
 // + 8 B lp written per reached vertex (parent/level split is 8 B more).
+#include <cstring>
+
 #include "device.cuh"
 #include "engine.h"
 #include "internal.h"
@@ -398,7 +400,7 @@ static int pull_smem_ok(int bytes) {
 }
 
 int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int mode,
-                   const EngineTuning &tune) {
+                   const EngineTuning &tune, bool run_policy) {
   byo_ctx *ctx = g->ctx;
   RoundStats *d_st = nullptr;
   BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 1, (uint64_t **)&d_st));
@@ -466,6 +468,7 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
            (const uint32_t *)out.list, (const RoundStats *)d_st, st.visited);
   }
   BYO_TRY(check_launch(ctx, "edge_map_round"));
+  if (run_policy) BYO_TRY(round_policy(g, d_st, st.reached, mode == MODE_PULL));
   RoundStats *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
   BYO_CU(ctx, cudaMemcpyAsync(h, d_st, sizeof(RoundStats), cudaMemcpyDeviceToHost, ctx->stream));
@@ -473,6 +476,10 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
   out.size = h->count;
   out.outdeg = h->outdeg;
   for (int i = 0; i < 8; i++) out.hist[i] = h->hist[i];
+  if (run_policy) {
+    out.next_mode = (int)h->mode;
+    for (int i = 0; i < 16; i++) out.feat[i] = h->feat[i];
+  }
   out.dense = (mode == MODE_PULL);
   out.has_list = true;
   out.has_bits = true;
@@ -512,6 +519,25 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
   fb.has_list = true;  // empty list: its bitmap is all zero
   const EngineTuning tune = default_tuning(g);
   ctx->rounds.clear();
+  // features (and the learned choice) are computed on the device after every
+  // round when the learned policy runs or rounds are being logged
+  const bool run_policy = policy == BYO_POLICY_LEARNED || ctx->time_rounds;
+  if (run_policy) {
+    RoundStats *d_st = nullptr, *h = nullptr;
+    BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 1, (uint64_t **)&d_st));
+    BYO_TRY(pinned(ctx, 4096, (void **)&h));
+    std::memset(h, 0, sizeof(RoundStats));
+    h->count = 1;
+    h->outdeg = dsrc;
+    int bin = dsrc ? (31 - __builtin_clz(dsrc)) / 2 : 0;
+    h->hist[bin > 7 ? 7 : bin] = 1;
+    BYO_CU(ctx, cudaMemcpyAsync(d_st, h, sizeof(RoundStats), cudaMemcpyHostToDevice, ctx->stream));
+    BYO_TRY(round_policy(g, d_st, 0, false));
+    BYO_CU(ctx, cudaMemcpyAsync(h, d_st, sizeof(RoundStats), cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+    fa.next_mode = (int)h->mode;
+    for (int i = 0; i < 16; i++) fa.feat[i] = h->feat[i];
+  }
   Frontier *cur = &fa, *nxt = &fb;
   uint32_t nr = 0;
   while (cur->size > 0) {
@@ -521,25 +547,7 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
       case BYO_POLICY_PULL: mode = MODE_PULL; break;
       case BYO_POLICY_BLOCKED: mode = MODE_BLOCKED; break;
       case BYO_POLICY_M20_BLOCKED: mode = m20_mode(g, *cur, -1, MODE_BLOCKED); break;
-      case BYO_POLICY_LEARNED: {
-        mode = m20_mode(g, *cur, -1, MODE_PUSH);
-        float feat[16];
-        const double lg = 1.0 / 32.0;
-        feat[0] = (float)(log2((double)cur->size + 1) * lg);
-        feat[1] = (float)(log2((double)cur->outdeg + 1) * lg);
-        feat[2] = (float)(log2((double)(n - st.reached) + 1) * lg);
-        feat[3] = (float)(log2((double)n + 1) * lg);
-        feat[4] = (float)(log2((double)g->m + 1) * lg);
-        feat[5] = cur->dense ? 1.f : 0.f;
-        double tot = 0;
-        for (int i = 0; i < 8; i++) tot += (double)cur->hist[i];
-        for (int i = 0; i < 8; i++) feat[6 + i] = tot > 0 ? (float)(cur->hist[i] / tot) : 0.f;
-        feat[14] = (float)((double)(cur->size + cur->outdeg) / ((double)g->m / 20.0 + 1.0));
-        feat[15] = 0.f;
-        int m2 = mode;
-        if (policy_choose(ctx, feat, 16, &m2) == BYO_OK) mode = m2;
-        break;
-      }
+      case BYO_POLICY_LEARNED: mode = cur->next_mode; break;  // network, or m/20 if untrained
       default: mode = m20_mode(g, *cur, -1, MODE_PUSH); break;
     }
     if (mode != MODE_PULL && cur->outdeg == 0) break;  // edge_map_data.h:290
@@ -551,9 +559,10 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
     lg.frontier = cur->size;
     lg.frontier_deg = cur->outdeg;
     lg.unvisited = n - st.reached;
+    for (int i = 0; i < 16; i++) lg.features[i] = cur->feat[i];
     if (ctx->time_rounds) BYO_CU(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
     nxt->size = 0;
-    BYO_TRY(edge_map_round(g, st, *cur, *nxt, mode, tune));
+    BYO_TRY(edge_map_round(g, st, *cur, *nxt, mode, tune, run_policy));
     if (ctx->time_rounds) {
       BYO_CU(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
       BYO_CU(ctx, cudaEventSynchronize(ctx->ev[1]));

@@ -31,6 +31,8 @@ struct RoundStats {
   unsigned long long ndefer;  // pull: deferred long scans; push: hubs
   unsigned long long edges;   // edges examined (diagnostic)
   unsigned long long hist[8]; // degree sketch of the next frontier (log4 bins)
+  unsigned long long mode;    // next round's mode chosen by the policy kernel
+  float feat[16];             // the features that choice was made from
 };
 
 struct Frontier {
@@ -41,6 +43,8 @@ struct Frontier {
   bool dense = false;        // produced by a dense round
   bool has_list = false, has_bits = false;
   unsigned long long hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int next_mode = 0;    // policy kernel's choice for the round consuming this frontier
+  float feat[16] = {0}; // its features
 };
 
 struct TravState {
@@ -64,12 +68,18 @@ int m20_mode(const byo_graph *g, const Frontier &f, int64_t threshold, int spars
 // Runs one edgeMap round over BFS_F semantics: reads `in`, writes `out`
 // (out.bits must be all zero; out.list capacity n).  Updates st.
 int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int mode,
-                   const EngineTuning &tune);
+                   const EngineTuning &tune, bool run_policy = false);
 // Zeroes a frontier bitmap using its list when that is cheaper.
 int clear_frontier_bits(byo_graph *g, Frontier &f);
 int ensure_bits(byo_graph *g, Frontier &f);
 int trav_init(byo_graph *g, TravState &st, uint32_t src);
 int trav_extract(byo_graph *g, const TravState &st, uint32_t *d_parent, uint32_t *d_level);
 EngineTuning default_tuning(const byo_graph *g);
+
+// Policy kernel after a round (mlp.cu): features of the frontier in d_st,
+// the m/20 rule's choice, and the network's choice when one is trained;
+// writes d_st->mode and d_st->feat.
+int round_policy(byo_graph *g, RoundStats *d_st, uint64_t reached_before, bool this_round_dense);
+bool policy_trained(const byo_ctx *ctx);
 
 }  // namespace byo

@@ -53,6 +53,8 @@ struct byo_ctx {
   std::vector<cudaEvent_t> kev;
   std::vector<const char *> ktags;
   size_t kev_used = 0;
+  int update_policy = BYO_UPDATE_MERGE;  // container update strategy
+  int last_update_strategy = 0;          // 0 merge, 1 rebuild (last batch)
 };
 
 struct byo_graph {
@@ -205,6 +207,9 @@ int pma_export_keys(byo_graph *g, uint64_t *d_keys_out);
 void pma_destroy(Pma *p);
 
 // ---------------------------------------------------------------- policy (mlp.cu)
-int policy_choose(byo_ctx *ctx, const float *features, int nfeat, int *mode);
+void policy_destroy(Mlp *p);
+// 0 = in-place merge, 1 = rebuild, from the trained network (0 when untrained)
+int update_strategy(byo_ctx *ctx, uint64_t batch, uint64_t m, uint64_t slots, int sorted, int insert);
+void update_features(uint64_t batch, uint64_t m, uint64_t slots, int sorted, int insert, float *x);
 
 }  // namespace byo

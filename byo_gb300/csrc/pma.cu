@@ -600,10 +600,16 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   const uint64_t total = h[0];
   if (changed) *changed = insert ? total - m_before : m_before - total;
   if (total == m_before) return BYO_OK;  // nothing new / nothing present
-  // 3. capacity: grow or shrink by full rebuild
+  // 3. strategy: in-place merge (default), or rebuild when asked for, chosen
+  // by the learned policy, or forced by capacity (grow / shrink)
+  int strategy = 0;
+  if (ctx->update_policy == BYO_UPDATE_REBUILD) strategy = 1;
+  else if (ctx->update_policy == BYO_UPDATE_LEARNED)
+    strategy = update_strategy(ctx, b, m_before, NL * kLeaf, sorted, insert);
   const double cap = (double)NL * kLeaf;
-  if ((double)total > kRootMax * cap || (!insert && (double)total < kRootMin * cap && NL > 1))
-    return pma_rebuild(g, batch, bstart, rpre, total, insert);
+  if ((double)total > kRootMax * cap || (!insert && (double)total < kRootMin * cap && NL > 1)) strategy = 1;
+  ctx->last_update_strategy = strategy;
+  if (strategy == 1) return pma_rebuild(g, batch, bstart, rpre, total, insert);
   // 4. windows for overflowing leaves
   BYO_TRY(ensure(ctx, p->marks, (uint64_t)(p->H + 1) * NL));
   BYO_TRY(ensure(ctx, p->win, NL * 4));
@@ -615,7 +621,10 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   const unsigned int *hf = (const unsigned int *)h;
-  if (hf[1]) return pma_rebuild(g, batch, bstart, rpre, total, insert);
+  if (hf[1]) {
+    ctx->last_update_strategy = 1;
+    return pma_rebuild(g, batch, bstart, rpre, total, insert);
+  }
   const bool any = hf[2] != 0;
   uint64_t *stg = nullptr;
   if (any) {

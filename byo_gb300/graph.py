@@ -102,7 +102,7 @@ class Context:
         arr = (_abi.RoundLog * max(n.value, 1))()
         check(lib().byo_last_rounds(self.h, arr, n.value, ctypes.byref(n)), self.h)
         return [dict(round=r.round, mode=r.mode, frontier=r.frontier, frontier_deg=r.frontier_deg,
-                     unvisited=r.unvisited, ms=r.ms) for r in arr[:n.value]]
+                     unvisited=r.unvisited, ms=r.ms, features=list(r.features)) for r in arr[:n.value]]
 
 
 class Graph:

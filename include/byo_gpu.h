@@ -225,7 +225,8 @@ typedef struct byo_round_log {
   uint64_t frontier;      /* |F| */
   uint64_t frontier_deg;  /* sum of out-degrees of F */
   uint64_t unvisited;     /* vertices not yet reached before the round */
-  float ms;               /* device time of the round */
+  float ms;               /* device time of the round (with round timing on) */
+  float features[16];     /* policy features of F (learned policy or timing on) */
 } byo_round_log;
 int byo_last_rounds(byo_ctx *ctx, byo_round_log *out, uint64_t cap, uint64_t *count);
 /* Times every round with CUDA events (adds one host wait per round). */
@@ -237,6 +238,43 @@ int byo_ctx_set_round_timing(byo_ctx *ctx, int on);
  * "tc_intersect", "sort_scatter", "pma_merge", "pma_redistribute". */
 int byo_ctx_kernel_timing(byo_ctx *ctx, const char *tag);
 int byo_ctx_kernel_time(byo_ctx *ctx, const char *tag, uint64_t *launches, double *ms);
+
+/* ------------------------------------------------------------------ learned policy
+ * A 16-32-32-5 FP32 MLP predicting log2(1 + microseconds)/16 of five actions:
+ * 0 push, 1 pull, 2 blocked (per edgeMap round) and 3 in-place merge,
+ * 4 rebuild (per container update).  Trained on the device by the library's
+ * own kernels on samples the engine logs (round logs with round timing on,
+ * byo_update_sample).  BYO_POLICY_LEARNED rounds and BYO_UPDATE_LEARNED
+ * batches use it; the m/20 rule (edge_map_data.h:254-307) and in-place merge
+ * remain the fallback and judge.  No counterpart in the reference beyond the
+ * rule it learns around. */
+#define BYO_POLICY_NFEATURES 16
+#define BYO_POLICY_NOUTPUTS 5
+#define BYO_POLICY_NPARAMS 1765
+enum byo_update_policy { BYO_UPDATE_MERGE = 0, BYO_UPDATE_LEARNED = 1, BYO_UPDATE_REBUILD = 2 };
+int byo_ctx_set_update_policy(byo_ctx *ctx, int policy);
+/* strategy of the last batch: 0 merge, 1 rebuild */
+int byo_ctx_last_update_strategy(const byo_ctx *ctx);
+/* Seeded Xavier initialisation of the 1765 parameters (W1,b1,W2,b2,W3,b3). */
+int byo_policy_init_params(uint64_t seed, float *h_params);
+int byo_policy_set_params(byo_ctx *ctx, const float *h_params);
+int byo_policy_get_params(byo_ctx *ctx, float *h_params);
+/* Forget the network: learned policies fall back to the rules. */
+int byo_policy_clear(byo_ctx *ctx);
+int byo_policy_forward(byo_ctx *ctx, const float *h_params, const float *h_x, uint64_t n, float *h_y);
+/* Mean squared error over the observed targets (bit o of mask[i] marks
+ * y[i][o]) and its gradient with respect to the 1765 parameters. */
+int byo_policy_loss_grad(byo_ctx *ctx, const float *h_params, const float *h_x, const float *h_y,
+                         const uint8_t *h_mask, uint64_t n, float *loss, float *h_grad);
+/* Adam on the device for `epochs` passes from h_init (NULL: seeded init);
+ * installs the result as the context's policy. */
+int byo_policy_train(byo_ctx *ctx, const float *h_init, const float *h_x, const float *h_y,
+                     const uint8_t *h_mask, uint64_t n, uint32_t epochs, float lr, uint64_t seed,
+                     float *h_loss_per_epoch);
+/* Times the batch as in-place merge and as rebuild, for insert and remove
+ * (contents restored in between); writes 2 samples (x[2][16], y[2][5], mask[2]). */
+int byo_update_sample(byo_graph *g, const uint64_t *h_keys, uint64_t count, float *h_x, float *h_y,
+                      uint8_t *h_mask);
 
 /* ------------------------------------------------------------------ allocation-free BFS
  * No counterpart in the reference.  For callers that cannot let a library

@@ -1,0 +1,116 @@
+"""The learned policy: device gradients against the FP64 oracle, training,
+bit-exact results under the learned policy, and what the trained network
+gains over the m/20 rule on rounds it was not trained on."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gradient_check(ctx):
+    from byo_gb300 import policy as P
+    from oracle import mlp_ref
+    rng = np.random.default_rng(0)
+    params = P.init_params(7) + rng.normal(0, 0.05, P.NP).astype(np.float32)
+    X = rng.random((300, P.NF)).astype(np.float32)
+    Y = rng.random((300, P.NO)).astype(np.float32)
+    M = rng.integers(1, 32, 300).astype(np.uint8)
+    loss, g = P.loss_grad(ctx, params, X, Y, M)
+    rl, rg = mlp_ref.loss_grad(params.astype(np.float64), X, Y, M)
+    assert abs(loss - rl) <= 1e-5 * max(1.0, rl)
+    # FP32 device accumulation vs FP64: relative error of the whole gradient
+    assert np.linalg.norm(g - rg) <= 1e-4 * np.linalg.norm(rg)
+    y = P.forward(ctx, params, X)
+    ry, _ = mlp_ref.forward(params.astype(np.float64), X)
+    assert np.abs(y - ry).max() <= 1e-5 * max(1.0, np.abs(ry).max())
+
+
+def test_training_fits(ctx):
+    from byo_gb300 import policy as P
+    rng = np.random.default_rng(1)
+    X = rng.random((2000, P.NF)).astype(np.float32)
+    Y = np.zeros((2000, P.NO), np.float32)
+    Y[:, 0] = 0.3 + 0.5 * X[:, 0] - 0.2 * X[:, 1]
+    Y[:, 1] = 0.6 - 0.4 * X[:, 0] + 0.3 * X[:, 14]
+    Y[:, 2] = 0.4 + 0.1 * np.sin(6 * X[:, 2])
+    M = np.full(2000, 0b00111, np.uint8)
+    params, losses = P.train(ctx, X, Y, M, epochs=150, lr=3e-3, seed=3)
+    assert losses[-1] < 0.1 * losses[0]
+    assert losses[-1] < 2e-3
+    P.clear(ctx)
+
+
+def test_learned_policy_is_bit_exact_and_gains(ctx, oracle_mod):
+    import byo_gb300 as byo
+    from byo_gb300 import policy as P
+    O = oracle_mod
+    graphs = [byo.Graph.generate(ctx, "rmat", seed=31, lg_n=18, draws=1 << 22),
+              byo.Graph.generate(ctx, "grid", n=256, draws=256),
+              byo.Graph.generate(ctx, "er", seed=5, n=1 << 17, draws=1 << 20)]
+    train_sets, test_sets = [], []
+    for G in graphs:
+        deg = G.degrees()
+        cand = np.nonzero(deg)[0]
+        rng = np.random.default_rng(G.N())
+        srcs = rng.choice(cand, 8, replace=False)
+        train_sets.append(P.collect_round_samples(G, srcs[:5]))
+        test_sets.append(P.collect_round_samples(G, srcs[5:], warm=False))
+    X, Y, M, _ = (np.concatenate(z) for z in zip(*train_sets))
+    params, losses = P.train(ctx, X, Y, M, epochs=300, lr=3e-3, seed=11)
+    assert losses[-1] < losses[0]
+    P.install(ctx, params)
+    # results do not depend on the policy
+    for G in graphs:
+        off, nb = G.export_csr()
+        for s in (0, 10):
+            par, lev = byo.BFS(G, s, policy=byo._abi.POLICY_LEARNED, levels=True)
+            opar, olev = O.bfs(off, nb, s)
+            assert np.array_equal(par, opar) and np.array_equal(lev, olev)
+    # cost of the held-out rounds under each decision rule, from logged times
+    Xt, Yt, Mt, Ct = (np.concatenate(z) for z in zip(*test_sets))
+    learned = P.round_choices(ctx, params, Xt, Ct)
+    t_m20 = P.round_cost(Yt, Ct)
+    t_learned = P.round_cost(Yt, learned)
+    t_best = P.round_cost(Yt, Yt[:, :3].argmin(1))
+    print("held-out rounds: m/20 %.0f us, learned %.0f us, oracle-best %.0f us" % (t_m20, t_learned, t_best))
+    assert t_learned <= 1.02 * t_m20
+    P.clear(ctx)
+    for G in graphs:
+        G.close()
+
+
+def test_update_policy_samples_and_parity(ctx, oracle_mod):
+    import byo_gb300 as byo
+    from byo_gb300 import policy as P
+    O = oracle_mod
+    G = byo.Graph.generate(ctx, "rmat", seed=4, lg_n=16, draws=1 << 20, container="pma")
+    s, d = O.rmat_edges(4, 16, 1 << 20)
+    off, nb = O.build_csr(1 << 16, s, d)
+    st = O.Store(off, nb)
+    batches = []
+    for k, b in enumerate((100, 3000, 100000, 1000000)):
+        us, ud = O.uniform_pairs(50 + k, 1 << 16, b)
+        batches.append(O.keys_from_pairs(us, ud))
+    X, Y, M = P.collect_update_samples(G, batches)
+    assert X.shape == (8, P.NF) and np.all(M == 0b11000)
+    assert np.all(Y[:, 3:] > 0)
+    # each sample restored the contents: replay the same operations on the model
+    for keys in batches:
+        st.insert_batch(keys)
+        st.remove_batch(keys)
+        st.insert_batch(keys)
+        st.remove_batch(keys)
+    ro, rn = st.export_csr()
+    go, gn = G.export_csr()
+    assert np.array_equal(go, ro) and np.array_equal(gn, rn)
+    # forced rebuild and learned strategies keep the contents exact
+    from byo_gb300 import _abi
+    for pol in (_abi.UPDATE_REBUILD, _abi.UPDATE_LEARNED):
+        _abi.check(_abi.lib().byo_ctx_set_update_policy(ctx.h, pol), ctx.h)
+        G.insert_batch(batches[2])
+        st.insert_batch(batches[2])
+        ro, rn = st.export_csr()
+        go, gn = G.export_csr()
+        assert np.array_equal(go, ro) and np.array_equal(gn, rn)
+    _abi.check(_abi.lib().byo_ctx_set_update_policy(ctx.h, _abi.UPDATE_MERGE), ctx.h)
+    G.close()
