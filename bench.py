@@ -147,7 +147,13 @@ def run_ours(args, rank, world, local_rank):
     G = byo.Graph.generate(ctx, "rmat", seed=SEED, lg_n=LG_N, draws=DRAWS, container=container)
     n, m0 = G.N(), G.M()
     log("graph: n=%d m=%d container=%s built in %.2fs" % (n, m0, container, time.time() - t0))
+    from byo_gb300 import policy as learned
+    have_net = learned.load_default(ctx)
+    if args.policy == "auto":
+        args.policy = "learned" if have_net else "m20"
     policy = POLICIES[args.policy]
+    if args.policy == "learned":
+        _abi.check(L.byo_ctx_set_update_policy(ctx.h, _abi.UPDATE_LEARNED), ctx.h)
     dev = torch.device("cuda", local_rank)
     B = 2 * BATCH
     keys = torch.empty(B, dtype=torch.int64, device=dev)
@@ -253,13 +259,15 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peaks()
     roof = {"bound": "hbm", "peak": peak, "unit": "GB/s", "kernel": dom, "peak_source": peak_kind}
     if dom == "pr_pull":
+        # one PageRank iteration = k_pr_units + k_pr_combine (both tagged pr_pull)
         per_iter = pr_iteration_bytes(n, m_trav, nslots)
         launches_dom, ms_dom = ktimes[dom]
         iters_total = pr_iters * args.steps
         achieved = per_iter * iters_total / (ms_dom / 1e3) / 1e9
-        roof.update({"achieved": achieved, "frac": achieved / peak,
-                     "algorithmic_bytes_per_launch": per_iter,
-                     "avg_launch_ms": ms_dom / max(launches_dom, 1), "launches": launches_dom})
+        roof.update({"kernel": "pr_pull (k_pr_units + k_pr_combine, per iteration)", "achieved": achieved,
+                     "frac": achieved / peak, "algorithmic_bytes_per_launch": per_iter,
+                     "avg_launch_ms": ms_dom / max(iters_total, 1), "launches": launches_dom,
+                     "iterations": iters_total})
     elif dom.startswith("bfs"):
         byts = bfs_bytes(n, bfs_edges, reached) * args.steps
         ms_bfs = sum(ktimes[t][1] for t in tags if t.startswith("bfs"))
@@ -267,7 +275,7 @@ def run_ours(args, rank, world, local_rank):
         roof.update({"achieved": achieved, "frac": achieved / peak, "kernel": "bfs (push+pull+blocked)"})
     else:
         roof.update({"achieved": None, "frac": None})
-    tr = traffic_table().get(roof["kernel"])
+    tr = traffic_table().get(dom)
     roof["traffic"] = tr.get("bytes_per_launch") if tr else None
     roof["kernel_ms_share"] = {t: round(ktimes[t][1] / max(elapsed_ms, 1e-9), 4) for t in tags if ktimes[t][0]}
 
@@ -284,6 +292,11 @@ def run_ours(args, rank, world, local_rank):
     if dynamic:
         components.update({"insert_edges_per_s": B / (comp[0] / 1e3), "remove_edges_per_s": B / (comp[4] / 1e3),
                            "insert_ms": comp[0], "remove_ms": comp[4]})
+
+    # the learned policy against the m/20 rule (and in-place merge) on the
+    # same state, same GPU: BFS and the update pair, median of 5
+    if have_net:
+        components["policy_compare"] = compare_policies(L, _abi, ctx, G, keys, B, parent, dynamic, torch, stream)
 
     # end to end through the public host API
     e2e = run_e2e(args, byo, G, ctx, torch, dynamic, keys, B, n, policy, total_units, world, dev)
@@ -303,6 +316,37 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
     }
     return res, ctx, G
+
+
+def compare_policies(L, _abi, ctx, G, keys, B, parent, dynamic, torch, stream):
+    ch = ctypes.c_uint64(0)
+    r = ctypes.c_uint32(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        ts = []
+        for _ in range(5):
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    out = {}
+    for name, pol in (("m20", POLICIES["m20"]), ("learned", POLICIES["learned"])):
+        out["bfs_ms_" + name] = timed(lambda: _abi.check(L.byo_bfs_device(G.h, SRC, parent.data_ptr(), None, pol,
+                                                                          ctypes.byref(r)), ctx.h))
+    if dynamic:
+        for name, up in (("merge", _abi.UPDATE_MERGE), ("learned", _abi.UPDATE_LEARNED)):
+            _abi.check(L.byo_ctx_set_update_policy(ctx.h, up), ctx.h)
+
+            def pair():
+                _abi.check(L.byo_graph_insert_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+                _abi.check(L.byo_graph_remove_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+            out["update_pair_ms_" + name] = timed(pair)
+        _abi.check(L.byo_ctx_set_update_policy(ctx.h, _abi.UPDATE_LEARNED), ctx.h)
+    return out
 
 
 def run_e2e(args, byo, G, ctx, torch, dynamic, keys, B, n, policy, total_units, world, dev):
@@ -422,7 +466,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static"])
-    ap.add_argument("--policy", default="m20", choices=sorted(POLICIES))
+    ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
+                    help="auto: the committed learned network if present, else m20")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -25,7 +25,9 @@ constexpr int kIn = 16, kH = 32, kOut = 5;
 constexpr int kW1 = 0, kB1 = kW1 + kH * kIn, kW2 = kB1 + kH, kB2 = kW2 + kH * kH, kW3 = kB2 + kH,
               kB3 = kW3 + kOut * kH, kParams = kB3 + kOut;  // 1765
 constexpr int kMb = 128;
-constexpr float kJudgeMargin = 0.05f;  // in log2 units / 16 of the target scale
+// The network must predict a gain of more than 2^(16*margin) - 1 (about 7%)
+// over the rule's choice before it overrides it.
+constexpr float kJudgeMargin = 0.006f;
 
 struct Mlp {
   float *d_params = nullptr;    // kParams, the network used for inference

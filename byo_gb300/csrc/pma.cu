@@ -216,12 +216,16 @@ __global__ void k_pma_cover(const uint8_t *__restrict__ marks, uint64_t NL, int 
 // ---------------------------------------------------------------- merge
 
 // One CTA per leaf with work.  Leaf A (<= kLeaf keys) is staged in shared
-// memory; batch segment B streams from global memory.
+// memory, and so is batch segment B when it has at most kSegCap keys (longer
+// segments are read from global memory).
 //   insert: pos(A[i]) = i + lb_B(A[i]) - PA[i]
 //           pos(B[k]) = k - PA[lb_A(B[k])] + lb_A(B[k])   for B[k] not in A
 //           (PA[i] = number of A[0..i) also present in B)
 //   remove: pos(A[i]) = i - PA[i] for A[i] not in B
+// One binary search of A[i] in B gives both lb_B(A[i]) and the presence bit.
 // Output goes in place (leaf not in a window) or to staging[rpre[leaf]...].
+constexpr uint32_t kSegCap = 1024;
+
 __global__ void __launch_bounds__(kPmaBlock) k_pma_merge(uint32_t *src, uint32_t *dst, uint32_t *cnt,
                                                         uint64_t NL, const uint64_t *__restrict__ keys,
                                                         const uint64_t *__restrict__ bstart,
@@ -229,90 +233,85 @@ __global__ void __launch_bounds__(kPmaBlock) k_pma_merge(uint32_t *src, uint32_t
                                                         const uint64_t *__restrict__ rpre, uint64_t *staging,
                                                         int insert, int all_windowed) {
   __shared__ uint64_t A[kLeaf];
+  __shared__ uint64_t Bs[kSegCap];
   __shared__ uint32_t PA[kLeaf + 1];
+  __shared__ uint32_t LB[kLeaf];
   __shared__ uint32_t wsum[kPmaBlock / 32 + 1];
+  constexpr int kPer = kLeaf / kPmaBlock;
   for (uint64_t j = blockIdx.x; j < NL; j += gridDim.x) {
     const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
     const bool windowed = all_windowed || win[j] != kNoWin;
     if (b0 == b1 && !windowed) continue;
     const uint32_t c = cnt[j];
+    const uint64_t nb = b1 - b0;
+    const bool bsm = nb <= kSegCap;
+    const uint64_t *B = bsm ? Bs : keys + b0;
     const uint64_t base = j * kLeaf;
     for (uint32_t i = threadIdx.x; i < c; i += kPmaBlock) A[i] = slot_key(src, dst, base + i);
+    if (bsm)
+      for (uint32_t k = threadIdx.x; k < nb; k += kPmaBlock) Bs[k] = keys[b0 + k];
     __syncthreads();
-    // presence of A[i] in B, then exclusive prefix PA (kLeaf <= 2 * block)
-    uint32_t f[kLeaf / kPmaBlock];
+    // lb_B(A[i]) and presence, then exclusive prefix PA (blocked: thread t owns
+    // A[t*kPer .. t*kPer+kPer))
+    uint32_t f[kPer];
 #pragma unroll
-    for (int q = 0; q < (int)(kLeaf / kPmaBlock); q++) {
-      uint32_t i = threadIdx.x * (kLeaf / kPmaBlock) + q;
+    for (int q = 0; q < kPer; q++) {
+      const uint32_t i = threadIdx.x * kPer + q;
       uint32_t hit = 0;
-      if (i < c && b1 > b0) {
-        uint64_t lo = b0, hi = b1, x = A[i];
+      if (i < c) {
+        uint64_t lo = 0, hi = nb;
+        const uint64_t x = A[i];
         while (lo < hi) {
           uint64_t mid = (lo + hi) >> 1;
-          if (keys[mid] < x) lo = mid + 1; else hi = mid;
+          if (B[mid] < x) lo = mid + 1; else hi = mid;
         }
-        hit = (lo < b1 && keys[lo] == x) ? 1u : 0u;
+        LB[i] = (uint32_t)lo;
+        hit = (lo < nb && B[lo] == x) ? 1u : 0u;
       }
       f[q] = hit;
     }
     uint32_t ts = 0;
 #pragma unroll
-    for (int q = 0; q < (int)(kLeaf / kPmaBlock); q++) ts += f[q];
+    for (int q = 0; q < kPer; q++) ts += f[q];
     uint32_t tot;
     uint32_t pre = block_exclusive_scan(ts, wsum, &tot);
 #pragma unroll
-    for (int q = 0; q < (int)(kLeaf / kPmaBlock); q++) {
-      PA[threadIdx.x * (kLeaf / kPmaBlock) + q] = pre;
+    for (int q = 0; q < kPer; q++) {
+      PA[threadIdx.x * kPer + q] = pre;
       pre += f[q];
     }
     if (threadIdx.x == 0) PA[kLeaf] = tot;
     __syncthreads();
-    // PA entries beyond c are tot (all q with i >= c have f = 0): PA[c] valid
-    const uint64_t r = insert ? (uint64_t)c + (b1 - b0) - tot : (uint64_t)c - tot;
-    uint32_t *osrc = src, *odst = dst;
-    uint64_t obase = base;
-    uint64_t *ostage = nullptr;
-    if (windowed) {
-      ostage = staging + rpre[j];
-    }
+    const uint64_t r = insert ? (uint64_t)c + nb - tot : (uint64_t)c - tot;
+    uint64_t *ostage = windowed ? staging + rpre[j] : nullptr;
     auto put = [&](uint64_t pos, uint64_t key) {
       if (ostage) {
         ostage[pos] = key;
       } else {
-        osrc[obase + pos] = (uint32_t)(key >> 32);
-        odst[obase + pos] = (uint32_t)key;
+        src[base + pos] = (uint32_t)(key >> 32);
+        dst[base + pos] = (uint32_t)key;
       }
     };
-    // A elements
     for (uint32_t i = threadIdx.x; i < c; i += kPmaBlock) {
-      const uint64_t x = A[i];
       if (insert) {
-        uint64_t lo = b0, hi = b1;  // lb_B(x)
-        while (lo < hi) {
-          uint64_t mid = (lo + hi) >> 1;
-          if (keys[mid] < x) lo = mid + 1; else hi = mid;
-        }
-        put(i + (lo - b0) - PA[i], x);
-      } else {
-        const bool gone = PA[i + 1] != PA[i];
-        if (!gone) put(i - PA[i], x);
+        put(i + LB[i] - PA[i], A[i]);
+      } else if (PA[i + 1] == PA[i]) {
+        put(i - PA[i], A[i]);
       }
     }
-    // B elements (insert only)
     if (insert) {
-      for (uint64_t k = b0 + threadIdx.x; k < b1; k += kPmaBlock) {
-        const uint64_t x = keys[k];
+      for (uint64_t k = threadIdx.x; k < nb; k += kPmaBlock) {
+        const uint64_t x = B[k];
         uint32_t lo = 0, hi = c;  // lb_A(x)
         while (lo < hi) {
           uint32_t mid = (lo + hi) >> 1;
           if (A[mid] < x) lo = mid + 1; else hi = mid;
         }
         if (lo < c && A[lo] == x) continue;  // already present
-        put((k - b0) - PA[lo] + lo, x);
+        put(k - PA[lo] + lo, x);
       }
     }
     if (!windowed) {
-      // pad what the leaf no longer holds (remove) and publish the count
       for (uint64_t p = r + threadIdx.x; p < c; p += kPmaBlock) {
         src[base + p] = kSentinel;
         dst[base + p] = kSentinel;

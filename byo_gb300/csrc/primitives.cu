@@ -175,44 +175,66 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_radix_hist(const uint64_t *__res
   hist[(uint64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
+// Stable scatter of one tile: keys are ranked inside the tile (match_any per
+// 256-key sub-round), placed in shared memory in digit order, then written
+// out in that order so each digit's run goes to consecutive global addresses.
 __global__ void __launch_bounds__(SORT_BLOCK) k_radix_scatter(const uint64_t *__restrict__ in,
                                                               uint64_t *__restrict__ out,
                                                               uint64_t count, int shift,
                                                               const uint64_t *__restrict__ offs,
+                                                              const uint32_t *__restrict__ hist,
                                                               uint32_t ntiles) {
-  __shared__ uint64_t run[256];
-  __shared__ uint64_t wh[SORT_WARPS][256];
+  __shared__ uint64_t tile[SORT_TILE];
+  __shared__ uint32_t run[256];     // next local slot per digit
+  __shared__ uint32_t lbase[256];   // local start of each digit
+  __shared__ uint64_t gbase[256];   // global start of each digit for this tile
+  __shared__ uint32_t wh[SORT_WARPS][256];
+  __shared__ uint32_t scan_tmp[SORT_BLOCK / 32 + 1];
   const unsigned t = threadIdx.x, w = t >> 5;
-  run[t] = offs[(uint64_t)t * ntiles + blockIdx.x];
+  {
+    const uint32_t c = hist[(uint64_t)t * ntiles + blockIdx.x];
+    uint32_t tot;
+    const uint32_t pre = block_exclusive_scan(c, scan_tmp, &tot);
+    lbase[t] = pre;
+    run[t] = pre;
+    gbase[t] = offs[(uint64_t)t * ntiles + blockIdx.x];
+  }
 #pragma unroll
   for (int q = 0; q < SORT_WARPS; q++) wh[q][t] = 0;
   __syncthreads();
   const uint64_t base = (uint64_t)blockIdx.x * SORT_TILE;
+  const uint32_t nt = (uint32_t)(count - base < SORT_TILE ? count - base : SORT_TILE);
   for (int k = 0; k < SORT_SUB; k++) {
-    uint64_t i = base + (uint64_t)k * SORT_BLOCK + t;
-    bool valid = i < count;
-    uint64_t key = valid ? in[i] : 0;
-    unsigned d = valid ? (unsigned)((key >> shift) & 255u) : 256u;
-    unsigned peers = __match_any_sync(kFull, d);
-    unsigned rank = __popc(peers & lanemask_lt());
+    const uint32_t li = k * SORT_BLOCK + t;
+    const bool valid = li < nt;
+    const uint64_t key = valid ? in[base + li] : 0;
+    const unsigned d = valid ? (unsigned)((key >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(kFull, d);
+    const unsigned rank = __popc(peers & lanemask_lt());
     if (valid && rank == 0) wh[w][d] = __popc(peers);
     __syncthreads();
     {
-      uint64_t r = run[t];
+      uint32_t r = run[t];
 #pragma unroll
       for (int q = 0; q < SORT_WARPS; q++) {
-        uint64_t c = wh[q][t];
+        const uint32_t c = wh[q][t];
         wh[q][t] = r;
         r += c;
       }
       run[t] = r;
     }
     __syncthreads();
-    if (valid) out[wh[w][d] + rank] = key;
+    if (valid) tile[wh[w][d] + rank] = key;
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < SORT_WARPS; q++) wh[q][t] = 0;
     __syncthreads();
+  }
+  // tile[] is in digit order: consecutive threads write consecutive addresses
+  for (uint32_t p = t; p < nt; p += SORT_BLOCK) {
+    const uint64_t key = tile[p];
+    const unsigned d = (unsigned)((key >> shift) & 255u);
+    out[gbase[d] + (p - lbase[d])] = key;
   }
 }
 
@@ -231,7 +253,7 @@ int sort_u64(byo_ctx *ctx, uint64_t *keys, uint64_t *tmp, uint64_t count, uint64
              count, shift, hist, (uint32_t)ntiles);
       BYO_TRY(scan_u32_to_u64(ctx, hist, 256 * ntiles, offs));
       launch_t(ctx, "sort_scatter", k_radix_scatter, dim3((unsigned)ntiles), dim3(SORT_BLOCK), 0, (const uint64_t *)a,
-             b, count, shift, (const uint64_t *)offs, (uint32_t)ntiles);
+               b, count, shift, (const uint64_t *)offs, (const uint32_t *)hist, (uint32_t)ntiles);
       uint64_t *s = a;
       a = b;
       b = s;

@@ -13,7 +13,11 @@ Targets are log2(1 + microseconds) / 16.  A trained network is installed with
 install(); BFS(..., policy=POLICY_LEARNED) and update policy UPDATE_LEARNED use
 it, and the m/20 rule stays the fallback and the judge inside the engine.
 """
+import argparse
 import ctypes
+import json
+import os
+import time
 
 import numpy as np
 
@@ -129,7 +133,7 @@ def loss_grad(ctx, params, X, Y, M):
     return float(loss.value), g
 
 
-JUDGE_MARGIN = 0.05  # the engine's kJudgeMargin
+JUDGE_MARGIN = 0.006  # the engine's kJudgeMargin (a predicted gain of about 7%)
 
 
 def round_choices(ctx, params, X, fallback):
@@ -144,3 +148,84 @@ def round_choices(ctx, params, X, fallback):
 def round_cost(Y, choice):
     """Total microseconds of the rounds under a choice per round."""
     return float(micros(Y[np.arange(len(Y)), choice]).sum())
+
+
+# ------------------------------------------------------------------ training run
+DEFAULT_PARAMS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "policy_gb300.npy")
+
+
+def load_default(ctx, path=DEFAULT_PARAMS):
+    """Installs the committed network if present; returns True if it did."""
+    if not os.path.exists(path):
+        return False
+    install(ctx, np.load(path))
+    return True
+
+
+def _graphs(ctx, scale):
+    from .graph import Graph
+    s = scale
+    return [
+        ("rmat", Graph.generate(ctx, "rmat", seed=101, lg_n=18 + s, draws=1 << (22 + s))),
+        ("rmat-sparse", Graph.generate(ctx, "rmat", seed=102, lg_n=18 + s, draws=1 << (20 + s))),
+        ("er", Graph.generate(ctx, "er", seed=103, n=1 << (18 + s), draws=1 << (21 + s))),
+        ("grid", Graph.generate(ctx, "grid", n=1 << (8 + s // 2), draws=1 << (8 + s // 2))),
+        ("chung-lu", Graph.generate(ctx, "chung_lu", seed=104, n=1 << (18 + s), draws=1 << (21 + s), exponent=2.1)),
+    ]
+
+
+def main():
+    ap = argparse.ArgumentParser(description="collect engine timings on this GPU and train the policy")
+    ap.add_argument("--out", default=DEFAULT_PARAMS)
+    ap.add_argument("--scale", type=int, default=2, help="graphs of 2^(18+scale) vertices")
+    ap.add_argument("--sources", type=int, default=12)
+    ap.add_argument("--epochs", type=int, default=600)
+    args = ap.parse_args()
+    from .graph import Context, Graph
+    ctx = Context(0)
+    t0 = time.time()
+    tr, te, report = [], [], {}
+    for name, G in _graphs(ctx, args.scale):
+        deg = G.degrees()
+        rng = np.random.default_rng(G.N() + len(name))
+        srcs = rng.choice(np.nonzero(deg)[0], args.sources, replace=False)
+        k = (2 * args.sources) // 3
+        tr.append(collect_round_samples(G, srcs[:k]))
+        te.append((name, collect_round_samples(G, srcs[k:], warm=False)))
+        G.close()
+    # update samples on the packed-memory-array container: symmetrised uniform
+    # batches, log-uniform sizes
+    G = Graph.generate(ctx, "rmat", seed=105, lg_n=20 + args.scale, draws=1 << (24 + args.scale), container="pma")
+    n = G.N()
+    rng = np.random.default_rng(7)
+    batches = []
+    for b in np.unique(np.logspace(2, 7, 16).astype(np.int64)):
+        u = rng.integers(0, n, b, dtype=np.uint64)
+        v = rng.integers(0, n, b, dtype=np.uint64)
+        batches.append(np.concatenate([(u << np.uint64(32)) | v, (v << np.uint64(32)) | u]))
+    ux, uy, um = collect_update_samples(G, batches)
+    G.close()
+    X = np.concatenate([t[0] for t in tr] + [ux])
+    Y = np.concatenate([t[1] for t in tr] + [uy])
+    M = np.concatenate([t[2] for t in tr] + [um])
+    params, losses = train(ctx, X, Y, M, epochs=args.epochs, lr=3e-3, seed=1)
+    for name, (Xt, Yt, Mt, Ct) in te:
+        ch = round_choices(ctx, params, Xt, Ct)
+        report[name] = {"rounds": int(len(Xt)), "m20_us": round_cost(Yt, Ct), "learned_us": round_cost(Yt, ch),
+                        "best_us": round_cost(Yt, Yt[:, :3].argmin(1))}
+    pu = forward(ctx, params, ux)
+    upd = {"samples": int(len(ux)), "merge_us": float(micros(uy[:, 3]).sum()),
+           "learned_us": float(micros(np.where(pu[:, 3] - pu[:, 4] > JUDGE_MARGIN, uy[:, 4], uy[:, 3])).sum()),
+           "best_us": float(micros(uy[:, 3:5].min(1)).sum())}
+    np.save(args.out, params)
+    meta = {"train_samples": int(len(X)), "epochs": args.epochs, "loss_first": float(losses[0]),
+            "loss_last": float(losses[-1]), "held_out_rounds": report, "updates_in_sample": upd,
+            "seconds": round(time.time() - t0, 1)}
+    with open(os.path.splitext(args.out)[0] + ".json", "w") as f:
+        json.dump(meta, f, indent=1)
+    print(json.dumps(meta))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
