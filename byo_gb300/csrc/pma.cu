@@ -64,6 +64,7 @@ struct Pma {
   DevBuf staging;         // uint64[...]  windowed elements
   DevBuf misc;            // flags / counters
   DevBuf epre;            // uint64[NL+1] element prefix for the view
+  DevBuf ovf, ovf_off;    // overflow area of the optimistic merge, per-leaf offsets
   uint64_t rebuilds = 0, windows = 0;
 };
 
@@ -146,23 +147,46 @@ __device__ __forceinline__ bool leaf_contains(const uint32_t *src, const uint32_
   return lo < c && slot_key(src, dst, base + lo) == key;
 }
 
-// rcount[i] = elements of leaf i after the update; one warp per leaf
-__global__ void k_pma_count(const uint32_t *__restrict__ src, const uint32_t *__restrict__ dst,
-                            const uint32_t *__restrict__ cnt, uint64_t NL, const uint64_t *__restrict__ keys,
-                            const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount) {
+// rcount[i] = elements of leaf i after the update.  One warp per leaf; the
+// leaf's keys are staged in the warp's shared memory, then every batch key of
+// the leaf's segment is looked up there.
+constexpr int kPmaWarps = 8;
+__global__ void __launch_bounds__(32 * kPmaWarps) k_pma_count(const uint32_t *__restrict__ src,
+                                                             const uint32_t *__restrict__ dst,
+                                                             const uint32_t *__restrict__ cnt, uint64_t NL,
+                                                             const uint64_t *__restrict__ keys,
+                                                             const uint64_t *__restrict__ bstart, int insert,
+                                                             uint32_t *rcount) {
+  __shared__ uint64_t As[kPmaWarps][kLeaf];
+  uint64_t *A = As[threadIdx.x >> 5];
+  const unsigned lane = lane_id();
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t i = gw; i < NL; i += nw) {
     const uint64_t b0 = bstart[i], b1 = bstart[i + 1];
     const uint32_t c = cnt[i];
+    if (b0 == b1) {
+      if (lane == 0) rcount[i] = c;
+      continue;
+    }
+    for (uint32_t e = lane; e < c; e += 32) A[e] = slot_key(src, dst, i * kLeaf + e);
+    __syncwarp();
     uint64_t present = 0;
-    for (uint64_t k = b0 + lane_id(); k < b1; k += 32)
-      present += leaf_contains(src, dst, i * kLeaf, c, keys[k]);
+    for (uint64_t k = b0 + lane; k < b1; k += 32) {
+      const uint64_t x = keys[k];
+      uint32_t lo = 0, hi = c;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (A[mid] < x) lo = mid + 1; else hi = mid;
+      }
+      present += (lo < c && A[lo] == x);
+    }
     present = warp_sum(present);
-    if (lane_id() == 0) {
-      uint64_t r = insert ? (uint64_t)c + (b1 - b0) - present : (uint64_t)c - present;
+    if (lane == 0) {
+      const uint64_t r = insert ? (uint64_t)c + (b1 - b0) - present : (uint64_t)c - present;
       rcount[i] = (uint32_t)(r > 0xFFFFFFFFull ? 0xFFFFFFFFull : r);
     }
+    __syncwarp();
   }
 }
 
@@ -215,73 +239,76 @@ __global__ void k_pma_cover(const uint8_t *__restrict__ marks, uint64_t NL, int 
 
 // ---------------------------------------------------------------- merge
 
-// One CTA per leaf with work.  Leaf A (<= kLeaf keys) is staged in shared
-// memory, and so is batch segment B when it has at most kSegCap keys (longer
-// segments are read from global memory).
+// One warp per leaf with work.  Leaf A (<= kLeaf keys) and, when it has at
+// most kSegCap keys, batch segment B are staged in the warp's shared memory
+// (longer segments are read from global memory).  Every output position comes
+// from ranks, no serial merge:
 //   insert: pos(A[i]) = i + lb_B(A[i]) - PA[i]
 //           pos(B[k]) = k - PA[lb_A(B[k])] + lb_A(B[k])   for B[k] not in A
 //           (PA[i] = number of A[0..i) also present in B)
 //   remove: pos(A[i]) = i - PA[i] for A[i] not in B
-// One binary search of A[i] in B gives both lb_B(A[i]) and the presence bit.
-// Output goes in place (leaf not in a window) or to staging[rpre[leaf]...].
-constexpr uint32_t kSegCap = 1024;
+// Lane l owns A[16l .. 16l+16): one binary search in B gives lb_B and the
+// presence bit, a warp scan of the presence counts gives PA.  Output goes in
+// place (leaf not in a window) or to staging[rpre[leaf]...].
+constexpr uint32_t kSegCap = 256;
+constexpr int kMergeWarps = 4;
+constexpr int kOwn = kLeaf / 32;
 
-__global__ void __launch_bounds__(kPmaBlock) k_pma_merge(uint32_t *src, uint32_t *dst, uint32_t *cnt,
-                                                        uint64_t NL, const uint64_t *__restrict__ keys,
-                                                        const uint64_t *__restrict__ bstart,
-                                                        const uint32_t *__restrict__ win,
-                                                        const uint64_t *__restrict__ rpre, uint64_t *staging,
-                                                        int insert, int all_windowed) {
-  __shared__ uint64_t A[kLeaf];
-  __shared__ uint64_t Bs[kSegCap];
-  __shared__ uint32_t PA[kLeaf + 1];
-  __shared__ uint32_t LB[kLeaf];
-  __shared__ uint32_t wsum[kPmaBlock / 32 + 1];
-  constexpr int kPer = kLeaf / kPmaBlock;
-  for (uint64_t j = blockIdx.x; j < NL; j += gridDim.x) {
+__global__ void __launch_bounds__(32 * kMergeWarps) k_pma_merge(uint32_t *src, uint32_t *dst, uint32_t *cnt,
+                                                               uint64_t NL, const uint64_t *__restrict__ keys,
+                                                               const uint64_t *__restrict__ bstart,
+                                                               const uint32_t *__restrict__ win,
+                                                               const uint64_t *__restrict__ rpre,
+                                                               uint64_t *staging, int insert, int all_windowed) {
+  __shared__ uint64_t As[kMergeWarps][kLeaf];
+  __shared__ uint64_t Bsh[kMergeWarps][kSegCap];
+  __shared__ uint32_t PAs[kMergeWarps][kLeaf + 1];
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  uint64_t *A = As[w];
+  uint32_t *PA = PAs[w];
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t j = gw; j < NL; j += nw) {
     const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
     const bool windowed = all_windowed || win[j] != kNoWin;
     if (b0 == b1 && !windowed) continue;
     const uint32_t c = cnt[j];
     const uint64_t nb = b1 - b0;
     const bool bsm = nb <= kSegCap;
-    const uint64_t *B = bsm ? Bs : keys + b0;
+    const uint64_t *B = bsm ? Bsh[w] : keys + b0;
     const uint64_t base = j * kLeaf;
-    for (uint32_t i = threadIdx.x; i < c; i += kPmaBlock) A[i] = slot_key(src, dst, base + i);
+    for (uint32_t e = lane; e < c; e += 32) A[e] = slot_key(src, dst, base + e);
     if (bsm)
-      for (uint32_t k = threadIdx.x; k < nb; k += kPmaBlock) Bs[k] = keys[b0 + k];
-    __syncthreads();
-    // lb_B(A[i]) and presence, then exclusive prefix PA (blocked: thread t owns
-    // A[t*kPer .. t*kPer+kPer))
-    uint32_t f[kPer];
+      for (uint32_t k = lane; k < nb; k += 32) Bsh[w][k] = keys[b0 + k];
+    __syncwarp();
+    uint32_t lb[kOwn];
+    uint32_t hits = 0;
 #pragma unroll
-    for (int q = 0; q < kPer; q++) {
-      const uint32_t i = threadIdx.x * kPer + q;
-      uint32_t hit = 0;
+    for (int q = 0; q < kOwn; q++) {
+      const uint32_t i = lane * kOwn + q;
+      lb[q] = 0;
       if (i < c) {
-        uint64_t lo = 0, hi = nb;
         const uint64_t x = A[i];
+        uint64_t lo = 0, hi = nb;
         while (lo < hi) {
-          uint64_t mid = (lo + hi) >> 1;
+          const uint64_t mid = (lo + hi) >> 1;
           if (B[mid] < x) lo = mid + 1; else hi = mid;
         }
-        LB[i] = (uint32_t)lo;
-        hit = (lo < nb && B[lo] == x) ? 1u : 0u;
+        lb[q] = (uint32_t)lo;
+        if (lo < nb && B[lo] == x) hits |= 1u << q;
       }
-      f[q] = hit;
     }
-    uint32_t ts = 0;
+    const uint32_t mine = __popc(hits);
+    const uint32_t incl = warp_inclusive_scan(mine);
+    const uint32_t tot = __shfl_sync(kFull, incl, 31);
+    uint32_t run = incl - mine;
 #pragma unroll
-    for (int q = 0; q < kPer; q++) ts += f[q];
-    uint32_t tot;
-    uint32_t pre = block_exclusive_scan(ts, wsum, &tot);
-#pragma unroll
-    for (int q = 0; q < kPer; q++) {
-      PA[threadIdx.x * kPer + q] = pre;
-      pre += f[q];
+    for (int q = 0; q < kOwn; q++) {
+      PA[lane * kOwn + q] = run;
+      run += (hits >> q) & 1u;
     }
-    if (threadIdx.x == 0) PA[kLeaf] = tot;
-    __syncthreads();
+    if (lane == 31) PA[kLeaf] = tot;
+    __syncwarp();
     const uint64_t r = insert ? (uint64_t)c + nb - tot : (uint64_t)c - tot;
     uint64_t *ostage = windowed ? staging + rpre[j] : nullptr;
     auto put = [&](uint64_t pos, uint64_t key) {
@@ -292,19 +319,22 @@ __global__ void __launch_bounds__(kPmaBlock) k_pma_merge(uint32_t *src, uint32_t
         dst[base + pos] = (uint32_t)key;
       }
     };
-    for (uint32_t i = threadIdx.x; i < c; i += kPmaBlock) {
-      if (insert) {
-        put(i + LB[i] - PA[i], A[i]);
-      } else if (PA[i + 1] == PA[i]) {
-        put(i - PA[i], A[i]);
+    // A elements (each lane its own run: positions increase along it)
+#pragma unroll
+    for (int q = 0; q < kOwn; q++) {
+      const uint32_t i = lane * kOwn + q;
+      if (i < c) {
+        const uint32_t pa = PA[i];
+        if (insert) put(i + lb[q] - pa, A[i]);
+        else if (!((hits >> q) & 1u)) put(i - pa, A[i]);
       }
     }
     if (insert) {
-      for (uint64_t k = threadIdx.x; k < nb; k += kPmaBlock) {
+      for (uint64_t k = lane; k < nb; k += 32) {
         const uint64_t x = B[k];
         uint32_t lo = 0, hi = c;  // lb_A(x)
         while (lo < hi) {
-          uint32_t mid = (lo + hi) >> 1;
+          const uint32_t mid = (lo + hi) >> 1;
           if (A[mid] < x) lo = mid + 1; else hi = mid;
         }
         if (lo < c && A[lo] == x) continue;  // already present
@@ -312,13 +342,163 @@ __global__ void __launch_bounds__(kPmaBlock) k_pma_merge(uint32_t *src, uint32_t
       }
     }
     if (!windowed) {
-      for (uint64_t p = r + threadIdx.x; p < c; p += kPmaBlock) {
+      for (uint64_t p = r + lane; p < c; p += 32) {
         src[base + p] = kSentinel;
         dst[base + p] = kSentinel;
       }
-      if (threadIdx.x == 0) cnt[j] = (uint32_t)r;
+      if (lane == 0) cnt[j] = (uint32_t)r;
     }
-    __syncthreads();
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- optimistic merge
+// One warp per leaf with a batch segment.  The leaf (A) and, when short, the
+// segment (B) are staged in the warp's shared memory.  The merged sequence of
+// A and B (ties: A first) is cut into 32 equal diagonals (merge path, one
+// binary search per lane); each lane walks its diagonal twice: once to count
+// the elements it keeps, then -- after a warp scan -- to write them at their
+// final positions.
+//   insert keeps every A, and B[j] unless it equals the A element before it;
+//   remove keeps A[i] unless it equals the B element it is compared with.
+// When the result fits the leaf it is written in place; otherwise it goes to
+// the overflow area (ovf) and the leaf is redistributed afterwards.
+constexpr int kOptWarps = 6;
+constexpr uint32_t kOptSeg = 256;
+
+__device__ __forceinline__ uint64_t bval(const uint64_t *B, uint64_t j) { return B[j]; }
+
+__global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
+    uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
+    const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
+    unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta) {
+  __shared__ uint64_t As[kOptWarps][kLeaf];
+  __shared__ uint64_t Bsh[kOptWarps][kOptSeg];
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  const uint64_t *A = As[w];
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  long long dsum = 0;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
+    const uint32_t c = cnt[j];
+    if (b0 == b1) {
+      if (lane == 0) rcount[j] = c;
+      continue;
+    }
+    const uint64_t nb = b1 - b0;
+    const uint64_t *B = nb <= kOptSeg ? Bsh[w] : keys + b0;
+    const uint64_t base = j * kLeaf;
+    for (uint32_t e = lane; e < c; e += 32) As[w][e] = slot_key(src, dst, base + e);
+    if (nb <= kOptSeg)
+      for (uint32_t k = lane; k < nb; k += 32) Bsh[w][k] = keys[b0 + k];
+    __syncwarp();
+    // this lane's diagonal [d0, d1) of the merged sequence
+    const uint64_t T = c + nb, per = (T + 31) / 32;
+    const uint64_t d0 = lane * per < T ? lane * per : T, d1 = d0 + per < T ? d0 + per : T;
+    uint64_t lo = d0 > nb ? d0 - nb : 0, hi = d0 < c ? d0 : c;
+    while (lo < hi) {  // number of A elements among the first d0 merged
+      const uint64_t mid = (lo + hi) >> 1;
+      if (A[mid] <= bval(B, d0 - mid - 1)) lo = mid + 1; else hi = mid;
+    }
+    const uint64_t i0 = lo, j0 = d0 - lo;
+    // pass 1: count kept elements
+    uint32_t keep = 0;
+    {
+      uint64_t i = i0, k = j0;
+      for (uint64_t d = d0; d < d1; d++) {
+        if (i < c && (k >= nb || A[i] <= bval(B, k))) {
+          const uint64_t x = A[i];
+          if (insert) keep++;
+          else if (!(k < nb && bval(B, k) == x)) keep++;
+          i++;
+        } else {
+          const uint64_t x = bval(B, k);
+          if (insert && !(i > 0 && A[i - 1] == x)) keep++;
+          k++;
+        }
+      }
+    }
+    const uint32_t incl = warp_inclusive_scan(keep);
+    const uint32_t r = __shfl_sync(kFull, incl, 31);
+    uint32_t pos = incl - keep;
+    uint32_t *osrc = nullptr, *odst = nullptr;
+    uint64_t *ostage = nullptr;
+    if (r <= kLeaf) {
+      osrc = src + base;
+      odst = dst + base;
+    } else {
+      unsigned long long at = 0;
+      if (lane == 0) {
+        at = atomicAdd(&ctr[0], (unsigned long long)r);
+        atomicAdd(&ctr[1], 1ull);
+        ovf_off[j] = at;
+      }
+      at = __shfl_sync(kFull, at, 0);
+      ostage = ovf + at;
+    }
+    __syncwarp();  // every lane has read A before any in-place write
+    {
+      uint64_t i = i0, k = j0;
+      for (uint64_t d = d0; d < d1; d++) {
+        uint64_t x;
+        bool kept;
+        if (i < c && (k >= nb || A[i] <= bval(B, k))) {
+          x = A[i];
+          kept = insert || !(k < nb && bval(B, k) == x);
+          i++;
+        } else {
+          x = bval(B, k);
+          kept = insert && !(i > 0 && A[i - 1] == x);
+          k++;
+        }
+        if (kept) {
+          if (ostage) {
+            ostage[pos] = x;
+          } else {
+            osrc[pos] = (uint32_t)(x >> 32);
+            odst[pos] = (uint32_t)x;
+          }
+          pos++;
+        }
+      }
+    }
+    if (!ostage) {
+      for (uint32_t q = r + lane; q < c; q += 32) {
+        src[base + q] = kSentinel;
+        dst[base + q] = kSentinel;
+      }
+      if (lane == 0) cnt[j] = r;
+    }
+    if (lane == 0) {
+      rcount[j] = r;
+      dsum += (long long)r - (long long)c;
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && dsum) atomicAdd((unsigned long long *)delta, (unsigned long long)dsum);
+}
+
+// Copies the current contents of every leaf in a window (all leaves when
+// `all`) to staging[rpre[leaf] ...]: from the overflow area for a leaf that
+// overflowed, from the leaf itself otherwise.
+__global__ void k_pma_gather(const uint32_t *__restrict__ src, const uint32_t *__restrict__ dst,
+                             const uint32_t *__restrict__ rcount, const uint32_t *__restrict__ cnt, uint64_t NL,
+                             const uint32_t *__restrict__ win, int all, const uint64_t *__restrict__ rpre,
+                             const uint64_t *__restrict__ ovf, const uint64_t *__restrict__ ovf_off,
+                             uint64_t *staging) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    if (!all && win[j] == kNoWin) continue;
+    const uint32_t r = rcount[j];
+    uint64_t *out = staging + rpre[j];
+    if (r > kLeaf || r != cnt[j]) {  // overflowed: its merge result is in ovf
+      const uint64_t *in = ovf + ovf_off[j];
+      for (uint32_t e = lane_id(); e < r; e += 32) out[e] = in[e];
+    } else {
+      for (uint32_t e = lane_id(); e < r; e += 32) out[e] = slot_key(src, dst, j * kLeaf + e);
+    }
   }
 }
 
@@ -516,7 +696,7 @@ void pma_destroy(Pma *p) {
   if (!p) return;
   pma_free_arrays(p);
   for (DevBuf *b : {&p->keys_a, &p->keys_b, &p->bstart, &p->rcount, &p->rpre, &p->win, &p->marks, &p->staging,
-                    &p->misc, &p->epre})
+                    &p->misc, &p->epre, &p->ovf, &p->ovf_off})
     free_buf(*b);
   delete p;
 }
@@ -539,8 +719,9 @@ static int pma_rebuild(byo_graph *g, const uint64_t *keys, const uint64_t *bstar
   Pma *p = g->pma;
   BYO_TRY(ensure(ctx, p->staging, (total ? total : 1) * 8));
   uint64_t *stg = (uint64_t *)p->staging.p;
-  launch_t(ctx, "pma_merge", k_pma_merge, dim3(grid_for(ctx, p->NL, 1, 16)), dim3(kPmaBlock), 0, p->src, p->dst,
-           p->cnt, p->NL, keys, bstart, (const uint32_t *)nullptr, rpre, stg, insert, 1);
+  launch_t(ctx, "pma_merge", k_pma_merge, dim3(grid_for(ctx, p->NL * 32, 32 * kMergeWarps, 6)),
+           dim3(32 * kMergeWarps), 0, p->src, p->dst, p->cnt, p->NL, keys, bstart, (const uint32_t *)nullptr, rpre,
+           stg, insert, 1);
   BYO_TRY(check_launch(ctx, "pma_rebuild merge"));
   p->rebuilds++;
   return pma_layout(g, stg, total, leaves_for(total));
@@ -555,11 +736,11 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   // 1. validate, copy, sort, unique
   BYO_TRY(ensure(ctx, p->keys_a, count * 8));
   BYO_TRY(ensure(ctx, p->keys_b, count * 8));
-  BYO_TRY(ensure(ctx, p->misc, 64));
+  BYO_TRY(ensure(ctx, p->misc, 128));
   uint64_t *ka = (uint64_t *)p->keys_a.p, *kb = (uint64_t *)p->keys_b.p;
   unsigned long long *bounds = (unsigned long long *)p->misc.p;
-  unsigned int *flags = (unsigned int *)(bounds + 2);  // [0] unsorted, [1] grow, [2] any overflow
-  BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 64, ctx->stream));
+  unsigned int *flags = (unsigned int *)(bounds + 2);  // [0] unsorted, [1] grow, [2] any overflow, [4..] counters
+  BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 128, ctx->stream));
   launch(ctx, k_key_bounds, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, bounds);
   if (sorted)
     launch(ctx, k_check_sorted, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, flags);
@@ -574,14 +755,11 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   if (sorted) {
     batch = const_cast<uint64_t *>(d_keys_in);
   } else {
-    BYO_CU(ctx, cudaMemcpyAsync(ka, d_keys_in, count * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-    uint64_t *s = nullptr;
-    BYO_TRY(sort_u64(ctx, ka, kb, count, sig_mask_for(g->n), &s));
-    uint64_t *u = s == ka ? kb : ka;
-    BYO_TRY(unique_u64(ctx, s, count, 0, u, &b));
-    batch = u;
+    BYO_TRY(sort_bucketed(ctx, d_keys_in, count, g->n, ka, kb));
+    BYO_TRY(unique_u64(ctx, ka, count, 0, kb, &b));
+    batch = kb;
   }
-  // 2. route and count
+  // 2. route
   const uint64_t NL = p->NL;
   BYO_TRY(ensure(ctx, p->bstart, (NL + 1) * 8));
   BYO_TRY(ensure(ctx, p->rcount, NL * 4));
@@ -590,58 +768,78 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   uint32_t *rcount = (uint32_t *)p->rcount.p;
   launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
          (const uint64_t *)batch, b, bstart);
-  launch(ctx, k_pma_count, dim3(grid_for(ctx, NL * 32, 256, 16)), dim3(256), 0, (const uint32_t *)p->src,
-         (const uint32_t *)p->dst, (const uint32_t *)p->cnt, NL, (const uint64_t *)batch,
-         (const uint64_t *)bstart, insert, rcount);
-  BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
-  BYO_CU(ctx, cudaMemcpyAsync(h, rpre + NL, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const uint64_t total = h[0];
-  if (changed) *changed = insert ? total - m_before : m_before - total;
-  if (total == m_before) return BYO_OK;  // nothing new / nothing present
-  // 3. strategy: in-place merge (default), or rebuild when asked for, chosen
-  // by the learned policy, or forced by capacity (grow / shrink)
+  // 3. strategy: in-place merge (default), rebuild when asked for or chosen by
+  // the learned policy; capacity may still force a rebuild below
   int strategy = 0;
   if (ctx->update_policy == BYO_UPDATE_REBUILD) strategy = 1;
   else if (ctx->update_policy == BYO_UPDATE_LEARNED)
     strategy = update_strategy(ctx, b, m_before, NL * kLeaf, sorted, insert);
-  const double cap = (double)NL * kLeaf;
-  if ((double)total > kRootMax * cap || (!insert && (double)total < kRootMin * cap && NL > 1)) strategy = 1;
   ctx->last_update_strategy = strategy;
-  if (strategy == 1) return pma_rebuild(g, batch, bstart, rpre, total, insert);
-  // 4. windows for overflowing leaves
-  BYO_TRY(ensure(ctx, p->marks, (uint64_t)(p->H + 1) * NL));
-  BYO_TRY(ensure(ctx, p->win, NL * 4));
-  uint8_t *marks = (uint8_t *)p->marks.p;
-  uint32_t *win = (uint32_t *)p->win.p;
-  BYO_CU(ctx, cudaMemsetAsync(marks, 0, (uint64_t)(p->H + 1) * NL, ctx->stream));
-  launch(ctx, k_pma_windows, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint32_t *)rcount,
-         (const uint64_t *)rpre, NL, p->H, marks, flags + 1, flags + 2);
-  BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const unsigned int *hf = (const unsigned int *)h;
-  if (hf[1]) {
-    ctx->last_update_strategy = 1;
+  if (strategy == 1) {
+    launch(ctx, k_pma_count, dim3(grid_for(ctx, NL * 32, 32 * kPmaWarps, 4)), dim3(32 * kPmaWarps), 0,
+           (const uint32_t *)p->src, (const uint32_t *)p->dst, (const uint32_t *)p->cnt, NL,
+           (const uint64_t *)batch, (const uint64_t *)bstart, insert, rcount);
+    BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
+    BYO_CU(ctx, cudaMemcpyAsync(h, rpre + NL, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+    const uint64_t total = h[0];
+    if (changed) *changed = insert ? total - m_before : m_before - total;
+    if (total == m_before) return BYO_OK;
     return pma_rebuild(g, batch, bstart, rpre, total, insert);
   }
-  const bool any = hf[2] != 0;
-  uint64_t *stg = nullptr;
-  if (any) {
-    launch(ctx, k_pma_cover, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint8_t *)marks, NL, p->H, win);
-    BYO_TRY(ensure(ctx, p->staging, total * 8));
-    stg = (uint64_t *)p->staging.p;
-    p->windows++;
-  } else {
-    BYO_CU(ctx, cudaMemsetAsync(win, 0xFF, NL * 4, ctx->stream));
+  // 4. optimistic merge: leaves that fit are done in place
+  BYO_TRY(ensure(ctx, p->ovf, (NL * kLeaf + b + 1) * 8));
+  BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
+  unsigned long long *ctr = (unsigned long long *)(flags + 4);  // [0] cursor, [1] leaves, [2] delta
+  BYO_CU(ctx, cudaMemsetAsync(ctr, 0, 24, ctx->stream));
+  launch_t(ctx, "pma_merge", k_pma_merge_opt, dim3(grid_for(ctx, NL * 32, 32 * kOptWarps, 6)), dim3(32 * kOptWarps),
+           0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch, (const uint64_t *)bstart, insert, rcount,
+           (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2));
+  BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 24, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const uint64_t novf = h[1];
+  const long long delta = (long long)h[2];
+  const uint64_t total = (uint64_t)((long long)m_before + delta);
+  if (changed) *changed = insert ? total - m_before : m_before - total;
+  const double cap = (double)NL * kLeaf;
+  const bool shrink = !insert && (double)total < kRootMin * cap && NL > 1;
+  if (novf == 0 && !shrink) {
+    BYO_TRY(check_launch(ctx, "pma_update"));
+    return pma_view(g);
   }
-  // 5. merge (in place, or into staging for windowed leaves), then spread
-  launch_t(ctx, "pma_merge", k_pma_merge, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0, p->src, p->dst,
-           p->cnt, NL, (const uint64_t *)batch, (const uint64_t *)bstart, (const uint32_t *)win,
-           (const uint64_t *)rpre, stg, insert, 0);
-  if (any)
-    launch_t(ctx, "pma_redistribute", k_pma_spread, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0,
-             (const uint64_t *)stg, (const uint64_t *)rpre, (const uint32_t *)win, NL, p->src, p->dst, p->cnt,
-             p->sep, NL, 0, (const uint64_t *)p->sep);
+  // 5. overflow (or shrink): windows over the counts after the merge
+  BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
+  BYO_TRY(ensure(ctx, p->win, NL * 4));
+  uint32_t *win = (uint32_t *)p->win.p;
+  bool rebuild = shrink || (double)total > kRootMax * cap;
+  if (!rebuild) {
+    BYO_TRY(ensure(ctx, p->marks, (uint64_t)(p->H + 1) * NL));
+    uint8_t *marks = (uint8_t *)p->marks.p;
+    BYO_CU(ctx, cudaMemsetAsync(marks, 0, (uint64_t)(p->H + 1) * NL, ctx->stream));
+    BYO_CU(ctx, cudaMemsetAsync(flags + 1, 0, 8, ctx->stream));
+    launch(ctx, k_pma_windows, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint32_t *)rcount,
+           (const uint64_t *)rpre, NL, p->H, marks, flags + 1, flags + 2);
+    BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+    rebuild = ((const unsigned int *)h)[1] != 0;
+    if (!rebuild) launch(ctx, k_pma_cover, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint8_t *)marks, NL,
+                         p->H, win);
+  }
+  BYO_TRY(ensure(ctx, p->staging, (total ? total : 1) * 8));
+  uint64_t *stg = (uint64_t *)p->staging.p;
+  launch(ctx, k_pma_gather, dim3(grid_for(ctx, NL * 32, 256, 16)), dim3(256), 0, (const uint32_t *)p->src,
+         (const uint32_t *)p->dst, (const uint32_t *)rcount, (const uint32_t *)p->cnt, NL, (const uint32_t *)win,
+         rebuild ? 1 : 0, (const uint64_t *)rpre, (const uint64_t *)p->ovf.p, (const uint64_t *)p->ovf_off.p, stg);
+  BYO_TRY(check_launch(ctx, "pma_gather"));
+  if (rebuild) {
+    ctx->last_update_strategy = 1;
+    p->rebuilds++;
+    return pma_layout(g, stg, total, leaves_for(total));
+  }
+  p->windows++;
+  launch_t(ctx, "pma_redistribute", k_pma_spread, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0,
+           (const uint64_t *)stg, (const uint64_t *)rpre, (const uint32_t *)win, NL, p->src, p->dst, p->cnt, p->sep,
+           NL, 0, (const uint64_t *)p->sep);
   BYO_TRY(check_launch(ctx, "pma_update"));
   return pma_view(g);
 }

@@ -9,6 +9,8 @@
 //              256-key sub-round at a time, then one store per key.
 // Algorithmic bytes per pass: 8 (histogram read) + 8 + 8 (scatter read/write)
 // per key.
+#include <vector>
+
 #include "device.cuh"
 #include "internal.h"
 #include "scan.cuh"
@@ -261,6 +263,171 @@ int sort_u64(byo_ctx *ctx, uint64_t *keys, uint64_t *tmp, uint64_t count, uint64
   }
   *sorted = a;
   return check_launch(ctx, "sort_u64");
+}
+
+// ---------------------------------------------------------------- bucketed batch sort
+// For update batches: keys (src << 32 | dst) with src, dst < n.  One counting
+// pass partitions the keys into buckets by the top bits of src (about 24 keys
+// per bucket for a uniform batch),
+// then one warp per bucket sorts it by rank in shared memory.  Buckets larger
+// than kWarpBucket fall back to the LSD sort on their range.
+// Traffic: read, read + write, read + write = 40 bytes per key (LSD over 44
+// significant bits needs 6 passes of 24 bytes).
+
+__global__ void k_bucket_count(const uint64_t *__restrict__ keys, uint64_t count, int shift,
+                               unsigned int *cnt) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    atomicAdd(cnt + ((keys[i] >> 32) >> shift), 1u);
+}
+
+__global__ void k_bucket_scatter(const uint64_t *__restrict__ keys, uint64_t count, int shift,
+                                 const uint64_t *__restrict__ boff, unsigned int *cursor, uint64_t *out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[i];
+    const uint64_t b = (k >> 32) >> shift;
+    out[boff[b] + atomicAdd(cursor + b, 1u)] = k;
+  }
+}
+
+// One warp per bucket: bitonic network in registers.  Element r*32 + lane
+// lives in register r of that lane: strides below 32 exchange through
+// shuffles, larger strides swap registers inside a lane, so the sort touches
+// no shared memory.  Buckets are padded with ~0 to R*32 keys; buckets above
+// kWarpBucket keys are listed for the LSD fallback.
+constexpr uint32_t kWarpBucket = 512;
+
+template <int R>
+__device__ __forceinline__ void warp_bitonic(uint64_t (&v)[R]) {
+  const unsigned lane = lane_id();
+#pragma unroll
+  for (int size = 2; size <= R * 32; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride >= 32) {
+        const int rs = stride / 32;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          if ((r & rs) == 0) {
+            const bool up = ((r * 32) & size) == 0;
+            const uint64_t x = v[r], y = v[r ^ rs];
+            if ((x > y) == up) {
+              v[r] = y;
+              v[r ^ rs] = x;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const unsigned i = r * 32 + lane;
+          const uint64_t x = v[r];
+          const uint64_t y = __shfl_xor_sync(kFull, x, stride);
+          const bool up = (i & size) == 0, lower = (lane & stride) == 0;
+          const uint64_t lo = x < y ? x : y, hi = x < y ? y : x;
+          v[r] = (lower == up) ? lo : hi;
+        }
+      }
+    }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void bucket_sort_regs(const uint64_t *__restrict__ in, uint64_t *out, uint64_t lo,
+                                                 uint32_t s) {
+  uint64_t v[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const uint32_t i = r * 32 + lane_id();
+    v[r] = i < s ? in[lo + i] : ~0ull;
+  }
+  warp_bitonic<R>(v);
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const uint32_t i = r * 32 + lane_id();
+    if (i < s) out[lo + i] = v[r];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bucket_sort(const uint64_t *__restrict__ in, uint64_t *out,
+                                                    const uint64_t *__restrict__ boff, uint64_t nb,
+                                                    unsigned int *large, unsigned int *nlarge) {
+  const unsigned lane = lane_id();
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t b = gw; b < nb; b += nw) {
+    const uint64_t lo = boff[b], s = boff[b + 1] - lo;
+    if (s == 0) continue;
+    if (s > kWarpBucket) {
+      if (lane == 0) large[atomicAdd(nlarge, 1u)] = (unsigned int)b;
+      continue;
+    }
+    if (s <= 32) bucket_sort_regs<1>(in, out, lo, (uint32_t)s);
+    else if (s <= 64) bucket_sort_regs<2>(in, out, lo, (uint32_t)s);
+    else if (s <= 128) bucket_sort_regs<4>(in, out, lo, (uint32_t)s);
+    else if (s <= 256) bucket_sort_regs<8>(in, out, lo, (uint32_t)s);
+    else bucket_sort_regs<16>(in, out, lo, (uint32_t)s);
+  }
+}
+
+int sort_bucketed(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t n, uint64_t *out, uint64_t *tmp) {
+  if (count == 0) return BYO_OK;
+  int lg = 0;
+  while ((1ull << lg) < n) lg++;
+  // about 24 keys per bucket: most buckets sort in one or two registers a lane
+  int D = 8;
+  while (D < 24 && (1ull << D) * 24 < count) D++;
+  if (D > lg) D = lg;
+  const int shift = lg - D;
+  const uint64_t nb = ((n - 1) >> shift) + 1;
+  if (count > nb * (kWarpBucket / 2)) {
+    // buckets would mostly overflow the register sort: global LSD instead
+    uint64_t *res = nullptr;
+    BYO_CU(ctx, cudaMemcpyAsync(out, in, count * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    BYO_TRY(sort_u64(ctx, out, tmp, count, sig_mask_for(n), &res));
+    if (res != out) BYO_CU(ctx, cudaMemcpyAsync(out, res, count * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    return check_launch(ctx, "sort_bucketed");
+  }
+  unsigned int *cnt = nullptr;
+  uint64_t *boff = nullptr;
+  BYO_TRY(scratch(ctx, 4, 2 * nb + 8, &cnt));  // counts, cursors, large-bucket count
+  BYO_TRY(scratch(ctx, 5, nb + 1, &boff));
+  unsigned int *cursor = cnt + nb, *nlarge = cnt + 2 * nb;
+  BYO_CU(ctx, cudaMemsetAsync(cnt, 0, (2 * nb + 8) * 4, ctx->stream));
+  launch(ctx, k_bucket_count, dim3(grid_for(ctx, count, 256, 16)), dim3(256), 0, in, count, shift, cnt);
+  BYO_TRY(scan_u32_to_u64(ctx, cnt, nb, boff));
+  launch(ctx, k_bucket_scatter, dim3(grid_for(ctx, count, 256, 16)), dim3(256), 0, in, count, shift,
+         (const uint64_t *)boff, cursor, tmp);
+  // the large-bucket list reuses the count array (the counts live in boff now)
+  launch_t(ctx, "sort_scatter", k_bucket_sort, dim3(grid_for(ctx, nb * 32, 256, 8)), dim3(256), 0,
+           (const uint64_t *)tmp, out, (const uint64_t *)boff, nb, cnt, nlarge);
+  BYO_TRY(check_launch(ctx, "sort_bucketed"));
+  unsigned int *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, nlarge, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned int nl = h[0];
+  if (nl) {
+    // the LSD sort below reuses scratch slots 4 and 5 (counts, offsets):
+    // take every large bucket's range first
+    std::vector<unsigned int> big(nl);
+    std::vector<uint64_t> ranges(2 * (size_t)nl);
+    BYO_CU(ctx, cudaMemcpy(big.data(), cnt, nl * 4, cudaMemcpyDeviceToHost));
+    for (unsigned int q = 0; q < nl; q++)
+      BYO_CU(ctx, cudaMemcpy(&ranges[2 * q], boff + big[q], 16, cudaMemcpyDeviceToHost));
+    const uint64_t low_src = ((1ull << shift) - 1) << 32;
+    const uint64_t dst_mask = (lg >= 32) ? 0xFFFFFFFFull : ((1ull << lg) - 1);
+    for (unsigned int q = 0; q < nl; q++) {
+      const uint64_t lo = ranges[2 * q], sz = ranges[2 * q + 1] - ranges[2 * q];
+      uint64_t *res = nullptr;
+      BYO_CU(ctx, cudaMemcpyAsync(out + lo, tmp + lo, sz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+      BYO_TRY(sort_u64(ctx, out + lo, tmp + lo, sz, low_src | dst_mask, &res));
+      if (res != out + lo)
+        BYO_CU(ctx, cudaMemcpyAsync(out + lo, res, sz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+  }
+  return check_launch(ctx, "sort_bucketed");
 }
 
 // ---------------------------------------------------------------- unique / compaction
