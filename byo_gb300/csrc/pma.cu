@@ -359,7 +359,9 @@ __global__ void __launch_bounds__(32 * kMergeWarps) k_pma_merge(uint32_t *src, u
 // binary search per lane); each lane walks its diagonal twice: once to count
 // the elements it keeps, then -- after a warp scan -- to write them at their
 // final positions.
-//   insert keeps every A, and B[j] unless it equals the A element before it;
+//   insert keeps every A, and B[j] unless it equals the A element before it
+//   or the B element before it (B may hold duplicates: it is sorted, not
+//   deduplicated);
 //   remove keeps A[i] unless it equals the B element it is compared with.
 // When the result fits the leaf it is written in place; otherwise it goes to
 // the overflow area (ovf) and the leaf is redistributed afterwards.
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
           i++;
         } else {
           const uint64_t x = bval(B, k);
-          if (insert && !(i > 0 && A[i - 1] == x)) keep++;
+          if (insert && !(i > 0 && A[i - 1] == x) && !(k > 0 && bval(B, k - 1) == x)) keep++;
           k++;
         }
       }
@@ -449,7 +451,7 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
           i++;
         } else {
           x = bval(B, k);
-          kept = insert && !(i > 0 && A[i - 1] == x);
+          kept = insert && !(i > 0 && A[i - 1] == x) && !(k > 0 && bval(B, k - 1) == x);
           k++;
         }
         if (kept) {
@@ -755,9 +757,9 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   if (sorted) {
     batch = const_cast<uint64_t *>(d_keys_in);
   } else {
+    // sorted, duplicates kept: the optimistic merge drops them itself
     BYO_TRY(sort_bucketed(ctx, d_keys_in, count, g->n, ka, kb));
-    BYO_TRY(unique_u64(ctx, ka, count, 0, kb, &b));
-    batch = kb;
+    batch = ka;
   }
   // 2. route
   const uint64_t NL = p->NL;
@@ -776,6 +778,12 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     strategy = update_strategy(ctx, b, m_before, NL * kLeaf, sorted, insert);
   ctx->last_update_strategy = strategy;
   if (strategy == 1) {
+    if (!sorted) {  // the counting merge wants unique keys
+      BYO_TRY(unique_u64(ctx, ka, count, 0, kb, &b));
+      batch = kb;
+      launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
+             (const uint64_t *)batch, b, bstart);
+    }
     launch(ctx, k_pma_count, dim3(grid_for(ctx, NL * 32, 32 * kPmaWarps, 4)), dim3(32 * kPmaWarps), 0,
            (const uint32_t *)p->src, (const uint32_t *)p->dst, (const uint32_t *)p->cnt, NL,
            (const uint64_t *)batch, (const uint64_t *)bstart, insert, rcount);
