@@ -95,6 +95,8 @@ SIGNATURES = {
     "byo_gen_uniform_keys_device": (_int, [_vp, _u64, _u64, _u64, _vp]),
     "byo_bfs": (_int, [_vp, _u32, _vp, _vp, _int, _P(_u32)]),
     "byo_bfs_device": (_int, [_vp, _u32, _vp, _vp, _int, _P(_u32)]),
+    "byo_bfs_multi": (_int, [_vp, _vp, _u32, _vp, _P(_u32)]),
+    "byo_bfs_multi_device": (_int, [_vp, _vp, _u32, _vp, _P(_u32)]),
     "byo_cc": (_int, [_vp, _vp]),
     "byo_cc_device": (_int, [_vp, _vp]),
     "byo_bfs_cc": (_int, [_vp, _vp]),

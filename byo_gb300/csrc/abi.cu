@@ -266,6 +266,19 @@ int byo_bfs(byo_graph *g, uint32_t src, uint32_t *h_parent, uint32_t *h_level, i
   return BYO_OK;
 }
 
+int byo_bfs_multi_device(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint32_t *rounds) {
+  if (!g || !h_srcs || !d_levels) return BYO_EINVAL;
+  return bfs_multi_run(g, h_srcs, k, d_levels, rounds);
+}
+
+int byo_bfs_multi(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *h_levels, uint32_t *rounds) {
+  if (!g || !h_srcs || !h_levels) return BYO_EINVAL;
+  uint32_t *d = nullptr;
+  BYO_TRY(ws(g, WS_TC_NBR, (uint64_t)k * g->n + 1, &d));
+  BYO_TRY(bfs_multi_run(g, h_srcs, k, d, rounds));
+  return copy_to_host(g->ctx, h_levels, d, (uint64_t)k * g->n * 4);
+}
+
 int byo_cc_device(byo_graph *g, uint32_t *d_label) {
   if (!g || !d_label) return BYO_EINVAL;
   return cc_run(g, d_label);

@@ -196,6 +196,9 @@ int gen_uniform_keys(byo_ctx *ctx, uint64_t seed, uint64_t n, uint64_t count, ui
 int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, int policy,
             uint32_t *rounds);
 
+// ---------------------------------------------------------------- 64-source BFS (msbfs.cu)
+int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint32_t *rounds);
+
 // ---------------------------------------------------------------- algorithms (algos.cu)
 int cc_run(byo_graph *g, uint32_t *d_label);
 int bfs_cc_run(byo_graph *g, uint32_t *d_label);

@@ -317,6 +317,15 @@ def BFS(G, src, policy=_abi.POLICY_M20, levels=False, out=None):
     return (par, lev) if levels else par
 
 
+def BFS_multi(G, sources):
+    """Levels from up to 64 sources in one bit-lane traversal: array [k, n]."""
+    srcs = np.ascontiguousarray(sources, np.uint32)
+    out = np.empty((len(srcs), G.N()), np.uint32)
+    r = ctypes.c_uint32(0)
+    check(lib().byo_bfs_multi(G.h, _ptr(srcs), len(srcs), _ptr(out), ctypes.byref(r)), G.ctx.h)
+    return out
+
+
 def SimpleUnionAsync(G, out=None):
     out = out if out is not None else np.empty(G.N(), np.uint32)
     check(lib().byo_cc(G.h, _ptr(out)), G.ctx.h)

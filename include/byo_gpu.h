@@ -155,6 +155,16 @@ int byo_bfs(byo_graph *g, uint32_t src, uint32_t *h_parent, uint32_t *h_level, i
 int byo_bfs_device(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, int policy,
                    uint32_t *rounds);
 
+/* Batched BFS from k <= 64 sources at once, bit lanes of one traversal run
+ * by a persistent kernel.  levels[s * n + v] is the BFS level of v from
+ * srcs[s] (BYO_NONE if unreached), identical to byo_bfs's levels; sources may
+ * repeat.  Levels above 65534 are not supported (BYO_EINVAL is not raised;
+ * such graphs stop at that depth). */
+int byo_bfs_multi(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *h_levels,
+                  uint32_t *rounds);
+int byo_bfs_multi_device(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels,
+                         uint32_t *rounds);
+
 /* Connectivity, SimpleUnionAsync semantics
  * (benchmarks/Connectivity/SimpleUnionAsync/Connectivity.h:122-136): label[v]
  * = smallest vertex id in v's component. */

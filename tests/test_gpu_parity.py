@@ -171,3 +171,31 @@ def test_empty_and_isolated(ctx, oracle_mod):
     assert byo.Triangle_degree_ordering(G) == 0
     p = byo.PageRank(G, 1e-6, 10)
     assert np.allclose(p, 0.15 / 4)
+
+
+def test_bfs_multi_matches_single(ctx, oracle_mod):
+    """64 sources in bit lanes give every source's single-BFS levels."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    for spec in (dict(kind="rmat", seed=12, lg_n=14, draws=1 << 17), dict(kind="grid", n=40, draws=70),
+                 dict(kind="er", seed=3, n=3000, draws=6000)):
+        kind = spec.pop("kind")
+        G = byo.Graph.generate(ctx, kind, **spec)
+        off, nb = G.export_csr()
+        n = len(off) - 1
+        rng = np.random.default_rng(n)
+        for k in (1, 7, 64):
+            srcs = rng.integers(0, n, k).astype(np.uint32)
+            srcs[-1] = srcs[0]  # a repeated source
+            lev = byo.BFS_multi(G, srcs)
+            for s_i, s in enumerate(srcs):
+                _, olev = O.bfs(off, nb, int(s))
+                assert np.array_equal(lev[s_i], olev), (kind, k, s_i)
+        G.close()
+    G = byo.Graph.generate(ctx, "rmat", seed=12, lg_n=10, draws=1 << 12, container="pma")
+    off, nb = G.export_csr()
+    lev = byo.BFS_multi(G, [0, 1, 2])
+    for s_i in range(3):
+        assert np.array_equal(lev[s_i], O.bfs(off, nb, s_i)[1])
+    with pytest.raises(byo.ByoError):
+        byo.BFS_multi(G, np.arange(65))
