@@ -53,6 +53,18 @@ _dbl = ctypes.c_double
 _P = ctypes.POINTER
 
 
+TUNE_BFS = 1
+TUNE_MULTI = 2
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("push_group", _u32), ("hub_min", _u32), ("pull_cap", _u32), ("blocked_tile", _u32),
+                ("ms_heavy_deg", _u32), ("ms_hub_deg", _u32), ("ms_push_div", _u32), ("reserved", _u32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 class GenSpec(ctypes.Structure):
     _fields_ = [("kind", _int), ("seed", _u64), ("lg_n", _u32), ("n", _u64), ("draws", _u64),
                 ("a", _dbl), ("b", _dbl), ("c", _dbl), ("exponent", _dbl)]
@@ -97,6 +109,9 @@ SIGNATURES = {
     "byo_bfs_device": (_int, [_vp, _u32, _vp, _vp, _int, _P(_u32)]),
     "byo_bfs_multi": (_int, [_vp, _vp, _u32, _vp, _P(_u32)]),
     "byo_bfs_multi_device": (_int, [_vp, _vp, _u32, _vp, _P(_u32)]),
+    "byo_graph_get_tuning": (_int, [_vp, _P(Tuning)]),
+    "byo_graph_set_tuning": (_int, [_vp, _P(Tuning)]),
+    "byo_graph_autotune": (_int, [_vp, _u32, _u32, _P(Tuning)]),
     "byo_cc": (_int, [_vp, _vp]),
     "byo_cc_device": (_int, [_vp, _vp]),
     "byo_bfs_cc": (_int, [_vp, _vp]),

@@ -279,6 +279,27 @@ int byo_bfs_multi(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *h_
   return copy_to_host(g->ctx, h_levels, d, (uint64_t)k * g->n * 4);
 }
 
+int byo_graph_get_tuning(byo_graph *g, byo_tuning *out) {
+  if (!g || !out) return BYO_EINVAL;
+  *out = effective_tuning(g);
+  return BYO_OK;
+}
+
+int byo_graph_set_tuning(byo_graph *g, const byo_tuning *t) {
+  if (!g || !t) return BYO_EINVAL;
+  BYO_TRY(check_tuning(g->ctx, t));
+  g->tune = *t;
+  return BYO_OK;
+}
+
+int byo_graph_autotune(byo_graph *g, uint32_t what, uint32_t trials, byo_tuning *out) {
+  if (!g) return BYO_EINVAL;
+  BYO_TRY(need(g->ctx, what != 0 && (what & ~(BYO_TUNE_BFS | BYO_TUNE_MULTI)) == 0, "autotune: unknown flags"));
+  BYO_TRY(autotune(g, what, trials));
+  if (out) *out = effective_tuning(g);
+  return BYO_OK;
+}
+
 int byo_cc_device(byo_graph *g, uint32_t *d_label) {
   if (!g || !d_label) return BYO_EINVAL;
   return cc_run(g, d_label);

@@ -332,12 +332,48 @@ __global__ void k_trav_extract(const uint64_t *__restrict__ lp, uint64_t n, uint
 
 // ---------------------------------------------------------------- host side
 
+byo_tuning effective_tuning(const byo_graph *g) {
+  byo_tuning t = g->tune;
+  const double avg = g->n ? (double)g->m / (double)g->n : 0.0;
+  if (!t.push_group) t.push_group = avg >= 24 ? 32 : avg >= 12 ? 16 : avg >= 6 ? 8 : 4;
+  if (!t.hub_min) t.hub_min = 4096;
+  if (!t.pull_cap) t.pull_cap = 32;
+  if (!t.blocked_tile) t.blocked_tile = 2048;
+  if (!t.ms_heavy_deg) t.ms_heavy_deg = 32;
+  if (!t.ms_hub_deg) t.ms_hub_deg = 2048;
+  if (!t.ms_push_div) t.ms_push_div = 20;
+  t.reserved = 0;
+  return t;
+}
+
+int check_tuning(byo_ctx *ctx, const byo_tuning *t) {
+  const char *bad = nullptr;
+  if (t->push_group && t->push_group != 4 && t->push_group != 8 && t->push_group != 16 && t->push_group != 32)
+    bad = "push_group must be 4, 8, 16 or 32";
+  else if (t->hub_min && t->hub_min < 32)
+    bad = "hub_min must be >= 32";
+  else if (t->pull_cap > 4096)
+    bad = "pull_cap must be <= 4096";
+  else if (t->blocked_tile && (t->blocked_tile < 64 || t->blocked_tile > 65536))
+    bad = "blocked_tile must be in [64, 65536]";
+  else if (t->ms_heavy_deg > 65536)
+    bad = "ms_heavy_deg must be <= 65536";
+  else if (t->ms_hub_deg && (t->ms_hub_deg < 32 || t->ms_hub_deg > (1u << 20)))
+    bad = "ms_hub_deg must be in [32, 2^20]";
+  else if (t->reserved)
+    bad = "reserved field must be zero";
+  return bad ? set_error(ctx, BYO_EINVAL, bad) : BYO_OK;
+}
+
 EngineTuning default_tuning(const byo_graph *g) {
   EngineTuning t;
   const uint64_t W = (g->n + 31) / 32;
   t.pull_stage_words = (int)(W < 32768 ? W : 32768);
-  double avg = g->n ? (double)g->m / (double)g->n : 0.0;
-  t.push_group = avg >= 24 ? 32 : avg >= 12 ? 16 : avg >= 6 ? 8 : 4;
+  const byo_tuning e = effective_tuning(g);
+  t.push_group = (int)e.push_group;
+  t.hub_min = e.hub_min;
+  t.pull_cap = (int)e.pull_cap;
+  t.blocked_tile = (int)e.blocked_tile;
   return t;
 }
 

@@ -67,6 +67,7 @@ struct byo_graph {
   uint32_t *d_deg = nullptr;
   byo::Pma *pma = nullptr;
   byo::DevBuf ws[24];  // per-graph workspaces, indexed by the Ws enum
+  byo_tuning tune = {};  // launch shapes set by the caller or the autotuner (0 = automatic)
 };
 
 namespace byo {
@@ -198,6 +199,10 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
 
 // ---------------------------------------------------------------- 64-source BFS (msbfs.cu)
 int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint32_t *rounds);
+// Launch shapes in effect: g->tune where set, else the defaults for g.
+byo_tuning effective_tuning(const byo_graph *g);
+int check_tuning(byo_ctx *ctx, const byo_tuning *t);
+int autotune(byo_graph *g, uint32_t what, uint32_t trials);
 
 // ---------------------------------------------------------------- algorithms (algos.cu)
 int cc_run(byo_graph *g, uint32_t *d_label);

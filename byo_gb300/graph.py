@@ -159,6 +159,26 @@ class Graph:
         """Slots of the traversal view (edges plus the PMA's gaps)."""
         return int(lib().byo_graph_num_slots(self.h))
 
+    def tuning(self):
+        """Launch shapes in effect for this graph (dict of byo_tuning fields)."""
+        t = _abi.Tuning()
+        check(lib().byo_graph_get_tuning(self.h, ctypes.byref(t)), self.ctx.h)
+        return t.as_dict()
+
+    def set_tuning(self, **fields):
+        """Sets launch-shape fields (0 = automatic); others keep their values."""
+        cur = self.tuning()
+        cur.update(fields)
+        t = _abi.Tuning(**cur)
+        check(lib().byo_graph_set_tuning(self.h, ctypes.byref(t)), self.ctx.h)
+
+    def autotune(self, bfs=True, multi=False, trials=3):
+        """Times candidate launch shapes on this graph and installs the best."""
+        what = (_abi.TUNE_BFS if bfs else 0) | (_abi.TUNE_MULTI if multi else 0)
+        t = _abi.Tuning()
+        check(lib().byo_graph_autotune(self.h, what, trials, ctypes.byref(t)), self.ctx.h)
+        return t.as_dict()
+
     @property
     def container(self):
         return "pma" if lib().byo_graph_container(self.h) == _abi.CONTAINER_PMA else "csr"

@@ -158,12 +158,41 @@ int byo_bfs_device(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_l
 /* Batched BFS from k <= 64 sources at once, bit lanes of one traversal run
  * by a persistent kernel.  levels[s * n + v] is the BFS level of v from
  * srcs[s] (BYO_NONE if unreached), identical to byo_bfs's levels; sources may
- * repeat.  Levels above 65534 are not supported (BYO_EINVAL is not raised;
- * such graphs stop at that depth). */
+ * repeat.  *rounds (may be NULL) = rounds run.  No reference counterpart:
+ * the reference answers one source per BFS call
+ * (benchmarks/BFS/NonDeterministicBFS/BFS.h:47-64). */
 int byo_bfs_multi(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *h_levels,
                   uint32_t *rounds);
 int byo_bfs_multi_device(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels,
                          uint32_t *rounds);
+
+/* Launch shapes of the traversal kernels, kept per graph: the degree
+ * boundaries at which work per vertex moves from a thread to a group of lanes,
+ * a warp or a CTA, and tile sizes.  Results never depend on them.  In
+ * byo_graph_set_tuning a zero field means "automatic"; byo_graph_get_tuning
+ * reports the values in effect.  No reference counterpart (the reference's
+ * shapes are compile-time constants: kEMBlockSize gbbs/macros.h:80,
+ * vertex_ops::kBlockSize gbbs/vertex.h:35). */
+typedef struct byo_tuning {
+  uint32_t push_group;   /* single-source push: lanes per frontier vertex (4, 8, 16 or 32) */
+  uint32_t hub_min;      /* single-source push: degree from which one CTA takes a vertex (>= 32) */
+  uint32_t pull_cap;     /* single-source pull: slots a thread scans before a warp takes over (1..4096) */
+  uint32_t blocked_tile; /* blocked push: slots per tile (64..65536) */
+  uint32_t ms_heavy_deg; /* 64-source pull: slots above which a warp takes a vertex (1..65536) */
+  uint32_t ms_hub_deg;   /* 64-source push: frontier vertices above this many slots are cut into
+                            chunks of this size, a warp each (32..2^20) */
+  uint32_t ms_push_div;  /* 64-source: push while the frontier's slots < all slots / ms_push_div */
+  uint32_t reserved;     /* zero */
+} byo_tuning;
+int byo_graph_get_tuning(byo_graph *g, byo_tuning *out);
+int byo_graph_set_tuning(byo_graph *g, const byo_tuning *t);
+/* Picks the tuning fields by timing the kernels on this graph: coordinate
+ * descent over candidate values of each field, BFS from `trials` seeded
+ * sources per candidate.  what: BYO_TUNE_BFS and/or BYO_TUNE_MULTI.  The
+ * result is installed on the graph and copied to *out (may be NULL). */
+#define BYO_TUNE_BFS 1u
+#define BYO_TUNE_MULTI 2u
+int byo_graph_autotune(byo_graph *g, uint32_t what, uint32_t trials, byo_tuning *out);
 
 /* Connectivity, SimpleUnionAsync semantics
  * (benchmarks/Connectivity/SimpleUnionAsync/Connectivity.h:122-136): label[v]

@@ -199,3 +199,77 @@ def test_bfs_multi_matches_single(ctx, oracle_mod):
         assert np.array_equal(lev[s_i], O.bfs(off, nb, s_i)[1])
     with pytest.raises(byo.ByoError):
         byo.BFS_multi(G, np.arange(65))
+
+
+def _sym_csr(n, pairs):
+    """Symmetric sorted CSR (uint64 offsets, uint32 ids) from undirected pairs."""
+    p = np.asarray(pairs, np.int64)
+    src = np.concatenate([p[:, 0], p[:, 1]])
+    dst = np.concatenate([p[:, 1], p[:, 0]])
+    keys = np.unique(src.astype(np.uint64) << np.uint64(32) | dst.astype(np.uint64))
+    s = (keys >> np.uint64(32)).astype(np.int64)
+    off = np.zeros(n + 1, np.uint64)
+    np.add.at(off, s + 1, 1)
+    return np.cumsum(off).astype(np.uint64), (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+
+
+@pytest.mark.gpu
+def test_bfs_multi_launch_shapes(ctx, oracle_mod):
+    """Every direction and degree-bucket path of the 64-source kernel (forced
+    push, forced pull, warp-per-vertex pull, hub chunks) gives the levels of
+    single-source BFS."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    star = [(0, i) for i in range(1, 5001)] + [(5000 + i, 5001 + i) for i in range(99)]
+    off_s, nb_s = _sym_csr(5100, star)
+    graphs = [byo.Graph.generate(ctx, "rmat", seed=5, lg_n=13, draws=1 << 17),
+              byo.Graph.from_csr(ctx, off_s, nb_s),
+              byo.Graph.generate(ctx, "rmat", seed=6, lg_n=12, draws=1 << 15, container="pma"),
+              byo.Graph.generate(ctx, "grid", n=30, draws=30)]
+    shapes = [dict(ms_push_div=1), dict(ms_push_div=0xFFFFFFFF),
+              dict(ms_heavy_deg=1, ms_hub_deg=32, ms_push_div=1),
+              dict(ms_heavy_deg=1, ms_hub_deg=32, ms_push_div=0xFFFFFFFF),
+              dict(ms_heavy_deg=65536, ms_hub_deg=1 << 20, ms_push_div=5)]
+    for gi, G in enumerate(graphs):
+        off, nb = G.export_csr()
+        n = len(off) - 1
+        rng = np.random.default_rng(100 + gi)
+        srcs = rng.integers(0, n, 64).astype(np.uint32)
+        srcs[0] = 0
+        srcs[1] = n - 1
+        want = [O.bfs(off, nb, int(s))[1] for s in srcs]
+        for sh in shapes:
+            G.set_tuning(**sh)
+            lev = byo.BFS_multi(G, srcs)
+            for i in range(64):
+                assert np.array_equal(lev[i], want[i]), (gi, sh, i)
+        G.set_tuning(ms_heavy_deg=0, ms_hub_deg=0, ms_push_div=0)
+        G.close()
+
+
+@pytest.mark.gpu
+def test_tuning_api_and_autotune(ctx, oracle_mod):
+    """Launch shapes are per graph, validated, and never change a result."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    G = byo.Graph.generate(ctx, "rmat", seed=9, lg_n=13, draws=1 << 16)
+    off, nb = G.export_csr()
+    t = G.tuning()
+    assert all(v > 0 for v in t.values())
+    G.set_tuning(push_group=8, pull_cap=4)
+    assert G.tuning()["push_group"] == 8 and G.tuning()["pull_cap"] == 4
+    for bad in (dict(push_group=7), dict(hub_min=5), dict(blocked_tile=10), dict(ms_hub_deg=8)):
+        with pytest.raises(byo.ByoError):
+            G.set_tuning(**bad)
+    opar, olev = O.bfs(off, nb, 10)
+    for pol in (byo._abi.POLICY_M20, byo._abi.POLICY_M20_BLOCKED, byo._abi.POLICY_PUSH, byo._abi.POLICY_PULL):
+        par, lev = byo.BFS(G, 10, policy=pol, levels=True)
+        assert np.array_equal(par, opar) and np.array_equal(lev, olev)
+    t = G.autotune(bfs=True, multi=True, trials=2)
+    assert t["push_group"] in (4, 8, 16, 32) and t["ms_push_div"] in (5, 10, 20, 40, 80)
+    assert G.tuning() == t
+    par = byo.BFS(G, 10)
+    assert np.array_equal(par, opar)
+    lev = byo.BFS_multi(G, [10, 11])
+    assert np.array_equal(lev[0], olev)
+    G.close()
