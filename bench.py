@@ -386,6 +386,242 @@ def run_e2e(args, byo, G, ctx, torch, dynamic, keys, B, n, policy, total_units, 
             "d2h_bytes_per_step": 4 * n + 4 * n + 8 * n, "ms_per_step": dt * 1e3}
 
 
+# ------------------------------------------------------------------ mixed queries + updates
+MIXED_LG, MIXED_DRAWS, MIXED_SEED = 24, 8 << 24, 5
+MIXED_QUERIES, MIXED_BATCHES = 16, 8
+MIXED_METRIC = "mixed stream: 64-source BFS queries + insert/delete batches (log-uniform 1e2-1e6 pairs)"
+MIXED_UNIT = "G edge-ops/s (BFS traversed edges over all sources + inserted and removed keys)"
+
+
+def mixed_ops(seed):
+    """One step's op list: MIXED_QUERIES query groups and MIXED_BATCHES insert
+    batches, each deleted later in the same step, in a seeded random order;
+    batch sizes (pairs, symmetrised on insert) log-uniform in [1e2, 1e6]."""
+    rng = np.random.default_rng(seed)
+    sizes = np.round(10.0 ** rng.uniform(2, 6, MIXED_BATCHES)).astype(np.int64)
+    ops = ([("Q", i) for i in range(MIXED_QUERIES)] + [("I", j) for j in range(MIXED_BATCHES)]
+           + [("D", j) for j in range(MIXED_BATCHES)])
+    order = [ops[i] for i in rng.permutation(len(ops))]
+    pos = {op: i for i, op in enumerate(order)}
+    for j in range(MIXED_BATCHES):
+        a, b = pos[("I", j)], pos[("D", j)]
+        if b < a:
+            order[a], order[b] = order[b], order[a]
+    return order, sizes
+
+
+def mixed_sources(deg, seed):
+    rng = np.random.default_rng(seed + 17)
+    nz = np.nonzero(deg)[0]
+    return [np.ascontiguousarray(rng.choice(nz, 64), np.uint32) for _ in range(MIXED_QUERIES)]
+
+
+def size_bin(b):
+    return "1e%d-1e%d" % (int(np.log10(max(b, 1))), int(np.log10(max(b, 1))) + 1)
+
+
+def run_mixed(args, rank, world, local_rank):
+    import torch
+    import byo_gb300 as byo
+    from byo_gb300 import _abi
+    from byo_gb300 import policy as learned
+    L = _abi.lib()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = byo.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    t0 = time.time()
+    G = byo.Graph.generate(ctx, "rmat", seed=MIXED_SEED, lg_n=MIXED_LG, draws=MIXED_DRAWS, container="pma")
+    n, m0 = G.N(), G.M()
+    log("mixed: n=%d m=%d built in %.2fs" % (n, m0, time.time() - t0))
+    if learned.load_default(ctx):
+        _abi.check(L.byo_ctx_set_update_policy(ctx.h, _abi.UPDATE_LEARNED), ctx.h)
+    t0 = time.time()
+    tuning = G.autotune(bfs=False, multi=True, trials=3)
+    tune_s = time.time() - t0
+    order, sizes = mixed_ops(MIXED_SEED)
+    deg = G.degrees()
+    qsrc = mixed_sources(deg, MIXED_SEED)
+    bkeys = []
+    for j, b in enumerate(sizes):
+        k = torch.empty(2 * int(b), dtype=torch.int64, device=dev)
+        _abi.check(L.byo_gen_uniform_keys_device(ctx.h, MIXED_SEED * 1000 + j, n, int(b), k.data_ptr()), ctx.h)
+        bkeys.append(k)
+    levels = torch.empty(64 * n, dtype=torch.int32, device=dev)
+    ch = ctypes.c_uint64(0)
+    rounds = ctypes.c_uint32(0)
+
+    def run_op(op):
+        kind, i = op
+        if kind == "Q":
+            _abi.check(L.byo_bfs_multi_device(G.h, qsrc[i].ctypes.data, 64, levels.data_ptr(),
+                                              ctypes.byref(rounds)), ctx.h)
+        elif kind == "I":
+            k = bkeys[i]
+            _abi.check(L.byo_graph_insert_batch_device(G.h, k.data_ptr(), k.numel(), 0, ctypes.byref(ch)), ctx.h)
+        else:
+            k = bkeys[i]
+            _abi.check(L.byo_graph_remove_batch_device(G.h, k.data_ptr(), k.numel(), 0, ctypes.byref(ch)), ctx.h)
+
+    def step(lat):
+        for op in order:
+            a = time.perf_counter()
+            run_op(op)
+            lat.append((op, time.perf_counter() - a))
+
+    for _ in range(args.warmup):
+        step([])
+    ctx.synchronize()
+    # traversed edges of every query group on the step's start state
+    deg_t = torch.from_numpy(deg.astype(np.int64)).to(dev)
+    q_edges = []
+    for i in range(MIXED_QUERIES):
+        run_op(("Q", i))
+        ctx.synchronize()
+        reached = (levels.view(64, n) != -1)
+        q_edges.append(float((reached.to(torch.int64) * deg_t).sum().item()) / 2)
+    upd_keys = float(sum(2 * 2 * int(b) for b in sizes))
+    units = sum(q_edges) + upd_keys
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    ctx.kernel_timing("*")
+    launches0 = ctx.launches
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    lat = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    t_host = time.perf_counter()
+    for _ in range(args.steps):
+        step(lat)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_host = time.perf_counter() - t_host
+    clk = clocks.stop()
+    launches = ctx.launches - launches0
+    elapsed_ms = e0.elapsed_time(e1)
+    ms_launches, ms_kernel = ctx.kernel_time("bfs_multi")
+    ctx.kernel_timing(None)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([elapsed_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    step_ms = elapsed_ms / args.steps
+    qlat = np.array([x for (op, x) in lat if op[0] == "Q"]) * 1e3
+    ulat = {}
+    for (op, x) in lat:
+        if op[0] != "Q":
+            ulat.setdefault(size_bin(int(sizes[op[1]])), []).append(x * 1e3)
+    allu = np.array([x for v in ulat.values() for x in v])
+    peak, peak_kind = measured_peaks()
+    nslots = G.nslots()
+    # lower bound of one 64-source launch: levels written once, the adjacency
+    # read once, the three mask arrays (seen, F, N) read and written once
+    ms_bytes = 4 * 64 * n + 4 * nslots + 8 * (n + 1) + 6 * 8 * n
+    per_launch_ms = ms_kernel / max(ms_launches, 1)
+    achieved = ms_bytes / (per_launch_ms / 1e3) / 1e9
+    res = {
+        "metric": MIXED_METRIC, "value": world * units / (step_ms / 1e3) / 1e9, "unit": MIXED_UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32 ids, u64 source masks", "data": "synthetic (seeded RMAT, uniform update pairs)",
+        "config": {"workload": "mixed: RMAT 2^24 avg deg 16 (2^27 draws) PMA; per step %d query groups of 64 "
+                               "seeded sources + %d insert batches deleted later in the step" %
+                               (MIXED_QUERIES, MIXED_BATCHES),
+                   "n": n, "m": m0, "batch_pairs": [int(b) for b in sizes], "tuning": tuning,
+                   "autotune_s": tune_s, "parallelism": "replicas x%d" % world,
+                   "l2": "inputs larger than L2 (graph %.0f MB)" % ((8 * n + 4 * nslots) / 1e6)},
+        "components": {
+            "queries_per_s": 64 * MIXED_QUERIES / (step_ms / 1e3),
+            "update_keys_per_s": upd_keys / (step_ms / 1e3),
+            "query_latency_ms": {"p50": float(np.percentile(qlat, 50)), "p99": float(np.percentile(qlat, 99)),
+                                 "mean": float(qlat.mean())},
+            "update_latency_ms": {"p50": float(np.percentile(allu, 50)), "p99": float(np.percentile(allu, 99))},
+            "update_latency_ms_by_pairs": {k: {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)),
+                                               "count": len(v)} for k, v in sorted(ulat.items())},
+            "query_traversed_edges_per_group": float(np.mean(q_edges)),
+            "host_ms_per_step": t_host * 1e3 / args.steps,
+            "bfs_multi_kernel_ms": per_launch_ms,
+        },
+        "roofline": {"bound": "hbm", "kernel": "k_ms_bfs (one 64-source traversal)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": ms_bytes, "avg_launch_ms": per_launch_ms,
+                     "traffic": (traffic_table().get("bfs_multi") or {}).get("bytes_per_launch"),
+                     "kernel_ms_share": round(ms_kernel / max(elapsed_ms, 1e-9), 4)},
+        "gpu_launches": launches, "clocks": clk,
+    }
+    # end to end: batches from pinned host memory, every query's levels back to the host
+    hk = []
+    for k in bkeys:
+        h = torch.empty(k.numel(), dtype=torch.int64, pin_memory=True)
+        h.copy_(k.cpu())
+        hk.append(h.numpy().view(np.uint64))
+    hlev = torch.empty(64 * n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+
+    def e2e_op(op):
+        kind, i = op
+        if kind == "Q":
+            _abi.check(L.byo_bfs_multi(G.h, qsrc[i].ctypes.data, 64, hlev.ctypes.data, None), ctx.h)
+        elif kind == "I":
+            G.insert_batch(hk[i])
+        else:
+            G.remove_batch(hk[i])
+
+    for op in order:
+        e2e_op(op)
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    for _ in range(args.steps):
+        for op in order:
+            e2e_op(op)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - a) / args.steps
+    res["e2e"] = {"value": world * units / dt / 1e9, "unit": MIXED_UNIT,
+                  "h2d_bytes_per_step": int(upd_keys * 8),
+                  "d2h_bytes_per_step": 4 * 64 * n * MIXED_QUERIES, "ms_per_step": dt * 1e3}
+    return res, ctx, G
+
+
+def mixed_cpu_sample(steps=None):
+    """Bounded sample of the mixed stream on the oracle port: four of the
+    query groups' sources as single-source BFS and two update batches."""
+    from oracle import oracle as O
+    O.build()
+    s, d = O.rmat_edges(MIXED_SEED, MIXED_LG, MIXED_DRAWS)
+    off, nb = O.build_csr(1 << MIXED_LG, s, d)
+    del s, d
+    deg = np.diff(off.astype(np.int64))
+    qsrc = mixed_sources(deg.astype(np.uint32), MIXED_SEED)
+    order, sizes = mixed_ops(MIXED_SEED)
+    t0 = time.perf_counter()
+    edges = 0.0
+    nq = 4
+    for s_ in qsrc[0][:nq]:
+        par, _ = O.bfs(off, nb, int(s_))
+        edges += deg[par != O.NONE].sum() / 2
+    tq = time.perf_counter() - t0
+    store = O.Store(off, nb)
+    js = [int(np.argmin(sizes)), int(np.argmax(sizes))]
+    keys_total = 0
+    t1 = time.perf_counter()
+    for j in js:
+        us, ud = O.uniform_pairs(MIXED_SEED * 1000 + j, 1 << MIXED_LG, int(sizes[j]))
+        k = O.keys_from_pairs(us, ud)
+        store.insert_batch(k)
+        store.remove_batch(k)
+        keys_total += 2 * len(k)
+    tu = time.perf_counter() - t1
+    value = (edges + keys_total) / (tq + tu) / 1e9
+    return {"value": value, "unit": MIXED_UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": "%d single-source BFS from the first query group's sources + insert/remove of batches "
+                      "of %d and %d pairs on the oracle port (OpenMP, %d threads), %.1f s"
+                      % (nq, sizes[js[0]], sizes[js[1]], O.num_threads(), tq + tu),
+            "queries_per_s": nq / tq, "update_keys_per_s": keys_total / tu}
+
+
 # ------------------------------------------------------------------ CPU (oracle) legs
 def cpu_setup(dynamic):
     from oracle import oracle as O
@@ -465,7 +701,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static"])
+    ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static", "mixed"])
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
                     help="auto: the committed learned network if present, else m20")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -481,6 +717,15 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
+        if args.workload == "mixed":
+            cb = mixed_cpu_sample()
+            print(json.dumps({"metric": MIXED_METRIC, "value": cb["value"], "unit": MIXED_UNIT, "n_gpus": 0,
+                              "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                              "impl": "reference", "config": {"workload": "mixed (bounded sample)"},
+                              "cpu_baseline": cb, "data": "synthetic (seeded RMAT, uniform update pairs)",
+                              "e2e": {"value": cb["value"], "unit": MIXED_UNIT, "h2d_bytes_per_step": 0,
+                                      "d2h_bytes_per_step": 0}}), flush=True)
+            return 0
         print(json.dumps(run_reference(args, dynamic)), flush=True)
         return 0
 
@@ -490,12 +735,15 @@ def main():
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
-    res, ctx, G = run_ours(args, rank, world, local_rank)
+    if args.workload == "mixed":
+        res, ctx, G = run_mixed(args, rank, world, local_rank)
+    else:
+        res, ctx, G = run_ours(args, rank, world, local_rank)
     G.close()
     ctx.close()
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
-            res["cpu_baseline"] = cpu_baseline_sample(dynamic)
+            res["cpu_baseline"] = mixed_cpu_sample() if args.workload == "mixed" else cpu_baseline_sample(dynamic)
         print(json.dumps(res), flush=True)
     if world > 1:
         import torch.distributed as dist

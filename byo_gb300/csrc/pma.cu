@@ -370,10 +370,16 @@ constexpr uint32_t kOptSeg = 256;
 
 __device__ __forceinline__ uint64_t bval(const uint64_t *B, uint64_t j) { return B[j]; }
 
+// kList: the leaves with work come from a segment list (seg[2q] = leaf,
+// seg[2q + 1] = b0 << 32 | b1, *nseg entries) instead of bstart over every
+// leaf; rcount of the other leaves must already hold their counts.  When deg
+// is given, every key that enters or leaves adjusts deg[src].
+template <bool kList>
 __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
     uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
-    const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
-    unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta) {
+    const uint64_t *__restrict__ bstart, const uint64_t *__restrict__ seg, const unsigned long long *nseg,
+    int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
+    unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta, uint32_t *deg) {
   __shared__ uint64_t As[kOptWarps][kLeaf];
   __shared__ uint64_t Bsh[kOptWarps][kOptSeg];
   const unsigned w = threadIdx.x >> 5, lane = lane_id();
@@ -381,8 +387,18 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   long long dsum = 0;
-  for (uint64_t j = gw; j < NL; j += nw) {
-    const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
+  const uint64_t nwork = kList ? *nseg : NL;
+  for (uint64_t q = gw; q < nwork; q += nw) {
+    uint64_t j, b0, b1;
+    if (kList) {
+      j = seg[2 * q];
+      b0 = seg[2 * q + 1] >> 32;
+      b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
+    } else {
+      j = q;
+      b0 = bstart[j];
+      b1 = bstart[j + 1];
+    }
     const uint32_t c = cnt[j];
     if (b0 == b1) {
       if (lane == 0) rcount[j] = c;
@@ -448,10 +464,12 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
         if (i < c && (k >= nb || A[i] <= bval(B, k))) {
           x = A[i];
           kept = insert || !(k < nb && bval(B, k) == x);
+          if (deg && !kept) atomicAdd(deg + (x >> 32), 0xFFFFFFFFu);  // -1
           i++;
         } else {
           x = bval(B, k);
           kept = insert && !(i > 0 && A[i - 1] == x) && !(k > 0 && bval(B, k - 1) == x);
+          if (deg && kept) atomicAdd(deg + (x >> 32), 1u);
           k++;
         }
         if (kept) {
@@ -600,6 +618,120 @@ __global__ void k_pma_export(const uint32_t *__restrict__ src, const uint32_t *_
   }
 }
 
+// Leaves with work for a small sorted batch: key q starts a segment when it
+// routes to another leaf than key q-1; the segment ends at the first key >=
+// sep[leaf + 1].  seg[2s] = leaf, seg[2s + 1] = b0 << 32 | b1 (b < 2^32).
+__global__ void k_pma_segments(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
+                               uint64_t b, uint64_t *seg, unsigned long long *nseg) {
+  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < b;
+       base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t q = base + lane_id();
+    bool start = false;
+    uint64_t j = 0, b1 = b;
+    if (q < b) {
+      j = route(sep, NL, keys[q]);
+      start = q == 0 || route(sep, NL, keys[q - 1]) != j;
+      if (start && j + 1 < NL) {
+        const uint64_t lim = sep[j + 1];
+        uint64_t lo = q, hi = b;
+        while (lo < hi) {
+          const uint64_t mid = (lo + hi) >> 1;
+          if (keys[mid] < lim) lo = mid + 1; else hi = mid;
+        }
+        b1 = lo;
+      }
+    }
+    const uint64_t at = warp_append(start, nseg);
+    if (start) {
+      seg[2 * at] = j;
+      seg[2 * at + 1] = q << 32 | b1;
+    }
+  }
+}
+
+// One block sorts up to kSmallSort keys in shared memory (bitonic network
+// over the next power of two, padded with ~0) and reports the largest src
+// and dst in bounds[0], bounds[1].
+constexpr uint32_t kSmallSort = 4096;
+__global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict__ in, uint32_t count, uint64_t *out,
+                                                     unsigned long long *bounds) {
+  __shared__ uint64_t s[kSmallSort];
+  __shared__ uint64_t red[2][32];
+  uint32_t P = 2;
+  while (P < count) P <<= 1;
+  uint64_t ms = 0, md = 0;
+  for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+    const uint64_t k = i < count ? in[i] : ~0ull;
+    if (i < count) {
+      ms = ms > (k >> 32) ? ms : (k >> 32);
+      md = md > (k & 0xFFFFFFFFull) ? md : (k & 0xFFFFFFFFull);
+    }
+    s[i] = k;
+  }
+  __syncthreads();
+  for (uint32_t size = 2; size <= P; size <<= 1)
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t t = threadIdx.x; t < P / 2; t += blockDim.x) {
+        const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
+        const bool up = (i & size) == 0;
+        const uint64_t a = s[i], b = s[j];
+        if ((a > b) == up) {
+          s[i] = b;
+          s[j] = a;
+        }
+      }
+      __syncthreads();
+    }
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) out[i] = s[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t a = __shfl_xor_sync(kFull, ms, o), b = __shfl_xor_sync(kFull, md, o);
+    ms = ms > a ? ms : a;
+    md = md > b ? md : b;
+  }
+  if (lane_id() == 0) {
+    red[0][threadIdx.x >> 5] = ms;
+    red[1][threadIdx.x >> 5] = md;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (uint32_t w = 1; w < blockDim.x / 32; w++) {
+      ms = ms > red[0][w] ? ms : red[0][w];
+      md = md > red[1][w] ? md : red[1][w];
+    }
+    bounds[0] = ms;
+    bounds[1] = md;
+  }
+}
+
+__device__ __forceinline__ uint64_t ceil_src(uint64_t key) { return (key >> 32) + ((key & 0xFFFFFFFFull) != 0); }
+
+// The view after an in-place merge of the segment list: off[v] changes only
+// for the vertices v whose key (v, 0) routes to a merged leaf j, i.e. v in
+// [ceil(sep[j] / 2^32), ceil(sep[j+1] / 2^32)).  A warp per merged leaf.
+__global__ void k_pma_view_leaves(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
+                                  const uint64_t *__restrict__ sep, uint64_t NL, uint64_t n,
+                                  const uint64_t *__restrict__ seg, const unsigned long long *nseg, uint64_t *off) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t ns = *nseg;
+  for (uint64_t q = gw; q < ns; q += nw) {
+    const uint64_t j = seg[2 * q];
+    const uint64_t vlo = j == 0 ? 0 : min(ceil_src(sep[j]), n + 1);
+    const uint64_t vhi = j + 1 == NL ? n + 1 : min(ceil_src(sep[j + 1]), n + 1);
+    const uint32_t c = cnt[j];
+    const uint32_t *ls = src + j * kLeaf;
+    for (uint64_t v = vlo + lane_id(); v < vhi; v += 32) {
+      uint32_t lo = 0, hi = c;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (ls[mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
+      }
+      off[v] = j * kLeaf + lo;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- host side
 
 static int pma_alloc(byo_ctx *ctx, uint64_t NL, uint32_t **src, uint32_t **dst, uint32_t **cnt, uint64_t **sep) {
@@ -743,9 +875,16 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   unsigned long long *bounds = (unsigned long long *)p->misc.p;
   unsigned int *flags = (unsigned int *)(bounds + 2);  // [0] unsorted, [1] grow, [2] any overflow, [4..] counters
   BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 128, ctx->stream));
-  launch(ctx, k_key_bounds, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, bounds);
-  if (sorted)
-    launch(ctx, k_check_sorted, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, flags);
+  // a batch that fits one block is sorted there (with the bounds) before it is
+  // validated: that sort does not index by key
+  const bool small_sort = !sorted && count <= kSmallSort;
+  if (small_sort) {
+    launch(ctx, k_sort_small, dim3(1), dim3(1024), 0, d_keys_in, (uint32_t)count, ka, bounds);
+  } else {
+    launch(ctx, k_key_bounds, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, bounds);
+    if (sorted)
+      launch(ctx, k_check_sorted, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, flags);
+  }
   uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
   BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
@@ -756,28 +895,29 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   uint64_t b = count;
   if (sorted) {
     batch = const_cast<uint64_t *>(d_keys_in);
+  } else if (small_sort) {
+    batch = ka;
   } else {
     // sorted, duplicates kept: the optimistic merge drops them itself
     BYO_TRY(sort_bucketed(ctx, d_keys_in, count, g->n, ka, kb));
     batch = ka;
   }
-  // 2. route
+  // 2. strategy: in-place merge (default), rebuild when asked for or chosen by
+  // the learned policy; capacity may still force a rebuild below
   const uint64_t NL = p->NL;
   BYO_TRY(ensure(ctx, p->bstart, (NL + 1) * 8));
   BYO_TRY(ensure(ctx, p->rcount, NL * 4));
   BYO_TRY(ensure(ctx, p->rpre, (NL + 1) * 8));
   uint64_t *bstart = (uint64_t *)p->bstart.p, *rpre = (uint64_t *)p->rpre.p;
   uint32_t *rcount = (uint32_t *)p->rcount.p;
-  launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
-         (const uint64_t *)batch, b, bstart);
-  // 3. strategy: in-place merge (default), rebuild when asked for or chosen by
-  // the learned policy; capacity may still force a rebuild below
   int strategy = 0;
   if (ctx->update_policy == BYO_UPDATE_REBUILD) strategy = 1;
   else if (ctx->update_policy == BYO_UPDATE_LEARNED)
     strategy = update_strategy(ctx, b, m_before, NL * kLeaf, sorted, insert);
   ctx->last_update_strategy = strategy;
   if (strategy == 1) {
+    launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
+           (const uint64_t *)batch, b, bstart);
     if (!sorted) {  // the counting merge wants unique keys
       BYO_TRY(unique_u64(ctx, ka, count, 0, kb, &b));
       batch = kb;
@@ -795,14 +935,33 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     if (total == m_before) return BYO_OK;
     return pma_rebuild(g, batch, bstart, rpre, total, insert);
   }
-  // 4. optimistic merge: leaves that fit are done in place
+  // 3. optimistic merge: leaves that fit are done in place.  A batch much
+  // smaller than the leaf count visits only its own leaves (segment list),
+  // keeps the degrees up to date in the merge, and refreshes the view only
+  // around those leaves.
   BYO_TRY(ensure(ctx, p->ovf, (NL * kLeaf + b + 1) * 8));
   BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
-  unsigned long long *ctr = (unsigned long long *)(flags + 4);  // [0] cursor, [1] leaves, [2] delta
-  BYO_CU(ctx, cudaMemsetAsync(ctr, 0, 24, ctx->stream));
-  launch_t(ctx, "pma_merge", k_pma_merge_opt, dim3(grid_for(ctx, NL * 32, 32 * kOptWarps, 6)), dim3(32 * kOptWarps),
-           0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch, (const uint64_t *)bstart, insert, rcount,
-           (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2));
+  unsigned long long *ctr = (unsigned long long *)(flags + 4);  // [0] cursor, [1] leaves, [2] delta, [3] segments
+  BYO_CU(ctx, cudaMemsetAsync(ctr, 0, 32, ctx->stream));
+  const bool list = 2 * b <= NL && b < (1ull << 32);
+  if (list) {
+    uint64_t *seg = bstart;  // 2 * b <= NL words
+    launch(ctx, k_pma_segments, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
+           (const uint64_t *)batch, b, seg, ctr + 3);
+    BYO_CU(ctx, cudaMemcpyAsync(rcount, p->cnt, NL * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    launch_t(ctx, "pma_merge", k_pma_merge_opt<true>, dim3(grid_for(ctx, b * 32, 32 * kOptWarps, 6)),
+             dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
+             (const uint64_t *)nullptr, (const uint64_t *)seg, (const unsigned long long *)(ctr + 3), insert, rcount,
+             (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2), g->d_deg);
+  } else {
+    launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
+           (const uint64_t *)batch, b, bstart);
+    launch_t(ctx, "pma_merge", k_pma_merge_opt<false>, dim3(grid_for(ctx, NL * 32, 32 * kOptWarps, 6)),
+             dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
+             (const uint64_t *)bstart, (const uint64_t *)nullptr, (const unsigned long long *)nullptr, insert,
+             rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2),
+             (uint32_t *)nullptr);
+  }
   BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 24, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   const uint64_t novf = h[1];
@@ -812,10 +971,17 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   const double cap = (double)NL * kLeaf;
   const bool shrink = !insert && (double)total < kRootMin * cap && NL > 1;
   if (novf == 0 && !shrink) {
+    if (list) {
+      launch(ctx, k_pma_view_leaves, dim3(grid_for(ctx, b * 32, 256, 8)), dim3(256), 0, (const uint32_t *)p->src,
+             (const uint32_t *)p->cnt, (const uint64_t *)p->sep, NL, g->n, (const uint64_t *)bstart,
+             (const unsigned long long *)(ctr + 3), g->d_off);
+      g->m = total;
+      return check_launch(ctx, "pma_update");
+    }
     BYO_TRY(check_launch(ctx, "pma_update"));
     return pma_view(g);
   }
-  // 5. overflow (or shrink): windows over the counts after the merge
+  // 4. overflow (or shrink): windows over the counts after the merge
   BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
   BYO_TRY(ensure(ctx, p->win, NL * 4));
   uint32_t *win = (uint32_t *)p->win.p;

@@ -122,3 +122,39 @@ def test_small_batches_and_errors(ctx, oracle_mod):
     # the container is unchanged by rejected batches
     o2, n2 = G.export_csr()
     assert np.array_equal(o2, ro) and np.array_equal(n2, rn)
+
+
+@pytest.mark.parametrize("lg,draws,sizes", [(17, 1 << 20, (1, 7, 100, 1000, 1300)), (19, 1 << 22, (3000,))])
+def test_small_batch_fast_path(ctx, oracle_mod, lg, draws, sizes):
+    """Batches of at most half as many keys as there are leaves visit only
+    their own leaves (segment list), keep degrees current in the merge and
+    refresh the view around those leaves; checked after every batch, with
+    one batch that overflows a leaf (a hub gains 700 neighbours)."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 1 << lg
+    G = byo.Graph.generate(ctx, "rmat", seed=lg, lg_n=lg, draws=draws, container="pma")
+    s, d = O.rmat_edges(lg, lg, draws)
+    off, nb = O.build_csr(n, s, d)
+    st = O.Store(off, nb)
+    assert 2 * 2 * max(sizes) <= G.nslots() // 512
+    rng = np.random.default_rng(lg)
+    for size in sizes:
+        pairs = rng.integers(0, n, size=(size, 2))
+        keys = O.keys_from_pairs(pairs[:, 0], pairs[:, 1])
+        assert G.insert_batch(keys) == st.insert_batch(keys)
+        ro, rn = st.export_csr()
+        _check_view(byo, O, G, ro, rn, (10,))
+        half = O.keys_from_pairs(pairs[: size // 2 + 1, 0], pairs[: size // 2 + 1, 1])  # stays symmetric
+        assert G.remove_batch(half) == st.remove_batch(half)
+        ro, rn = st.export_csr()
+        _check_view(byo, O, G, ro, rn, (10,))
+    hub = 77
+    others = rng.choice(n, 700, replace=False).astype(np.uint64)
+    keys = np.concatenate([(np.uint64(hub) << np.uint64(32)) | others, (others << np.uint64(32)) | np.uint64(hub)])
+    assert G.insert_batch(keys) == st.insert_batch(keys)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (hub,))
+    assert G.remove_batch(keys) == st.remove_batch(keys)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (hub,))
