@@ -585,6 +585,73 @@ def run_mixed(args, rank, world, local_rank):
     return res, ctx, G
 
 
+def run_multi(args, rank, world, local_rank):
+    """64-source BFS only: one step = one query group of 64 seeded sources
+    (the groups of the mixed workload, in turn) on the PMA graph."""
+    import torch
+    import byo_gb300 as byo
+    from byo_gb300 import _abi
+    L = _abi.lib()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = byo.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    lg = args.lg or MIXED_LG
+    G = byo.Graph.generate(ctx, "rmat", seed=MIXED_SEED, lg_n=lg, draws=8 << lg, container="pma")
+    n, m0 = G.N(), G.M()
+    tuning = G.autotune(bfs=False, multi=True, trials=3) if not args.no_autotune else G.tuning()
+    deg = G.degrees()
+    qsrc = mixed_sources(deg, MIXED_SEED)
+    levels = torch.empty(64 * n, dtype=torch.int32, device=dev)
+    deg_t = torch.from_numpy(deg.astype(np.int64)).to(dev)
+    r = ctypes.c_uint32(0)
+
+    def q(i):
+        _abi.check(L.byo_bfs_multi_device(G.h, qsrc[i % MIXED_QUERIES].ctypes.data, 64, levels.data_ptr(),
+                                          ctypes.byref(r)), ctx.h)
+
+    for i in range(args.warmup):
+        q(i)
+    edges = []
+    for i in range(args.steps):
+        q(i)
+        ctx.synchronize()
+        edges.append(float(((levels.view(64, n) != -1).to(torch.int64) * deg_t).sum().item()) / 2)
+    torch.cuda.synchronize()
+    ctx.kernel_timing("*")
+    launches0 = ctx.launches
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        q(i)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    kl, kms = ctx.kernel_time("bfs_multi")
+    ctx.kernel_timing(None)
+    rounds_log = [(x["round"], x["mode"], x["frontier"], round(x["ms"], 3)) for x in ctx.last_rounds()]
+    peak, peak_kind = measured_peaks()
+    nslots = G.nslots()
+    ms_bytes = 4 * 64 * n + 4 * nslots + 8 * (n + 1) + 6 * 8 * n
+    per = kms / max(kl, 1)
+    units = sum(edges)
+    res = {"metric": "64-source bit-lane BFS, traversed edges over all sources", "value": units / (ms / 1e3) / 1e9,
+           "unit": "G traversed edges/s (sum over the 64 sources, Graph500 count)", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u64 source masks", "data": "synthetic (seeded RMAT)",
+           "config": {"workload": "64-source BFS on RMAT 2^%d, %d draws (PMA)" % (lg, 8 << lg), "n": n, "m": m0,
+                      "tuning": tuning, "rounds": rounds_log},
+           "roofline": {"bound": "hbm", "kernel": "k_ms_bfs", "achieved": ms_bytes / (per / 1e3) / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": ms_bytes / (per / 1e3) / 1e9 / peak, "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": ms_bytes, "avg_launch_ms": per,
+                        "traffic": (traffic_table().get("bfs_multi") or {}).get("bytes_per_launch")},
+           "gpu_launches": ctx.launches - launches0, "clocks": clk}
+    return res, ctx, G
+
+
 def mixed_cpu_sample(steps=None):
     """Bounded sample of the mixed stream on the oracle port: four of the
     query groups' sources as single-source BFS and two update batches."""
@@ -701,7 +768,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static", "mixed"])
+    ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static", "mixed", "multi"])
+    ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
                     help="auto: the committed learned network if present, else m20")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -737,6 +806,9 @@ def main():
         dist.init_process_group("nccl")
     if args.workload == "mixed":
         res, ctx, G = run_mixed(args, rank, world, local_rank)
+    elif args.workload == "multi":
+        res, ctx, G = run_multi(args, rank, world, local_rank)
+        args.no_cpu_baseline = True
     else:
         res, ctx, G = run_ours(args, rank, world, local_rank)
     G.close()

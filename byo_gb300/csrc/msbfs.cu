@@ -135,7 +135,7 @@ __device__ __forceinline__ void ms_levels(const MsArgs &a, uint32_t v, uint64_t 
   while (any) {
     const int s = __ffsll((long long)any) - 1;
     any &= any - 1;
-    if ((got >> s) & 1) a.levels[(uint64_t)s * a.n + v] = r;
+    if ((got >> s) & 1) __stcs(a.levels + (uint64_t)s * a.n + v, r);
   }
 }
 
@@ -160,8 +160,10 @@ __device__ __forceinline__ void ms_list(const MsArgs &a, int slot, int par, bool
   }
 }
 
-// One warp pushes F[u] over slots [b, e) of u.  Warp-uniform call.
-__device__ __forceinline__ void ms_push_range(const MsArgs &a, uint64_t mu, uint64_t b, uint64_t e, int par) {
+// One warp pushes F[u] over slots [b, e) of u; with `track`, the first
+// writer of X[v] appends v to the touched list.  Warp-uniform call.
+__device__ __forceinline__ void ms_push_range(const MsArgs &a, uint64_t mu, uint64_t b, uint64_t e, int par,
+                                              bool track) {
   const unsigned lane = threadIdx.x & 31;
   for (uint64_t base = b; base < e; base += 32) {
     const uint64_t j = base + lane;
@@ -171,11 +173,18 @@ __device__ __forceinline__ void ms_push_range(const MsArgs &a, uint64_t mu, uint
       v = __ldg(a.slots + j);
       if (v != kSentinel) {
         const uint64_t add = mu & ~ldm(a.seen, v);
-        if (add) first = atomicOr((unsigned long long *)a.X + v, (unsigned long long)add) == 0;
+        if (add) {
+          if (track)
+            first = atomicOr((unsigned long long *)a.X + v, (unsigned long long)add) == 0;
+          else
+            atomicOr((unsigned long long *)a.X + v, (unsigned long long)add);
+        }
       }
     }
-    const uint64_t slot = warp_append(first, &a.ctl->tc[par]);
-    if (first) a.T[slot] = v;
+    if (track) {
+      const uint64_t slot = warp_append(first, &a.ctl->tc[par]);
+      if (first) a.T[slot] = v;
+    }
   }
 }
 
@@ -203,7 +212,7 @@ __device__ __forceinline__ void ms_count(MsCtl *c, int cur, uint64_t cnt, uint64
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kMsBlock) k_ms_bfs(MsArgs a) {
+__global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
   MsCtl *c = a.ctl;
   const unsigned int nb = gridDim.x;
   const unsigned lane = threadIdx.x & 31;
@@ -276,7 +285,10 @@ __global__ void __launch_bounds__(kMsBlock) k_ms_bfs(MsArgs a) {
     const uint64_t fdeg = vload(&c->ldeg[prv]);
     const bool push = fdeg + fcnt < a.nslots / a.push_div;
     if (push) {
-      // phase A: a pull round left no list of its frontier; collect it from F
+      // a frontier with many edges is pushed without a touched list: its
+      // touched vertices are found by a pass over X, and it leaves no list
+      const bool dense = fdeg + fcnt >= n / 64;
+      // phase A: a round that left no list of its frontier; collect it from F
       if (!vload(&c->lvalid[prv])) {
         for (uint64_t base = warp * 32; base < n; base += nwarps * 32) {
           const uint64_t v = base + lane;
@@ -296,42 +308,60 @@ __global__ void __launch_bounds__(kMsBlock) k_ms_bfs(MsArgs a) {
       const uint64_t lcp = vload(&c->lc[prv]);
       for (uint64_t i = warp; i < lcp; i += nwarps) {
         const uint32_t u = __ldcg(a.L[prv] + i);
-        ms_push_range(a, ldm(F, u), a.off[u], a.off[u + 1], par);
+        ms_push_range(a, ldm(F, u), a.off[u], a.off[u + 1], par, !dense);
       }
       const uint64_t ccp = vload(&c->cc[ppar]);
       for (uint64_t i = warp; i < ccp; i += nwarps) {
         const uint64_t e = ldm(a.C[ppar], i);
         const uint32_t u = (uint32_t)(e >> 32);
         const uint64_t b = a.off[u] + (uint64_t)(uint32_t)e * a.hub_deg;
-        ms_push_range(a, ldm(F, u), b, min(b + a.hub_deg, a.off[u + 1]), par);
+        ms_push_range(a, ldm(F, u), b, min(b + a.hub_deg, a.off[u + 1]), par, !dense);
       }
       if (!grid_sync(c, nb)) return;
-      // phase 2: the touched vertices become L_r
+      // phase 2: the touched vertices become the next frontier
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         c->cnt[old] = c->ldeg[old] = c->lc[old] = c->hc[old] = c->lvalid[old] = 0;
         c->cc[ppar] = 0;
         c->tc[ppar] = 0;
-        c->lvalid[cur] = 1;
+        c->lvalid[cur] = dense ? 0 : 1;
         c->pushes++;
       }
-      const uint64_t tcount = vload(&c->tc[par]);
       uint64_t my_cnt = 0, my_deg = 0;
-      for (uint64_t base = warp * 32; base < tcount; base += nwarps * 32) {
-        const uint64_t i = base + lane;
-        uint32_t v = 0;
-        uint64_t got = 0, d = 0;
-        if (i < tcount) {
-          v = __ldcg(a.T + i);
-          got = ldm(a.X, v);
-          stm(a.X, v, 0);
-          stm(a.seen, v, ldm(a.seen, v) | got);
-          stm(N, v, got);
-          d = a.off[v + 1] - a.off[v];
-          my_cnt++;
-          my_deg += d;
+      if (dense) {
+        for (uint64_t base = warp * 32; base < n; base += nwarps * 32) {
+          const uint64_t v = base + lane;
+          uint64_t got = 0;
+          if (v < n) {
+            got = ldm(a.X, v);
+            if (got) {
+              stm(a.X, v, 0);
+              stm(a.seen, v, ldm(a.seen, v) | got);
+              stm(N, v, got);
+              my_cnt++;
+              my_deg += a.off[v + 1] - a.off[v];
+            }
+          }
+          ms_levels(a, (uint32_t)v, got, r);
         }
-        ms_list(a, cur, par, i < tcount, v, d);
-        ms_levels(a, v, got, r);
+      } else {
+        const uint64_t tcount = vload(&c->tc[par]);
+        for (uint64_t base = warp * 32; base < tcount; base += nwarps * 32) {
+          const uint64_t i = base + lane;
+          uint32_t v = 0;
+          uint64_t got = 0, d = 0;
+          if (i < tcount) {
+            v = __ldcg(a.T + i);
+            got = ldm(a.X, v);
+            stm(a.X, v, 0);
+            stm(a.seen, v, ldm(a.seen, v) | got);
+            stm(N, v, got);
+            d = a.off[v + 1] - a.off[v];
+            my_cnt++;
+            my_deg += d;
+          }
+          ms_list(a, cur, par, i < tcount, v, d);
+          ms_levels(a, v, got, r);
+        }
       }
       ms_count(c, cur, my_cnt, my_deg);
     } else {
@@ -473,7 +503,7 @@ __global__ void __launch_bounds__(kMsBlock) k_ms_bfs(MsArgs a) {
     while (any) {
       const int s = __ffsll((long long)any) - 1;
       any &= any - 1;
-      if ((miss >> s) & 1) a.levels[(uint64_t)s * n + v] = kSentinel;
+      if ((miss >> s) & 1) __stcs(a.levels + (uint64_t)s * n + v, kSentinel);
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) c->rounds = r - 1;
