@@ -652,6 +652,239 @@ def run_multi(args, rank, world, local_rank):
     return res, ctx, G
 
 
+# ------------------------------------------------------------------ scale and graph families
+SCALE_GRAPHS = [
+    ("rmat26", "RMAT 2^26, 2^30 draws (~2^31 directed)", dict(kind="rmat", seed=1, lg_n=26, draws=1 << 30)),
+    ("er26", "ER 2^26, avg degree 32", dict(kind="er", seed=2, n=1 << 26, draws=16 << 26)),
+]
+FAMILY_GRAPHS = SCALE_GRAPHS + [
+    ("grid4096", "grid 4096 x 4096, 4-neighbour", dict(kind="grid", n=4096, draws=4096)),
+    ("chung_lu24", "Chung-Lu 2^24, exponent 2.1, avg degree 16", dict(kind="chung_lu", seed=4, n=1 << 24,
+                                                                     draws=8 << 24, exponent=2.1)),
+]
+TC_GRAPH = ("rmat22_deg32", "RMAT 2^22, avg degree 32 (2^26 draws)", dict(kind="rmat", seed=1, lg_n=22,
+                                                                         draws=1 << 26))
+
+
+def _sources(deg, count, seed):
+    rng = np.random.default_rng(seed)
+    nz = np.nonzero(deg)[0]
+    out = [10] if deg[10] else []
+    while len(out) < count:
+        out.append(int(rng.choice(nz)))
+    return out
+
+
+class _Timer:
+    def __init__(self, torch, stream):
+        self.torch, self.stream = torch, stream
+        self.a = torch.cuda.Event(enable_timing=True)
+        self.b = torch.cuda.Event(enable_timing=True)
+
+    def __call__(self, fn, reps=1):
+        ts = []
+        for _ in range(reps):
+            self.a.record(self.stream)
+            fn()
+            self.b.record(self.stream)
+            self.b.synchronize()
+            ts.append(self.a.elapsed_time(self.b))
+        return float(np.median(ts))
+
+
+def run_scale(args, rank, world, local_rank):
+    """Config C3: BFS, CC and PageRank (FP32 compensated against FP64) on the
+    2^26-vertex RMAT and ER graphs in the CSR container; triangle counting on
+    RMAT 2^22 with average degree 32."""
+    import torch
+    import byo_gb300 as byo
+    from byo_gb300 import _abi
+    from byo_gb300 import policy as learned
+    L = _abi.lib()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = byo.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    timer = _Timer(torch, stream)
+    learned.load_default(ctx)
+    peak, peak_kind = measured_peaks()
+    comps, launches, pr_roof = {}, 0, None
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    for name, desc, spec in SCALE_GRAPHS:
+        spec = dict(spec)
+        kind = spec.pop("kind")
+        t0 = time.time()
+        G = byo.Graph.generate(ctx, kind, container="csr", **spec)
+        n, m = G.N(), G.M()
+        ctx.synchronize()
+        gen_s = time.time() - t0
+        deg = G.degrees()
+        deg_t = torch.from_numpy(deg.astype(np.int64)).to(dev)
+        par = torch.empty(n, dtype=torch.int32, device=dev)
+        par2 = torch.empty(n, dtype=torch.int32, device=dev)
+        lab = torch.empty(n, dtype=torch.int32, device=dev)
+        p32 = torch.empty(n, dtype=torch.float64, device=dev)
+        p64 = torch.empty(n, dtype=torch.float64, device=dev)
+        pf = torch.empty(n, dtype=torch.float64, device=dev)
+        it, l1, r = ctypes.c_uint32(0), ctypes.c_double(0), ctypes.c_uint32(0)
+        launches0 = ctx.launches
+        g = {"graph": desc, "n": n, "m": m, "generate_s": gen_s}
+        bfs = []
+        for src in _sources(deg, 4, 7):
+            row = {"src": src}
+            for pname, pol in (("m20", _abi.POLICY_M20), ("learned", _abi.POLICY_LEARNED)):
+                out = par if pname == "m20" else par2
+                _abi.check(L.byo_bfs_device(G.h, src, out.data_ptr(), None, pol, None), ctx.h)  # warm
+                row["ms_" + pname] = timer(lambda: _abi.check(L.byo_bfs_device(G.h, src, out.data_ptr(), None, pol,
+                                                                                ctypes.byref(r)), ctx.h), 3)
+            row["bit_exact"] = bool(torch.equal(par, par2))
+            row["edges"] = float((deg_t * (par != -1)).sum().item()) / 2
+            row["gteps_m20"] = row["edges"] / row["ms_m20"] / 1e6
+            row["gteps_learned"] = row["edges"] / row["ms_learned"] / 1e6
+            bfs.append(row)
+        g["bfs"] = bfs
+        _abi.check(L.byo_cc_device(G.h, lab.data_ptr()), ctx.h)
+        g["cc_ms"] = timer(lambda: _abi.check(L.byo_cc_device(G.h, lab.data_ptr()), ctx.h), 3)
+        g["cc_gteps"] = m / 2 / g["cc_ms"] / 1e6
+        lb = lab.to(torch.int64)
+        g["cc_components"] = int((lb == torch.arange(n, device=dev)).sum().item())
+        for key, prec, buf in (("fp32_kahan", _abi.PR_FP32_KAHAN, p32), ("fp64", _abi.PR_FP64, p64),
+                               ("fp32", _abi.PR_FP32, pf)):
+            _abi.check(L.byo_pagerank_device(G.h, 0.0, PR_ITERS, prec, buf.data_ptr(), ctypes.byref(it),
+                                             ctypes.byref(l1)), ctx.h)
+            ctx.kernel_timing("pr_pull")
+            ms = timer(lambda: _abi.check(L.byo_pagerank_device(G.h, 0.0, PR_ITERS, prec, buf.data_ptr(),
+                                                                ctypes.byref(it), ctypes.byref(l1)), ctx.h), 3)
+            kl, kms = ctx.kernel_time("pr_pull")
+            ctx.kernel_timing(None)
+            g["pr_" + key] = {"ms": ms, "iters": it.value, "gteps": m * it.value / ms / 1e6,
+                              "kernel_ms_per_iter": kms / max(3 * it.value, 1)}
+        g["pr_l1_fp32_kahan_vs_fp64"] = float((p32 - p64).abs().sum().item())
+        g["pr_l1_fp32_vs_fp64"] = float((pf - p64).abs().sum().item())
+        g["pr_sum_fp64"] = float(p64.sum().item())
+        per_iter = g["pr_fp32_kahan"]["kernel_ms_per_iter"]
+        achieved = pr_iteration_bytes(n, m, G.nslots()) / (per_iter / 1e3) / 1e9
+        if pr_roof is None:
+            pr_roof = {"bound": "hbm", "kernel": "pr_pull (k_pr_units + k_pr_combine) on " + name,
+                       "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "peak_source": peak_kind, "algorithmic_bytes_per_launch": pr_iteration_bytes(n, m, G.nslots()),
+                       "avg_launch_ms": per_iter, "traffic": None}
+        ms_lev = torch.empty(64 * n, dtype=torch.int32, device=dev)
+        srcs64 = np.ascontiguousarray(_sources(deg, 64, 11), np.uint32)
+        _abi.check(L.byo_bfs_multi_device(G.h, srcs64.ctypes.data, 64, ms_lev.data_ptr(), None), ctx.h)
+        g["bfs64_ms"] = timer(lambda: _abi.check(L.byo_bfs_multi_device(G.h, srcs64.ctypes.data, 64,
+                                                                         ms_lev.data_ptr(), None), ctx.h), 2)
+        del ms_lev
+        launches += ctx.launches - launches0
+        comps[name] = g
+        G.close()
+        del par, par2, lab, p32, p64, pf
+        torch.cuda.empty_cache()
+    # triangle counting
+    name, desc, spec = TC_GRAPH
+    spec = dict(spec)
+    kind = spec.pop("kind")
+    G = byo.Graph.generate(ctx, kind, container="csr", **spec)
+    cnt = byo.Triangle_degree_ordering(G)
+    tms = timer(lambda: byo.Triangle_degree_ordering(G), 3)
+    comps[name] = {"graph": desc, "n": G.N(), "m": G.M(), "triangles": int(cnt), "tc_ms": tms,
+                   "tc_edges_per_s": G.M() / tms * 1e3}
+    G.close()
+    clk = clocks.stop()
+    rm = comps["rmat26"]
+    bfs_ms = float(np.mean([b["ms_learned"] for b in rm["bfs"]]))
+    bfs_edges = float(np.mean([b["edges"] for b in rm["bfs"]]))
+    step_ms = bfs_ms + rm["cc_ms"] + rm["pr_fp32_kahan"]["ms"]
+    units = bfs_edges + rm["m"] / 2 + rm["m"] * rm["pr_fp32_kahan"]["iters"]
+    res = {"metric": "scale: BFS + CC + PageRank (FP32 compensated) edge-ops/s on RMAT 2^26 (2^31 directed)",
+           "value": units / step_ms / 1e6, "unit": "G edge-ops/s (BFS traversed + CC + PR edges x iters)",
+           "n_gpus": world, "steps": 3, "warmup": 1, "ms_per_step": step_ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u32 ids / fp32-kahan pagerank (fp64 residual)",
+           "data": "synthetic (seeded RMAT / ER)", "config": {"workload": "C3 scale (CSR container)",
+                                                               "pr_iters": PR_ITERS, "policy": "learned vs m20"},
+           "components": comps, "roofline": pr_roof, "gpu_launches": launches, "clocks": clk}
+    return res, ctx, None
+
+
+def run_families(args, rank, world, local_rank):
+    """Config C4: the learned policy against the m/20 rule on RMAT, ER, grid
+    and Chung-Lu graphs (PMA container): BFS time from four sources each, the
+    update pair (insert + remove of 10^6 pairs) with the learned update
+    strategy against the in-place merge, outputs compared bit for bit."""
+    import torch
+    import byo_gb300 as byo
+    from byo_gb300 import _abi
+    from byo_gb300 import policy as learned
+    L = _abi.lib()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = byo.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    timer = _Timer(torch, stream)
+    if not learned.load_default(ctx):
+        raise SystemExit("no trained policy to compare")
+    comps, launches = {}, 0
+    ch, r = ctypes.c_uint64(0), ctypes.c_uint32(0)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    tot = {"m20": 0.0, "learned": 0.0, "merge": 0.0, "learned_update": 0.0}
+    for name, desc, spec in FAMILY_GRAPHS:
+        spec = dict(spec)
+        kind = spec.pop("kind")
+        G = byo.Graph.generate(ctx, kind, container="pma", **spec)
+        n, m = G.N(), G.M()
+        deg = G.degrees()
+        par = torch.empty(n, dtype=torch.int32, device=dev)
+        par2 = torch.empty(n, dtype=torch.int32, device=dev)
+        launches0 = ctx.launches
+        g = {"graph": desc, "n": n, "m": m, "bfs": []}
+        for src in _sources(deg, 4, 9):
+            row = {"src": src}
+            for pname, pol, out in (("m20", _abi.POLICY_M20, par), ("learned", _abi.POLICY_LEARNED, par2)):
+                _abi.check(L.byo_bfs_device(G.h, src, out.data_ptr(), None, pol, None), ctx.h)
+                row["ms_" + pname] = timer(lambda: _abi.check(L.byo_bfs_device(G.h, src, out.data_ptr(), None, pol,
+                                                                                ctypes.byref(r)), ctx.h), 3)
+            row["rounds"] = r.value
+            row["bit_exact"] = bool(torch.equal(par, par2))
+            tot["m20"] += row["ms_m20"]
+            tot["learned"] += row["ms_learned"]
+            g["bfs"].append(row)
+        keys = torch.empty(2 * 1000000, dtype=torch.int64, device=dev)
+        _abi.check(L.byo_gen_uniform_keys_device(ctx.h, 77, n, 1000000, keys.data_ptr()), ctx.h)
+
+        def pair():
+            _abi.check(L.byo_graph_insert_batch_device(G.h, keys.data_ptr(), keys.numel(), 0, ctypes.byref(ch)),
+                       ctx.h)
+            _abi.check(L.byo_graph_remove_batch_device(G.h, keys.data_ptr(), keys.numel(), 0, ctypes.byref(ch)),
+                       ctx.h)
+        for uname, up in (("merge", _abi.UPDATE_MERGE), ("learned_update", _abi.UPDATE_LEARNED)):
+            _abi.check(L.byo_ctx_set_update_policy(ctx.h, up), ctx.h)
+            pair()
+            g["update_pair_ms_" + uname] = timer(pair, 3)
+            tot[uname] += g["update_pair_ms_" + uname]
+        _abi.check(L.byo_ctx_set_update_policy(ctx.h, _abi.UPDATE_MERGE), ctx.h)
+        lab = torch.empty(n, dtype=torch.int32, device=dev)
+        _abi.check(L.byo_cc_device(G.h, lab.data_ptr()), ctx.h)
+        g["cc_ms"] = timer(lambda: _abi.check(L.byo_cc_device(G.h, lab.data_ptr()), ctx.h), 3)
+        launches += ctx.launches - launches0
+        comps[name] = g
+        G.close()
+        del par, par2, lab, keys
+        torch.cuda.empty_cache()
+    clk = clocks.stop()
+    res = {"metric": "learned vs m/20 direction policy: summed BFS time over four graph families (bit-exact)",
+           "value": tot["m20"] / tot["learned"], "unit": "speed-up of the learned policy (m20 time / learned time)",
+           "n_gpus": world, "steps": 3, "warmup": 1, "ms_per_step": tot["learned"], "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u32 ids", "data": "synthetic (seeded graphs)",
+           "config": {"workload": "C4 policy comparison (PMA container)"},
+           "components": {"graphs": comps, "bfs_ms_total_m20": tot["m20"], "bfs_ms_total_learned": tot["learned"],
+                          "update_ms_total_merge": tot["merge"],
+                          "update_ms_total_learned": tot["learned_update"]},
+           "gpu_launches": launches, "clocks": clk}
+    return res, ctx, None
+
+
 def mixed_cpu_sample(steps=None):
     """Bounded sample of the mixed stream on the oracle port: four of the
     query groups' sources as single-source BFS and two update batches."""
@@ -768,7 +1001,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static", "mixed", "multi"])
+    ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static", "mixed", "multi", "scale", "families"])
     ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
@@ -809,9 +1042,14 @@ def main():
     elif args.workload == "multi":
         res, ctx, G = run_multi(args, rank, world, local_rank)
         args.no_cpu_baseline = True
+    elif args.workload in ("scale", "families"):
+        fn = run_scale if args.workload == "scale" else run_families
+        res, ctx, G = fn(args, rank, world, local_rank)
+        args.no_cpu_baseline = True
     else:
         res, ctx, G = run_ours(args, rank, world, local_rank)
-    G.close()
+    if G is not None:
+        G.close()
     ctx.close()
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:

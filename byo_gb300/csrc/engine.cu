@@ -6,6 +6,7 @@
 
 #include "device.cuh"
 #include "engine.h"
+#include "policy.cuh"
 #include "internal.h"
 #include "scan.cuh"
 
@@ -252,7 +253,7 @@ __global__ void __launch_bounds__(256) k_pull_long(const uint64_t *__restrict__ 
                                                    uint64_t *__restrict__ lp, uint32_t *visited,
                                                    uint32_t *out_list, uint32_t *out_bits,
                                                    RoundStats *st, uint64_t lvl,
-                                                   const uint32_t *__restrict__ defer, int cap) {
+                                                   const uint32_t *__restrict__ defer, int cap, PolicyTail pt) {
   const uint64_t nd = *(volatile unsigned long long *)&st->ndefer;
   const unsigned lane = lane_id();
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
@@ -283,17 +284,19 @@ __global__ void __launch_bounds__(256) k_pull_long(const uint64_t *__restrict__ 
       atomicAdd(&st->hist[log4_bin(d)], 1ull);
     }
   }
+  policy_tail(pt, st);
 }
 
 // ---------------------------------------------------------------- bookkeeping
-__global__ void k_mark_visited(const uint32_t *__restrict__ list, const RoundStats *st,
-                               uint32_t *visited) {
+__global__ void k_mark_visited(const uint32_t *__restrict__ list, RoundStats *st, uint32_t *visited,
+                               PolicyTail pt) {
   const uint64_t cnt = st->count;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
        i += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t v = list[i];
     atomicOr(visited + (v >> 5), 1u << (v & 31));
   }
+  policy_tail(pt, st);
 }
 
 __global__ void k_clear_words_from_list(const uint32_t *__restrict__ list, uint64_t cnt,
@@ -439,8 +442,11 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
                    const EngineTuning &tune, bool run_policy) {
   byo_ctx *ctx = g->ctx;
   RoundStats *d_st = nullptr;
-  BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 1, (uint64_t **)&d_st));
-  BYO_CU(ctx, cudaMemsetAsync(d_st, 0, sizeof(RoundStats), ctx->stream));
+  BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 2, (uint64_t **)&d_st));
+  BYO_CU(ctx, cudaMemsetAsync(d_st, 0, sizeof(RoundStats) + 8, ctx->stream));
+  // the policy for the next round runs as the epilogue of this round's last kernel
+  PolicyTail pt;
+  if (run_policy) BYO_TRY(policy_tail_args(g, (unsigned int *)(d_st + 1), st.reached, mode == MODE_PULL, &pt));
   uint32_t *defer = nullptr;
   BYO_TRY(ws(g, WS_DEFER, g->n + 1, &defer));
   const uint64_t lvl = (uint64_t)st.round << 32;
@@ -463,7 +469,7 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
            st.lp, st.visited, out.list, out.bits, d_st, lvl, defer, tune.pull_cap, stage);
     launch(ctx, k_pull_long, dim3(ctx->num_sms * 4), dim3(256), 0, (const uint64_t *)g->d_off,
            (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.bits, st.lp,
-           st.visited, out.list, out.bits, d_st, lvl, (const uint32_t *)defer, tune.pull_cap);
+           st.visited, out.list, out.bits, d_st, lvl, (const uint32_t *)defer, tune.pull_cap, pt);
   } else {
     if (!in.has_list) return set_error(ctx, BYO_EINVAL, "sparse round needs a frontier list");
     if (mode == MODE_PUSH) {
@@ -501,10 +507,9 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
              d_st, lvl, tune.blocked_tile);
     }
     launch(ctx, k_mark_visited, dim3(grid_for(ctx, in.outdeg + 1, 256)), dim3(256), 0,
-           (const uint32_t *)out.list, (const RoundStats *)d_st, st.visited);
+           (const uint32_t *)out.list, d_st, st.visited, pt);
   }
   BYO_TRY(check_launch(ctx, "edge_map_round"));
-  if (run_policy) BYO_TRY(round_policy(g, d_st, st.reached, mode == MODE_PULL));
   RoundStats *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
   BYO_CU(ctx, cudaMemcpyAsync(h, d_st, sizeof(RoundStats), cudaMemcpyDeviceToHost, ctx->stream));
@@ -560,7 +565,7 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
   const bool run_policy = policy == BYO_POLICY_LEARNED || ctx->time_rounds;
   if (run_policy) {
     RoundStats *d_st = nullptr, *h = nullptr;
-    BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 1, (uint64_t **)&d_st));
+    BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 2, (uint64_t **)&d_st));
     BYO_TRY(pinned(ctx, 4096, (void **)&h));
     std::memset(h, 0, sizeof(RoundStats));
     h->count = 1;

@@ -76,6 +76,18 @@ int trav_init(byo_graph *g, TravState &st, uint32_t src);
 int trav_extract(byo_graph *g, const TravState &st, uint32_t *d_parent, uint32_t *d_level);
 EngineTuning default_tuning(const byo_graph *g);
 
+// Arguments of the policy epilogue fused into a round's last kernel
+// (policy.cuh); on == 0 disables it.
+struct PolicyTail {
+  const float *P = nullptr;
+  float n = 0, m = 0, reached_before = 0;
+  int dense = 0, has_net = 0, on = 0, log = 0;
+  unsigned int *done = nullptr;  // blocks finished; the last one resets it
+};
+// Fills pt for a round reading a frontier of the given kind (mlp.cu).
+int policy_tail_args(byo_graph *g, unsigned int *done, uint64_t reached_before, bool this_round_dense,
+                     PolicyTail *pt);
+
 // Policy kernel after a round (mlp.cu): features of the frontier in d_st,
 // the m/20 rule's choice, and the network's choice when one is trained;
 // writes d_st->mode and d_st->feat.

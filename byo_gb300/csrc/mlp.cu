@@ -18,16 +18,11 @@
 #include "device.cuh"
 #include "engine.h"
 #include "internal.h"
+#include "policy.cuh"
 
 namespace byo {
 
-constexpr int kIn = 16, kH = 32, kOut = 5;
-constexpr int kW1 = 0, kB1 = kW1 + kH * kIn, kW2 = kB1 + kH, kB2 = kW2 + kH * kH, kW3 = kB2 + kH,
-              kB3 = kW3 + kOut * kH, kParams = kB3 + kOut;  // 1765
 constexpr int kMb = 128;
-// The network must predict a gain of more than 2^(16*margin) - 1 (about 7%)
-// over the rule's choice before it overrides it.
-constexpr float kJudgeMargin = 0.006f;
 
 struct Mlp {
   float *d_params = nullptr;    // kParams, the network used for inference
@@ -204,64 +199,11 @@ __global__ void __launch_bounds__(256) k_mlp_train(float *P, const float *__rest
 }
 
 // ---------------------------------------------------------------- round policy (inference)
-// Frontier statistics of the round just finished -> features -> network ->
-// chosen mode for the next round, written next to the statistics so the host
-// reads both with one copy.  One warp; lane k computes hidden unit k.
+// Stand-alone launch of the round policy, for the frontier a traversal starts
+// from (later rounds run it as the epilogue of their last kernel).
 __global__ void k_round_policy(const float *__restrict__ P, RoundStats *st, float n, float m, float reached_before,
-                               int dense, int has_net) {
-  __shared__ float x[kIn], h1[kH], h2[kH], y[kOut];
-  __shared__ int fallback;
-  const int lane = threadIdx.x;
-  if (lane == 0) {
-    const float inv = 1.f / 32.f;
-    const float f = (float)st->count, d = (float)st->outdeg;
-    const float unvisited = n - reached_before - f;
-    x[0] = log2f(f + 1.f) * inv;
-    x[1] = log2f(d + 1.f) * inv;
-    x[2] = log2f(fmaxf(unvisited, 0.f) + 1.f) * inv;
-    x[3] = log2f(n + 1.f) * inv;
-    x[4] = log2f(m + 1.f) * inv;
-    x[5] = 0.f;
-    float tot = 0.f;
-    for (int i = 0; i < 8; i++) tot += (float)st->hist[i];
-    for (int i = 0; i < 8; i++) x[6 + i] = tot > 0.f ? (float)st->hist[i] / tot : 0.f;
-    x[14] = (f + d) / (m / 20.f + 1.f);
-    x[15] = f / (n + 1.f);
-    // the GBBS rule (edge_map_data.h:263,291) for the next round
-    const unsigned long long fc = st->count, dc = st->outdeg;
-    const unsigned long long nn = (unsigned long long)n, mm = (unsigned long long)m;
-    fallback = ((dense && fc > nn / 10) || (fc + dc > mm / 20)) ? MODE_PULL : MODE_PUSH;
-    for (int i = 0; i < kIn; i++) st->feat[i] = x[i];
-    st->mode = (unsigned long long)fallback;
-  }
-  __syncwarp();
-  if (!has_net) return;
-  {
-    float a = P[kB1 + lane];
-    for (int k = 0; k < kIn; k++) a = fmaf(P[kW1 + lane * kIn + k], x[k], a);
-    h1[lane] = a > 0.f ? a : 0.f;
-  }
-  __syncwarp();
-  {
-    float a = P[kB2 + lane];
-    for (int k = 0; k < kH; k++) a = fmaf(P[kW2 + lane * kH + k], h1[k], a);
-    h2[lane] = a > 0.f ? a : 0.f;
-  }
-  __syncwarp();
-  if (lane < kOut) {
-    float a = P[kB3 + lane];
-    for (int k = 0; k < kH; k++) a = fmaf(P[kW3 + lane * kH + k], h2[k], a);
-    y[lane] = a;
-  }
-  __syncwarp();
-  if (lane == 0) {
-    int best = 0;
-    for (int o = 1; o < 3; o++)
-      if (y[o] < y[best]) best = o;
-    // the m/20 rule judges: keep its choice unless the predicted gain is clear
-    if (y[fallback] - y[best] <= kJudgeMargin) best = fallback;
-    st->mode = (unsigned long long)best;
-  }
+                               int dense, int has_net, int log) {
+  round_policy_warp(P, st, n, m, reached_before, dense, has_net, log);
 }
 
 // ---------------------------------------------------------------- host side
@@ -294,8 +236,23 @@ int round_policy(byo_graph *g, RoundStats *d_st, uint64_t reached_before, bool t
   byo_ctx *ctx = g->ctx;
   const bool net = policy_trained(ctx);
   launch(ctx, k_round_policy, dim3(1), dim3(32), 0, policy_params(ctx), d_st, (float)g->n, (float)g->m,
-         (float)reached_before, this_round_dense ? 1 : 0, net ? 1 : 0);
+         (float)reached_before, this_round_dense ? 1 : 0, net ? 1 : 0, ctx->time_rounds ? 1 : 0);
   return check_launch(ctx, "round_policy");
+}
+
+int policy_tail_args(byo_graph *g, unsigned int *done, uint64_t reached_before, bool this_round_dense,
+                     PolicyTail *pt) {
+  byo_ctx *ctx = g->ctx;
+  pt->P = policy_params(ctx);
+  pt->n = (float)g->n;
+  pt->m = (float)g->m;
+  pt->reached_before = (float)reached_before;
+  pt->dense = this_round_dense ? 1 : 0;
+  pt->has_net = policy_trained(ctx) ? 1 : 0;
+  pt->on = 1;
+  pt->log = ctx->time_rounds ? 1 : 0;
+  pt->done = done;
+  return BYO_OK;
 }
 
 // Xavier-uniform initialisation from a counter-based stream (seeded).

@@ -134,14 +134,18 @@ def loss_grad(ctx, params, X, Y, M):
 
 
 JUDGE_MARGIN = 0.006  # the engine's kJudgeMargin (a predicted gain of about 7%)
+GATE_FACTOR = 64      # the engine's kGateFactor
 
 
 def round_choices(ctx, params, X, fallback):
     """The engine's decision rule applied to predictions: argmin over the
-    three directions unless the rule's choice is within the judge margin."""
+    three directions unless the rule's choice is within the judge margin, and
+    the rule alone for frontiers far below its threshold (feature 14 is
+    (|F| + outdeg) / (m/20))."""
     P = forward(ctx, params, X)[:, :3]
     best = P.argmin(1)
     keep = P[np.arange(len(P)), fallback] - P[np.arange(len(P)), best] <= JUDGE_MARGIN
+    keep |= X[:, 14] * GATE_FACTOR <= 1.0
     return np.where(keep, fallback, best)
 
 
@@ -163,21 +167,23 @@ def load_default(ctx, path=DEFAULT_PARAMS):
 
 
 def _graphs(ctx, scale):
+    """Training graphs of 2^(18 + scale) vertices (seeds unlike the benchmark
+    graphs'): RMAT dense and sparse, ER, a square grid, Chung-Lu."""
     from .graph import Graph
     s = scale
-    return [
-        ("rmat", Graph.generate(ctx, "rmat", seed=101, lg_n=18 + s, draws=1 << (22 + s))),
-        ("rmat-sparse", Graph.generate(ctx, "rmat", seed=102, lg_n=18 + s, draws=1 << (20 + s))),
-        ("er", Graph.generate(ctx, "er", seed=103, n=1 << (18 + s), draws=1 << (21 + s))),
-        ("grid", Graph.generate(ctx, "grid", n=1 << (8 + s // 2), draws=1 << (8 + s // 2))),
-        ("chung-lu", Graph.generate(ctx, "chung_lu", seed=104, n=1 << (18 + s), draws=1 << (21 + s), exponent=2.1)),
-    ]
+    yield "rmat", Graph.generate(ctx, "rmat", seed=101 + s, lg_n=18 + s, draws=1 << (22 + s))
+    yield "rmat-sparse", Graph.generate(ctx, "rmat", seed=102 + s, lg_n=18 + s, draws=1 << (20 + s))
+    yield "er", Graph.generate(ctx, "er", seed=103 + s, n=1 << (18 + s), draws=1 << (21 + s))
+    yield "grid", Graph.generate(ctx, "grid", n=1 << (8 + s // 2), draws=1 << (8 + s // 2))
+    yield "chung-lu", Graph.generate(ctx, "chung_lu", seed=104 + s, n=1 << (18 + s), draws=1 << (21 + s),
+                                     exponent=2.1)
 
 
 def main():
     ap = argparse.ArgumentParser(description="collect engine timings on this GPU and train the policy")
     ap.add_argument("--out", default=DEFAULT_PARAMS)
-    ap.add_argument("--scale", type=int, default=2, help="graphs of 2^(18+scale) vertices")
+    ap.add_argument("--scales", default="0,2,4,6", help="graphs of 2^(18+scale) vertices, for each scale")
+    ap.add_argument("--large", type=int, default=8, help="also RMAT graphs of 2^(18+large) vertices (0: none)")
     ap.add_argument("--sources", type=int, default=12)
     ap.add_argument("--epochs", type=int, default=600)
     args = ap.parse_args()
@@ -185,7 +191,17 @@ def main():
     ctx = Context(0)
     t0 = time.time()
     tr, te, report = [], [], {}
-    for name, G in _graphs(ctx, args.scale):
+    def graphs():
+        for sc in [int(x) for x in args.scales.split(",") if x]:
+            for name, G in _graphs(ctx, sc):
+                yield "%s-%d" % (name, 18 + sc), G
+        if args.large:
+            lg = 18 + args.large
+            for name, draws in (("rmat", 1 << (lg + 4)), ("rmat-sparse", 1 << (lg + 2))):
+                yield "%s-%d" % (name, lg), Graph.generate(ctx, "rmat", seed=111 + len(name), lg_n=lg, draws=draws)
+            yield "er-%d" % lg, Graph.generate(ctx, "er", seed=113, n=1 << lg, draws=1 << (lg + 4))
+
+    for name, G in graphs():
         deg = G.degrees()
         rng = np.random.default_rng(G.N() + len(name))
         srcs = rng.choice(np.nonzero(deg)[0], args.sources, replace=False)
@@ -193,18 +209,26 @@ def main():
         tr.append(collect_round_samples(G, srcs[:k]))
         te.append((name, collect_round_samples(G, srcs[k:], warm=False)))
         G.close()
+        print(name, "samples", len(tr[-1][0]), "%.1fs" % (time.time() - t0), flush=True)
     # update samples on the packed-memory-array container: symmetrised uniform
     # batches, log-uniform sizes
-    G = Graph.generate(ctx, "rmat", seed=105, lg_n=20 + args.scale, draws=1 << (24 + args.scale), container="pma")
-    n = G.N()
-    rng = np.random.default_rng(7)
-    batches = []
-    for b in np.unique(np.logspace(2, 7, 16).astype(np.int64)):
-        u = rng.integers(0, n, b, dtype=np.uint64)
-        v = rng.integers(0, n, b, dtype=np.uint64)
-        batches.append(np.concatenate([(u << np.uint64(32)) | v, (v << np.uint64(32)) | u]))
-    ux, uy, um = collect_update_samples(G, batches)
-    G.close()
+    uxs, uys, ums = [], [], []
+    for lg in (20, 22, 24, 18 + args.large if args.large else 24):
+        G = Graph.generate(ctx, "rmat", seed=105 + lg, lg_n=lg, draws=1 << (lg + 4), container="pma")
+        n = G.N()
+        rng = np.random.default_rng(lg)
+        batches = []
+        for b in np.unique(np.logspace(2, 7, 11).astype(np.int64)):
+            u = rng.integers(0, n, b, dtype=np.uint64)
+            v = rng.integers(0, n, b, dtype=np.uint64)
+            batches.append(np.concatenate([(u << np.uint64(32)) | v, (v << np.uint64(32)) | u]))
+        x, y, mk = collect_update_samples(G, batches)
+        uxs.append(x)
+        uys.append(y)
+        ums.append(mk)
+        G.close()
+        print("updates lg", lg, "%.1fs" % (time.time() - t0), flush=True)
+    ux, uy, um = np.concatenate(uxs), np.concatenate(uys), np.concatenate(ums)
     X = np.concatenate([t[0] for t in tr] + [ux])
     Y = np.concatenate([t[1] for t in tr] + [uy])
     M = np.concatenate([t[2] for t in tr] + [um])
