@@ -117,6 +117,9 @@ SIGNATURES = {
     "byo_bfs_cc": (_int, [_vp, _vp]),
     "byo_pagerank": (_int, [_vp, _dbl, _u32, _int, _vp, _P(_u32), _P(_dbl)]),
     "byo_pagerank_device": (_int, [_vp, _dbl, _u32, _int, _vp, _P(_u32), _P(_dbl)]),
+    "byo_pagerank_edgemap": (_int, [_vp, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
+    "byo_pagerank_delta": (_int, [_vp, _dbl, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
+    "byo_pagerank_delta_device": (_int, [_vp, _dbl, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
     "byo_triangle_count": (_int, [_vp, _P(_u64)]),
     "byo_functor_bfs_create": (_int, [_vp, _u32, _P(_vp)]),
     "byo_functor_bfs_parents": (_int, [_vp, _vp]),

@@ -327,6 +327,26 @@ int byo_pagerank_device(byo_graph *g, double eps, uint32_t max_iters, int precis
   return pagerank_run(g, eps, max_iters, precision, d_p, iters, l1);
 }
 
+int byo_pagerank_edgemap(byo_graph *g, double eps, uint32_t max_iters, double *h_p, uint32_t *iters,
+                         double *l1) {
+  return byo_pagerank(g, eps, max_iters, BYO_PR_FP64, h_p, iters, l1);
+}
+
+int byo_pagerank_delta_device(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *d_p,
+                              uint32_t *rounds, double *l1) {
+  if (!g || !d_p) return BYO_EINVAL;
+  return pagerank_delta_run(g, eps, local_eps, max_iters, d_p, rounds, l1);
+}
+
+int byo_pagerank_delta(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *h_p,
+                       uint32_t *rounds, double *l1) {
+  if (!g || !h_p) return BYO_EINVAL;
+  double *d = nullptr;
+  BYO_TRY(ws(g, WS_TC_CNT, 2 * g->n + 2, (uint32_t **)&d));
+  BYO_TRY(pagerank_delta_run(g, eps, local_eps, max_iters, d, rounds, l1));
+  return copy_to_host(g->ctx, h_p, d, g->n * 8);
+}
+
 int byo_pagerank(byo_graph *g, double eps, uint32_t max_iters, int precision, double *h_p, uint32_t *iters,
                  double *l1) {
   if (!g || !h_p) return BYO_EINVAL;

@@ -367,6 +367,25 @@ def PageRank(G, eps=1e-6, max_iters=100, precision=_abi.PR_FP32_KAHAN, info=Fals
     return (p, it.value, l1.value) if info else p
 
 
+def PageRank_edgeMap(G, eps=1e-6, max_iters=100, info=False):
+    """PageRank_edgeMap (PageRank.h:80-123): PageRank's recurrence in FP64."""
+    p = np.empty(G.N(), np.float64)
+    it = ctypes.c_uint32(0)
+    l1 = ctypes.c_double(0)
+    check(lib().byo_pagerank_edgemap(G.h, eps, max_iters, _ptr(p), ctypes.byref(it), ctypes.byref(l1)), G.ctx.h)
+    return (p, it.value, l1.value) if info else p
+
+
+def PageRankDelta(G, eps=1e-6, local_eps=0.01, max_iters=100, info=False):
+    """delta::PageRankDelta (PageRank.h:340-398), FP64."""
+    p = np.empty(G.N(), np.float64)
+    r = ctypes.c_uint32(0)
+    l1 = ctypes.c_double(0)
+    check(lib().byo_pagerank_delta(G.h, eps, local_eps, max_iters, _ptr(p), ctypes.byref(r), ctypes.byref(l1)),
+          G.ctx.h)
+    return (p, r.value, l1.value) if info else p
+
+
 def Triangle_degree_ordering(G):
     c = ctypes.c_uint64(0)
     check(lib().byo_triangle_count(G.h, ctypes.byref(c)), G.ctx.h)

@@ -216,6 +216,26 @@ int byo_pagerank(byo_graph *g, double eps, uint32_t max_iters, int precision, do
 int byo_pagerank_device(byo_graph *g, double eps, uint32_t max_iters, int precision, double *d_p,
                         uint32_t *iters, double *l1);
 
+/* PageRank_edgeMap (benchmarks/PageRank/PageRank.h:80-123): its edgeMap runs
+ * with threshold 0 over the all-vertex frontier, which takes edgeMapDense, so
+ * it computes PageRank's recurrence; this runs the FP64 pull (precision
+ * BYO_PR_FP64 of byo_pagerank) and returns the last iterate. */
+int byo_pagerank_edgemap(byo_graph *g, double eps, uint32_t max_iters, double *h_p, uint32_t *iters,
+                         double *l1);
+
+/* delta::PageRankDelta (benchmarks/PageRank/PageRank.h:340-398), FP64: p0 = 0,
+ * delta0 = 1/n, frontier0 = all vertices; per round every vertex sums
+ * delta/deg of its neighbours in the frontier, the first round adds
+ * 0.85*sum + 0.15/n to p (active when the change beyond 1/n exceeds
+ * local_eps*p), later rounds add 0.85*sum when its magnitude exceeds
+ * local_eps*p (then active); stops when the sum of |delta| < eps or after
+ * max_iters rounds.  *rounds, *l1 may be NULL.  Reference defaults: eps 1e-4
+ * in run_all (run_unweighted.h:920), local_eps 0.01, 20 rounds. */
+int byo_pagerank_delta(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *h_p,
+                       uint32_t *rounds, double *l1);
+int byo_pagerank_delta_device(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *d_p,
+                              uint32_t *rounds, double *l1);
+
 /* Triangle counting, degree ordering
  * (benchmarks/TriangleCounting/ShunTangwongsan15/Triangle.h:167-204). */
 int byo_triangle_count(byo_graph *g, uint64_t *count);

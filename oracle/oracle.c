@@ -489,6 +489,83 @@ void orc_pagerank(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, dou
   free(p_div);
 }
 
+/* ------------------------------------------------------------------ PageRank, delta variant */
+
+void orc_pagerank_delta(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, double eps, double local_eps,
+                        uint32_t max_iters, double *p, uint32_t *rounds_out, double *l1_out) {
+  /* delta::PageRankDelta (PageRank.h:340-398).  nghSum[v] = sum of
+   * delta_over_degree over v's neighbours in the frontier: the dense branch of
+   * sparse_or_dense (PageRank.h:235-267, edgeMapReduce_dense over in-edges)
+   * and the push branch (PR_Delta_F, PageRank.h:207-229) compute the same
+   * sum; the restatement adds left to right over sorted neighbours. */
+  const double damping = 0.85;
+  const double one_over_n = 1 / (double)n;
+  const double added = (1 - damping) * one_over_n;
+  double *delta = xmalloc((n ? n : 1) * sizeof(double));
+  double *dod = xmalloc((n ? n : 1) * sizeof(double));
+  double *ngh = xmalloc((n ? n : 1) * sizeof(double));
+  uint8_t *front = xmalloc(n ? n : 1);
+  uint8_t *next = xmalloc(n ? n : 1);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < (int64_t)n; i++) {
+    p[i] = 0.0;
+    delta[i] = one_over_n;
+    dod[i] = one_over_n / (double)(offsets[i + 1] - offsets[i]); /* inf when deg 0, never read */
+    ngh[i] = 0.0;
+    front[i] = 1;
+  }
+  uint32_t round = 0;
+  double L1 = 0;
+  while (round++ < max_iters) {
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t v = 0; v < (int64_t)n; v++) {
+      double s = 0.0;
+      for (uint64_t j = offsets[v]; j < offsets[v + 1]; j++)
+        if (front[nbrs[j]]) s += dod[nbrs[j]];
+      ngh[v] = s;
+    }
+    /* vertexFilter over all vertices: PR_Vertex_F_FirstRound (:271-290) in the
+     * first round, PR_Vertex_F (:307-323) after */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+      const double deg = (double)(offsets[i + 1] - offsets[i]);
+      if (round == 1) {
+        const double pre_init = damping * ngh[i] + added;
+        p[i] += pre_init;
+        const double nd = pre_init - one_over_n;
+        delta[i] = nd;
+        dod[i] = nd / deg;
+        next[i] = nd > local_eps * p[i];
+      } else {
+        const double nd = ngh[i] * damping;
+        delta[i] = nd;
+        dod[i] = nd / deg;
+        if (fabs(nd) > local_eps * p[i]) {
+          p[i] += nd;
+          next[i] = 1;
+        } else {
+          next[i] = 0;
+        }
+      }
+      ngh[i] = 0.0;
+    }
+    L1 = 0;
+    for (uint64_t i = 0; i < n; i++) L1 += fabs(delta[i]);
+    if (L1 < eps) break;
+    uint8_t *t = front;
+    front = next;
+    next = t;
+  }
+  if (round > max_iters) round = max_iters;
+  if (rounds_out) *rounds_out = round;
+  if (l1_out) *l1_out = L1;
+  free(delta);
+  free(dod);
+  free(ngh);
+  free(front);
+  free(next);
+}
+
 /* ------------------------------------------------------------------ triangles */
 
 uint64_t orc_triangle_count(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs) {

@@ -115,6 +115,16 @@ void orc_bfs_cc(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, uint3
 void orc_pagerank(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, double eps,
                   uint32_t max_iters, double *p_out, uint32_t *iters_out, double *l1_out);
 
+/* PageRank, delta variant (benchmarks/PageRank/PageRank.h:340-398,
+ * delta::PageRankDelta): p0 = 0, delta0 = 1/n, frontier0 = all; each round
+ * nghSum[v] = sum over neighbours u in the frontier of delta[u]/deg(u); first
+ * round p += 0.85 nghSum + 0.15/n and delta = that - 1/n (active when delta >
+ * local_eps p), later rounds delta = 0.85 nghSum, applied (and active) when
+ * |delta| > local_eps p; stop when sum |delta| < eps or after max_iters rounds.
+ * rounds_out / l1_out may be NULL. */
+void orc_pagerank_delta(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, double eps, double local_eps,
+                        uint32_t max_iters, double *p, uint32_t *rounds_out, double *l1_out);
+
 /* Triangle counting, degree ordering (benchmarks/TriangleCounting/
  * ShunTangwongsan15/Triangle.h:57-68,99-150,167-204): rank by (degree, id),
  * orient u->v when rank[u] < rank[v], count |N+(u) cap N+(v)| over DAG edges by

@@ -59,6 +59,8 @@ def lib():
             "orc_bfs_cc": (None, [_c.c_uint64, _u64p, _u32p, _u32p]),
             "orc_pagerank": (None, [_c.c_uint64, _u64p, _u32p, _c.c_double, _c.c_uint32, _f64p,
                                     _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_double)]),
+            "orc_pagerank_delta": (None, [_c.c_uint64, _u64p, _u32p, _c.c_double, _c.c_double, _c.c_uint32,
+                                          _f64p, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_double)]),
             "orc_triangle_count": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p]),
             "orc_store_create": (_c.c_void_p, [_c.c_uint64, _u64p, _u32p]),
             "orc_store_destroy": (None, [_c.c_void_p]),
@@ -175,6 +177,16 @@ def pagerank(offsets, nbrs, eps=1e-6, max_iters=100):
     l1 = ctypes.c_double(0)
     lib().orc_pagerank(n, _u64(offsets), _u32(nbrs), eps, max_iters, p, ctypes.byref(it), ctypes.byref(l1))
     return p, it.value, l1.value
+
+
+def pagerank_delta(offsets, nbrs, eps=1e-6, local_eps=0.01, max_iters=100):
+    n = len(offsets) - 1
+    p = np.empty(n, np.float64)
+    r = ctypes.c_uint32(0)
+    l1 = ctypes.c_double(0)
+    lib().orc_pagerank_delta(n, _u64(offsets), _u32(nbrs), eps, local_eps, max_iters, p, ctypes.byref(r),
+                             ctypes.byref(l1))
+    return p, r.value, l1.value
 
 
 def triangle_count(offsets, nbrs):

@@ -273,3 +273,26 @@ def test_tuning_api_and_autotune(ctx, oracle_mod):
     lev = byo.BFS_multi(G, [10, 11])
     assert np.array_equal(lev[0], olev)
     G.close()
+
+
+@pytest.mark.gpu
+def test_pagerank_delta_and_edgemap(ctx, oracle_mod):
+    """PageRankDelta within 1e-6 L1 of the oracle with the same number of
+    rounds; PageRank_edgeMap equals PageRank's FP64 recurrence."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    graphs = [byo.Graph.generate(ctx, "rmat", seed=21, lg_n=15, draws=1 << 19),
+              byo.Graph.generate(ctx, "er", seed=22, n=20000, draws=80000),
+              byo.Graph.generate(ctx, "grid", n=60, draws=70),
+              byo.Graph.generate(ctx, "rmat", seed=23, lg_n=13, draws=1 << 16, container="pma")]
+    for G in graphs:
+        off, nb = G.export_csr()
+        for eps, leps, iters in ((1e-4, 0.01, 20), (1e-7, 1e-3, 100)):
+            p, r, _ = byo.PageRankDelta(G, eps, leps, iters, info=True)
+            op, orr, _ = O.pagerank_delta(off, nb, eps, leps, iters)
+            assert r == orr, (G.N(), eps)
+            assert float(np.abs(p - op).sum()) <= 1e-6, (G.N(), eps)
+        q, it, _ = byo.PageRank_edgeMap(G, 1e-6, 30, info=True)
+        oq, oit, _ = O.pagerank(off, nb, 1e-6, 30)
+        assert it == oit and float(np.abs(q - oq).sum()) <= 1e-6
+        G.close()

@@ -113,3 +113,58 @@ def test_store_model_random(oracle_mod):
         o2, n2 = st.export_csr()
         got = {(v, int(x)) for v in range(512) for x in n2[o2[v]:o2[v + 1]]}
         assert got == cur
+
+
+def _pagerank_delta_numpy(off, nb, eps, local_eps, max_iters):
+    """A second restatement of delta::PageRankDelta (PageRank.h:340-398) in
+    numpy, to pin the C oracle."""
+    n = len(off) - 1
+    deg = np.diff(off.astype(np.int64)).astype(np.float64)
+    src = np.repeat(np.arange(n), np.diff(off.astype(np.int64)))
+    p = np.zeros(n)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        dod = np.full(n, 1.0 / n) / deg
+    front = np.ones(n, bool)
+    rounds = 0
+    while rounds < max_iters:
+        rounds += 1
+        ngh = np.zeros(n)
+        contrib = np.where(front[nb], dod[nb], 0.0)
+        for v in range(n):  # left to right over sorted neighbours, like the oracle
+            s = 0.0
+            for x in contrib[off[v]:off[v + 1]]:
+                s += x
+            ngh[v] = s
+        if rounds == 1:
+            pre = 0.85 * ngh + (1 - 0.85) * (1 / n)
+            p = p + pre
+            nd = pre - 1.0 / n
+            nxt = nd > local_eps * p
+        else:
+            nd = ngh * 0.85
+            nxt = np.abs(nd) > local_eps * p
+            p = np.where(nxt, p + nd, p)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            dod = nd / deg
+        l1 = 0.0
+        for x in np.abs(nd):
+            l1 += x
+        if l1 < eps:
+            break
+        front = nxt
+    del src
+    return p, rounds
+
+
+@pytest.mark.parametrize("eps,leps", [(1e-4, 0.01), (1e-7, 1e-3)])
+def test_pagerank_delta_restatements_agree(oracle_mod, eps, leps):
+    O = oracle_mod
+    s, d = O.rmat_edges(3, 9, 1 << 12)
+    off, nb = O.build_csr(1 << 9, s, d)
+    p, r, l1 = O.pagerank_delta(off, nb, eps, leps, 50)
+    q, rq = _pagerank_delta_numpy(off, nb, eps, leps, 50)
+    assert r == rq
+    assert np.array_equal(p, q)
+    # it approaches PageRank's fixed point only loosely (round-one decreases
+    # never propagate), but every vertex with edges moved away from 0
+    assert np.all(p > 0)
