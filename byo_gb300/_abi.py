@@ -109,6 +109,9 @@ SIGNATURES = {
     "byo_bfs_device": (_int, [_vp, _u32, _vp, _vp, _int, _P(_u32)]),
     "byo_bfs_multi": (_int, [_vp, _vp, _u32, _vp, _P(_u32)]),
     "byo_bfs_multi_device": (_int, [_vp, _vp, _u32, _vp, _P(_u32)]),
+    "byo_adj_read": (_int, [ctypes.c_char_p, _int, _P(_u64), _P(_u64), _vp, _vp]),
+    "byo_graph_read_adj": (_int, [_vp, ctypes.c_char_p, _int, _int, _P(_vp)]),
+    "byo_graph_write_adj": (_int, [_vp, ctypes.c_char_p, _int]),
     "byo_graph_get_tuning": (_int, [_vp, _P(Tuning)]),
     "byo_graph_set_tuning": (_int, [_vp, _P(Tuning)]),
     "byo_graph_autotune": (_int, [_vp, _u32, _u32, _P(Tuning)]),

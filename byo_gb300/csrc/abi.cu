@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "engine.h"
 #include "internal.h"
@@ -105,6 +106,32 @@ int byo_graph_create_pma(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h
   if (!ctx || !out) return BYO_EINVAL;
   *out = nullptr;
   return graph_from_host_csr(ctx, BYO_CONTAINER_PMA, n, m, h_offsets, h_nbrs, out);
+}
+
+int byo_adj_read(const char *path, int binary, uint64_t *n, uint64_t *m, uint64_t *offsets, uint32_t *nbrs) {
+  if (!path || !n || !m || (offsets && !nbrs && *m)) return BYO_EINVAL;
+  return adj_read_host(nullptr, path, binary, n, m, offsets, nbrs);
+}
+
+int byo_graph_read_adj(byo_ctx *ctx, const char *path, int binary, int container, byo_graph **out) {
+  if (!ctx || !path || !out) return BYO_EINVAL;
+  *out = nullptr;
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+    return set_error(ctx, BYO_EINVAL, "unknown container");
+  uint64_t n = 0, m = 0;
+  BYO_TRY(adj_read_host(ctx, path, binary, &n, &m, nullptr, nullptr));
+  std::vector<uint64_t> off(n + 1);
+  std::vector<uint32_t> nb(m ? m : 1);
+  BYO_TRY(adj_read_host(ctx, path, binary, &n, &m, off.data(), nb.data()));
+  return graph_from_host_csr(ctx, container, n, m, off.data(), nb.data(), out);
+}
+
+int byo_graph_write_adj(byo_graph *g, const char *path, int binary) {
+  if (!g || !path) return BYO_EINVAL;
+  std::vector<uint64_t> off(g->n + 1);
+  std::vector<uint32_t> nb(g->m ? g->m : 1);
+  BYO_TRY(byo_graph_export_csr(g, off.data(), nb.data()));
+  return adj_write_host(g->ctx, path, binary, g->n, g->m, off.data(), nb.data());
 }
 
 int byo_graph_generate(byo_ctx *ctx, int container, const byo_gen_spec *spec, byo_graph **out) {
@@ -518,13 +545,14 @@ int byo_edge_map(byo_graph *g, byo_vertex_subset *vs, byo_functor *f, int64_t th
   bool empty = vs->f.size == 0;
   if (!empty) {
     if ((flags & BYO_FL_DENSE_ONLY) || (vs->f.dense && vs->f.size > g->n / 10)) {
-      mode = MODE_PULL;
+      mode = (flags & BYO_FL_DENSE_FORWARD) ? MODE_DENSE_FWD : MODE_PULL;
     } else if (vs->f.outdeg == 0) {
       empty = true;
     } else {
       const int sparse = (flags & BYO_FL_SPARSE_BLOCKED) ? MODE_BLOCKED : MODE_PUSH;
       mode = m20_mode(g, vs->f, threshold, sparse);
       if (mode == MODE_PULL && (flags & BYO_FL_NO_DENSE)) mode = sparse;
+      if (mode == MODE_PULL && (flags & BYO_FL_DENSE_FORWARD)) mode = MODE_DENSE_FWD;
     }
   }
   if (rc == BYO_OK && !empty) {

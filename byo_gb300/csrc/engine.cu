@@ -96,6 +96,42 @@ __global__ void __launch_bounds__(256) k_push(const uint64_t *__restrict__ off,
   flush_dsum(dsum, st);
 }
 
+// edgeMapDenseForward (edge_map_data.h:180-247): every vertex of a dense
+// frontier pushes to its neighbours; a warp takes a 32-vertex bitmap word and
+// walks the adjacency of each of its set bits with all lanes.
+__global__ void __launch_bounds__(256) k_push_dense_fwd(const uint64_t *__restrict__ off,
+                                                        const uint32_t *__restrict__ slots,
+                                                        const uint32_t *__restrict__ deg,
+                                                        const uint32_t *__restrict__ Fbits, uint64_t n,
+                                                        uint64_t *lp, const uint32_t *__restrict__ visited,
+                                                        uint32_t *out_list, uint32_t *out_bits, RoundStats *st,
+                                                        uint64_t lvl) {
+  const unsigned lane = lane_id();
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t W = (n + 31) / 32;
+  uint64_t dsum = 0;
+  for (uint64_t w = gw; w < W; w += nw) {
+    unsigned word = Fbits[w];
+    while (word) {
+      const uint32_t u = (uint32_t)(w * 32 + __ffs(word) - 1);
+      word &= word - 1;
+      const uint64_t b = off[u], e = off[u + 1];
+      for (uint64_t base = b; base < e; base += 32) {
+        const uint64_t j = base + lane;
+        bool em = false;
+        uint32_t v = kSentinel;
+        if (j < e) {
+          v = slots[j];
+          em = visit(u, v, lvl, lp, visited);
+        }
+        emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+      }
+    }
+  }
+  flush_dsum(dsum, st);
+}
+
 // One CTA per hub vertex (degree >= hub_min).
 __global__ void __launch_bounds__(256) k_push_hubs(const uint64_t *__restrict__ off,
                                                    const uint32_t *__restrict__ slots,
@@ -471,8 +507,15 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
            (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.bits, st.lp,
            st.visited, out.list, out.bits, d_st, lvl, (const uint32_t *)defer, tune.pull_cap, pt);
   } else {
-    if (!in.has_list) return set_error(ctx, BYO_EINVAL, "sparse round needs a frontier list");
-    if (mode == MODE_PUSH) {
+    if (mode == MODE_DENSE_FWD) {
+      BYO_TRY(ensure_bits(g, in));
+      const uint64_t W = (g->n + 31) / 32;
+      launch_t(ctx, "bfs_push", k_push_dense_fwd, dim3(grid_for(ctx, W * 32, 256, 16)), dim3(256), 0,
+               (const uint64_t *)g->d_off, (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg,
+               (const uint32_t *)in.bits, g->n, st.lp, (const uint32_t *)st.visited, out.list, out.bits, d_st, lvl);
+    } else if (!in.has_list) {
+      return set_error(ctx, BYO_EINVAL, "sparse round needs a frontier list");
+    } else if (mode == MODE_PUSH) {
       const int grid = grid_for(ctx, (in.size * (uint64_t)tune.push_group + 255) / 256 * 256, 256, 16);
       switch (tune.push_group) {
 #define PUSH_CASE(GS)                                                                            \
@@ -521,7 +564,7 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
     out.next_mode = (int)h->mode;
     for (int i = 0; i < 16; i++) out.feat[i] = h->feat[i];
   }
-  out.dense = (mode == MODE_PULL);
+  out.dense = (mode == MODE_PULL || mode == MODE_DENSE_FWD);
   out.has_list = true;
   out.has_bits = true;
   st.round++;

@@ -23,7 +23,9 @@
 
 namespace byo {
 
-enum Mode { MODE_PUSH = 0, MODE_PULL = 1, MODE_BLOCKED = 2 };
+// MODE_DENSE_FWD (edgeMapDenseForward) is asked for only through the edgeMap
+// API's flag; the direction policies choose among the first three.
+enum Mode { MODE_PUSH = 0, MODE_PULL = 1, MODE_BLOCKED = 2, MODE_DENSE_FWD = 3 };
 
 struct RoundStats {
   unsigned long long count;   // |next frontier|

@@ -201,6 +201,11 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
 int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint32_t *rounds);
 int pagerank_delta_run(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *d_p,
                        uint32_t *rounds, double *l1);
+// Graph files (graphio.cu).  With offsets == NULL only *n and *m are read.
+int adj_read_host(byo_ctx *ctx, const char *path, int binary, uint64_t *n, uint64_t *m, uint64_t *offsets,
+                  uint32_t *nbrs);
+int adj_write_host(byo_ctx *ctx, const char *path, int binary, uint64_t n, uint64_t m, const uint64_t *offsets,
+                   const uint32_t *nbrs);
 // Launch shapes in effect: g->tune where set, else the defaults for g.
 byo_tuning effective_tuning(const byo_graph *g);
 int check_tuning(byo_ctx *ctx, const byo_tuning *t);

@@ -17,6 +17,7 @@ Errors surface as ByoError carrying the library's status code.
 """
 import atexit
 import ctypes
+import os
 import weakref
 
 import numpy as np
@@ -217,13 +218,18 @@ class Graph:
         check(lib().byo_graph_export_csr(self.h, _ptr(off), _ptr(nb)), self.ctx.h)
         return off, nb[:self.M()]
 
-    def write_adj(self, path):
-        """AdjacencyGraph text of the current contents (graph.h:3018-3044)."""
-        off, nb = self.export_csr()
-        with open(path, "w") as f:
-            f.write("AdjacencyGraph\n%d\n%d\n" % (self.N(), self.M()))
-            f.write("".join("%d\n" % x for x in off[:-1]))
-            f.write("".join("%d\n" % x for x in nb))
+    def write_adj(self, path, binary=False):
+        """The sorted adjacency as an AdjacencyGraph text file (graph.h:3018-3044)
+        or the binary CSR layout."""
+        check(lib().byo_graph_write_adj(self.h, os.fsencode(path), int(binary)), self.ctx.h)
+
+    @classmethod
+    def read_adj(cls, ctx, path, binary=False, container="csr"):
+        """read_unweighted_symmetric_graph (graph_io.h:98-124) into a container."""
+        h = ctypes.c_void_p()
+        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        check(lib().byo_graph_read_adj(ctx.h, os.fsencode(path), int(binary), cont, ctypes.byref(h)), ctx.h)
+        return cls(ctx, h)
 
     @staticmethod
     def _keys(batch):
@@ -365,6 +371,17 @@ def PageRank(G, eps=1e-6, max_iters=100, precision=_abi.PR_FP32_KAHAN, info=Fals
     check(lib().byo_pagerank(G.h, eps, max_iters, precision, _ptr(p), ctypes.byref(it),
                              ctypes.byref(l1)), G.ctx.h)
     return (p, it.value, l1.value) if info else p
+
+
+def read_adj_host(path, binary=False):
+    """Parses a graph file on the host (no device): (offsets, nbrs)."""
+    n, m = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    p = os.fsencode(path)
+    check(lib().byo_adj_read(p, int(binary), ctypes.byref(n), ctypes.byref(m), None, None))
+    off = np.empty(n.value + 1, np.uint64)
+    nb = np.empty(max(m.value, 1), np.uint32)
+    check(lib().byo_adj_read(p, int(binary), ctypes.byref(n), ctypes.byref(m), _ptr(off), _ptr(nb)))
+    return off, nb[:m.value]
 
 
 def PageRank_edgeMap(G, eps=1e-6, max_iters=100, info=False):

@@ -109,6 +109,25 @@ int byo_graph_insert_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t
 int byo_graph_remove_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted,
                                   uint64_t *changed);
 
+/* ------------------------------------------------------------------ graph files
+ * The reference's input formats (gbbs/graph_io.cc:35-95, read by
+ * read_unweighted_symmetric_graph, gbbs/graph_io.h:98-124):
+ *   text    "AdjacencyGraph", n, m, n offsets, m neighbour ids (whitespace
+ *           separated); binary = 0
+ *   binary  int64 n, int64 m, int64 file size, uint64 offsets[n+1],
+ *           uint32 ids[m] (the layout of the reference's -DLONG build);
+ *           binary = 1
+ * byo_adj_read parses on the host without a device: call it with offsets =
+ * nbrs = NULL for *n and *m, then with arrays of n+1 and m entries.  Offsets
+ * must run from 0 to m without decreasing and ids must be below n (BYO_EINVAL
+ * otherwise).  byo_graph_read_adj loads a file into a new container (which
+ * also requires each adjacency sorted, as the loaders do);
+ * byo_graph_write_adj writes the sorted adjacency in either format (text =
+ * Graph::write_adj, gbbs/graph.h:3018-3044). */
+int byo_adj_read(const char *path, int binary, uint64_t *n, uint64_t *m, uint64_t *offsets, uint32_t *nbrs);
+int byo_graph_read_adj(byo_ctx *ctx, const char *path, int binary, int container, byo_graph **out);
+int byo_graph_write_adj(byo_graph *g, const char *path, int binary);
+
 /* ------------------------------------------------------------------ generators
  * Synthetic graphs built on the device (counter-based streams; a slice of any
  * stream is reproducible on the host bit for bit).  Pairs are symmetrised,

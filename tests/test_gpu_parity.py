@@ -127,7 +127,8 @@ def test_edge_map_api_matches_bfs(ctx, oracle_mod):
     G = byo.Graph.generate(ctx, "rmat", seed=11, lg_n=13, draws=1 << 16)
     off, nb = G.export_csr()
     for flags in (byo._abi.FL_DENSE_PARALLEL | byo._abi.FL_SPARSE_BLOCKED, byo._abi.FL_NO_DENSE,
-                  byo._abi.FL_DENSE_ONLY):
+                  byo._abi.FL_DENSE_ONLY, byo._abi.FL_DENSE_FORWARD,
+                  byo._abi.FL_DENSE_ONLY | byo._abi.FL_DENSE_FORWARD):
         F = byo.BFS_F(G, 10)
         frontier = byo.vertexSubset(G, 10)
         sizes = []
@@ -296,3 +297,22 @@ def test_pagerank_delta_and_edgemap(ctx, oracle_mod):
         oq, oit, _ = O.pagerank(off, nb, 1e-6, 30)
         assert it == oit and float(np.abs(q - oq).sum()) <= 1e-6
         G.close()
+
+
+@pytest.mark.gpu
+def test_graph_files_round_trip(ctx, oracle_mod, tmp_path):
+    """write_adj then read_adj, both layouts, into both containers."""
+    import byo_gb300 as byo
+    G = byo.Graph.generate(ctx, "rmat", seed=17, lg_n=12, draws=1 << 15, container="pma")
+    G.insert_batch(np.array([(1 << 32) | 2, (2 << 32) | 1], np.uint64))
+    off, nb = G.export_csr()
+    for binary in (False, True):
+        p = str(tmp_path / ("g.bin" if binary else "g.adj"))
+        G.write_adj(p, binary)
+        for cont in ("csr", "pma"):
+            H = byo.Graph.read_adj(ctx, p, binary, container=cont)
+            o2, n2 = H.export_csr()
+            assert np.array_equal(o2, off) and np.array_equal(n2, nb)
+            assert np.array_equal(byo.BFS(H, 1), oracle_mod.bfs(off, nb, 1)[0])
+            H.close()
+    G.close()
