@@ -628,7 +628,11 @@ int byo_update_sample(byo_graph *g, const uint64_t *h_keys, uint64_t count, floa
   const int saved = ctx->update_policy;
   float t[4] = {0, 0, 0, 0};
   uint64_t m0 = g->m, slots0 = g->nslots;
-  int rc = BYO_OK;
+  // an untimed merge pair first sizes every update buffer for this batch, so
+  // no allocation falls inside a timed update
+  ctx->update_policy = BYO_UPDATE_MERGE;
+  int rc = update_common(g, h_keys, count, 0, 1, 1, nullptr);
+  if (rc == BYO_OK) rc = update_common(g, h_keys, count, 0, 0, 1, nullptr);
   for (int k = 0; k < 4 && rc == BYO_OK; k++) {
     const int insert = (k % 2) == 0;
     ctx->update_policy = k < 2 ? BYO_UPDATE_MERGE : BYO_UPDATE_REBUILD;

@@ -290,6 +290,8 @@ __global__ void __launch_bounds__(256) k_pull_long(const uint64_t *__restrict__ 
                                                    uint32_t *out_list, uint32_t *out_bits,
                                                    RoundStats *st, uint64_t lvl,
                                                    const uint32_t *__restrict__ defer, int cap, PolicyTail pt) {
+  __shared__ float4 sP[kParamChunks];
+  policy_prefetch(pt, sP);
   const uint64_t nd = *(volatile unsigned long long *)&st->ndefer;
   const unsigned lane = lane_id();
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
@@ -320,19 +322,21 @@ __global__ void __launch_bounds__(256) k_pull_long(const uint64_t *__restrict__ 
       atomicAdd(&st->hist[log4_bin(d)], 1ull);
     }
   }
-  policy_tail(pt, st);
+  policy_tail(pt, st, sP);
 }
 
 // ---------------------------------------------------------------- bookkeeping
 __global__ void k_mark_visited(const uint32_t *__restrict__ list, RoundStats *st, uint32_t *visited,
                                PolicyTail pt) {
+  __shared__ float4 sP[kParamChunks];
+  policy_prefetch(pt, sP);
   const uint64_t cnt = st->count;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
        i += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t v = list[i];
     atomicOr(visited + (v >> 5), 1u << (v & 31));
   }
-  policy_tail(pt, st);
+  policy_tail(pt, st, sP);
 }
 
 __global__ void k_clear_words_from_list(const uint32_t *__restrict__ list, uint64_t cnt,
@@ -503,6 +507,7 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
     launch_t(ctx, "bfs_pull", k_pull, dim3(grid), dim3(block), (size_t)smem, (const uint64_t *)g->d_off,
            (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.bits, g->n,
            st.lp, st.visited, out.list, out.bits, d_st, lvl, defer, tune.pull_cap, stage);
+    pt.prefetch = 1;
     launch(ctx, k_pull_long, dim3(ctx->num_sms * 4), dim3(256), 0, (const uint64_t *)g->d_off,
            (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const uint32_t *)in.bits, st.lp,
            st.visited, out.list, out.bits, d_st, lvl, (const uint32_t *)defer, tune.pull_cap, pt);
@@ -549,8 +554,9 @@ int edge_map_round(byo_graph *g, TravState &st, Frontier &in, Frontier &out, int
              in.size, (const uint64_t *)pre, st.lp, (const uint32_t *)st.visited, out.list, out.bits,
              d_st, lvl, tune.blocked_tile);
     }
-    launch(ctx, k_mark_visited, dim3(grid_for(ctx, in.outdeg + 1, 256)), dim3(256), 0,
-           (const uint32_t *)out.list, d_st, st.visited, pt);
+    const int mgrid = grid_for(ctx, in.outdeg + 1, 256);
+    pt.prefetch = mgrid >= ctx->num_sms;
+    launch(ctx, k_mark_visited, dim3(mgrid), dim3(256), 0, (const uint32_t *)out.list, d_st, st.visited, pt);
   }
   BYO_TRY(check_launch(ctx, "edge_map_round"));
   RoundStats *h = nullptr;

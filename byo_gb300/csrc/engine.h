@@ -83,7 +83,7 @@ EngineTuning default_tuning(const byo_graph *g);
 struct PolicyTail {
   const float *P = nullptr;
   float n = 0, m = 0, reached_before = 0;
-  int dense = 0, has_net = 0, on = 0, log = 0;
+  int dense = 0, has_net = 0, on = 0, log = 0, prefetch = 0;
   unsigned int *done = nullptr;  // blocks finished; the last one resets it
 };
 // Fills pt for a round reading a frontier of the given kind (mlp.cu).

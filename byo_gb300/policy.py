@@ -135,17 +135,20 @@ def loss_grad(ctx, params, X, Y, M):
 
 JUDGE_MARGIN = 0.006  # the engine's kJudgeMargin (a predicted gain of about 7%)
 GATE_FACTOR = 64      # the engine's kGateFactor
+GATE_HUB_BIN = 5      # the engine's kGateHubBin (degree >= 4^5)
 
 
 def round_choices(ctx, params, X, fallback):
     """The engine's decision rule applied to predictions: argmin over the
     three directions unless the rule's choice is within the judge margin, and
-    the rule alone for frontiers far below its threshold (feature 14 is
-    (|F| + outdeg) / (m/20))."""
+    the rule alone for frontiers far below its threshold without a hub
+    (feature 14 is (|F| + outdeg) / (m/20), features 6..13 the degree
+    histogram by powers of 4)."""
     P = forward(ctx, params, X)[:, :3]
     best = P.argmin(1)
     keep = P[np.arange(len(P)), fallback] - P[np.arange(len(P)), best] <= JUDGE_MARGIN
-    keep |= X[:, 14] * GATE_FACTOR <= 1.0
+    hub = (X[:, 6 + GATE_HUB_BIN:14] > 0).any(1)
+    keep |= (X[:, 14] * GATE_FACTOR <= 1.0) & ~hub
     return np.where(keep, fallback, best)
 
 
