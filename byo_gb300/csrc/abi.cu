@@ -145,6 +145,11 @@ int byo_graph_generate(byo_ctx *ctx, int container, const byo_gen_spec *spec, by
 void byo_graph_destroy(byo_graph *g) {
   if (!g) return;
   if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+  if (g->snap) {
+    g->snap->d_deg = nullptr;  // the container's, freed below
+    byo_graph_destroy(g->snap);
+    g->snap = nullptr;
+  }
   for (auto &b : g->ws) free_buf(b);
   if (g->pma) pma_destroy(g->pma);
   else if (g->d_slots) cudaFree(g->d_slots);
@@ -277,7 +282,9 @@ int byo_bfs_device(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_l
                    uint32_t *rounds) {
   if (!g) return BYO_EINVAL;
   BYO_TRY(need(g->ctx, policy >= 0 && policy <= BYO_POLICY_M20_BLOCKED, "unknown policy"));
-  return bfs_run(g, src, d_parent, d_level, policy, rounds);
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  return bfs_run(t, src, d_parent, d_level, policy, rounds);
 }
 
 int byo_bfs(byo_graph *g, uint32_t src, uint32_t *h_parent, uint32_t *h_level, int policy,
@@ -295,14 +302,18 @@ int byo_bfs(byo_graph *g, uint32_t src, uint32_t *h_parent, uint32_t *h_level, i
 
 int byo_bfs_multi_device(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint32_t *rounds) {
   if (!g || !h_srcs || !d_levels) return BYO_EINVAL;
-  return bfs_multi_run(g, h_srcs, k, d_levels, rounds);
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  return bfs_multi_run(t, h_srcs, k, d_levels, rounds);
 }
 
 int byo_bfs_multi(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *h_levels, uint32_t *rounds) {
   if (!g || !h_srcs || !h_levels) return BYO_EINVAL;
   uint32_t *d = nullptr;
   BYO_TRY(ws(g, WS_TC_NBR, (uint64_t)k * g->n + 1, &d));
-  BYO_TRY(bfs_multi_run(g, h_srcs, k, d, rounds));
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  BYO_TRY(bfs_multi_run(t, h_srcs, k, d, rounds));
   return copy_to_host(g->ctx, h_levels, d, (uint64_t)k * g->n * 4);
 }
 
@@ -329,14 +340,18 @@ int byo_graph_autotune(byo_graph *g, uint32_t what, uint32_t trials, byo_tuning 
 
 int byo_cc_device(byo_graph *g, uint32_t *d_label) {
   if (!g || !d_label) return BYO_EINVAL;
-  return cc_run(g, d_label);
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  return cc_run(t, d_label);
 }
 
 int byo_cc(byo_graph *g, uint32_t *h_label) {
   if (!g || !h_label) return BYO_EINVAL;
   uint32_t *d = nullptr;
   BYO_TRY(ws(g, WS_PR_A, g->n + 1, &d));
-  BYO_TRY(cc_run(g, d));
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  BYO_TRY(cc_run(t, d));
   return copy_to_host(g->ctx, h_label, d, g->n * 4);
 }
 
@@ -344,14 +359,18 @@ int byo_bfs_cc(byo_graph *g, uint32_t *h_label) {
   if (!g || !h_label) return BYO_EINVAL;
   uint32_t *d = nullptr;
   BYO_TRY(ws(g, WS_PR_B, g->n + 1, &d));
-  BYO_TRY(bfs_cc_run(g, d));
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  BYO_TRY(bfs_cc_run(t, d));
   return copy_to_host(g->ctx, h_label, d, g->n * 4);
 }
 
 int byo_pagerank_device(byo_graph *g, double eps, uint32_t max_iters, int precision, double *d_p,
                         uint32_t *iters, double *l1) {
   if (!g || !d_p) return BYO_EINVAL;
-  return pagerank_run(g, eps, max_iters, precision, d_p, iters, l1);
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  return pagerank_run(t, eps, max_iters, precision, d_p, iters, l1);
 }
 
 int byo_pagerank_edgemap(byo_graph *g, double eps, uint32_t max_iters, double *h_p, uint32_t *iters,
@@ -362,7 +381,9 @@ int byo_pagerank_edgemap(byo_graph *g, double eps, uint32_t max_iters, double *h
 int byo_pagerank_delta_device(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *d_p,
                               uint32_t *rounds, double *l1) {
   if (!g || !d_p) return BYO_EINVAL;
-  return pagerank_delta_run(g, eps, local_eps, max_iters, d_p, rounds, l1);
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  return pagerank_delta_run(t, eps, local_eps, max_iters, d_p, rounds, l1);
 }
 
 int byo_pagerank_delta(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *h_p,
@@ -370,7 +391,9 @@ int byo_pagerank_delta(byo_graph *g, double eps, double local_eps, uint32_t max_
   if (!g || !h_p) return BYO_EINVAL;
   double *d = nullptr;
   BYO_TRY(ws(g, WS_TC_CNT, 2 * g->n + 2, (uint32_t **)&d));
-  BYO_TRY(pagerank_delta_run(g, eps, local_eps, max_iters, d, rounds, l1));
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  BYO_TRY(pagerank_delta_run(t, eps, local_eps, max_iters, d, rounds, l1));
   return copy_to_host(g->ctx, h_p, d, g->n * 8);
 }
 
@@ -379,13 +402,17 @@ int byo_pagerank(byo_graph *g, double eps, uint32_t max_iters, int precision, do
   if (!g || !h_p) return BYO_EINVAL;
   double *d = nullptr;
   BYO_TRY(ws(g, WS_TC_CNT, 2 * g->n + 2, (uint32_t **)&d));
-  BYO_TRY(pagerank_run(g, eps, max_iters, precision, d, iters, l1));
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  BYO_TRY(pagerank_run(t, eps, max_iters, precision, d, iters, l1));
   return copy_to_host(g->ctx, h_p, d, g->n * 8);
 }
 
 int byo_triangle_count(byo_graph *g, uint64_t *count) {
   if (!g || !count) return BYO_EINVAL;
-  return tc_run(g, count);
+  byo_graph *t = nullptr;
+  BYO_TRY(traversal_view(g, &t));
+  return tc_run(t, count);
 }
 
 // ---------------------------------------------------------------- edgeMap API

@@ -61,6 +61,8 @@ int autotune(byo_graph *g, uint32_t what, uint32_t trials) {
 
   // score of the current g->tune for one kernel family, in ms
   auto score = [&](bool multi, int policy, float *ms) -> int {
+    byo_graph *tg = nullptr;
+    BYO_TRY(traversal_view(g, &tg));  // carries g->tune
     float total = 0;
     const uint32_t runs = multi ? std::max<uint32_t>(1, trials / 2) : trials;
     for (uint32_t i = 0; i < runs; i++) {
@@ -69,9 +71,9 @@ int autotune(byo_graph *g, uint32_t what, uint32_t trials) {
         // rotate the 64-source set so each run starts from different sources
         std::vector<uint32_t> q(kq);
         for (uint32_t s = 0; s < kq; s++) q[s] = srcs[(s + i * 7) % srcs.size()];
-        BYO_TRY(bfs_multi_run(g, q.data(), kq, d_levels, nullptr));
+        BYO_TRY(bfs_multi_run(tg, q.data(), kq, d_levels, nullptr));
       } else {
-        BYO_TRY(bfs_run(g, srcs[i % srcs.size()], d_parent, nullptr, policy, nullptr));
+        BYO_TRY(bfs_run(tg, srcs[i % srcs.size()], d_parent, nullptr, policy, nullptr));
       }
       BYO_CU(ctx, cudaEventRecord(t.b, ctx->stream));
       BYO_CU(ctx, cudaEventSynchronize(t.b));

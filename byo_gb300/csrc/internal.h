@@ -68,6 +68,12 @@ struct byo_graph {
   byo::Pma *pma = nullptr;
   byo::DevBuf ws[24];  // per-graph workspaces, indexed by the Ws enum
   byo_tuning tune = {};  // launch shapes set by the caller or the autotuner (0 = automatic)
+  // A PMA keeps a compact CSR snapshot of its contents for the read-only
+  // algorithms, rebuilt on first use after an update (version counts updates).
+  uint64_t version = 0;
+  byo_graph *snap = nullptr;
+  uint64_t snap_version = 0;
+  uint64_t slots_cap = 0;  // snapshot: capacity of d_slots
 };
 
 namespace byo {
@@ -201,6 +207,12 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
 int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint32_t *rounds);
 int pagerank_delta_run(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *d_p,
                        uint32_t *rounds, double *l1);
+// The graph the read-only algorithms traverse: g itself for a CSR, the
+// compact snapshot of a PMA's contents (rebuilt if stale) otherwise.
+int traversal_view(byo_graph *g, byo_graph **out);
+// Copies the PMA's keys, leaf by leaf, into a compact neighbour array
+// (sorted adjacency in CSR order).
+int pma_compact(byo_graph *g, uint32_t *d_slots_out);
 // Graph files (graphio.cu).  With offsets == NULL only *n and *m are read.
 int adj_read_host(byo_ctx *ctx, const char *path, int binary, uint64_t *n, uint64_t *m, uint64_t *offsets,
                   uint32_t *nbrs);

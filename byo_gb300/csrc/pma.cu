@@ -732,6 +732,19 @@ __global__ void k_pma_view_leaves(const uint32_t *__restrict__ src, const uint32
   }
 }
 
+// One warp per leaf: its cnt keys (packed at the leaf's start) go to
+// out[epre[leaf] ...].
+__global__ void k_pma_compact(const uint32_t *__restrict__ dst, const uint32_t *__restrict__ cnt,
+                              const uint64_t *__restrict__ epre, uint64_t NL, uint32_t *out) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t i = gw; i < NL; i += nw) {
+    const uint32_t c = cnt[i];
+    const uint64_t o = epre[i];
+    for (uint32_t e = lane_id(); e < c; e += 32) out[o + e] = __ldcs(dst + i * kLeaf + e);
+  }
+}
+
 // ---------------------------------------------------------------- host side
 
 static int pma_alloc(byo_ctx *ctx, uint64_t NL, uint32_t **src, uint32_t **dst, uint32_t **cnt, uint64_t **sep) {
@@ -861,11 +874,63 @@ static int pma_rebuild(byo_graph *g, const uint64_t *keys, const uint64_t *bstar
   return pma_layout(g, stg, total, leaves_for(total));
 }
 
+int pma_compact(byo_graph *g, uint32_t *out) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  BYO_TRY(ensure(ctx, p->epre, (p->NL + 1) * 8));
+  uint64_t *epre = (uint64_t *)p->epre.p;
+  BYO_TRY(scan_u32_to_u64(ctx, p->cnt, p->NL, epre));
+  launch(ctx, k_pma_compact, dim3(grid_for(ctx, p->NL * 32, 256, 16)), dim3(256), 0, (const uint32_t *)p->dst,
+         (const uint32_t *)p->cnt, (const uint64_t *)epre, p->NL, out);
+  return check_launch(ctx, "pma_compact");
+}
+
+int traversal_view(byo_graph *g, byo_graph **out) {
+  *out = g;
+  if (g->container != BYO_CONTAINER_PMA || !g->pma) return BYO_OK;
+  byo_ctx *ctx = g->ctx;
+  byo_graph *s = g->snap;
+  if (!s) {
+    s = new byo_graph();
+    s->ctx = ctx;
+    s->container = BYO_CONTAINER_CSR;
+    g->snap = s;
+  }
+  s->tune = g->tune;
+  if (s->d_off && s->n == g->n && g->snap_version == g->version) {
+    *out = s;
+    return BYO_OK;
+  }
+  if (!s->d_off || s->n != g->n) {
+    if (s->d_off) cudaFree(s->d_off);
+    s->d_off = nullptr;
+    BYO_CU(ctx, cudaMalloc(&s->d_off, (g->n + 1) * 8));
+  }
+  if (!s->d_slots || s->slots_cap < g->m + 16) {
+    if (s->d_slots) cudaFree(s->d_slots);
+    s->d_slots = nullptr;
+    s->slots_cap = 0;
+    const uint64_t cap = g->m + g->m / 16 + 16;  // room for a few batches of growth
+    BYO_CU(ctx, cudaMalloc(&s->d_slots, cap * 4));
+    s->slots_cap = cap;
+  }
+  s->n = g->n;
+  s->m = g->m;
+  s->nslots = g->m;
+  s->d_deg = g->d_deg;
+  BYO_TRY(scan_u32_to_u64(ctx, g->d_deg, g->n, s->d_off));
+  BYO_TRY(pma_compact(g, s->d_slots));
+  g->snap_version = g->version;
+  *out = s;
+  return BYO_OK;
+}
+
 int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sorted, int insert,
                uint64_t *changed) {
   byo_ctx *ctx = g->ctx;
   Pma *p = g->pma;
   if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PMA container");
+  g->version++;  // any snapshot of the contents is stale from here on
   const uint64_t m_before = g->m;
   // 1. validate, copy, sort, unique
   BYO_TRY(ensure(ctx, p->keys_a, count * 8));
