@@ -97,6 +97,7 @@ int autotune(byo_graph *g, uint32_t what, uint32_t trials) {
     fields.push_back({&byo_tuning::hub_min, {1024, 4096, 16384}, false, BYO_POLICY_M20});
     fields.push_back({&byo_tuning::pull_cap, {8, 16, 32, 64, 128}, false, BYO_POLICY_M20});
     fields.push_back({&byo_tuning::blocked_tile, {512, 2048, 8192}, false, BYO_POLICY_M20_BLOCKED});
+    fields.push_back({&byo_tuning::pull_stage_words, {8192, 16384, 32768}, false, BYO_POLICY_M20});
   }
   if (what & BYO_TUNE_MULTI) {
     fields.push_back({&byo_tuning::ms_heavy_deg, {8, 16, 32, 64, 128, 256}, true, 0});

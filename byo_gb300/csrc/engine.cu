@@ -17,20 +17,42 @@ __device__ __forceinline__ int log4_bin(uint32_t d) {
   return b > 7 ? 7 : b;
 }
 
+// The degree sketch of the next frontier is counted per block in shared
+// memory (a warp adds one count per bin it holds) and added to the round's
+// statistics once per block, so no global counter sees one atomic per vertex.
+__device__ __forceinline__ void hist_init(unsigned long long *sh) {
+  if (threadIdx.x < 8) sh[threadIdx.x] = 0;
+  __syncthreads();
+}
+__device__ __forceinline__ void hist_warp_add(unsigned long long *sh, bool has, uint32_t d) {
+  if (!__ballot_sync(kFull, has)) return;
+  const int bin = log4_bin(d);
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    const unsigned m = __ballot_sync(kFull, has && bin == b);
+    if (m && lane_id() == 0) atomicAdd(sh + b, (unsigned long long)__popc(m));
+  }
+}
+__device__ __forceinline__ void hist_flush(unsigned long long *sh, RoundStats *st) {
+  __syncthreads();
+  if (threadIdx.x < 8 && sh[threadIdx.x]) atomicAdd(&st->hist[threadIdx.x], sh[threadIdx.x]);
+}
+
 // Emits v (if `emit`) to the next frontier list and bitmap; accumulates its
 // degree for the round statistics.  Warp-collective.
 __device__ __forceinline__ void emit_next(bool emit, uint32_t v, uint32_t *out_list,
                                           uint32_t *out_bits, RoundStats *st,
                                           const uint32_t *__restrict__ deg, uint64_t &dsum,
-                                          bool set_bits) {
+                                          bool set_bits, unsigned long long *sh) {
   uint64_t slot = warp_append(emit, &st->count);
+  uint32_t d = 0;
   if (emit) {
     out_list[slot] = v;
     if (set_bits) atomicOr(out_bits + (v >> 5), 1u << (v & 31));
-    uint32_t d = deg[v];
+    d = deg[v];
     dsum += d;
-    atomicAdd(&st->hist[log4_bin(d)], 1ull);
   }
+  hist_warp_add(sh, emit, d);
 }
 
 __device__ __forceinline__ void flush_dsum(uint64_t dsum, RoundStats *st) {
@@ -58,6 +80,8 @@ __global__ void __launch_bounds__(256) k_push(const uint64_t *__restrict__ off,
                                               uint32_t *out_list, uint32_t *out_bits,
                                               RoundStats *st, uint64_t lvl, uint32_t *hubs,
                                               uint32_t hub_min) {
+  __shared__ unsigned long long s_hist[8];
+  hist_init(s_hist);
   constexpr int PER_WARP = 32 / GS;
   const unsigned lane = lane_id(), g = lane / GS, gl = lane % GS;
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
@@ -90,9 +114,10 @@ __global__ void __launch_bounds__(256) k_push(const uint64_t *__restrict__ off,
         v = slots[j];
         em = visit(u, v, lvl, lp, visited);
       }
-      emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+      emit_next(em, v, out_list, out_bits, st, deg, dsum, true, s_hist);
     }
   }
+  hist_flush(s_hist, st);
   flush_dsum(dsum, st);
 }
 
@@ -106,6 +131,8 @@ __global__ void __launch_bounds__(256) k_push_dense_fwd(const uint64_t *__restri
                                                         uint64_t *lp, const uint32_t *__restrict__ visited,
                                                         uint32_t *out_list, uint32_t *out_bits, RoundStats *st,
                                                         uint64_t lvl) {
+  __shared__ unsigned long long s_hist[8];
+  hist_init(s_hist);
   const unsigned lane = lane_id();
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -125,10 +152,11 @@ __global__ void __launch_bounds__(256) k_push_dense_fwd(const uint64_t *__restri
           v = slots[j];
           em = visit(u, v, lvl, lp, visited);
         }
-        emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+        emit_next(em, v, out_list, out_bits, st, deg, dsum, true, s_hist);
       }
     }
   }
+  hist_flush(s_hist, st);
   flush_dsum(dsum, st);
 }
 
@@ -140,6 +168,8 @@ __global__ void __launch_bounds__(256) k_push_hubs(const uint64_t *__restrict__ 
                                                    uint64_t *lp, const uint32_t *__restrict__ visited,
                                                    uint32_t *out_list, uint32_t *out_bits,
                                                    RoundStats *st, uint64_t lvl) {
+  __shared__ unsigned long long s_hist[8];
+  hist_init(s_hist);
   const uint64_t nh = *(volatile unsigned long long *)&st->ndefer;
   uint64_t dsum = 0;
   for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
@@ -153,9 +183,10 @@ __global__ void __launch_bounds__(256) k_push_hubs(const uint64_t *__restrict__ 
         v = slots[j];
         em = visit(u, v, lvl, lp, visited);
       }
-      emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+      emit_next(em, v, out_list, out_bits, st, deg, dsum, true, s_hist);
     }
   }
+  hist_flush(s_hist, st);
   flush_dsum(dsum, st);
 }
 
@@ -172,6 +203,8 @@ __global__ void __launch_bounds__(256) k_push_blocked(const uint64_t *__restrict
                                                       const uint32_t *__restrict__ visited,
                                                       uint32_t *out_list, uint32_t *out_bits,
                                                       RoundStats *st, uint64_t lvl, int tile) {
+  __shared__ unsigned long long s_hist[8];
+  hist_init(s_hist);
   const uint64_t total = pre[fsize];
   const uint64_t ntiles = (total + tile - 1) / tile;
   __shared__ uint64_t s_lo, s_hi;
@@ -210,10 +243,11 @@ __global__ void __launch_bounds__(256) k_push_blocked(const uint64_t *__restrict
         v = slots[off[u] + (e - pre[lo])];
         em = visit(u, v, lvl, lp, visited);
       }
-      emit_next(em, v, out_list, out_bits, st, deg, dsum, true);
+      emit_next(em, v, out_list, out_bits, st, deg, dsum, true, s_hist);
     }
     __syncthreads();
   }
+  hist_flush(s_hist, st);
   flush_dsum(dsum, st);
 }
 
@@ -234,7 +268,9 @@ __global__ void __launch_bounds__(1024) k_pull(const uint64_t *__restrict__ off,
                                                RoundStats *st, uint64_t lvl, uint32_t *defer,
                                                int cap, int stage_words) {
   extern __shared__ uint32_t s_bits[];
+  __shared__ unsigned long long s_hist[8];
   for (int i = threadIdx.x; i < stage_words; i += blockDim.x) s_bits[i] = Fbits[i];
+  if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
   __syncthreads();
   const uint64_t W = (n + 31) >> 5;
   const unsigned lane = lane_id();
@@ -251,14 +287,21 @@ __global__ void __launch_bounds__(1024) k_pull(const uint64_t *__restrict__ off,
     if (active) {
       const uint64_t b = off[v], e = off[v + 1];
       const uint64_t lim = (e - b > (uint64_t)cap) ? b + cap : e;
-      for (uint64_t j = b; j < lim; j++) {
-        uint32_t u = slots[j];
-        if (u == kSentinel) continue;
-        if (in_frontier(s_bits, stage_words, Fbits, u)) {
-          found = true;
-          parent = u;
-          break;
-        }
+      // eight neighbours at a time: their ids, then their frontier bits, are
+      // loaded together; the first hit in slot order is the parent
+      for (uint64_t j0 = b; j0 < lim && !found; j0 += 8) {
+        uint32_t u[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) u[q] = j0 + q < lim ? slots[j0 + q] : kSentinel;
+        bool h[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) h[q] = u[q] != kSentinel && in_frontier(s_bits, stage_words, Fbits, u[q]);
+#pragma unroll
+        for (int q = 7; q >= 0; q--)
+          if (h[q]) {
+            found = true;
+            parent = u[q];
+          }
       }
       deferred = !found && lim < e;
     }
@@ -269,15 +312,17 @@ __global__ void __launch_bounds__(1024) k_pull(const uint64_t *__restrict__ off,
       visited[w] = vword | fb;
     }
     uint64_t slot = warp_append(found, &st->count);
+    uint32_t d = 0;
     if (found) {
       out_list[slot] = (uint32_t)v;
-      uint32_t d = deg[v];
+      d = deg[v];
       dsum += d;
-      atomicAdd(&st->hist[log4_bin(d)], 1ull);
     }
+    hist_warp_add(s_hist, found, d);
     uint64_t ds = warp_append(deferred, &st->ndefer);
     if (deferred) defer[ds] = (uint32_t)v;
   }
+  hist_flush(s_hist, st);
   flush_dsum(dsum, st);
 }
 
@@ -291,7 +336,9 @@ __global__ void __launch_bounds__(256) k_pull_long(const uint64_t *__restrict__ 
                                                    RoundStats *st, uint64_t lvl,
                                                    const uint32_t *__restrict__ defer, int cap, PolicyTail pt) {
   __shared__ float4 sP[kParamChunks];
+  __shared__ unsigned long long s_hist[8];
   policy_prefetch(pt, sP);
+  hist_init(s_hist);
   const uint64_t nd = *(volatile unsigned long long *)&st->ndefer;
   const unsigned lane = lane_id();
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
@@ -311,17 +358,19 @@ __global__ void __launch_bounds__(256) k_pull_long(const uint64_t *__restrict__ 
         parent = __shfl_sync(kFull, u, __ffs(m) - 1);
       }
     }
+    uint32_t d = 0;
     if (found && lane == 0) {
       lp[v] = lvl | parent;
       atomicOr(out_bits + (v >> 5), 1u << (v & 31));
       atomicOr(visited + (v >> 5), 1u << (v & 31));
       unsigned long long slot = atomicAdd(&st->count, 1ull);
       out_list[slot] = v;
-      uint32_t d = deg[v];
+      d = deg[v];
       atomicAdd(&st->outdeg, (unsigned long long)d);
-      atomicAdd(&st->hist[log4_bin(d)], 1ull);
     }
+    hist_warp_add(s_hist, found && lane == 0, d);
   }
+  hist_flush(s_hist, st);
   policy_tail(pt, st, sP);
 }
 
@@ -385,7 +434,10 @@ byo_tuning effective_tuning(const byo_graph *g) {
   if (!t.ms_heavy_deg) t.ms_heavy_deg = 32;
   if (!t.ms_hub_deg) t.ms_hub_deg = 2048;
   if (!t.ms_push_div) t.ms_push_div = 20;
-  t.reserved = 0;
+  if (!t.pull_stage_words) {
+    const uint64_t W = (g->n + 31) / 32;
+    t.pull_stage_words = (uint32_t)(W < 16384 ? (W < 256 ? 256 : W) : 16384);
+  }
   return t;
 }
 
@@ -403,16 +455,16 @@ int check_tuning(byo_ctx *ctx, const byo_tuning *t) {
     bad = "ms_heavy_deg must be <= 65536";
   else if (t->ms_hub_deg && (t->ms_hub_deg < 32 || t->ms_hub_deg > (1u << 20)))
     bad = "ms_hub_deg must be in [32, 2^20]";
-  else if (t->reserved)
-    bad = "reserved field must be zero";
+  else if (t->pull_stage_words && (t->pull_stage_words < 256 || t->pull_stage_words > 49152))
+    bad = "pull_stage_words must be in [256, 49152]";
   return bad ? set_error(ctx, BYO_EINVAL, bad) : BYO_OK;
 }
 
 EngineTuning default_tuning(const byo_graph *g) {
   EngineTuning t;
   const uint64_t W = (g->n + 31) / 32;
-  t.pull_stage_words = (int)(W < 32768 ? W : 32768);
   const byo_tuning e = effective_tuning(g);
+  t.pull_stage_words = (int)(W < e.pull_stage_words ? W : e.pull_stage_words);
   t.push_group = (int)e.push_group;
   t.hub_min = e.hub_min;
   t.pull_cap = (int)e.pull_cap;

@@ -201,7 +201,8 @@ typedef struct byo_tuning {
   uint32_t ms_hub_deg;   /* 64-source push: frontier vertices above this many slots are cut into
                             chunks of this size, a warp each (32..2^20) */
   uint32_t ms_push_div;  /* 64-source: push while the frontier's slots < all slots / ms_push_div */
-  uint32_t reserved;     /* zero */
+  uint32_t pull_stage_words; /* single-source pull: frontier bitmap words staged in shared memory
+                                (256..49152; fewer words let two CTAs share an SM) */
 } byo_tuning;
 int byo_graph_get_tuning(byo_graph *g, byo_tuning *out);
 int byo_graph_set_tuning(byo_graph *g, const byo_tuning *t);
