@@ -2,6 +2,7 @@
 // See engine.h for the design.  Algorithmic bytes of one BFS traversal:
 // 4 B per adjacency entry of every reached vertex + 8 B offsets per vertex
 // + 8 B lp written per reached vertex (parent/level split is 8 B more).
+#include <algorithm>
 #include <cstring>
 
 #include "device.cuh"
@@ -12,8 +13,12 @@
 
 namespace byo {
 
-__device__ __forceinline__ int log4_bin(uint32_t d) {
+__host__ __device__ __forceinline__ int log4_bin(uint32_t d) {
+#ifdef __CUDA_ARCH__
   int b = d ? (31 - __clz(d)) / 2 : 0;  // 0:[0,4) 1:[4,16) ...
+#else
+  int b = d ? (31 - __builtin_clz(d)) / 2 : 0;
+#endif
   return b > 7 ? 7 : b;
 }
 
@@ -656,6 +661,7 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   fa.size = 1;
   fa.outdeg = dsrc;
+  fa.hist[log4_bin(dsrc)] = 1;
   fa.has_list = fa.has_bits = true;
   fb.size = 0;
   fb.has_list = true;  // empty list: its bitmap is all zero
@@ -682,6 +688,14 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
   }
   Frontier *cur = &fa, *nxt = &fb;
   uint32_t nr = 0;
+  // small push rounds run back to back in one persistent kernel (not while
+  // rounds are timed one by one for the policy's training samples)
+  const bool small_ok = !ctx->time_rounds &&
+                        (policy == BYO_POLICY_M20 || policy == BYO_POLICY_LEARNED || policy == BYO_POLICY_PUSH);
+  const uint64_t small_limit = std::max<uint64_t>(4096, g->m / 20 / 64);
+  // a frontier holding a vertex of degree >= 4^5 goes to the round kernels,
+  // which give such vertices whole CTAs (and which the learned policy inspects)
+  const bool gate_hub = true;
   while (cur->size > 0) {
     int mode;
     switch (policy) {
@@ -695,6 +709,27 @@ int bfs_run(byo_graph *g, uint32_t src, uint32_t *d_parent, uint32_t *d_level, i
     if (mode != MODE_PULL && cur->outdeg == 0) break;  // edge_map_data.h:290
     // next's bitmap still holds the frontier before `cur`: clear it
     BYO_TRY(clear_frontier_bits(g, *nxt));
+    bool hub = false;
+    for (int q = 5; q < 8; q++) hub |= cur->hist[q] != 0;
+    if (small_ok && mode == MODE_PUSH && cur->has_list && cur->size + cur->outdeg <= small_limit &&
+        !(gate_hub && hub)) {
+      RoundStats *d_st = nullptr;
+      BYO_TRY(ws(g, WS_STATS, sizeof(RoundStats) / sizeof(uint64_t) + 2, (uint64_t **)&d_st));
+      uint32_t R = 0;
+      BYO_TRY(bfs_small_rounds(g, st, cur, nxt, small_limit, gate_hub, run_policy ? d_st : nullptr, &R));
+      nr += R;
+      if (run_policy && cur->size > 0) {
+        // the policy for the frontier the kernel stopped at
+        RoundStats *h = nullptr;
+        BYO_TRY(round_policy(g, d_st, st.reached - cur->size, false));
+        BYO_TRY(pinned(ctx, 4096, (void **)&h));
+        BYO_CU(ctx, cudaMemcpyAsync(h, d_st, sizeof(RoundStats), cudaMemcpyDeviceToHost, ctx->stream));
+        BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+        cur->next_mode = (int)h->mode;
+        for (int i = 0; i < 16; i++) cur->feat[i] = h->feat[i];
+      }
+      continue;
+    }
     byo_round_log lg{};
     lg.round = st.round;
     lg.mode = (uint32_t)mode;

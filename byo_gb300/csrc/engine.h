@@ -77,6 +77,13 @@ int ensure_bits(byo_graph *g, Frontier &f);
 int trav_init(byo_graph *g, TravState &st, uint32_t src);
 int trav_extract(byo_graph *g, const TravState &st, uint32_t *d_parent, uint32_t *d_level);
 EngineTuning default_tuning(const byo_graph *g);
+// Runs push rounds from *cur in one persistent kernel while the frontier
+// stays within `limit` edges (and, with gate_hub, holds no vertex of degree
+// >= 4^5); on return *cur is the frontier reached and *nxt a clean buffer
+// (bfs_small.cu).  With d_st, the final frontier's statistics are written
+// there for the policy.
+int bfs_small_rounds(byo_graph *g, TravState &st, Frontier *&cur, Frontier *&nxt, uint64_t limit, bool gate_hub,
+                     RoundStats *d_st, uint32_t *rounds_run);
 
 // Arguments of the policy epilogue fused into a round's last kernel
 // (policy.cuh); on == 0 disables it.

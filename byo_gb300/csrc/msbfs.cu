@@ -34,12 +34,12 @@
 #include <vector>
 
 #include "device.cuh"
+#include "gridsync.cuh"
 #include "internal.h"
 
 namespace byo {
 
 constexpr int kMsBlock = 256;
-constexpr uint64_t kBarrierNs = 4000000000ull;  // 4 s
 constexpr int kMsLog = 64;                       // rounds recorded for byo_last_rounds
 
 struct MsCtl {
@@ -51,7 +51,8 @@ struct MsCtl {
   unsigned long long cc[2];    // hub chunks of L_r, by round parity
   unsigned long long tc[2];    // touched vertices of a push round, by parity
   unsigned long long nheavy, nmega, nmc;
-  unsigned int count, gen, err, rounds, pushes, pad;
+  GridBar bar;
+  unsigned int rounds, pushes;
   unsigned long long t0;               // globaltimer after the set-up phase
   unsigned long long rlog[kMsLog][4];  // per round: end time, push?, |F|, slots of F
 };
@@ -73,12 +74,6 @@ struct MsArgs {
   uint32_t max_rounds, heavy_deg, hub_deg, push_div;
 };
 
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
 __device__ __forceinline__ uint64_t vload(const unsigned long long *p) {
   return *(const volatile unsigned long long *)p;
 }
@@ -93,38 +88,6 @@ __device__ __forceinline__ uint64_t warp_or64(uint64_t x) {
   const unsigned lo = __reduce_or_sync(kFull, (unsigned)x);
   const unsigned hi = __reduce_or_sync(kFull, (unsigned)(x >> 32));
   return (uint64_t)hi << 32 | lo;
-}
-
-// Counting barrier across all blocks of a cooperative launch.  Returns false
-// (and sets c->err) when the other blocks did not arrive within kBarrierNs or
-// another block already gave up.
-__device__ __forceinline__ bool grid_sync(MsCtl *c, unsigned int nblocks) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ok = 1;
-    volatile unsigned int *gen = &c->gen;
-    const unsigned int g = *gen;
-    __threadfence();
-    if (atomicAdd(&c->count, 1u) == nblocks - 1) {
-      c->count = 0;
-      __threadfence();
-      atomicAdd(&c->gen, 1u);
-    } else {
-      const uint64_t t0 = globaltimer_ns();
-      while (*gen == g) {
-        if (*(volatile unsigned int *)&c->err || globaltimer_ns() - t0 > kBarrierNs) {
-          atomicOr(&c->err, 1u);
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return ok != 0;
 }
 
 // Writes the levels of the lanes' newly reached (source, vertex) pairs: one
@@ -155,7 +118,7 @@ __device__ __forceinline__ void ms_list(const MsArgs &a, int slot, int par, bool
       if (cb + nch <= a.ccap)
         for (uint64_t t = 0; t < nch; t++) a.C[par][cb + t] = (uint64_t)v << 32 | t;
       else
-        atomicOr(&c->err, 2u);
+        atomicOr(&c->bar.err, 2u);
     }
   }
 }
@@ -243,11 +206,11 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
         if (cb + nch <= a.ccap)
           for (uint64_t t = 0; t < nch; t++) a.MC[cb + t] = v << 32 | t;
         else
-          atomicOr(&c->err, 2u);
+          atomicOr(&c->bar.err, 2u);
       }
     }
   }
-  if (!grid_sync(c, nb)) return;
+  if (!grid_sync(&c->bar, nb)) return;
   // the seeds form L_0 (sources may repeat)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     for (uint32_t s = 0; s < a.k; s++) {
@@ -271,7 +234,7 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
     c->lvalid[0] = 1;
     c->lvalid[2] = 1;  // an empty list: round 1 has nothing to clear
   }
-  if (!grid_sync(c, nb)) return;
+  if (!grid_sync(&c->bar, nb)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) c->t0 = globaltimer_ns();
   const uint64_t nheavy = vload(&c->nheavy), nmega = vload(&c->nmega), nmc = vload(&c->nmc);
 
@@ -295,7 +258,7 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
           const bool has = v < n && ldm(F, v) != 0;
           ms_list(a, prv, ppar, has, (uint32_t)v, has ? a.off[v + 1] - a.off[v] : 0);
         }
-        if (!grid_sync(c, nb)) return;
+        if (!grid_sync(&c->bar, nb)) return;
       }
       // phase 1: free N of round r-2's entries; scatter L_{r-1} into X
       if (vload(&c->lvalid[old])) {
@@ -317,7 +280,7 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
         const uint64_t b = a.off[u] + (uint64_t)(uint32_t)e * a.hub_deg;
         ms_push_range(a, ldm(F, u), b, min(b + a.hub_deg, a.off[u + 1]), par, !dense);
       }
-      if (!grid_sync(c, nb)) return;
+      if (!grid_sync(&c->bar, nb)) return;
       // phase 2: the touched vertices become the next frontier
       if (blockIdx.x == 0 && threadIdx.x == 0) {
         c->cnt[old] = c->ldeg[old] = c->lc[old] = c->hc[old] = c->lvalid[old] = 0;
@@ -463,7 +426,7 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
         if (lane == 0 && (got & ~ldm(a.X, v))) atomicOr((unsigned long long *)a.X + v, (unsigned long long)got);
       }
       if (nmega) {
-        if (!grid_sync(c, nb)) return;
+        if (!grid_sync(&c->bar, nb)) return;
         for (uint64_t base = warp * 32; base < nmega; base += nwarps * 32) {
           const uint64_t i = base + lane;
           uint32_t v = 0;
@@ -484,7 +447,7 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
       }
       ms_count(c, cur, my_cnt, my_deg);
     }
-    if (!grid_sync(c, nb)) return;
+    if (!grid_sync(&c->bar, nb)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0 && r <= kMsLog) {
       c->rlog[r - 1][0] = globaltimer_ns();
       c->rlog[r - 1][1] = push;
@@ -571,8 +534,8 @@ int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_
   BYO_TRY(pinned(ctx, sizeof(MsCtl), (void **)&h));
   BYO_CU(ctx, cudaMemcpyAsync(h, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  if (h->err & 2u) return set_error(ctx, BYO_EDEVICE, "bfs_multi: hub chunk list overflow");
-  if (h->err) return set_error(ctx, BYO_ETIMEDOUT, "bfs_multi: grid barrier timed out");
+  if (h->bar.err & 2u) return set_error(ctx, BYO_EDEVICE, "bfs_multi: hub chunk list overflow");
+  if (h->bar.err) return set_error(ctx, BYO_ETIMEDOUT, "bfs_multi: grid barrier timed out");
   if (rounds) *rounds = h->rounds;
   ctx->rounds.clear();
   uint64_t prev = h->t0;
