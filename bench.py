@@ -101,6 +101,26 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ------------------------------------------------------------------ replicas
+def max_over_ranks(x, world):
+    """The largest of every rank's x (each rank is an independent replica;
+    the job's time is its slowest rank's).  nccl reduces on the device,
+    gloo on the host."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, world, ms_max):
+    """Whole-job rate: every rank's units over the slowest rank's time (G/s)."""
+    return world * units_per_rank / (ms_max / 1e3) / 1e9
+
+
 # ------------------------------------------------------------------ NVTX
 def nvtx_push(torch, name):
     """Marks the timed region (ncu --nvtx --nvtx-include "timed/" captures it alone)."""
@@ -260,11 +280,9 @@ def run_ours(args, rank, world, local_rank):
     clk = clocks.stop()
     elapsed_ms = t_start.elapsed_time(t_end)
     launches = ctx.launches - launches0
+    elapsed_ms = max_over_ranks(elapsed_ms, world)
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
         dist.barrier()
 
     # per-kernel shares over the timed region
@@ -297,7 +315,7 @@ def run_ours(args, rank, world, local_rank):
     roof["kernel_ms_share"] = {t: round(ktimes[t][1] / max(elapsed_ms, 1e-9), 4) for t in tags if ktimes[t][0]}
 
     step_ms = elapsed_ms / args.steps
-    value = world * total_units / (step_ms / 1e3) / 1e9
+    value = replica_value(total_units, world, step_ms)
     comp = comp_ms / args.steps
     components = {
         "bfs_gteps": units["bfs"] / (comp[1] / 1e3) / 1e9,
@@ -393,11 +411,7 @@ def run_e2e(args, byo, G, ctx, torch, dynamic, keys, B, n, policy, total_units, 
         step()
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([dt], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
+    dt = max_over_ranks(dt, world)
     return {"value": world * total_units / dt / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": (2 * 8 * B) if dynamic else 0,
             "d2h_bytes_per_step": 4 * n + 4 * n + 8 * n, "ms_per_step": dt * 1e3}
@@ -523,11 +537,7 @@ def run_mixed(args, rank, world, local_rank):
     elapsed_ms = e0.elapsed_time(e1)
     ms_launches, ms_kernel = ctx.kernel_time("bfs_multi")
     ctx.kernel_timing(None)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, world)
     step_ms = elapsed_ms / args.steps
     qlat = np.array([x for (op, x) in lat if op[0] == "Q"]) * 1e3
     ulat = {}
