@@ -313,8 +313,9 @@ int byo_ctx_set_round_timing(byo_ctx *ctx, int on);
 /* Brackets every launch of the kernels tagged `tag` ("*": all tags, NULL: off)
  * with CUDA events on the context's stream; byo_ctx_kernel_time sums the
  * launches of one tag (NULL: all) since the last byo_ctx_kernel_timing call.
- * Tags: "bfs_push", "bfs_pull", "bfs_blocked", "cc_finish", "pr_pull",
- * "tc_intersect", "sort_scatter", "pma_merge", "pma_redistribute". */
+ * Tags: "bfs_push", "bfs_pull", "bfs_blocked", "bfs_multi", "cc_finish",
+ * "pr_pull", "pr_delta", "tc_intersect", "sort_scatter", "pma_merge",
+ * "pma_redistribute". */
 int byo_ctx_kernel_timing(byo_ctx *ctx, const char *tag);
 int byo_ctx_kernel_time(byo_ctx *ctx, const char *tag, uint64_t *launches, double *ms);
 
