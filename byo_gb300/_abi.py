@@ -59,10 +59,11 @@ TUNE_MULTI = 2
 
 class Tuning(ctypes.Structure):
     _fields_ = [("push_group", _u32), ("hub_min", _u32), ("pull_cap", _u32), ("blocked_tile", _u32),
-                ("ms_heavy_deg", _u32), ("ms_hub_deg", _u32), ("ms_push_div", _u32), ("pull_stage_words", _u32)]
+                ("ms_heavy_deg", _u32), ("ms_hub_deg", _u32), ("ms_push_div", _u32), ("pull_stage_words", _u32),
+                ("tc_stage", _u32), ("reserved", _u32)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
 class GenSpec(ctypes.Structure):

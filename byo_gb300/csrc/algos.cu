@@ -746,41 +746,122 @@ __global__ void k_tc_fill(const uint64_t *__restrict__ off, const uint32_t *__re
   }
 }
 
-// Lane groups per DAG vertex u; for each v in N+(u), the group counts
-// |N+(u) cap N+(v)| by binary-searching the elements of the shorter list in
-// the longer one.
-template <int GS>
-__global__ void __launch_bounds__(256) k_tc_intersect(const uint64_t *__restrict__ doff,
-                                                      const uint32_t *__restrict__ dn, uint64_t n,
-                                                      unsigned long long *total) {
-  __shared__ unsigned long long sm[9];
-  const unsigned gl = threadIdx.x % GS;
-  const uint64_t gid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / GS;
-  const uint64_t ng = ((uint64_t)gridDim.x * blockDim.x) / GS;
-  unsigned long long cnt = 0;
-  for (uint64_t u = gid; u < n; u += ng) {
-    const uint64_t ab = doff[u], ae = doff[u + 1];
-    for (uint64_t k = ab; k < ae; k++) {
-      const uint32_t v = dn[k];
-      const uint64_t bb = doff[v], be = doff[v + 1];
-      // shorter list S is scanned, longer L searched
-      uint64_t sb = ab, se = ae, lb = bb, le = be;
-      if (be - bb < ae - ab) {
-        sb = bb; se = be; lb = ab; le = ae;
-      }
-      for (uint64_t j = sb + gl; j < se; j += GS) {
-        const uint32_t x = dn[j];
-        uint64_t lo = lb, hi = le;
-        while (lo < hi) {
-          uint64_t mid = (lo + hi) >> 1;
-          if (dn[mid] < x) lo = mid + 1; else hi = mid;
-        }
-        cnt += (lo < le && dn[lo] == x);
-      }
-    }
+// Wedge counting over the DAG.  For a vertex u, A = N+(u) is staged in
+// shared memory; every w of N+(v) for v in A is looked up in A by binary
+// search, and each hit is one triangle (u, v, w) with rank(u) < rank(v) <
+// rank(w), so every triangle counts once (Triangle.h:99-150 counts the same
+// |N+(u) cap N+(v)| per DAG edge).  A warp enumerates the wedges of 32 v's at
+// a time flattened by a warp scan over their out-degrees, so lanes stay busy
+// whatever the degrees.
+constexpr uint32_t kTcWarpCap = 512;  // N+(u) a warp stages (2 KB per warp)
+
+__device__ __forceinline__ bool tc_member(const uint32_t *A, uint32_t na, uint32_t x) {
+  uint32_t lo = 0, hi = na;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (A[mid] < x) lo = mid + 1; else hi = mid;
   }
-  cnt = block_sum(cnt, sm);
-  if (threadIdx.x == 0 && cnt) atomicAdd(total, cnt);
+  return lo < na && A[lo] == x;
+}
+
+// Wedges of the v's at positions c, c + stride, ... (chunks of 32) of A.
+// Warp-collective; pre/bas are this warp's 32-entry scratch.
+__device__ __forceinline__ uint64_t tc_wedges(const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dn,
+                                              const uint32_t *A, uint32_t na, uint32_t c0, uint32_t stride,
+                                              uint32_t *pre, uint64_t *bas) {
+  const unsigned lane = lane_id();
+  uint64_t cnt = 0;
+  for (uint32_t c = c0; c < na; c += stride) {
+    const uint32_t i = c + lane;
+    uint32_t d = 0;
+    uint64_t b = 0;
+    if (i < na) {
+      const uint32_t v = A[i];
+      b = doff[v];
+      d = (uint32_t)(doff[v + 1] - b);
+    }
+    const uint32_t incl = warp_inclusive_scan(d);
+    pre[lane] = incl;
+    bas[lane] = b;
+    __syncwarp();
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    for (uint32_t t = lane; t < total; t += 32) {
+      uint32_t lo = 0, hi = 31;  // first lane whose inclusive prefix exceeds t
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (pre[mid] <= t) lo = mid + 1; else hi = mid;
+      }
+      const uint32_t start = lo ? pre[lo - 1] : 0;
+      const uint32_t w = dn[bas[lo] + (t - start)];
+      cnt += tc_member(A, na, w);
+    }
+    __syncwarp();
+  }
+  return cnt;
+}
+
+// A warp per vertex with 2 <= |N+(u)| <= kTcWarpCap.
+__global__ void __launch_bounds__(256) k_tc_warp(const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dn,
+                                                 uint64_t n, unsigned long long *total) {
+  __shared__ uint32_t As[8][kTcWarpCap];
+  __shared__ uint32_t pre[8][32];
+  __shared__ uint64_t bas[8][32];
+  __shared__ unsigned long long sm[9];
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint64_t cnt = 0;
+  for (uint64_t u = gw; u < n; u += nw) {
+    const uint64_t ab = doff[u];
+    const uint32_t na = (uint32_t)(doff[u + 1] - ab);
+    if (na < 2 || na > kTcWarpCap) continue;
+    for (uint32_t i = lane; i < na; i += 32) As[w][i] = dn[ab + i];
+    __syncwarp();
+    cnt += tc_wedges(doff, dn, As[w], na, 0, 32, pre[w], bas[w]);
+    __syncwarp();
+  }
+  const unsigned long long tot = block_sum((unsigned long long)cnt, sm);
+  if (threadIdx.x == 0 && tot) atomicAdd(total, tot);
+}
+
+// A CTA per vertex with |N+(u)| > kTcWarpCap (listed in big[]); N+(u) is
+// staged in dynamic shared memory when it fits `stage` entries, else read in
+// place.  The CTA's warps take interleaved chunks of 32 v's.
+__global__ void __launch_bounds__(256) k_tc_block(const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dn,
+                                                  const uint32_t *__restrict__ big, const unsigned long long *nbig,
+                                                  uint32_t stage, unsigned long long *total) {
+  extern __shared__ uint32_t Ablk[];
+  __shared__ uint32_t pre[8][32];
+  __shared__ uint64_t bas[8][32];
+  __shared__ unsigned long long sm[9];
+  const unsigned w = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  const uint64_t nb = *nbig;
+  uint64_t cnt = 0;
+  for (uint64_t k = blockIdx.x; k < nb; k += gridDim.x) {
+    const uint32_t u = big[k];
+    const uint64_t ab = doff[u];
+    const uint32_t na = (uint32_t)(doff[u + 1] - ab);
+    const uint32_t *A = dn + ab;
+    if (na <= stage) {
+      for (uint32_t i = threadIdx.x; i < na; i += blockDim.x) Ablk[i] = dn[ab + i];
+      A = Ablk;
+    }
+    __syncthreads();
+    cnt += tc_wedges(doff, dn, A, na, w * 32, nwb * 32, pre[w], bas[w]);
+    __syncthreads();
+  }
+  const unsigned long long tot = block_sum((unsigned long long)cnt, sm);
+  if (threadIdx.x == 0 && tot) atomicAdd(total, tot);
+}
+
+__global__ void k_tc_big(const uint64_t *__restrict__ doff, uint64_t n, uint32_t *big, unsigned long long *nbig) {
+  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+       base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t u = base + lane_id();
+    const bool b = u < n && doff[u + 1] - doff[u] > kTcWarpCap;
+    const uint64_t at = warp_append(b, nbig);
+    if (b) big[at] = (uint32_t)u;
+  }
 }
 
 int tc_run(byo_graph *g, uint64_t *count) {
@@ -817,9 +898,21 @@ int tc_run(byo_graph *g, uint64_t *count) {
          (const uint32_t *)g->d_slots, (const uint32_t *)rank, n, (const uint64_t *)doff, dn);
   unsigned long long *d_total = nullptr;
   BYO_TRY(ws(g, WS_MISC, 4, (uint32_t **)&d_total));
-  BYO_CU(ctx, cudaMemsetAsync(d_total, 0, 8, ctx->stream));
-  launch_t(ctx, "tc_intersect", k_tc_intersect<8>, dim3(grid_for(ctx, n * 8, 256, 16)), dim3(256), 0, (const uint64_t *)doff,
-         (const uint32_t *)dn, n, d_total);
+  BYO_CU(ctx, cudaMemsetAsync(d_total, 0, 16, ctx->stream));  // total, big count
+  uint32_t *big = dcnt;  // reuse: the counts are in doff now
+  launch(ctx, k_tc_big, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint64_t *)doff, n, big, d_total + 1);
+  launch_t(ctx, "tc_intersect", k_tc_warp, dim3(grid_for(ctx, n * 32, 256, 8)), dim3(256), 0,
+           (const uint64_t *)doff, (const uint32_t *)dn, n, d_total);
+  const byo_tuning tn = effective_tuning(g);
+  const uint32_t stage = tn.tc_stage;
+  static int configured = 0;
+  const int smem = (int)(stage * 4);
+  if (smem > 48 * 1024 && configured < smem) {
+    BYO_CU(ctx, cudaFuncSetAttribute(k_tc_block, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    configured = smem;
+  }
+  launch_t(ctx, "tc_intersect", k_tc_block, dim3(ctx->num_sms), dim3(256), (size_t)smem, (const uint64_t *)doff,
+           (const uint32_t *)dn, (const uint32_t *)big, (const unsigned long long *)(d_total + 1), stage, d_total);
   BYO_CU(ctx, cudaMemcpyAsync(h, d_total, 8, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   *count = h[0];

@@ -439,6 +439,8 @@ byo_tuning effective_tuning(const byo_graph *g) {
   if (!t.ms_heavy_deg) t.ms_heavy_deg = 32;
   if (!t.ms_hub_deg) t.ms_hub_deg = 2048;
   if (!t.ms_push_div) t.ms_push_div = 20;
+  if (!t.tc_stage) t.tc_stage = 40960;
+  t.reserved = 0;
   if (!t.pull_stage_words) {
     const uint64_t W = (g->n + 31) / 32;
     t.pull_stage_words = (uint32_t)(W < 16384 ? (W < 256 ? 256 : W) : 16384);
@@ -462,6 +464,10 @@ int check_tuning(byo_ctx *ctx, const byo_tuning *t) {
     bad = "ms_hub_deg must be in [32, 2^20]";
   else if (t->pull_stage_words && (t->pull_stage_words < 256 || t->pull_stage_words > 49152))
     bad = "pull_stage_words must be in [256, 49152]";
+  else if (t->tc_stage && (t->tc_stage < 512 || t->tc_stage > 49152))
+    bad = "tc_stage must be in [512, 49152]";
+  else if (t->reserved)
+    bad = "reserved field must be zero";
   return bad ? set_error(ctx, BYO_EINVAL, bad) : BYO_OK;
 }
 

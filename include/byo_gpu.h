@@ -203,6 +203,9 @@ typedef struct byo_tuning {
   uint32_t ms_push_div;  /* 64-source: push while the frontier's slots < all slots / ms_push_div */
   uint32_t pull_stage_words; /* single-source pull: frontier bitmap words staged in shared memory
                                 (256..49152; fewer words let two CTAs share an SM) */
+  uint32_t tc_stage;     /* triangle counting: DAG out-lists up to this many entries are staged in
+                            a CTA's shared memory, longer ones are searched in place (512..49152) */
+  uint32_t reserved;     /* zero */
 } byo_tuning;
 int byo_graph_get_tuning(byo_graph *g, byo_tuning *out);
 int byo_graph_set_tuning(byo_graph *g, const byo_tuning *t);

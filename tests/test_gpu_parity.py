@@ -316,3 +316,25 @@ def test_graph_files_round_trip(ctx, oracle_mod, tmp_path):
             assert np.array_equal(byo.BFS(H, 1), oracle_mod.bfs(off, nb, 1)[0])
             H.close()
     G.close()
+
+
+@pytest.mark.gpu
+def test_triangle_count_paths(ctx, oracle_mod):
+    """Warp-staged, CTA-staged and in-place out-lists give the oracle's count:
+    a 700-clique (DAG out-lists up to 699) over an RMAT background."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    s, d = O.rmat_edges(29, 12, 1 << 15)
+    k = np.arange(700, dtype=np.int64) * 5 + 3
+    cs, cd = np.meshgrid(k, k, indexing="ij")
+    mask = cs < cd
+    src = np.concatenate([s.astype(np.int64), cs[mask]])
+    dst = np.concatenate([d.astype(np.int64), cd[mask]])
+    off, nb = O.build_csr(1 << 12, src.astype(np.uint32), dst.astype(np.uint32))
+    want = O.triangle_count(off, nb)
+    for cont in ("csr", "pma"):
+        G = byo.Graph.from_csr(ctx, off, nb, container=cont)
+        for stage in (0, 512):
+            G.set_tuning(tc_stage=stage)
+            assert byo.Triangle_degree_ordering(G) == want, (cont, stage)
+        G.close()
