@@ -338,13 +338,14 @@ struct InLightLen {
   }
 };
 
-// tile starts: v == 0, v heavy, v-1 heavy, or the light prefix crossed a
-// multiple of kPrTile between v-1 and v
+// tile starts: v == 0, v heavy, v-1 heavy, the light prefix crossed a
+// multiple of kPrTile between v-1 and v, or v is a multiple of kPrTile (so a
+// tile never holds more than kPrTile vertices, however many have no edges)
 struct InTileStart {
   const uint64_t *off;
   const uint64_t *pre;
   __device__ uint64_t operator()(uint64_t v) const {
-    if (v == 0) return 1;
+    if (v == 0 || v % kPrTile == 0) return 1;
     bool heavy = off[v + 1] - off[v] > kPrLightMax;
     bool prev_heavy = off[v] - off[v - 1] > kPrLightMax;
     return (heavy || prev_heavy || (pre[v] / kPrTile) != (pre[v - 1] / kPrTile)) ? 1 : 0;
