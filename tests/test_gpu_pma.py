@@ -158,3 +158,31 @@ def test_small_batch_fast_path(ctx, oracle_mod, lg, draws, sizes):
     assert G.remove_batch(keys) == st.remove_batch(keys)
     ro, rn = st.export_csr()
     _check_view(byo, O, G, ro, rn, (hub,))
+
+
+def test_large_batches(ctx, oracle_mod):
+    """Batches of more than 2^20 keys: a uniform one, and one where a few
+    sources get more than 512 keys each (their buckets go to the LSD
+    fallback of the batch sort)."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 20
+    n = 1 << lg
+    G = byo.Graph.generate(ctx, "rmat", seed=7, lg_n=lg, draws=1 << 22, container="pma")
+    s, d = O.rmat_edges(7, lg, 1 << 22)
+    off, nb = O.build_csr(n, s, d)
+    st = O.Store(off, nb)
+    us, ud = O.uniform_pairs(300, n, 700000)
+    keys = O.keys_from_pairs(us, ud)
+    assert G.insert_batch(keys) == st.insert_batch(keys)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (10,))
+    rng = np.random.default_rng(3)
+    hubs = np.array([5, 99, 12345], np.uint64)
+    extra = np.concatenate([(h << np.uint64(32)) | rng.choice(n, 900, replace=False).astype(np.uint64) for h in hubs])
+    skew = np.concatenate([O.keys_from_pairs(us[:600000], ud[:600000]), extra,
+                           ((extra & np.uint64(0xFFFFFFFF)) << np.uint64(32)) | (extra >> np.uint64(32))])
+    assert G.remove_batch(skew) == st.remove_batch(skew)
+    assert G.insert_batch(skew) == st.insert_batch(skew)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (5,))
