@@ -591,6 +591,32 @@ __global__ void k_pr_init(const uint32_t *__restrict__ deg, uint64_t n, T *p_cur
   }
 }
 
+// State of the graph-driven iteration loop (device side).
+struct PrLoop {
+  double l1;
+  uint32_t iters;
+  int32_t last;  // -1: no iteration ran; 0: the last iterate is in pb; 1: in pa
+};
+
+// After an iteration: records its L1 norm, clears the accumulators, and
+// tells the loop whether another iteration runs (PageRank.h:176-190: stop
+// when L1 < eps or after max_iters).  half 0 ends the first iteration of a
+// loop body (pa -> pb) and sets both conditions; half 1 ends the second
+// (pb -> pa) and sets the loop's.
+__global__ void k_pr_check(double *d_l1, double eps, uint32_t max_iters, PrLoop *st, int half,
+                           cudaGraphConditionalHandle h_if, cudaGraphConditionalHandle h_while) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint32_t it = ++st->iters;
+  const double L = d_l1[0];
+  st->l1 = L;
+  st->last = half;
+  d_l1[0] = 0.0;
+  d_l1[1] = 0.0;
+  const unsigned cont = (!(L < eps) && it < max_iters) ? 1u : 0u;
+  if (half == 0) cudaGraphSetConditional(h_if, cont);
+  cudaGraphSetConditional(h_while, cont);
+}
+
 template <typename T>
 __global__ void k_to_f64(const T *__restrict__ in, uint64_t n, double *out) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
@@ -607,7 +633,7 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   BYO_TRY(ws(g, WS_PR_A, n + 2, &pa));
   BYO_TRY(ws(g, WS_PR_B, n, &pb));
   BYO_TRY(ws(g, WS_PR_C, n, &da));
-  BYO_TRY(ws(g, WS_PR_D, n, &db));
+  BYO_TRY(ws(g, WS_PR_D, n + 2 + (sizeof(PrLoop) + sizeof(T) - 1) / sizeof(T) + 2, &db));  // p_div, loop state
   // plan
   uint64_t *pre = nullptr;
   uint32_t *lists = nullptr;
@@ -653,32 +679,131 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   const T added = (T)((1 - 0.85) * (1 / (double)n));
   const int grid_c = grid_for(ctx, nheavy * 32, 256, 8);
   const int grid_u = grid_for(ctx, nunits * 32, kPrBlock, sizeof(T) == 4 ? 5 : 3);
+  // The iterations run as one CUDA graph: a WHILE node whose body holds two
+  // iterations (pa -> pb, then under an IF node pb -> pa), each ending in
+  // k_pr_check, which sets the conditions from the L1 norm on the device.
+  // No host round trip happens between iterations.
+  PrLoop *loop = reinterpret_cast<PrLoop *>((reinterpret_cast<uintptr_t>(db + n + 2) + 7) & ~(uintptr_t)7);
+  BYO_CU(ctx, cudaMemsetAsync(d_l1, 0, 16, ctx->stream));
+  {
+    PrLoop z{0.0, 0u, -1};
+    BYO_CU(ctx, cudaMemcpyAsync(loop, &z, sizeof(PrLoop), cudaMemcpyHostToDevice, ctx->stream));
+  }
   uint32_t it = 0;
   double L1 = 0.0;
-  T *p_curr = pa, *p_next = pb, *pdiv = da, *pdiv_next = db, *last = nullptr;
-  double *hl = (double *)h;
-  while (it++ < max_iters) {
-    BYO_CU(ctx, cudaMemsetAsync(d_l1, 0, 16, ctx->stream));
-    launch_t(ctx, "pr_pull", k_pr_units<kComp, T>, dim3(grid_u), dim3(kPrBlock), 0, (const uint64_t *)g->d_off,
-             (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, (const PrDesc *)desc, nunits,
-             (const T *)pdiv, (const T *)p_curr, p_next, pdiv_next, part, damping, added, d_l1);
-    if (nheavy)
-      launch_t(ctx, "pr_pull", k_pr_combine<kComp, T>, dim3(grid_c), dim3(256), 0, (const uint32_t *)heavy,
-               (const uint64_t *)cbase, nheavy, (const T *)part, (const uint32_t *)g->d_deg, (const T *)p_curr,
-               p_next, pdiv_next, damping, added, d_l1);
-    BYO_CU(ctx, cudaMemcpyAsync(hl, d_l1, 16, cudaMemcpyDeviceToHost, ctx->stream));
-    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-    L1 = hl[0];
-    std::swap(pdiv, pdiv_next);
-    last = p_next;
-    if (L1 < eps) break;
-    std::swap(p_curr, p_next);
+  const T *last = pa;
+  if (max_iters > 0) {
+    cudaGraph_t graph = nullptr, body = nullptr, second = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int rc = BYO_OK;
+    auto fail = [&](const char *what, cudaError_t e) {
+      if (rc == BYO_OK) rc = set_error(ctx, BYO_EDEVICE, what, e);
+    };
+    cudaError_t e = cudaGraphCreate(&graph, 0);
+    if (e != cudaSuccess) fail("pagerank graph", e);
+    cudaGraphConditionalHandle h_while = 0, h_if = 0;
+    cudaGraphNode_t wnode = nullptr, inode = nullptr;
+    if (rc == BYO_OK && (e = cudaGraphConditionalHandleCreate(&h_while, graph, 1, cudaGraphCondAssignDefault)) !=
+                            cudaSuccess)
+      fail("pagerank loop condition", e);
+    if (rc == BYO_OK) {
+      cudaGraphNodeParams wp = {};
+      wp.type = cudaGraphNodeTypeConditional;
+      wp.conditional.handle = h_while;
+      wp.conditional.type = cudaGraphCondTypeWhile;
+      wp.conditional.size = 1;
+      if ((e = cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &wp)) != cudaSuccess) fail("pagerank loop", e);
+      else body = wp.conditional.phGraph_out[0];
+    }
+    if (rc == BYO_OK &&
+        (e = cudaGraphConditionalHandleCreate(&h_if, graph, 0, cudaGraphCondAssignDefault)) != cudaSuccess)
+      fail("pagerank half condition", e);
+    // one iteration: units, combine, check; returns its last node
+    const uint64_t *off_ = g->d_off;
+    const uint32_t *slots_ = g->d_slots, *deg_ = g->d_deg, *heavy_ = heavy;
+    const uint64_t *cbase_ = cbase;
+    const PrDesc *desc_ = desc;
+    T *pa_ = pa, *pb_ = pb, *da_ = da, *db_ = db;
+    double *l1_ = d_l1;
+    PrLoop *loop_ = loop;
+    const double eps_ = eps;
+    const uint32_t maxit_ = max_iters;
+    T damping_ = damping, added_ = added;
+    uint64_t nunits_ = nunits, nheavy_ = nheavy;
+    int half0 = 0, half1 = 1;
+    const T *pdiv_in[2] = {da_, db_}, *pcur[2] = {pa_, pb_};
+    T *pnext[2] = {pb_, pa_}, *pdiv_out[2] = {db_, da_};
+    auto add_iter = [&](cudaGraph_t gr, int h, cudaGraphNode_t dep, cudaGraphNode_t *lastn) {
+      if (rc != BYO_OK) return;
+      cudaKernelNodeParams kp = {};
+      cudaGraphNode_t nu = nullptr, nc = nullptr, nk = nullptr;
+      void *ua[] = {(void *)&off_, (void *)&slots_, (void *)&deg_, (void *)&desc_, (void *)&nunits_,
+                    (void *)&pdiv_in[h], (void *)&pcur[h], (void *)&pnext[h], (void *)&pdiv_out[h], (void *)&part,
+                    (void *)&damping_, (void *)&added_, (void *)&l1_};
+      kp.func = (void *)k_pr_units<kComp, T>;
+      kp.gridDim = dim3(grid_u);
+      kp.blockDim = dim3(kPrBlock);
+      kp.kernelParams = ua;
+      cudaError_t x = cudaGraphAddKernelNode(&nu, gr, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
+      if (x != cudaSuccess) return fail("pagerank units node", x);
+      cudaGraphNode_t prev = nu;
+      if (nheavy_) {
+        void *ca[] = {(void *)&heavy_, (void *)&cbase_, (void *)&nheavy_, (void *)&part, (void *)&deg_,
+                      (void *)&pcur[h], (void *)&pnext[h], (void *)&pdiv_out[h], (void *)&damping_, (void *)&added_,
+                      (void *)&l1_};
+        kp.func = (void *)k_pr_combine<kComp, T>;
+        kp.gridDim = dim3(grid_c);
+        kp.blockDim = dim3(256);
+        kp.kernelParams = ca;
+        x = cudaGraphAddKernelNode(&nc, gr, &prev, 1, &kp);
+        if (x != cudaSuccess) return fail("pagerank combine node", x);
+        prev = nc;
+      }
+      void *ka[] = {(void *)&l1_, (void *)&eps_, (void *)&maxit_, (void *)&loop_, (void *)(h ? &half1 : &half0),
+                    (void *)&h_if, (void *)&h_while};
+      kp.func = (void *)k_pr_check;
+      kp.gridDim = dim3(1);
+      kp.blockDim = dim3(32);
+      kp.kernelParams = ka;
+      x = cudaGraphAddKernelNode(&nk, gr, &prev, 1, &kp);
+      if (x != cudaSuccess) return fail("pagerank check node", x);
+      *lastn = nk;
+    };
+    cudaGraphNode_t k0 = nullptr, k1 = nullptr;
+    add_iter(body, 0, nullptr, &k0);
+    if (rc == BYO_OK) {
+      cudaGraphNodeParams ip = {};
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = h_if;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      if ((e = cudaGraphAddNode(&inode, body, &k0, nullptr, 1, &ip)) != cudaSuccess) fail("pagerank half", e);
+      else second = ip.conditional.phGraph_out[0];
+    }
+    add_iter(second, 1, nullptr, &k1);
+    if (rc == BYO_OK && (e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) fail("pagerank instantiate", e);
+    if (rc == BYO_OK) {
+      const bool timed = !ctx->ktag.empty() && ktimer_begin(ctx, "pr_pull");
+      if ((e = cudaGraphLaunch(exec, ctx->stream)) != cudaSuccess) fail("pagerank launch", e);
+      if (timed) ktimer_end(ctx);
+      ctx->launches += 1;
+    }
+    PrLoop hs{0.0, 0u, -1};
+    if (rc == BYO_OK && (e = cudaMemcpyAsync(&hs, loop, sizeof(PrLoop), cudaMemcpyDeviceToHost, ctx->stream)) !=
+                            cudaSuccess)
+      fail("pagerank state", e);
+    if (rc == BYO_OK && (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) fail("pagerank sync", e);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    BYO_TRY(rc);
+    ctx->launches += (uint64_t)(nheavy ? 3 : 2) * hs.iters - 1;  // kernels the graph ran
+    it = hs.iters;
+    L1 = hs.l1;
+    last = hs.last == 0 ? pb : pa;
   }
-  if (it > max_iters) it = max_iters;
   // the last computed iterate (the reference's final swap would hand back the
   // zeroed previous one when max_iters ends the loop, PageRank.h:181-192)
-  launch(ctx, k_to_f64<T>, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const T *)(last ? last : p_curr), n,
-         d_p);
+  launch(ctx, k_to_f64<T>, dim3(grid_for(ctx, n, 256)), dim3(256), 0, last, n, d_p);
   if (iters_out) *iters_out = it;
   if (l1_out) *l1_out = L1;
   return check_launch(ctx, "pagerank");
