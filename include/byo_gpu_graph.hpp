@@ -13,8 +13,9 @@
 // insert_sorted_batch / remove_sorted_batch(std::tuple<uint32_t,uint32_t>*, n).
 // Neighbour maps run on the host over a mirror of the device adjacency that is
 // refreshed after every update, so any GBBS algorithm still works; the hot
-// algorithms run on the GPU through the free functions gpu_bfs, gpu_cc,
-// gpu_pagerank and gpu_triangle_count.
+// algorithms run on the GPU through the free functions gpu_bfs, gpu_bfs_multi,
+// gpu_cc, gpu_bfs_cc, gpu_pagerank, gpu_pagerank_delta and
+// gpu_triangle_count.
 //
 // Errors from the C ABI throw byo::Error (the reference aborts instead).
 #pragma once
@@ -234,6 +235,27 @@ inline uint64_t gpu_triangle_count(const detail::DeviceGraph &G) {
   uint64_t c = 0;
   Context::get().check(byo_triangle_count(G.handle(), &c), "triangle_count");
   return c;
+}
+// delta::PageRankDelta (PageRank.h:340-398).
+inline std::vector<double> gpu_pagerank_delta(const detail::DeviceGraph &G, double eps = 1e-6, double local_eps = 0.01,
+                                              uint32_t iters = 100) {
+  std::vector<double> p(G.num_vertices());
+  Context::get().check(byo_pagerank_delta(G.handle(), eps, local_eps, iters, p.data(), nullptr, nullptr),
+                       "pagerank_delta");
+  return p;
+}
+// BFS levels from up to 64 sources in one traversal: levels[s * n + v].
+inline std::vector<uint32_t> gpu_bfs_multi(const detail::DeviceGraph &G, const std::vector<uint32_t> &sources) {
+  std::vector<uint32_t> levels(sources.size() * G.num_vertices());
+  Context::get().check(byo_bfs_multi(G.handle(), sources.data(), (uint32_t)sources.size(), levels.data(), nullptr),
+                       "bfs_multi");
+  return levels;
+}
+// SimpleUnionAsync's labels through BFS-CC (Connectivity.h:33-88 of BFSCC).
+inline std::vector<uint32_t> gpu_bfs_cc(const detail::DeviceGraph &G) {
+  std::vector<uint32_t> label(G.num_vertices());
+  Context::get().check(byo_bfs_cc(G.handle(), label.data()), "bfs_cc");
+  return label;
 }
 
 }  // namespace byo

@@ -53,6 +53,13 @@ int main() {
   double sum = 0;
   for (double x : pr) sum += x;
   CHECK(sum > 0.5 && sum < 1.01);
+  auto prd = byo::gpu_pagerank_delta(csr);
+  CHECK(prd.size() == n && prd[3] > 0);
+  CHECK((byo::gpu_bfs_cc(csr) == lab));
+  // levels from 2 and 0 in one traversal
+  auto lv = byo::gpu_bfs_multi(csr, {2, 0});
+  CHECK((std::vector<uint32_t>(lv.begin(), lv.begin() + n) == std::vector<uint32_t>{X, X, 0, 1, 2, 2, 3}));
+  CHECK((std::vector<uint32_t>(lv.begin() + n, lv.end()) == std::vector<uint32_t>{0, 1, X, X, X, X, X}));
 
   byo::GPU_PMA_graph<int> pma(vd.data(), n, edges.size(), nullptr, edges.data());
   CHECK(pma.num_edges() == 12);
