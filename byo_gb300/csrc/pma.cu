@@ -377,7 +377,7 @@ __device__ __forceinline__ uint64_t bval(const uint64_t *B, uint64_t j) { return
 template <bool kList>
 __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
     uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
-    const uint64_t *__restrict__ bstart, const uint64_t *__restrict__ seg, const unsigned long long *nseg,
+    const uint64_t *__restrict__ bstart, uint64_t *seg, const unsigned long long *nseg,
     int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
     unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta, uint32_t *deg) {
   __shared__ uint64_t As[kOptWarps][kLeaf];
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
   for (uint64_t q = gw; q < nwork; q += nw) {
     uint64_t j, b0, b1;
     if (kList) {
-      j = seg[2 * q];
+      j = seg[2 * q] & 0xFFFFFFFFull;
       b0 = seg[2 * q + 1] >> 32;
       b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
     } else {
@@ -400,6 +400,8 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       b1 = bstart[j + 1];
     }
     const uint32_t c = cnt[j];
+    if (kList && lane == 0)  // the leaf's last src before the merge, for the view refresh
+      seg[2 * q] = j | (uint64_t)(c ? src[j * kLeaf + c - 1] : 0xFFFFFFFFu) << 32;
     if (b0 == b1) {
       if (lane == 0) rcount[j] = c;
       continue;
@@ -581,8 +583,9 @@ __global__ void __launch_bounds__(kPmaBlock) k_pma_spread(const uint64_t *__rest
 
 // ---------------------------------------------------------------- graph view
 
-// off[v] = slot of the first key >= (v,0); elem[v] = number of keys < (v,0);
-// for v in [0, n]
+// off[v] = slot of the first key >= (v,0) in the leaf (v,0) routes to, or the
+// start of the next leaf when that leaf has no such key; elem[v] = number of
+// keys < (v,0); for v in [0, n]
 __global__ void k_pma_view(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
                            const uint64_t *__restrict__ sep, const uint64_t *__restrict__ epre, uint64_t NL,
                            uint64_t n, uint64_t *off, uint64_t *elem) {
@@ -596,8 +599,10 @@ __global__ void k_pma_view(const uint32_t *__restrict__ src, const uint32_t *__r
       uint32_t mid = (lo + hi) >> 1;
       if (src[i * kLeaf + mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
     }
-    // every key of leaf i is >= sep[i]; keys < (v,0) in leaf i are a prefix
-    off[v] = i * kLeaf + lo;
+    // every key of leaf i is >= sep[i]; keys < (v,0) in leaf i are a prefix.
+    // A vertex past the leaf's last key starts at the next leaf: its (empty)
+    // range then does not depend on how many keys leaf i holds
+    off[v] = lo < c ? i * kLeaf + lo : (i + 1) * kLeaf;
     elem[v] = epre[i] + lo;
   }
 }
@@ -621,8 +626,13 @@ __global__ void k_pma_export(const uint32_t *__restrict__ src, const uint32_t *_
 // Leaves with work for a small sorted batch: key q starts a segment when it
 // routes to another leaf than key q-1; the segment ends at the first key >=
 // sep[leaf + 1].  seg[2s] = leaf, seg[2s + 1] = b0 << 32 | b1 (b < 2^32).
+// With `bounds` set (a batch not yet validated on the host), a batch with a
+// src or dst >= n or flagged unsorted yields no segments, so the merge after
+// it changes nothing and the host reports the error once it reads the flags.
 __global__ void k_pma_segments(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
-                               uint64_t b, uint64_t *seg, unsigned long long *nseg) {
+                               uint64_t b, uint64_t *seg, unsigned long long *nseg,
+                               const unsigned long long *bounds, uint64_t n, const unsigned int *unsorted) {
+  if (bounds && (bounds[0] >= n || bounds[1] >= n || *unsorted)) return;
   for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < b;
        base += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t q = base + lane_id();
@@ -709,25 +719,77 @@ __device__ __forceinline__ uint64_t ceil_src(uint64_t key) { return (key >> 32) 
 // The view after an in-place merge of the segment list: off[v] changes only
 // for the vertices v whose key (v, 0) routes to a merged leaf j, i.e. v in
 // [ceil(sep[j] / 2^32), ceil(sep[j+1] / 2^32)).  A warp per merged leaf.
-__global__ void k_pma_view_leaves(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
+// Of those, only v in (min(s0, L), U] can change, where s0 is the smallest
+// src of the batch keys merged into j, L the smaller and U the larger of the
+// leaf's last src before and after the merge (U also >= the largest batch
+// src): below that the prefix counts are unchanged, above it every vertex
+// starts at the next leaf either way.  The range can be long (a key for a
+// vertex far past the leaf's last key moves every vertex between them), so a
+// thread per merged leaf only computes its range and cuts it into chunks of
+// kViewChunk vertices; k_pma_view_chunks fills the chunks with the whole grid.
+constexpr uint32_t kViewChunk = 1024, kViewThreads = 256;
+
+__global__ void k_pma_view_ranges(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
                                   const uint64_t *__restrict__ sep, uint64_t NL, uint64_t n,
-                                  const uint64_t *__restrict__ seg, const unsigned long long *nseg, uint64_t *off) {
-  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+                                  const uint64_t *__restrict__ seg, const unsigned long long *nseg,
+                                  const uint64_t *__restrict__ keys, uint64_t *range, uint64_t *chunks,
+                                  unsigned long long *nchunks, const unsigned long long *ctr, uint64_t m_before,
+                                  double shrink_below) {
+  // an overflowing leaf or a shrink sends the update down the windowed path,
+  // which rebuilds the whole view
+  if (ctr[1] || (double)((long long)m_before + (long long)ctr[2]) < shrink_below) return;
   const uint64_t ns = *nseg;
-  for (uint64_t q = gw; q < ns; q += nw) {
-    const uint64_t j = seg[2 * q];
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < ns; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t j = seg[2 * q] & 0xFFFFFFFFull;
+    const uint32_t old_last = (uint32_t)(seg[2 * q] >> 32);  // 0xFFFFFFFF: the leaf was empty
+    const uint64_t b0 = seg[2 * q + 1] >> 32, b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
     const uint64_t vlo = j == 0 ? 0 : min(ceil_src(sep[j]), n + 1);
     const uint64_t vhi = j + 1 == NL ? n + 1 : min(ceil_src(sep[j + 1]), n + 1);
     const uint32_t c = cnt[j];
+    const uint64_t smin = keys[b0] >> 32, smax = keys[b1 - 1] >> 32;
+    const bool had = old_last != 0xFFFFFFFFu, has = c != 0;
+    const uint64_t new_last = has ? src[j * kLeaf + c - 1] : 0;
+    // L + 1 and U + 1 with "no keys" as vlo - 1
+    const uint64_t l1 = !had || !has ? vlo : min((uint64_t)old_last, new_last) + 1;
+    uint64_t u1 = smax + 1;
+    if (had) u1 = max(u1, (uint64_t)old_last + 1);
+    if (has) u1 = max(u1, new_last + 1);
+    const uint64_t a = max(vlo, min(smin, l1)), e = max(a, min(vhi, u1));
+    range[2 * q] = a;
+    range[2 * q + 1] = e;
+    const uint64_t nch = (e - a + kViewChunk - 1) / kViewChunk;
+    const uint64_t at = nch ? atomicAdd(nchunks, (unsigned long long)nch) : 0;
+    for (uint64_t t = 0; t < nch; t++) chunks[at + t] = q << 32 | t;
+  }
+}
+
+// A block per chunk; each thread fills kViewChunk / kViewThreads vertices a
+// block width apart, each by its own binary search over the leaf (the
+// searches are independent, so their loads overlap).
+__global__ void __launch_bounds__(kViewThreads)
+    k_pma_view_chunks(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
+                      const uint64_t *__restrict__ seg, const uint64_t *__restrict__ range,
+                      const uint64_t *__restrict__ chunks, const unsigned long long *nchunks, uint64_t *off) {
+  const uint64_t nc = *nchunks;
+  constexpr uint32_t kPer = kViewChunk / kViewThreads;
+  for (uint64_t i = blockIdx.x; i < nc; i += gridDim.x) {
+    const uint64_t ch = chunks[i];
+    const uint64_t q = ch >> 32, t = ch & 0xFFFFFFFFull;
+    const uint64_t j = seg[2 * q] & 0xFFFFFFFFull;
+    const uint64_t e = range[2 * q + 1];
+    const uint64_t v0 = range[2 * q] + t * kViewChunk + threadIdx.x;
+    const uint32_t c = cnt[j];
     const uint32_t *ls = src + j * kLeaf;
-    for (uint64_t v = vlo + lane_id(); v < vhi; v += 32) {
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; k++) {
+      const uint64_t v = v0 + (uint64_t)k * kViewThreads;
+      if (v >= e) break;
       uint32_t lo = 0, hi = c;
       while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (ls[mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
+        if (__ldg(ls + mid) < (uint32_t)v) lo = mid + 1; else hi = mid;
       }
-      off[v] = j * kLeaf + lo;
+      off[v] = lo < c ? j * kLeaf + lo : (j + 1) * kLeaf;
     }
   }
 }
@@ -952,10 +1014,18 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   }
   uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
-  BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  if (h[0] >= g->n || h[1] >= g->n) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
-  if (sorted && (((unsigned int *)(h + 2))[0])) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  // A batch small enough for the segment-list merge that needs no bucketed
+  // sort is validated on the device (the segment kernel drops an invalid
+  // batch) and checked here after the single synchronisation of the update.
+  const bool list = 2 * count <= p->NL && count < (1ull << 32);
+  const bool defer = list && (sorted || small_sort) && ctx->update_policy != BYO_UPDATE_REBUILD &&
+                     ctx->update_policy != BYO_UPDATE_LEARNED;
+  if (!defer) {
+    BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h[0] >= g->n || h[1] >= g->n) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+    if (sorted && (((unsigned int *)(h + 2))[0])) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  }
   uint64_t *batch = nullptr;
   uint64_t b = count;
   if (sorted) {
@@ -1006,40 +1076,57 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   // around those leaves.
   BYO_TRY(ensure(ctx, p->ovf, (NL * kLeaf + b + 1) * 8));
   BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
-  unsigned long long *ctr = (unsigned long long *)(flags + 4);  // [0] cursor, [1] leaves, [2] delta, [3] segments
-  BYO_CU(ctx, cudaMemsetAsync(ctr, 0, 32, ctx->stream));
-  const bool list = 2 * b <= NL && b < (1ull << 32);
+  // counters, cleared with the rest of misc: [0] cursor, [1] overflowing
+  // leaves, [2] delta, [3] segments, [4] view chunks
+  unsigned long long *ctr = (unsigned long long *)(flags + 4);
+  const double cap = (double)NL * kLeaf;
   if (list) {
     uint64_t *seg = bstart;  // 2 * b <= NL words
     launch(ctx, k_pma_segments, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
-           (const uint64_t *)batch, b, seg, ctr + 3);
+           (const uint64_t *)batch, b, seg, ctr + 3, defer ? (const unsigned long long *)bounds : nullptr, g->n,
+           (const unsigned int *)flags);
     BYO_CU(ctx, cudaMemcpyAsync(rcount, p->cnt, NL * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     launch_t(ctx, "pma_merge", k_pma_merge_opt<true>, dim3(grid_for(ctx, b * 32, 32 * kOptWarps, 6)),
              dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
-             (const uint64_t *)nullptr, (const uint64_t *)seg, (const unsigned long long *)(ctr + 3), insert, rcount,
+             (const uint64_t *)nullptr, seg, (const unsigned long long *)(ctr + 3), insert, rcount,
              (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2), g->d_deg);
   } else {
     launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
            (const uint64_t *)batch, b, bstart);
     launch_t(ctx, "pma_merge", k_pma_merge_opt<false>, dim3(grid_for(ctx, NL * 32, 32 * kOptWarps, 6)),
              dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
-             (const uint64_t *)bstart, (const uint64_t *)nullptr, (const unsigned long long *)nullptr, insert,
+             (const uint64_t *)bstart, (uint64_t *)nullptr, (const unsigned long long *)nullptr, insert,
              rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2),
              (uint32_t *)nullptr);
   }
-  BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 24, cudaMemcpyDeviceToHost, ctx->stream));
+  const double shrink_below = !insert && NL > 1 ? kRootMin * cap : -1.0;
+  if (list) {
+    // offsets of the vertices around the merged leaves, issued before the
+    // counters are read: the range kernel does nothing when the update
+    // overflowed or shrinks (rpre and win are free here)
+    BYO_TRY(ensure(ctx, p->win, ((g->n + 1) / kViewChunk + b + 64) * 8));
+    launch(ctx, k_pma_view_ranges, dim3(grid_for(ctx, b, 256, 8)), dim3(256), 0, (const uint32_t *)p->src,
+           (const uint32_t *)p->cnt, (const uint64_t *)p->sep, NL, g->n, (const uint64_t *)bstart,
+           (const unsigned long long *)(ctr + 3), (const uint64_t *)batch, rpre, (uint64_t *)p->win.p, ctr + 4,
+           (const unsigned long long *)ctr, m_before, shrink_below);
+    launch(ctx, k_pma_view_chunks, dim3(ctx->num_sms * 8), dim3(kViewThreads), 0, (const uint32_t *)p->src,
+           (const uint32_t *)p->cnt, (const uint64_t *)bstart, (const uint64_t *)rpre, (const uint64_t *)p->win.p,
+           (const unsigned long long *)(ctr + 4), g->d_off);
+  }
+  BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 72, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const uint64_t novf = h[1];
-  const long long delta = (long long)h[2];
+  if (defer) {
+    if (h[0] >= g->n || h[1] >= g->n) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+    if (sorted && (((unsigned int *)(h + 2))[0])) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  }
+  const uint64_t *hc = h + 4;  // the counters
+  const uint64_t novf = hc[1];
+  const long long delta = (long long)hc[2];
   const uint64_t total = (uint64_t)((long long)m_before + delta);
   if (changed) *changed = insert ? total - m_before : m_before - total;
-  const double cap = (double)NL * kLeaf;
-  const bool shrink = !insert && (double)total < kRootMin * cap && NL > 1;
+  const bool shrink = (double)total < shrink_below;
   if (novf == 0 && !shrink) {
     if (list) {
-      launch(ctx, k_pma_view_leaves, dim3(grid_for(ctx, b * 32, 256, 8)), dim3(256), 0, (const uint32_t *)p->src,
-             (const uint32_t *)p->cnt, (const uint64_t *)p->sep, NL, g->n, (const uint64_t *)bstart,
-             (const unsigned long long *)(ctr + 3), g->d_off);
       g->m = total;
       return check_launch(ctx, "pma_update");
     }

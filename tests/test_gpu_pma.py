@@ -119,6 +119,15 @@ def test_small_batches_and_errors(ctx, oracle_mod):
     with pytest.raises(byo.ByoError) as e:
         G.insert_batch(np.array([(5 << 32) | 7, (5 << 32) | 3], np.uint64), sorted=True)
     assert e.value.code == byo._abi.BYO_EINVAL
+    # valid keys next to an invalid one: nothing of the batch is applied
+    for bad in ((n << 32) | 1, (1 << 32) | (n + 3)):
+        with pytest.raises(byo.ByoError) as e:
+            G.insert_batch(np.array([(3 << 32) | 4, (4 << 32) | 3, bad], np.uint64))
+        assert e.value.code == byo._abi.BYO_EINVAL
+        u = int(np.flatnonzero(np.diff(ro))[0])  # an edge that exists
+        with pytest.raises(byo.ByoError) as e:
+            G.remove_batch(np.array([(u << 32) | int(rn[ro[u]]), bad], np.uint64))
+        assert e.value.code == byo._abi.BYO_EINVAL
     # the container is unchanged by rejected batches
     o2, n2 = G.export_csr()
     assert np.array_equal(o2, ro) and np.array_equal(n2, rn)
