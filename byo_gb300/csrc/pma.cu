@@ -352,6 +352,93 @@ __global__ void __launch_bounds__(32 * kMergeWarps) k_pma_merge(uint32_t *src, u
   }
 }
 
+// ---------------------------------------------------------------- view refresh after a small merge
+//
+// After an in-place merge of the segment list, off[v] changes only for the
+// vertices v whose key (v, 0) routes to a merged leaf j, i.e. v in
+// [ceil(sep[j] / 2^32), ceil(sep[j+1] / 2^32)).  Of those, only v in
+// (min(s0, L), U] can change, where s0 is the smallest src of the batch keys
+// merged into j, L the smaller and U the larger of the leaf's last src before
+// and after the merge (U also >= the largest batch src): below that the
+// prefix counts are unchanged, above it every vertex starts at the next leaf
+// either way.  The merging warp refreshes that range itself, up to
+// kViewWarpMax vertices, as a merge of the vertex sequence [a, e) with the
+// leaf's src list (staged in shared memory), each lane taking one diagonal
+// band of the merge path, so that off[v] = the leaf position of the first key
+// with src >= v.  A longer range (a key for a vertex far past the leaf's last
+// key moves every vertex between them) is cut into chunks of kViewChunk
+// vertices that k_pma_view_chunks fills with the whole grid.
+constexpr uint32_t kViewChunk = 1024, kViewThreads = 256, kViewWarpMax = 1u << 10;
+
+__device__ __forceinline__ uint64_t ceil_src(uint64_t key) { return (key >> 32) + ((key & 0xFFFFFFFFull) != 0); }
+
+// The warp's part for merged leaf j (c keys now, old_last the src of its last
+// key before the merge or 0xFFFFFFFF if it was empty) and segment q.
+__device__ __forceinline__ void view_refresh_warp(const uint32_t *src, const uint64_t *__restrict__ sep, uint64_t NL,
+                                                  uint64_t n, uint64_t j, uint32_t c, uint32_t old_last,
+                                                  uint64_t smin, uint64_t smax, uint32_t *Y, uint64_t *off,
+                                                  uint64_t q, uint64_t *vrange, uint64_t *chunks,
+                                                  unsigned long long *nchunks) {
+  const unsigned lane = lane_id();
+  const uint32_t *ls = src + j * kLeaf;
+  const uint64_t vlo = j == 0 ? 0 : min(ceil_src(sep[j]), n + 1);
+  const uint64_t vhi = j + 1 == NL ? n + 1 : min(ceil_src(sep[j + 1]), n + 1);
+  const bool had = old_last != 0xFFFFFFFFu, has = c != 0;
+  const uint64_t new_last = has ? ls[c - 1] : 0;
+  // L + 1 and U + 1 with "no keys" as vlo - 1
+  const uint64_t l1 = !had || !has ? vlo : min((uint64_t)old_last, new_last) + 1;
+  uint64_t u1 = smax + 1;
+  if (had) u1 = max(u1, (uint64_t)old_last + 1);
+  if (has) u1 = max(u1, new_last + 1);
+  const uint64_t a = max(vlo, min(smin, l1)), e = max(a, min(vhi, u1));
+  if (e - a > kViewWarpMax) {
+    if (lane == 0) {
+      vrange[2 * q] = a;
+      vrange[2 * q + 1] = e;
+      const uint64_t nch = (e - a + kViewChunk - 1) / kViewChunk;
+      const uint64_t at = atomicAdd(nchunks, (unsigned long long)nch);
+      for (uint64_t t = 0; t < nch; t++) chunks[at + t] = q << 32 | t;
+    }
+    return;
+  }
+  if (e == a) return;
+  for (uint32_t i = lane; i < c; i += 32) Y[i] = ls[i];
+  __syncwarp();
+  // keys with src in [a, e): positions [p0, p1)
+  uint32_t p0 = 0, p1 = c;
+  {
+    uint32_t hi = c;
+    while (p0 < hi) {
+      const uint32_t mid = (p0 + hi) >> 1;
+      if (Y[mid] < a) p0 = mid + 1; else hi = mid;
+    }
+    uint32_t lo = p0;
+    while (lo < p1) {
+      const uint32_t mid = (lo + p1) >> 1;
+      if (Y[mid] < e) lo = mid + 1; else p1 = mid;
+    }
+  }
+  const uint32_t nx = (uint32_t)(e - a), ny = p1 - p0, T = nx + ny, per = (T + 31) / 32;
+  const uint32_t d0 = lane * per < T ? lane * per : T, d1 = d0 + per < T ? d0 + per : T;
+  // vertices among the first d0 merged (a vertex v goes before a key with src >= v)
+  uint32_t lo = d0 > ny ? d0 - ny : 0, hi = d0 < nx ? d0 : nx;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a + mid <= Y[p0 + d0 - mid - 1]) lo = mid + 1; else hi = mid;
+  }
+  uint32_t i = lo, k = d0 - lo;
+  const uint64_t base = j * kLeaf, next = (j + 1) * kLeaf;
+  for (uint32_t d = d0; d < d1; d++) {
+    if (i < nx && (k >= ny || a + i <= Y[p0 + k])) {
+      const uint32_t pos = p0 + k;
+      off[a + i] = pos < c ? base + pos : next;
+      i++;
+    } else {
+      k++;
+    }
+  }
+}
+
 // ---------------------------------------------------------------- optimistic merge
 // One warp per leaf with a batch segment.  The leaf (A) and, when short, the
 // segment (B) are staged in the warp's shared memory.  The merged sequence of
@@ -372,14 +459,24 @@ __device__ __forceinline__ uint64_t bval(const uint64_t *B, uint64_t j) { return
 
 // kList: the leaves with work come from a segment list (seg[2q] = leaf,
 // seg[2q + 1] = b0 << 32 | b1, *nseg entries) instead of bstart over every
-// leaf; rcount of the other leaves must already hold their counts.  When deg
-// is given, every key that enters or leaves adjusts deg[src].
+// leaf.  Then rcount is not written: the count after the merge goes to the
+// high half of seg[2q] instead.  When deg is given, every key that enters or
+// leaves adjusts deg[src].  When off is given (list mode), a leaf merged in
+// place also refreshes the view offsets around it (view_refresh_warp).
+struct ViewOut {
+  const uint64_t *sep;
+  uint64_t n;
+  uint64_t *off, *range, *chunks;
+  unsigned long long *nchunks;
+};
+
 template <bool kList>
 __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
     uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
     const uint64_t *__restrict__ bstart, uint64_t *seg, const unsigned long long *nseg,
     int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
-    unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta, uint32_t *deg) {
+    unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta, uint32_t *deg,
+    ViewOut view) {
   __shared__ uint64_t As[kOptWarps][kLeaf];
   __shared__ uint64_t Bsh[kOptWarps][kOptSeg];
   const unsigned w = threadIdx.x >> 5, lane = lane_id();
@@ -400,23 +497,43 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       b1 = bstart[j + 1];
     }
     const uint32_t c = cnt[j];
-    if (kList && lane == 0)  // the leaf's last src before the merge, for the view refresh
-      seg[2 * q] = j | (uint64_t)(c ? src[j * kLeaf + c - 1] : 0xFFFFFFFFu) << 32;
+    // the leaf's last src before the merge, for the view refresh
+    const uint32_t old_last = kList && view.off && c ? src[j * kLeaf + c - 1] : 0xFFFFFFFFu;
     if (b0 == b1) {
-      if (lane == 0) rcount[j] = c;
+      if (lane == 0) {
+        if (kList) seg[2 * q] = j | (uint64_t)c << 32;
+        else rcount[j] = c;
+      }
       continue;
     }
     const uint64_t nb = b1 - b0;
     const uint64_t *B = nb <= kOptSeg ? Bsh[w] : keys + b0;
     const uint64_t base = j * kLeaf;
-    for (uint32_t e = lane; e < c; e += 32) As[w][e] = slot_key(src, dst, base + e);
+    // The s leaf keys below the first batch key keep their slots: the merge
+    // reads and writes only the rest.  s by two rounds of lane-parallel
+    // probes: every stride-th key, then the keys of the one stride that holds
+    // the boundary.
+    uint32_t s = 0;
+    if (c) {
+      const uint64_t first = keys[b0];
+      const uint32_t stride = (c + 31) / 32;  // <= kLeaf / 32
+      const uint32_t ps = lane * stride;
+      const uint32_t t = __popc(__ballot_sync(kFull, ps < c && slot_key(src, dst, base + ps) < first));
+      if (t) {
+        const uint32_t p0 = (t - 1) * stride + 1, pe = t * stride < c ? t * stride : c;
+        const uint32_t pp = p0 + lane;
+        s = p0 + __popc(__ballot_sync(kFull, pp < pe && slot_key(src, dst, base + pp) < first));
+      }
+    }
+    const uint32_t ca = c - s;  // the leaf keys that take part in the merge
+    for (uint32_t e = lane; e < ca; e += 32) As[w][e] = slot_key(src, dst, base + s + e);
     if (nb <= kOptSeg)
       for (uint32_t k = lane; k < nb; k += 32) Bsh[w][k] = keys[b0 + k];
     __syncwarp();
     // this lane's diagonal [d0, d1) of the merged sequence
-    const uint64_t T = c + nb, per = (T + 31) / 32;
+    const uint64_t T = ca + nb, per = (T + 31) / 32;
     const uint64_t d0 = lane * per < T ? lane * per : T, d1 = d0 + per < T ? d0 + per : T;
-    uint64_t lo = d0 > nb ? d0 - nb : 0, hi = d0 < c ? d0 : c;
+    uint64_t lo = d0 > nb ? d0 - nb : 0, hi = d0 < ca ? d0 : ca;
     while (lo < hi) {  // number of A elements among the first d0 merged
       const uint64_t mid = (lo + hi) >> 1;
       if (A[mid] <= bval(B, d0 - mid - 1)) lo = mid + 1; else hi = mid;
@@ -427,7 +544,7 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
     {
       uint64_t i = i0, k = j0;
       for (uint64_t d = d0; d < d1; d++) {
-        if (i < c && (k >= nb || A[i] <= bval(B, k))) {
+        if (i < ca && (k >= nb || A[i] <= bval(B, k))) {
           const uint64_t x = A[i];
           if (insert) keep++;
           else if (!(k < nb && bval(B, k) == x)) keep++;
@@ -440,13 +557,13 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       }
     }
     const uint32_t incl = warp_inclusive_scan(keep);
-    const uint32_t r = __shfl_sync(kFull, incl, 31);
+    const uint32_t r = s + __shfl_sync(kFull, incl, 31);
     uint32_t pos = incl - keep;
     uint32_t *osrc = nullptr, *odst = nullptr;
     uint64_t *ostage = nullptr;
     if (r <= kLeaf) {
-      osrc = src + base;
-      odst = dst + base;
+      osrc = src + base + s;
+      odst = dst + base + s;
     } else {
       unsigned long long at = 0;
       if (lane == 0) {
@@ -455,7 +572,8 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
         ovf_off[j] = at;
       }
       at = __shfl_sync(kFull, at, 0);
-      ostage = ovf + at;
+      for (uint32_t e = lane; e < s; e += 32) ovf[at + e] = slot_key(src, dst, base + e);
+      ostage = ovf + at + s;
     }
     __syncwarp();  // every lane has read A before any in-place write
     {
@@ -463,7 +581,7 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       for (uint64_t d = d0; d < d1; d++) {
         uint64_t x;
         bool kept;
-        if (i < c && (k >= nb || A[i] <= bval(B, k))) {
+        if (i < ca && (k >= nb || A[i] <= bval(B, k))) {
           x = A[i];
           kept = insert || !(k < nb && bval(B, k) == x);
           if (deg && !kept) atomicAdd(deg + (x >> 32), 0xFFFFFFFFu);  // -1
@@ -486,16 +604,21 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       }
     }
     if (!ostage) {
-      for (uint32_t q = r + lane; q < c; q += 32) {
-        src[base + q] = kSentinel;
-        dst[base + q] = kSentinel;
+      for (uint32_t t = r + lane; t < c; t += 32) {
+        src[base + t] = kSentinel;
+        dst[base + t] = kSentinel;
       }
       if (lane == 0) cnt[j] = r;
     }
     if (lane == 0) {
-      rcount[j] = r;
+      if (kList) seg[2 * q] = j | (uint64_t)r << 32;
+      else rcount[j] = r;
       dsum += (long long)r - (long long)c;
     }
+    __syncwarp();  // the leaf's new contents (and A's last reads) are done warp-wide
+    if (kList && view.off && !ostage)
+      view_refresh_warp(src, view.sep, NL, view.n, j, r, old_last, keys[b0] >> 32, keys[b1 - 1] >> 32,
+                        reinterpret_cast<uint32_t *>(As[w]), view.off, q, view.range, view.chunks, view.nchunks);
     __syncwarp();
   }
   if (lane == 0 && dsum) atomicAdd((unsigned long long *)delta, (unsigned long long)dsum);
@@ -633,23 +756,39 @@ __global__ void k_pma_segments(const uint64_t *__restrict__ sep, uint64_t NL, co
                                uint64_t b, uint64_t *seg, unsigned long long *nseg,
                                const unsigned long long *bounds, uint64_t n, const unsigned int *unsorted) {
   if (bounds && (bounds[0] >= n || bounds[1] >= n || *unsorted)) return;
+  const unsigned lane = lane_id();
   for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < b;
        base += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t q = base + lane_id();
-    bool start = false;
-    uint64_t j = 0, b1 = b;
-    if (q < b) {
-      j = route(sep, NL, keys[q]);
-      start = q == 0 || route(sep, NL, keys[q - 1]) != j;
-      if (start && j + 1 < NL) {
-        const uint64_t lim = sep[j + 1];
-        uint64_t lo = q, hi = b;
-        while (lo < hi) {
-          const uint64_t mid = (lo + hi) >> 1;
-          if (keys[mid] < lim) lo = mid + 1; else hi = mid;
-        }
-        b1 = lo;
+    const uint64_t q = base + lane;
+    // the leaf of key q, and lane 0 also that of key base - 1, in one search
+    // loop whose trip count depends only on NL (the two searches overlap)
+    const uint64_t kq = q < b ? keys[q] : ~0ull;
+    const uint64_t kp = lane == 0 && base > 0 ? keys[base - 1] : 0;
+    uint64_t lo = 0, lp = 0, len = NL;
+    while (len > 1) {
+      const uint64_t half = len >> 1;
+      if (sep[lo + half] <= kq) lo += half;
+      if (lane == 0 && sep[lp + half] <= kp) lp += half;
+      len -= half;
+    }
+    const uint64_t j = lo;
+    uint64_t jprev = __shfl_up_sync(kFull, j, 1);
+    if (lane == 0) jprev = base > 0 ? lp : ~0ull;
+    const bool start = q < b && j != jprev;
+    // a segment ends at the next start in the warp, else past the warp
+    const unsigned starts = __ballot_sync(kFull, start);
+    const unsigned later = lane == 31 ? 0u : starts >> (lane + 1) << (lane + 1);
+    uint64_t b1 = b;  // also when j is the last leaf
+    if (start && later) {
+      b1 = base + (uint64_t)__ffs(later) - 1;
+    } else if (start && base + 32 < b && j + 1 < NL) {
+      const uint64_t lim = sep[j + 1];
+      uint64_t l = base + 32, h = b;
+      while (l < h) {
+        const uint64_t mid = (l + h) >> 1;
+        if (keys[mid] < lim) l = mid + 1; else h = mid;
       }
+      b1 = l;
     }
     const uint64_t at = warp_append(start, nseg);
     if (start) {
@@ -679,6 +818,10 @@ __global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict_
     s[i] = k;
   }
   __syncthreads();
+  // Pair t compares elements i = 2t - (t mod stride) and i + stride.  For
+  // stride <= 32 the pairs of one warp's t values lie in 64-element blocks
+  // that no other warp touches, so consecutive such passes need only a warp
+  // barrier; a pass with a wider stride, or followed by one, needs the block.
   for (uint32_t size = 2; size <= P; size <<= 1)
     for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
       for (uint32_t t = threadIdx.x; t < P / 2; t += blockDim.x) {
@@ -690,8 +833,11 @@ __global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict_
           s[j] = a;
         }
       }
-      __syncthreads();
+      const uint32_t next = stride > 1 ? stride >> 1 : size;  // the next pass's stride
+      if (stride > 32 || next > 32) __syncthreads();
+      else __syncwarp();
     }
+  __syncthreads();
   for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) out[i] = s[i];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -714,62 +860,18 @@ __global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict_
   }
 }
 
-__device__ __forceinline__ uint64_t ceil_src(uint64_t key) { return (key >> 32) + ((key & 0xFFFFFFFFull) != 0); }
 
-// The view after an in-place merge of the segment list: off[v] changes only
-// for the vertices v whose key (v, 0) routes to a merged leaf j, i.e. v in
-// [ceil(sep[j] / 2^32), ceil(sep[j+1] / 2^32)).  A warp per merged leaf.
-// Of those, only v in (min(s0, L), U] can change, where s0 is the smallest
-// src of the batch keys merged into j, L the smaller and U the larger of the
-// leaf's last src before and after the merge (U also >= the largest batch
-// src): below that the prefix counts are unchanged, above it every vertex
-// starts at the next leaf either way.  The range can be long (a key for a
-// vertex far past the leaf's last key moves every vertex between them), so a
-// thread per merged leaf only computes its range and cuts it into chunks of
-// kViewChunk vertices; k_pma_view_chunks fills the chunks with the whole grid.
-constexpr uint32_t kViewChunk = 1024, kViewThreads = 256;
-
-__global__ void k_pma_view_ranges(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
-                                  const uint64_t *__restrict__ sep, uint64_t NL, uint64_t n,
-                                  const uint64_t *__restrict__ seg, const unsigned long long *nseg,
-                                  const uint64_t *__restrict__ keys, uint64_t *range, uint64_t *chunks,
-                                  unsigned long long *nchunks, const unsigned long long *ctr, uint64_t m_before,
-                                  double shrink_below) {
-  // an overflowing leaf or a shrink sends the update down the windowed path,
-  // which rebuilds the whole view
-  if (ctr[1] || (double)((long long)m_before + (long long)ctr[2]) < shrink_below) return;
-  const uint64_t ns = *nseg;
-  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < ns; q += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t j = seg[2 * q] & 0xFFFFFFFFull;
-    const uint32_t old_last = (uint32_t)(seg[2 * q] >> 32);  // 0xFFFFFFFF: the leaf was empty
-    const uint64_t b0 = seg[2 * q + 1] >> 32, b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
-    const uint64_t vlo = j == 0 ? 0 : min(ceil_src(sep[j]), n + 1);
-    const uint64_t vhi = j + 1 == NL ? n + 1 : min(ceil_src(sep[j + 1]), n + 1);
-    const uint32_t c = cnt[j];
-    const uint64_t smin = keys[b0] >> 32, smax = keys[b1 - 1] >> 32;
-    const bool had = old_last != 0xFFFFFFFFu, has = c != 0;
-    const uint64_t new_last = has ? src[j * kLeaf + c - 1] : 0;
-    // L + 1 and U + 1 with "no keys" as vlo - 1
-    const uint64_t l1 = !had || !has ? vlo : min((uint64_t)old_last, new_last) + 1;
-    uint64_t u1 = smax + 1;
-    if (had) u1 = max(u1, (uint64_t)old_last + 1);
-    if (has) u1 = max(u1, new_last + 1);
-    const uint64_t a = max(vlo, min(smin, l1)), e = max(a, min(vhi, u1));
-    range[2 * q] = a;
-    range[2 * q + 1] = e;
-    const uint64_t nch = (e - a + kViewChunk - 1) / kViewChunk;
-    const uint64_t at = nch ? atomicAdd(nchunks, (unsigned long long)nch) : 0;
-    for (uint64_t t = 0; t < nch; t++) chunks[at + t] = q << 32 | t;
-  }
-}
-
-// A block per chunk; each thread fills kViewChunk / kViewThreads vertices a
-// block width apart, each by its own binary search over the leaf (the
-// searches are independent, so their loads overlap).
+// A block per chunk of a long range; the leaf's src list is staged in shared
+// memory and each thread fills kViewChunk / kViewThreads vertices a block
+// width apart, each by its own binary search.  Nothing to do when a leaf
+// overflowed or the update shrinks: the windowed path rebuilds the whole view.
 __global__ void __launch_bounds__(kViewThreads)
     k_pma_view_chunks(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
                       const uint64_t *__restrict__ seg, const uint64_t *__restrict__ range,
-                      const uint64_t *__restrict__ chunks, const unsigned long long *nchunks, uint64_t *off) {
+                      const uint64_t *__restrict__ chunks, const unsigned long long *nchunks, uint64_t *off,
+                      const unsigned long long *ctr, uint64_t m_before, double shrink_below) {
+  __shared__ uint32_t Y[kLeaf];
+  if (ctr[1] || (double)((long long)m_before + (long long)ctr[2]) < shrink_below) return;
   const uint64_t nc = *nchunks;
   constexpr uint32_t kPer = kViewChunk / kViewThreads;
   for (uint64_t i = blockIdx.x; i < nc; i += gridDim.x) {
@@ -779,7 +881,9 @@ __global__ void __launch_bounds__(kViewThreads)
     const uint64_t e = range[2 * q + 1];
     const uint64_t v0 = range[2 * q] + t * kViewChunk + threadIdx.x;
     const uint32_t c = cnt[j];
-    const uint32_t *ls = src + j * kLeaf;
+    __syncthreads();  // the previous chunk's searches are done with Y
+    for (uint32_t k = threadIdx.x; k < c; k += kViewThreads) Y[k] = src[j * kLeaf + k];
+    __syncthreads();
 #pragma unroll
     for (uint32_t k = 0; k < kPer; k++) {
       const uint64_t v = v0 + (uint64_t)k * kViewThreads;
@@ -787,11 +891,20 @@ __global__ void __launch_bounds__(kViewThreads)
       uint32_t lo = 0, hi = c;
       while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(ls + mid) < (uint32_t)v) lo = mid + 1; else hi = mid;
+        if (Y[mid] < v) lo = mid + 1; else hi = mid;
       }
       off[v] = lo < c ? j * kLeaf + lo : (j + 1) * kLeaf;
     }
   }
+}
+
+// rcount after a list-mode merge: the counts of every leaf (copied from cnt
+// beforehand), then the merged leaves' counts from the segment list.
+__global__ void k_pma_seg_counts(const uint64_t *__restrict__ seg, const unsigned long long *nseg,
+                                 uint32_t *rcount) {
+  const uint64_t ns = *nseg;
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < ns; q += (uint64_t)gridDim.x * blockDim.x)
+    rcount[seg[2 * q] & 0xFFFFFFFFull] = (uint32_t)(seg[2 * q] >> 32);
 }
 
 // One warp per leaf: its cnt keys (packed at the leaf's start) go to
@@ -1080,16 +1193,24 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   // leaves, [2] delta, [3] segments, [4] view chunks
   unsigned long long *ctr = (unsigned long long *)(flags + 4);
   const double cap = (double)NL * kLeaf;
+  const double shrink_below = !insert && NL > 1 ? kRootMin * cap : -1.0;
   if (list) {
     uint64_t *seg = bstart;  // 2 * b <= NL words
     launch(ctx, k_pma_segments, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
            (const uint64_t *)batch, b, seg, ctr + 3, defer ? (const unsigned long long *)bounds : nullptr, g->n,
            (const unsigned int *)flags);
-    BYO_CU(ctx, cudaMemcpyAsync(rcount, p->cnt, NL * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    // the merge refreshes the offsets around the leaves it merged in place:
+    // ranges in rpre, chunks of long ranges in win (both free here)
+    BYO_TRY(ensure(ctx, p->win, ((g->n + 1) / kViewChunk + b + 64) * 8));
+    ViewOut view{(const uint64_t *)p->sep, g->n, g->d_off, rpre, (uint64_t *)p->win.p, ctr + 4};
     launch_t(ctx, "pma_merge", k_pma_merge_opt<true>, dim3(grid_for(ctx, b * 32, 32 * kOptWarps, 6)),
              dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
              (const uint64_t *)nullptr, seg, (const unsigned long long *)(ctr + 3), insert, rcount,
-             (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2), g->d_deg);
+             (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2), g->d_deg, view);
+    launch(ctx, k_pma_view_chunks, dim3(ctx->num_sms * 8), dim3(kViewThreads), 0, (const uint32_t *)p->src,
+           (const uint32_t *)p->cnt, (const uint64_t *)seg, (const uint64_t *)rpre, (const uint64_t *)p->win.p,
+           (const unsigned long long *)(ctr + 4), g->d_off, (const unsigned long long *)ctr, m_before,
+           shrink_below);
   } else {
     launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
            (const uint64_t *)batch, b, bstart);
@@ -1097,21 +1218,7 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
              dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
              (const uint64_t *)bstart, (uint64_t *)nullptr, (const unsigned long long *)nullptr, insert,
              rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2),
-             (uint32_t *)nullptr);
-  }
-  const double shrink_below = !insert && NL > 1 ? kRootMin * cap : -1.0;
-  if (list) {
-    // offsets of the vertices around the merged leaves, issued before the
-    // counters are read: the range kernel does nothing when the update
-    // overflowed or shrinks (rpre and win are free here)
-    BYO_TRY(ensure(ctx, p->win, ((g->n + 1) / kViewChunk + b + 64) * 8));
-    launch(ctx, k_pma_view_ranges, dim3(grid_for(ctx, b, 256, 8)), dim3(256), 0, (const uint32_t *)p->src,
-           (const uint32_t *)p->cnt, (const uint64_t *)p->sep, NL, g->n, (const uint64_t *)bstart,
-           (const unsigned long long *)(ctr + 3), (const uint64_t *)batch, rpre, (uint64_t *)p->win.p, ctr + 4,
-           (const unsigned long long *)ctr, m_before, shrink_below);
-    launch(ctx, k_pma_view_chunks, dim3(ctx->num_sms * 8), dim3(kViewThreads), 0, (const uint32_t *)p->src,
-           (const uint32_t *)p->cnt, (const uint64_t *)bstart, (const uint64_t *)rpre, (const uint64_t *)p->win.p,
-           (const unsigned long long *)(ctr + 4), g->d_off);
+             (uint32_t *)nullptr, ViewOut{});
   }
   BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 72, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1134,6 +1241,11 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     return pma_view(g);
   }
   // 4. overflow (or shrink): windows over the counts after the merge
+  if (list) {
+    BYO_CU(ctx, cudaMemcpyAsync(rcount, p->cnt, NL * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    launch(ctx, k_pma_seg_counts, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)bstart,
+           (const unsigned long long *)(ctr + 3), rcount);
+  }
   BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
   BYO_TRY(ensure(ctx, p->win, NL * 4));
   uint32_t *win = (uint32_t *)p->win.p;
