@@ -798,62 +798,104 @@ __global__ void k_pma_segments(const uint64_t *__restrict__ sep, uint64_t NL, co
   }
 }
 
-// One block sorts up to kSmallSort keys in shared memory (bitonic network
-// over the next power of two, padded with ~0) and reports the largest src
-// and dst in bounds[0], bounds[1].
+// One block of 1024 threads sorts up to kSmallSort keys (a bitonic network
+// over P = 1024 K keys, padded with ~0) and reports the largest src and dst
+// in bounds[0], bounds[1].  The keys live in registers: lane l of warp w holds
+// keys w*32K + 32k + l (k < K).  Compare-exchanges over a stride below 32 are
+// lane shuffles, strides from 32 to 32K - 1 pair registers of one thread, and
+// only the strides that cross warps go through shared memory.
 constexpr uint32_t kSmallSort = 4096;
+
+template <int K, int M>
+__device__ __forceinline__ void sort_regs_cx(uint64_t (&x)[K], uint32_t ibase, uint32_t size) {
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    if ((k & M) == 0 && (k | M) < K) {
+      const bool up = ((ibase + 32u * k) & size) == 0;
+      const uint64_t a = x[k], b = x[k | M];
+      const bool sw = (a > b) == up;
+      x[k] = sw ? b : a;
+      x[k | M] = sw ? a : b;
+    }
+  }
+}
+
+template <int K>
 __global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict__ in, uint32_t count, uint64_t *out,
                                                      unsigned long long *bounds) {
-  __shared__ uint64_t s[kSmallSort];
+  constexpr uint32_t P = 1024u * K, kWarpSpan = 32u * K;
+  __shared__ uint64_t s[P];
   __shared__ uint64_t red[2][32];
-  uint32_t P = 2;
-  while (P < count) P <<= 1;
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+  const uint32_t ibase = w * kWarpSpan + lane;
+  uint64_t x[K];
   uint64_t ms = 0, md = 0;
-  for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-    const uint64_t k = i < count ? in[i] : ~0ull;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const uint32_t i = ibase + 32u * k;
+    x[k] = i < count ? in[i] : ~0ull;
     if (i < count) {
-      ms = ms > (k >> 32) ? ms : (k >> 32);
-      md = md > (k & 0xFFFFFFFFull) ? md : (k & 0xFFFFFFFFull);
+      ms = ms > (x[k] >> 32) ? ms : (x[k] >> 32);
+      md = md > (x[k] & 0xFFFFFFFFull) ? md : (x[k] & 0xFFFFFFFFull);
     }
-    s[i] = k;
   }
-  __syncthreads();
-  // Pair t compares elements i = 2t - (t mod stride) and i + stride.  For
-  // stride <= 32 the pairs of one warp's t values lie in 64-element blocks
-  // that no other warp touches, so consecutive such passes need only a warp
-  // barrier; a pass with a wider stride, or followed by one, needs the block.
-  for (uint32_t size = 2; size <= P; size <<= 1)
-    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-      for (uint32_t t = threadIdx.x; t < P / 2; t += blockDim.x) {
-        const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
-        const bool up = (i & size) == 0;
-        const uint64_t a = s[i], b = s[j];
-        if ((a > b) == up) {
-          s[i] = b;
-          s[j] = a;
+  for (uint32_t size = 2; size <= P; size <<= 1) {
+    uint32_t stride = size >> 1;
+    if (stride >= kWarpSpan) {
+      __syncthreads();  // every warp has read back the previous round
+#pragma unroll
+      for (int k = 0; k < K; k++) s[ibase + 32u * k] = x[k];
+      __syncthreads();
+      for (; stride >= kWarpSpan; stride >>= 1) {
+        for (uint32_t t = threadIdx.x; t < P / 2; t += blockDim.x) {
+          const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
+          const bool up = (i & size) == 0;
+          const uint64_t a = s[i], b = s[j];
+          if ((a > b) == up) {
+            s[i] = b;
+            s[j] = a;
+          }
         }
+        __syncthreads();
       }
-      const uint32_t next = stride > 1 ? stride >> 1 : size;  // the next pass's stride
-      if (stride > 32 || next > 32) __syncthreads();
-      else __syncwarp();
+#pragma unroll
+      for (int k = 0; k < K; k++) x[k] = s[ibase + 32u * k];
     }
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) out[i] = s[i];
+    for (; stride >= 32; stride >>= 1) {
+      if (stride == 32) sort_regs_cx<K, 1>(x, ibase, size);
+      else sort_regs_cx<K, 2>(x, ibase, size);  // stride 64 < kWarpSpan: K == 4
+    }
+    for (; stride > 0; stride >>= 1) {
+      const bool lower = (lane & stride) == 0;
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const uint64_t y = __shfl_xor_sync(kFull, x[k], stride);
+        const bool up = ((ibase + 32u * k) & size) == 0;
+        const bool take_min = lower == up;
+        x[k] = take_min ? (x[k] < y ? x[k] : y) : (x[k] < y ? y : x[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    const uint32_t i = ibase + 32u * k;
+    if (i < count) out[i] = x[k];
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const uint64_t a = __shfl_xor_sync(kFull, ms, o), b = __shfl_xor_sync(kFull, md, o);
     ms = ms > a ? ms : a;
     md = md > b ? md : b;
   }
-  if (lane_id() == 0) {
-    red[0][threadIdx.x >> 5] = ms;
-    red[1][threadIdx.x >> 5] = md;
+  if (lane == 0) {
+    red[0][w] = ms;
+    red[1][w] = md;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (uint32_t w = 1; w < blockDim.x / 32; w++) {
-      ms = ms > red[0][w] ? ms : red[0][w];
-      md = md > red[1][w] ? md : red[1][w];
+    for (uint32_t v = 1; v < 32; v++) {
+      ms = ms > red[0][v] ? ms : red[0][v];
+      md = md > red[1][v] ? md : red[1][v];
     }
     bounds[0] = ms;
     bounds[1] = md;
@@ -1119,7 +1161,12 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   // validated: that sort does not index by key
   const bool small_sort = !sorted && count <= kSmallSort;
   if (small_sort) {
-    launch(ctx, k_sort_small, dim3(1), dim3(1024), 0, d_keys_in, (uint32_t)count, ka, bounds);
+    if (count <= 1024)
+      launch(ctx, k_sort_small<1>, dim3(1), dim3(1024), 0, d_keys_in, (uint32_t)count, ka, bounds);
+    else if (count <= 2048)
+      launch(ctx, k_sort_small<2>, dim3(1), dim3(1024), 0, d_keys_in, (uint32_t)count, ka, bounds);
+    else
+      launch(ctx, k_sort_small<4>, dim3(1), dim3(1024), 0, d_keys_in, (uint32_t)count, ka, bounds);
   } else {
     launch(ctx, k_key_bounds, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, bounds);
     if (sorted)
@@ -1207,10 +1254,6 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
              dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
              (const uint64_t *)nullptr, seg, (const unsigned long long *)(ctr + 3), insert, rcount,
              (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2), g->d_deg, view);
-    launch(ctx, k_pma_view_chunks, dim3(ctx->num_sms * 8), dim3(kViewThreads), 0, (const uint32_t *)p->src,
-           (const uint32_t *)p->cnt, (const uint64_t *)seg, (const uint64_t *)rpre, (const uint64_t *)p->win.p,
-           (const unsigned long long *)(ctr + 4), g->d_off, (const unsigned long long *)ctr, m_before,
-           shrink_below);
   } else {
     launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
            (const uint64_t *)batch, b, bstart);
@@ -1234,6 +1277,13 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   const bool shrink = (double)total < shrink_below;
   if (novf == 0 && !shrink) {
     if (list) {
+      // long ranges left by the merge (rare: keys far past a leaf's last key)
+      const uint64_t nch = hc[4];
+      if (nch)
+        launch(ctx, k_pma_view_chunks, dim3(grid_for(ctx, nch, 1, 8)), dim3(kViewThreads), 0,
+               (const uint32_t *)p->src, (const uint32_t *)p->cnt, (const uint64_t *)bstart,
+               (const uint64_t *)rpre, (const uint64_t *)p->win.p, (const unsigned long long *)(ctr + 4), g->d_off,
+               (const unsigned long long *)ctr, m_before, shrink_below);
       g->m = total;
       return check_launch(ctx, "pma_update");
     }
