@@ -2,7 +2,8 @@
 """Benchmark of the BYO hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dynamic|static] [--policy m20|learned|...]
+                    [--workload dynamic|static|mixed|multi|scale|families|map]
+                    [--policy m20|learned|...]
 
 Workloads (synthetic: seeded RMAT a=.57 b=.19 c=.19 d=.05, symmetrised,
 deduplicated, no self loops; the reference publishes no dataset for them):
@@ -14,6 +15,12 @@ deduplicated, no self loops; the reference publishes no dataset for them):
            Batch_insert_runner (benchmarks/run_unweighted.h:781-893), so the
            state seen by the traversals repeats exactly.
   static   the same RMAT graph in the CSR container; BFS + CC + PageRank.
+  mixed    64-source BFS groups interleaved with update batches (RMAT 2^24).
+  multi    64-source BFS groups only.
+  scale    RMAT 2^26 / 2^30 draws and ER 2^26: BFS, CC, PageRank precisions, TC.
+  families learned policy vs m/20 on RMAT, ER, a grid and Chung-Lu.
+  map      Test_Map and Test_Map_Remote (every remote width) on the dynamic
+           workload's graph, CSR and PMA.
 
 The metric is BASELINE's composite; `value` is the step's edge operations per
 second in G/s: BFS traversed edges (undirected, Graph500 convention) + CC
@@ -683,6 +690,134 @@ def run_multi(args, rank, world, local_rank):
     return res, ctx, G
 
 
+# ------------------------------------------------------------------ neighbour maps
+MAP_WIDTHS = (0, 1, 2, 4, 8, 16, 32)
+
+
+def map_remote_array(n, width, seed):
+    """Map_Remote_runner's array (run_unweighted.h:50-126): n zeros of `width`
+    bytes with one seeded random entry set to 1 (width 0: a bitmap)."""
+    one = int(np.random.default_rng(seed).integers(0, n))
+    if width == 0:
+        a = np.zeros((n + 63) // 64, np.uint64)
+        a[one >> 6] = np.uint64(1) << np.uint64(one & 63)
+    elif width <= 8:
+        a = np.zeros(n, {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[width])
+        a[one] = 1
+    else:
+        a = np.zeros((n, width // 8), np.uint64)
+        a[one, 0] = 1
+    return a
+
+
+def run_map(args, rank, world, local_rank):
+    """Map and Map_Remote (run_all's first applications, run_unweighted.h:
+    27-126, 943-957) on the dynamic workload's graph in both containers: one
+    step = Test_Map and Test_Map_Remote for every width, on the CSR and on the
+    PMA (its leaves scanned as they lie)."""
+    import torch
+    import byo_gb300 as byo
+    from byo_gb300 import _abi
+    L = _abi.lib()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = byo.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    graphs = [byo.Graph.generate(ctx, "rmat", seed=SEED, lg_n=LG_N, draws=DRAWS, container=c) for c in ("csr", "pma")]
+    n, m0 = graphs[0].N(), graphs[0].M()
+    remotes = {w: torch.from_numpy(map_remote_array(n, w, 100 + w).view(np.uint8).copy()).to(dev) for w in MAP_WIDTHS}
+    out = ctypes.c_uint64(0)
+    sums = {}
+
+    def step(record=False):
+        for G, name in zip(graphs, ("csr", "pma")):
+            _abi.check(L.byo_map_sum(G.h, ctypes.byref(out)), ctx.h)
+            if record:
+                sums[name + "/map"] = out.value
+            for w in MAP_WIDTHS:
+                _abi.check(L.byo_map_remote_device(G.h, remotes[w].data_ptr(), w, ctypes.byref(out)), ctx.h)
+                if record:
+                    sums["%s/remote%d" % (name, w)] = out.value
+
+    for i in range(args.warmup):
+        step(record=i == 0)
+    torch.cuda.synchronize()
+    ctx.kernel_timing("map")
+    launches0 = ctx.launches
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pushed = nvtx_push(torch, "timed")
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    nvtx_pop(torch, pushed)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    kl, kms = ctx.kernel_time("map")
+    ctx.kernel_timing(None)
+    # per kind: time of one launch (device) and its rate
+    per_kind = {}
+    for G, name in zip(graphs, ("csr", "pma")):
+        for w in (None,) + MAP_WIDTHS:
+            ctx.kernel_timing("map")
+            for _ in range(3):
+                if w is None:
+                    _abi.check(L.byo_map_sum(G.h, ctypes.byref(out)), ctx.h)
+                else:
+                    _abi.check(L.byo_map_remote_device(G.h, remotes[w].data_ptr(), w, ctypes.byref(out)), ctx.h)
+            cl, cms = ctx.kernel_time("map")
+            ctx.kernel_timing(None)
+            t = cms / max(cl, 1)
+            per_kind["%s/%s" % (name, "map" if w is None else "remote%d" % w)] = {
+                "ms": round(t, 4), "G_edges_s": round(G.M() / (t / 1e3) / 1e9, 1),
+                "slot_GBs": round(4 * G.nslots() / (t / 1e3) / 1e9, 1)}
+    peak, peak_kind = measured_peaks()
+    edges_per_step = sum(G.M() for G in graphs) * (1 + len(MAP_WIDTHS))
+    slot_bytes = sum(4 * G.nslots() for G in graphs) * (1 + len(MAP_WIDTHS))
+    per = kms / max(kl, 1)
+    avg_bytes = slot_bytes / max(kl / args.steps, 1)
+    res = {"metric": "Test_Map + Test_Map_Remote edges/s (run_all's Map applications)",
+           "value": edges_per_step * args.steps / (ms / 1e3) / 1e9, "unit": "G edges/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u32 ids, u64 sums", "data": "synthetic (seeded RMAT)",
+           "config": {"workload": "map: RMAT 2^%d, %d draws, CSR and PMA, widths %s" % (LG_N, DRAWS, list(MAP_WIDTHS)),
+                      "n": n, "m": m0, "per_kind": per_kind, "sums": sums},
+           "roofline": {"bound": "hbm", "kernel": "k_map_sum", "achieved": avg_bytes / (per / 1e3) / 1e9,
+                        "peak": peak, "unit": "GB/s", "frac": avg_bytes / (per / 1e3) / 1e9 / peak,
+                        "peak_source": peak_kind, "algorithmic_bytes_per_launch": avg_bytes, "avg_launch_ms": per,
+                        "traffic": None},
+           "gpu_launches": ctx.launches - launches0, "clocks": clk}
+    for G in graphs[1:]:
+        G.close()
+    return res, ctx, graphs[0]
+
+
+def map_cpu_sample():
+    """The oracle's Test_Map / Test_Map_Remote on the CSR of the same graph
+    (OpenMP, all host threads): one pass of each kind."""
+    O, off, nb, _ = cpu_setup(False)
+    n = len(off) - 1
+    remotes = {w: map_remote_array(n, w, 100 + w) for w in MAP_WIDTHS}
+    passes, secs = 0, 0.0
+    while secs < 3.0:  # whole passes, at least 3 s of CPU work
+        t0 = time.time()
+        for w in (None,) + MAP_WIDTHS:
+            if w is None:
+                O.map_sum(off, nb)
+            else:
+                O.map_remote(off, nb, remotes[w], w)
+        secs += time.time() - t0
+        passes += 1
+    m = len(nb)
+    return {"value": m * (1 + len(MAP_WIDTHS)) * passes / secs / 1e9, "unit": "G edges/s",
+            "cores": O.num_threads(), "kind": "port",
+            "sample": "%d passes of Test_Map and Test_Map_Remote per width on the CSR (oracle port, OpenMP, "
+                      "%d threads), %.1f s" % (passes, O.num_threads(), secs)}
+
+
 # ------------------------------------------------------------------ scale and graph families
 SCALE_GRAPHS = [
     ("rmat26", "RMAT 2^26, 2^30 draws (~2^31 directed)", dict(kind="rmat", seed=1, lg_n=26, draws=1 << 30)),
@@ -1032,7 +1167,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dynamic", choices=["dynamic", "static", "mixed", "multi", "scale", "families"])
+    ap.add_argument("--workload", default="dynamic",
+                    choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map"])
     ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
@@ -1059,6 +1195,16 @@ def main():
                               "e2e": {"value": cb["value"], "unit": MIXED_UNIT, "h2d_bytes_per_step": 0,
                                       "d2h_bytes_per_step": 0}}), flush=True)
             return 0
+        if args.workload == "map":
+            cb = map_cpu_sample()
+            print(json.dumps({"metric": "Test_Map + Test_Map_Remote edges/s (run_all's Map applications)",
+                              "value": cb["value"], "unit": cb["unit"], "n_gpus": 0, "steps": args.steps,
+                              "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
+                              "config": {"workload": "map (one pass per kind, CSR)"}, "cpu_baseline": cb,
+                              "data": "synthetic (seeded RMAT)",
+                              "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0,
+                                      "d2h_bytes_per_step": 0}}), flush=True)
+            return 0
         print(json.dumps(run_reference(args, dynamic)), flush=True)
         return 0
 
@@ -1072,6 +1218,11 @@ def main():
         res, ctx, G = run_mixed(args, rank, world, local_rank)
     elif args.workload == "multi":
         res, ctx, G = run_multi(args, rank, world, local_rank)
+        args.no_cpu_baseline = True
+    elif args.workload == "map":
+        res, ctx, G = run_map(args, rank, world, local_rank)
+        if rank == 0 and not args.no_cpu_baseline:
+            res["cpu_baseline"] = map_cpu_sample()
         args.no_cpu_baseline = True
     elif args.workload in ("scale", "families"):
         fn = run_scale if args.workload == "scale" else run_families

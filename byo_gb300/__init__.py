@@ -9,6 +9,7 @@ by byo_gb300.build); this package is the Python view of that ABI.
 from . import _abi  # noqa: F401
 from ._abi import ByoError  # noqa: F401
 from .graph import (BFS, BFS_F, BFS_multi, Context, Graph, PageRank, PageRank_edgeMap, PageRankDelta,  # noqa: F401
-                    SimpleUnionAsync, Triangle_degree_ordering, UINT_E_MAX, bfs_cc, edgeMap, vertexSubset)
+                    SimpleUnionAsync, Test_Map, Test_Map_Remote, Triangle_degree_ordering, UINT_E_MAX, bfs_cc,
+                    edgeMap, vertexSubset)
 
 __version__ = "0.1.0"

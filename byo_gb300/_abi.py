@@ -125,6 +125,9 @@ SIGNATURES = {
     "byo_pagerank_delta": (_int, [_vp, _dbl, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
     "byo_pagerank_delta_device": (_int, [_vp, _dbl, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
     "byo_triangle_count": (_int, [_vp, _P(_u64)]),
+    "byo_map_sum": (_int, [_vp, _P(_u64)]),
+    "byo_map_remote": (_int, [_vp, _vp, _u32, _P(_u64)]),
+    "byo_map_remote_device": (_int, [_vp, _vp, _u32, _P(_u64)]),
     "byo_functor_bfs_create": (_int, [_vp, _u32, _P(_vp)]),
     "byo_functor_bfs_parents": (_int, [_vp, _vp]),
     "byo_functor_destroy": (None, [_vp]),

@@ -415,6 +415,29 @@ int byo_triangle_count(byo_graph *g, uint64_t *count) {
   return tc_run(t, count);
 }
 
+// ---------------------------------------------------------------- neighbour maps
+
+int byo_map_sum(byo_graph *g, uint64_t *sum) {
+  if (!g || !sum) return BYO_EINVAL;
+  return map_run(g, -1, nullptr, sum);
+}
+
+int byo_map_remote_device(byo_graph *g, const void *d_remote, uint32_t width, uint64_t *sum) {
+  if (!g || !sum || (!d_remote && g->n)) return BYO_EINVAL;
+  return map_run(g, (int)width, d_remote, sum);
+}
+
+int byo_map_remote(byo_graph *g, const void *h_remote, uint32_t width, uint64_t *sum) {
+  if (!g || !sum || (!h_remote && g->n)) return BYO_EINVAL;
+  if (width > 32 || (width & (width - 1)))
+    return set_error(g->ctx, BYO_EINVAL, "map: remote width must be 0, 1, 2, 4, 8, 16 or 32");
+  const uint64_t bytes = map_remote_bytes(g->n, width);
+  uint64_t *d = nullptr;
+  BYO_TRY(ws(g, WS_TC_NBR, bytes / 8 + 1, &d));
+  if (bytes) BYO_CU(g->ctx, cudaMemcpyAsync(d, h_remote, bytes, cudaMemcpyHostToDevice, g->ctx->stream));
+  return map_run(g, (int)width, d, sum);
+}
+
 // ---------------------------------------------------------------- edgeMap API
 
 int byo_functor_bfs_create(byo_graph *g, uint32_t src, byo_functor **out) {

@@ -229,6 +229,8 @@ int bfs_cc_run(byo_graph *g, uint32_t *d_label);
 int pagerank_run(byo_graph *g, double eps, uint32_t max_iters, int precision, double *d_p,
                  uint32_t *iters, double *l1);
 int tc_run(byo_graph *g, uint64_t *count);
+int map_run(byo_graph *g, int width, const void *d_remote, uint64_t *sum);
+uint64_t map_remote_bytes(uint64_t n, uint32_t width);
 
 // ---------------------------------------------------------------- PMA (pma.cu)
 int pma_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);

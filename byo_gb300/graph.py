@@ -403,6 +403,27 @@ def PageRankDelta(G, eps=1e-6, local_eps=0.01, max_iters=100, info=False):
     return (p, r.value, l1.value) if info else p
 
 
+def Test_Map(G):
+    """Test_Map (benchmarks/Map/Base/Map.h:8-18): sum of every edge's destination."""
+    c = ctypes.c_uint64(0)
+    check(lib().byo_map_sum(G.h, ctypes.byref(c)), G.ctx.h)
+    return int(c.value)
+
+
+def Test_Map_Remote(G, remote, width):
+    """Test_Map_Remote (benchmarks/Map/RemoteRead/Map.h:21-33): sum over every
+    edge (u, v) of remote[v].  `remote` holds n elements of `width` bytes
+    (0: a bitmap of uint64 words, least significant bit first; 16, 32: a
+    uint64 at the start of each element), as a host array or a CUDA tensor."""
+    c = ctypes.c_uint64(0)
+    if hasattr(remote, "data_ptr"):
+        check(lib().byo_map_remote_device(G.h, remote.data_ptr(), width, ctypes.byref(c)), G.ctx.h)
+    else:
+        buf = np.ascontiguousarray(remote)
+        check(lib().byo_map_remote(G.h, buf.ctypes.data_as(ctypes.c_void_p), width, ctypes.byref(c)), G.ctx.h)
+    return int(c.value)
+
+
 def Triangle_degree_ordering(G):
     c = ctypes.c_uint64(0)
     check(lib().byo_triangle_count(G.h, ctypes.byref(c)), G.ctx.h)

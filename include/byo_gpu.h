@@ -263,6 +263,21 @@ int byo_pagerank_delta_device(byo_graph *g, double eps, double local_eps, uint32
  * (benchmarks/TriangleCounting/ShunTangwongsan15/Triangle.h:167-204). */
 int byo_triangle_count(byo_graph *g, uint64_t *count);
 
+/* ------------------------------------------------------------------ neighbour maps
+ * Test_Map (benchmarks/Map/Base/Map.h:8-18): the sum over every edge (u, v)
+ * of v, by one scan of the container's own slots (a PMA's leaves as they lie,
+ * gaps skipped). */
+int byo_map_sum(byo_graph *g, uint64_t *sum);
+/* Test_Map_Remote (benchmarks/Map/RemoteRead/Map.h:21-33, as run by
+ * Map_Remote_runner<G, W>, benchmarks/run_unweighted.h:50-126): the sum over
+ * every edge (u, v) of remote[v], remote an n-entry array of `width`-byte
+ * elements.  width 0: a bitmap, bit v of 64-bit word v/64 (std::vector<bool>
+ * packs least significant bit first); 1, 2, 4, 8: unsigned integers; 16, 32:
+ * an unsigned 64-bit value at the start of each element (wide_int<size_t, W>).
+ * byo_map_remote copies h_remote (host) in; the _device form reads d_remote. */
+int byo_map_remote(byo_graph *g, const void *h_remote, uint32_t width, uint64_t *sum);
+int byo_map_remote_device(byo_graph *g, const void *d_remote, uint32_t width, uint64_t *sum);
+
 /* ------------------------------------------------------------------ edgeMap API
  * vertexSubset (gbbs/vertex_subset.h:202-371) and edgeMap
  * (gbbs/edge_map_data.h:254-315) over device functors.  The functor set is

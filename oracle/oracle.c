@@ -566,6 +566,36 @@ void orc_pagerank_delta(uint64_t n, const uint64_t *offsets, const uint32_t *nbr
   free(next);
 }
 
+/* Map.h:8-18 and RemoteRead/Map.h:21-33: a parallel_for over vertices, each
+ * summing over its neighbours, combined by a Reducer_sum<size_t>. */
+uint64_t orc_map_sum(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs) {
+  uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : total)
+  for (int64_t i = 0; i < (int64_t)n; i++)
+    for (uint64_t e = offsets[i]; e < offsets[i + 1]; e++) total += nbrs[e];
+  return total;
+}
+
+static uint64_t remote_at(const unsigned char *r, uint32_t width, uint32_t v) {
+  switch (width) {
+    case 0: return (((const uint64_t *)r)[v >> 6] >> (v & 63)) & 1u;
+    case 1: return r[v];
+    case 2: return ((const uint16_t *)r)[v];
+    case 4: return ((const uint32_t *)r)[v];
+    default: return *(const uint64_t *)(r + (uint64_t)v * width);
+  }
+}
+
+uint64_t orc_map_remote(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, const void *remote,
+                        uint32_t width) {
+  const unsigned char *r = (const unsigned char *)remote;
+  uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : total)
+  for (int64_t i = 0; i < (int64_t)n; i++)
+    for (uint64_t e = offsets[i]; e < offsets[i + 1]; e++) total += remote_at(r, width, nbrs[e]);
+  return total;
+}
+
 /* ------------------------------------------------------------------ triangles */
 
 uint64_t orc_triangle_count(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs) {

@@ -125,6 +125,16 @@ void orc_pagerank(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, dou
 void orc_pagerank_delta(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, double eps, double local_eps,
                         uint32_t max_iters, double *p, uint32_t *rounds_out, double *l1_out);
 
+/* Test_Map (benchmarks/Map/Base/Map.h:8-18): sum over every edge of its
+ * destination id.  Test_Map_Remote (benchmarks/Map/RemoteRead/Map.h:21-33):
+ * sum over every edge (u, v) of remote[v], remote an n-entry array of
+ * `width`-byte elements (0: bitmap of 64-bit words, least significant bit
+ * first; 1, 2, 4, 8: unsigned integers; 16, 32: a uint64 at the start of the
+ * element). */
+uint64_t orc_map_sum(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs);
+uint64_t orc_map_remote(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, const void *remote,
+                        uint32_t width);
+
 /* Triangle counting, degree ordering (benchmarks/TriangleCounting/
  * ShunTangwongsan15/Triangle.h:57-68,99-150,167-204): rank by (degree, id),
  * orient u->v when rank[u] < rank[v], count |N+(u) cap N+(v)| over DAG edges by

@@ -62,6 +62,8 @@ def lib():
             "orc_pagerank_delta": (None, [_c.c_uint64, _u64p, _u32p, _c.c_double, _c.c_double, _c.c_uint32,
                                           _f64p, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_double)]),
             "orc_triangle_count": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p]),
+            "orc_map_sum": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p]),
+            "orc_map_remote": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p, _c.c_void_p, _c.c_uint32]),
             "orc_store_create": (_c.c_void_p, [_c.c_uint64, _u64p, _u32p]),
             "orc_store_destroy": (None, [_c.c_void_p]),
             "orc_store_num_edges": (_c.c_uint64, [_c.c_void_p]),
@@ -187,6 +189,17 @@ def pagerank_delta(offsets, nbrs, eps=1e-6, local_eps=0.01, max_iters=100):
     lib().orc_pagerank_delta(n, _u64(offsets), _u32(nbrs), eps, local_eps, max_iters, p, ctypes.byref(r),
                              ctypes.byref(l1))
     return p, r.value, l1.value
+
+
+def map_sum(offsets, nbrs):
+    n = len(offsets) - 1
+    return int(lib().orc_map_sum(n, _u64(offsets), _u32(nbrs)))
+
+
+def map_remote(offsets, nbrs, remote, width):
+    n = len(offsets) - 1
+    buf = np.ascontiguousarray(remote)
+    return int(lib().orc_map_remote(n, _u64(offsets), _u32(nbrs), buf.ctypes.data_as(ctypes.c_void_p), width))
 
 
 def triangle_count(offsets, nbrs):

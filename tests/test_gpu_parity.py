@@ -338,3 +338,59 @@ def test_triangle_count_paths(ctx, oracle_mod):
             G.set_tuning(tc_stage=stage)
             assert byo.Triangle_degree_ordering(G) == want, (cont, stage)
         G.close()
+
+
+def _remote_arrays(n, rng):
+    """A remote array per width, as Map_Remote_runner builds them
+    (run_unweighted.h:50-126: zeros with one random entry set) plus a random one."""
+    out = {}
+    for w in (0, 1, 2, 4, 8, 16, 32):
+        one = int(rng.integers(0, n))
+        if w == 0:
+            bits = np.zeros(n, bool)
+            bits[one] = True
+            rnd = rng.integers(0, 2, size=n).astype(bool)
+            pack = lambda b: np.concatenate([np.packbits(b, bitorder="little"),  # noqa: E731
+                                             np.zeros((-((n + 7) // 8)) % 8, np.uint8)]).view(np.uint64)
+            out[w] = [pack(bits), pack(rnd)]
+        elif w <= 8:
+            dt = {1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[w]
+            a = np.zeros(n, dt)
+            a[one] = 1
+            out[w] = [a, rng.integers(0, 250, size=n).astype(dt)]
+        else:
+            a = np.zeros((n, w // 8), np.uint64)
+            a[one, 0] = 1
+            b = np.full((n, w // 8), 3, np.uint64)  # padding words are not read
+            b[:, 0] = rng.integers(0, 1 << 40, size=n)
+            out[w] = [a, b]
+    return out
+
+
+@pytest.mark.gpu
+def test_map_benchmarks(ctx, oracle_mod):
+    """Test_Map and Test_Map_Remote (every width) equal the oracle on a CSR and
+    on a PMA (scanned with its gaps, before and after a batch), from host and
+    device remote arrays."""
+    import torch
+    import byo_gb300 as byo
+    O = oracle_mod
+    rng = np.random.default_rng(12)
+    G1 = byo.Graph.generate(ctx, "rmat", seed=41, lg_n=15, draws=1 << 19)
+    G2 = byo.Graph.generate(ctx, "rmat", seed=42, lg_n=14, draws=1 << 18, container="pma")
+    for G in (G1, G2):
+        for step in range(2):
+            if step == 1 and G is G2:
+                pairs = rng.integers(0, G.N(), size=(5000, 2))
+                G.insert_batch(O.keys_from_pairs(pairs[:, 0], pairs[:, 1]))
+            off, nb = G.export_csr()
+            assert byo.Test_Map(G) == O.map_sum(off, nb)
+            for w, arrs in _remote_arrays(G.N(), rng).items():
+                for a in arrs:
+                    exp = O.map_remote(off, nb, a, w)
+                    assert byo.Test_Map_Remote(G, a, w) == exp, (w,)
+                    t = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()).cuda()
+                    assert byo.Test_Map_Remote(G, t, w) == exp, (w, "device")
+        with pytest.raises(byo.ByoError):
+            byo.Test_Map_Remote(G, np.zeros(G.N(), np.uint32), 3)
+        G.close()

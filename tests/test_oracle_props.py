@@ -168,3 +168,27 @@ def test_pagerank_delta_restatements_agree(oracle_mod, eps, leps):
     # it approaches PageRank's fixed point only loosely (round-one decreases
     # never propagate), but every vertex with edges moved away from 0
     assert np.all(p > 0)
+
+
+def test_map_restatement(oracle_mod):
+    """Test_Map / Test_Map_Remote in the oracle equal a numpy gather-and-sum
+    for every remote element width, bitmap included."""
+    O = oracle_mod
+    s, d = O.rmat_edges(3, 10, 1 << 13)
+    off, nb = O.build_csr(1 << 10, s, d)
+    n = len(off) - 1
+    assert O.map_sum(off, nb) == int(nb.astype(np.uint64).sum())
+    rng = np.random.default_rng(1)
+    for w in (0, 1, 2, 4, 8, 16, 32):
+        if w == 0:
+            bits = rng.integers(0, 2, size=n).astype(bool)
+            words = np.packbits(bits, bitorder="little")
+            words = np.concatenate([words, np.zeros((-len(words)) % 8, np.uint8)]).view(np.uint64)
+            assert O.map_remote(off, nb, words, 0) == int(bits[nb].sum())
+        elif w <= 8:
+            r = rng.integers(0, 200, size=n).astype({1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[w])
+            assert O.map_remote(off, nb, r, w) == int(r[nb].astype(np.uint64).sum())
+        else:
+            r = np.full((n, w // 8), 7, np.uint64)
+            r[:, 0] = rng.integers(0, 1000, size=n)
+            assert O.map_remote(off, nb, r, w) == int(r[nb, 0].sum())
