@@ -539,21 +539,24 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       if (A[mid] <= bval(B, d0 - mid - 1)) lo = mid + 1; else hi = mid;
     }
     const uint64_t i0 = lo, j0 = d0 - lo;
+    // The walk along the diagonal band, without branches: each step takes
+    // the smaller head (A first on ties), and keeps it by the rule above;
+    // lastA / lastB are the A and B elements before the heads (~0: none, no
+    // key equals it).
+    const uint64_t lastA0 = i0 > 0 ? A[i0 - 1] : ~0ull, lastB0 = j0 > 0 ? bval(B, j0 - 1) : ~0ull;
     // pass 1: count kept elements
     uint32_t keep = 0;
     {
-      uint64_t i = i0, k = j0;
+      uint64_t i = i0, k = j0, lastA = lastA0, lastB = lastB0;
       for (uint64_t d = d0; d < d1; d++) {
-        if (i < ca && (k >= nb || A[i] <= bval(B, k))) {
-          const uint64_t x = A[i];
-          if (insert) keep++;
-          else if (!(k < nb && bval(B, k) == x)) keep++;
-          i++;
-        } else {
-          const uint64_t x = bval(B, k);
-          if (insert && !(i > 0 && A[i - 1] == x) && !(k > 0 && bval(B, k - 1) == x)) keep++;
-          k++;
-        }
+        const uint64_t a = i < ca ? A[i] : ~0ull, bk = k < nb ? bval(B, k) : ~0ull;
+        const bool takeA = i < ca && a <= bk;
+        const uint64_t x = takeA ? a : bk;
+        keep += insert ? (takeA || (x != lastA && x != lastB)) : (takeA && bk != a);
+        lastA = takeA ? a : lastA;
+        lastB = takeA ? lastB : bk;
+        i += takeA;
+        k += !takeA;
       }
     }
     const uint32_t incl = warp_inclusive_scan(keep);
@@ -577,21 +580,18 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
     }
     __syncwarp();  // every lane has read A before any in-place write
     {
-      uint64_t i = i0, k = j0;
+      uint64_t i = i0, k = j0, lastA = lastA0, lastB = lastB0;
       for (uint64_t d = d0; d < d1; d++) {
-        uint64_t x;
-        bool kept;
-        if (i < ca && (k >= nb || A[i] <= bval(B, k))) {
-          x = A[i];
-          kept = insert || !(k < nb && bval(B, k) == x);
-          if (deg && !kept) atomicAdd(deg + (x >> 32), 0xFFFFFFFFu);  // -1
-          i++;
-        } else {
-          x = bval(B, k);
-          kept = insert && !(i > 0 && A[i - 1] == x) && !(k > 0 && bval(B, k - 1) == x);
-          if (deg && kept) atomicAdd(deg + (x >> 32), 1u);
-          k++;
-        }
+        const uint64_t a = i < ca ? A[i] : ~0ull, bk = k < nb ? bval(B, k) : ~0ull;
+        const bool takeA = i < ca && a <= bk;
+        const uint64_t x = takeA ? a : bk;
+        const bool kept = insert ? (takeA || (x != lastA && x != lastB)) : (takeA && bk != a);
+        if (deg && takeA != kept)  // a key left (A dropped) or entered (B kept)
+          atomicAdd(deg + (x >> 32), takeA ? 0xFFFFFFFFu : 1u);
+        lastA = takeA ? a : lastA;
+        lastB = takeA ? lastB : bk;
+        i += takeA;
+        k += !takeA;
         if (kept) {
           if (ostage) {
             ostage[pos] = x;

@@ -14,8 +14,8 @@
 // Neighbour maps run on the host over a mirror of the device adjacency that is
 // refreshed after every update, so any GBBS algorithm still works; the hot
 // algorithms run on the GPU through the free functions gpu_bfs, gpu_bfs_multi,
-// gpu_cc, gpu_bfs_cc, gpu_pagerank, gpu_pagerank_delta and
-// gpu_triangle_count.
+// gpu_cc, gpu_bfs_cc, gpu_pagerank, gpu_pagerank_delta, gpu_triangle_count,
+// gpu_map and gpu_map_remote.
 //
 // Errors from the C ABI throw byo::Error (the reference aborts instead).
 #pragma once
@@ -235,6 +235,21 @@ inline uint64_t gpu_triangle_count(const detail::DeviceGraph &G) {
   uint64_t c = 0;
   Context::get().check(byo_triangle_count(G.handle(), &c), "triangle_count");
   return c;
+}
+// Test_Map (benchmarks/Map/Base/Map.h:8-18).
+inline uint64_t gpu_map(const detail::DeviceGraph &G) {
+  uint64_t s = 0;
+  Context::get().check(byo_map_sum(G.handle(), &s), "map");
+  return s;
+}
+// Test_Map_Remote (benchmarks/Map/RemoteRead/Map.h:21-33) over a host array of
+// W-byte elements (W = 1, 2, 4, 8; wider elements through byo_map_remote).
+template <class T>
+inline uint64_t gpu_map_remote(const detail::DeviceGraph &G, const std::vector<T> &remote) {
+  static_assert(sizeof(T) <= 8 && (sizeof(T) & (sizeof(T) - 1)) == 0, "1, 2, 4 or 8-byte elements");
+  uint64_t s = 0;
+  Context::get().check(byo_map_remote(G.handle(), remote.data(), (uint32_t)sizeof(T), &s), "map_remote");
+  return s;
 }
 // delta::PageRankDelta (PageRank.h:340-398).
 inline std::vector<double> gpu_pagerank_delta(const detail::DeviceGraph &G, double eps = 1e-6, double local_eps = 0.01,

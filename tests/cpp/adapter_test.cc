@@ -56,6 +56,11 @@ int main() {
   auto prd = byo::gpu_pagerank_delta(csr);
   CHECK(prd.size() == n && prd[3] > 0);
   CHECK((byo::gpu_bfs_cc(csr) == lab));
+  // edge destination sum: 1+0+3+2+4+5+3+5+3+4+6+5 = 41; remote[3] = 1 counts 3's in-edges
+  CHECK(byo::gpu_map(csr) == 41);
+  std::vector<uint16_t> remote(n, 0);
+  remote[3] = 1;
+  CHECK(byo::gpu_map_remote(csr, remote) == 3);
   // levels from 2 and 0 in one traversal
   auto lv = byo::gpu_bfs_multi(csr, {2, 0});
   CHECK((std::vector<uint32_t>(lv.begin(), lv.begin() + n) == std::vector<uint32_t>{X, X, 0, 1, 2, 2, 3}));
