@@ -297,6 +297,7 @@ __global__ void k_bucket_scatter(const uint64_t *__restrict__ keys, uint64_t cou
 // no shared memory.  Buckets are padded with ~0 to R*32 keys; buckets above
 // kWarpBucket keys are listed for the LSD fallback.
 constexpr uint32_t kWarpBucket = 512;
+constexpr uint64_t kTwoLevelMin = 1ull << 21;  // batches from this size take the two-level sort
 
 template <int R>
 __device__ __forceinline__ void warp_bitonic(uint64_t (&v)[R]) {
@@ -371,8 +372,298 @@ __global__ void __launch_bounds__(256) k_bucket_sort(const uint64_t *__restrict_
   }
 }
 
+// ---------------------------------------------------------------- two-level batch sort
+// For batches of millions of keys the bucketed sort's scatter (one returning
+// atomic and one random 8-byte write per key) dominates.  Two levels instead:
+//   1. coarse bins by the top C bits of src (2^C <= kBins, ~10K keys each):
+//      a global histogram (block-aggregated), then each CTA partitions a
+//      tile of kBinTile keys by bin in shared memory, reserves one run per
+//      bin with a single returning atomic, and writes the runs with
+//      consecutive stores;
+//   2. one CTA per bin: a counting sort in shared memory by the next 10 key
+//      bits (fine buckets of ~10 keys), then a warp per fine bucket sorts it
+//      in registers (warp_bitonic) and writes it out.
+// Bins above kBinCap keys and fine buckets above kWarpBucket keys (skewed
+// batches) are listed and sorted afterwards by the LSD sort on their range.
+constexpr int kBinThreads = 1024;
+constexpr uint32_t kBins = 2048;
+constexpr uint32_t kBinTile = 8192;
+constexpr uint32_t kBinPer = 12;                      // keys per thread in the per-bin sort
+constexpr uint32_t kBinCap = kBinPer * 1024;          // keys of one coarse bin sorted in shared memory
+constexpr uint32_t kFine = 4096;  // fine buckets per bin (12 bits)
+constexpr uint32_t kRankMax = 64;  // fine buckets sorted by counting ranks
+
+__device__ __forceinline__ uint32_t coarse_bin(uint64_t key, int shift, uint32_t nbins) {
+  const uint64_t b = key >> shift;
+  return b < nbins ? (uint32_t)b : nbins - 1;
+}
+
+__global__ void __launch_bounds__(kBinThreads) k_bin_hist(const uint64_t *__restrict__ keys, uint64_t count,
+                                                          int shift, uint32_t nbins, unsigned int *gcnt) {
+  __shared__ unsigned int h[kBins];
+  for (uint32_t i = threadIdx.x; i < nbins; i += kBinThreads) h[i] = 0;
+  __syncthreads();
+  for (uint64_t i = blockIdx.x * (uint64_t)kBinThreads + threadIdx.x; i < count;
+       i += (uint64_t)gridDim.x * kBinThreads)
+    atomicAdd(&h[coarse_bin(__ldg(keys + i), shift, nbins)], 1u);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < nbins; i += kBinThreads)
+    if (h[i]) atomicAdd(&gcnt[i], h[i]);
+}
+
+__global__ void __launch_bounds__(kBinThreads) k_bin_scatter(const uint64_t *__restrict__ keys, uint64_t count,
+                                                             int shift, uint32_t nbins,
+                                                             const uint64_t *__restrict__ gstart,
+                                                             unsigned int *gcursor, uint64_t *out) {
+  extern __shared__ unsigned long long bin_smem[];
+  uint64_t *S = reinterpret_cast<uint64_t *>(bin_smem);  // kBinTile keys grouped by bin
+  uint64_t *base = S + kBinTile;                          // [nbins] where the tile's run of a bin starts in out
+  unsigned int *cnt = reinterpret_cast<unsigned int *>(base + kBins);  // [nbins]
+  unsigned int *off = cnt + kBins;                                      // [nbins + 1] exclusive prefix
+  __shared__ unsigned int wsum[kBinThreads / 32];
+  constexpr uint32_t kPer = kBinTile / kBinThreads;
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  for (uint64_t t0 = (uint64_t)blockIdx.x * kBinTile; t0 < count; t0 += (uint64_t)gridDim.x * kBinTile) {
+    const uint32_t tn = (uint32_t)(count - t0 < kBinTile ? count - t0 : kBinTile);
+    for (uint32_t i = threadIdx.x; i < nbins; i += kBinThreads) cnt[i] = 0;
+    __syncthreads();
+    uint64_t k[kPer];
+    uint32_t rank[kPer];
+#pragma unroll
+    for (uint32_t q = 0; q < kPer; q++) {
+      const uint32_t i = q * kBinThreads + threadIdx.x;
+      k[q] = i < tn ? __ldcs(keys + t0 + i) : 0;
+      rank[q] = i < tn ? atomicAdd(&cnt[coarse_bin(k[q], shift, nbins)], 1u) : 0;
+    }
+    __syncthreads();
+    // exclusive prefix over the bins: two bins per thread, then a block scan
+    {
+      const uint32_t b0 = 2 * threadIdx.x;
+      const uint32_t c0 = b0 < nbins ? cnt[b0] : 0, c1 = b0 + 1 < nbins ? cnt[b0 + 1] : 0;
+      const uint32_t v = c0 + c1;
+      uint32_t inc = warp_inclusive_scan(v);
+      if (lane == 31) wsum[warp] = inc;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t w = wsum[lane];
+        const uint32_t wi = warp_inclusive_scan(w);
+        wsum[lane] = wi - w;
+      }
+      __syncthreads();
+      const uint32_t ex = wsum[warp] + inc - v;
+      if (b0 < nbins) off[b0] = ex;
+      if (b0 + 1 < nbins) off[b0 + 1] = ex + c0;
+      if (threadIdx.x == 0) off[nbins] = tn;
+    }
+    // one run per bin in the output
+    for (uint32_t b = threadIdx.x; b < nbins; b += kBinThreads)
+      if (cnt[b]) base[b] = gstart[b] + atomicAdd(&gcursor[b], cnt[b]);
+    __syncthreads();
+#pragma unroll
+    for (uint32_t q = 0; q < kPer; q++) {
+      const uint32_t i = q * kBinThreads + threadIdx.x;
+      if (i < tn) S[off[coarse_bin(k[q], shift, nbins)] + rank[q]] = k[q];
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < tn; i += kBinThreads) {
+      const uint64_t x = S[i];
+      const uint32_t b = coarse_bin(x, shift, nbins);
+      out[base[b] + (i - off[b])] = x;
+    }
+    __syncthreads();
+  }
+}
+
+// One CTA per coarse bin.  Fine buckets by the next kFineBits bits of the
+// significant key sig = src << lg | dst (2 lg bits; coarse bins are its top C
+// bits), shifted down by fsh.
+__device__ __forceinline__ uint32_t fine_digit(uint64_t x, int lg, int fsh) {
+  const uint64_t sig = ((x >> 32) << lg) | (x & 0xFFFFFFFFull);
+  return (uint32_t)(sig >> fsh) & (kFine - 1);
+}
+
+__global__ void __launch_bounds__(kBinThreads) k_bin_sort(const uint64_t *__restrict__ in, uint64_t *out,
+                                                          const uint64_t *__restrict__ gstart, uint32_t nbins,
+                                                          int lg, int fsh, unsigned long long *large,
+                                                          unsigned int *nlarge) {
+  extern __shared__ unsigned long long bin_smem[];
+  uint64_t *S = reinterpret_cast<uint64_t *>(bin_smem);               // [kBinCap]
+  unsigned int *fcnt = reinterpret_cast<unsigned int *>(S + kBinCap);  // [kFine]
+  unsigned int *foff = fcnt + kFine;                                   // [kFine + 1]
+  __shared__ unsigned int wsum[kBinThreads / 32];
+  __shared__ unsigned int big[kBinCap / (kRankMax + 1) + 1], nbig;
+  constexpr uint32_t kPerT = kFine / kBinThreads;  // fine counters per thread in the scan
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+  for (uint32_t bin = blockIdx.x; bin < nbins; bin += gridDim.x) {
+    const uint64_t s0 = gstart[bin], sz = gstart[bin + 1] - s0;
+    if (sz == 0) continue;
+    if (sz > kBinCap) {  // copied unsorted, sorted afterwards on its range
+      for (uint64_t i = threadIdx.x; i < sz; i += kBinThreads) out[s0 + i] = in[s0 + i];
+      if (threadIdx.x == 0) {
+        const unsigned int at = atomicAdd(nlarge, 1u);
+        large[2 * at] = s0;
+        large[2 * at + 1] = sz;
+      }
+      continue;
+    }
+    const uint32_t n32 = (uint32_t)sz;
+    // the bin's keys in registers, all loads in flight at once
+    uint64_t kx[kBinPer];
+#pragma unroll
+    for (uint32_t q = 0; q < kBinPer; q++) {
+      const uint32_t i = q * kBinThreads + threadIdx.x;
+      kx[q] = i < n32 ? __ldcs(in + s0 + i) : 0;
+    }
+#pragma unroll
+    for (uint32_t t = 0; t < kPerT; t++) fcnt[t * kBinThreads + threadIdx.x] = 0;
+    if (threadIdx.x == 0) nbig = 0;
+    __syncthreads();
+#pragma unroll
+    for (uint32_t q = 0; q < kBinPer; q++)
+      if (q * kBinThreads + threadIdx.x < n32) atomicAdd(&fcnt[fine_digit(kx[q], lg, fsh)], 1u);
+    __syncthreads();
+    {  // exclusive prefix: kPerT consecutive counters per thread, then a block scan
+      uint32_t c[kPerT], v = 0;
+#pragma unroll
+      for (uint32_t t = 0; t < kPerT; t++) {
+        c[t] = fcnt[threadIdx.x * kPerT + t];
+        v += c[t];
+      }
+      const uint32_t inc = warp_inclusive_scan(v);
+      if (lane == 31) wsum[warp] = inc;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t w = wsum[lane];
+        wsum[lane] = warp_inclusive_scan(w) - w;
+      }
+      __syncthreads();
+      uint32_t ex = wsum[warp] + inc - v;
+#pragma unroll
+      for (uint32_t t = 0; t < kPerT; t++) {
+        const uint32_t f = threadIdx.x * kPerT + t;
+        foff[f] = ex;
+        fcnt[f] = 0;  // reused as the fill cursor
+        if (c[t] > kRankMax) big[atomicAdd(&nbig, 1u)] = f;
+        ex += c[t];
+      }
+      if (threadIdx.x == 0) foff[kFine] = n32;
+    }
+    __syncthreads();
+#pragma unroll
+    for (uint32_t q = 0; q < kBinPer; q++) {
+      if (q * kBinThreads + threadIdx.x >= n32) continue;
+      const uint64_t x = kx[q];
+      const uint32_t f = fine_digit(x, lg, fsh);
+      S[foff[f] + atomicAdd(&fcnt[f], 1u)] = x;
+    }
+    __syncthreads();
+    // fine buckets of up to kRankMax keys (nearly all): every key counts the
+    // keys of its bucket that go before it (ties by position) and writes
+    // itself at that rank
+    for (uint32_t i = threadIdx.x; i < n32; i += kBinThreads) {
+      const uint64_t x = S[i];
+      const uint32_t f = fine_digit(x, lg, fsh);
+      const uint32_t lo = foff[f], hi = foff[f + 1];
+      if (hi - lo > kRankMax) continue;
+      uint32_t r = 0;
+      for (uint32_t q = lo; q < hi; q++) {
+        const uint64_t y = S[q];
+        r += (y < x) | ((y == x) & (q < i));
+      }
+      out[s0 + lo + r] = x;
+    }
+    // larger ones: a warp each
+    for (uint32_t t = warp; t < nbig; t += kBinThreads / 32) {
+      const uint32_t f = big[t];
+      const uint32_t lo = foff[f], fs = foff[f + 1] - lo;
+      if (fs > kWarpBucket) {  // copied unsorted, sorted afterwards on its range
+        for (uint32_t i = lane; i < fs; i += 32) out[s0 + lo + i] = S[lo + i];
+        if (lane == 0) {
+          const unsigned int at = atomicAdd(nlarge, 1u);
+          large[2 * at] = s0 + lo;
+          large[2 * at + 1] = fs;
+        }
+        continue;
+      }
+      const uint64_t *src = S + lo;
+      uint64_t *dst = out + s0 + lo;
+      if (fs <= 128) {
+        uint64_t v[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) v[r] = r * 32 + lane < fs ? src[r * 32 + lane] : ~0ull;
+        warp_bitonic<4>(v);
+#pragma unroll
+        for (int r = 0; r < 4; r++)
+          if (r * 32 + lane < fs) dst[r * 32 + lane] = v[r];
+      } else {
+        uint64_t v[16];
+#pragma unroll
+        for (int r = 0; r < 16; r++) v[r] = r * 32 + lane < fs ? src[r * 32 + lane] : ~0ull;
+        warp_bitonic<16>(v);
+#pragma unroll
+        for (int r = 0; r < 16; r++)
+          if (r * 32 + lane < fs) dst[r * 32 + lane] = v[r];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+int sort_two_level(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t n, uint64_t *out, uint64_t *tmp) {
+  int lg = 0;
+  while ((1ull << lg) < n) lg++;
+  // about 8K keys per coarse bin (at most kBins bins)
+  int C = 1;
+  while (C < 11 && C < lg && (count >> C) > 8192) C++;
+  const uint32_t nbins = 1u << C;
+  const int shift = 32 + lg - C;
+  const int fsh = 2 * lg - C - 12 > 0 ? 2 * lg - C - 12 : 0;  // fine digit: the next 12 bits of src << lg | dst
+  // one scratch buffer (slot 6; the scan below uses slot 7): bin starts
+  // [nbins + 1], the list of ranges left for the LSD sort, then 32-bit bin
+  // counts, cursors and the list length
+  uint64_t *gstart = nullptr;
+  const uint64_t nlist = 2 * (count / kWarpBucket + nbins + 1);
+  BYO_TRY(scratch(ctx, 6, (uint64_t)nbins + 1 + nlist + nbins + 4, &gstart));
+  unsigned long long *large = reinterpret_cast<unsigned long long *>(gstart + nbins + 1);
+  unsigned int *gcnt = reinterpret_cast<unsigned int *>(gstart + nbins + 1 + nlist);
+  unsigned int *gcursor = gcnt + nbins, *nlarge = gcnt + 2 * nbins;
+  BYO_CU(ctx, cudaMemsetAsync(gcnt, 0, (2 * (uint64_t)nbins + 8) * 4, ctx->stream));
+  launch(ctx, k_bin_hist, dim3(grid_for(ctx, count, kBinThreads, 2)), dim3(kBinThreads), 0, in, count, shift, nbins,
+         gcnt);
+  BYO_TRY(scan_u32_to_u64(ctx, gcnt, nbins, gstart));
+  const size_t smem1 = (kBinTile + kBins) * 8 + (2 * kBins + 1) * 4;
+  const size_t smem2 = kBinCap * 8 + (2 * kFine + 1) * 4;
+  BYO_CU(ctx, cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1));
+  BYO_CU(ctx, cudaFuncSetAttribute(k_bin_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
+  const uint64_t tiles = (count + kBinTile - 1) / kBinTile;
+  launch_t(ctx, "sort_scatter", k_bin_scatter, dim3((unsigned)std::min<uint64_t>(tiles, 2ull * ctx->num_sms)),
+           dim3(kBinThreads), smem1, in, count, shift, nbins, (const uint64_t *)gstart, gcursor, tmp);
+  launch_t(ctx, "sort_bins", k_bin_sort, dim3(std::min<uint32_t>(nbins, 2u * ctx->num_sms)), dim3(kBinThreads),
+           smem2, (const uint64_t *)tmp, out, (const uint64_t *)gstart, nbins, lg, fsh, large, nlarge);
+  BYO_TRY(check_launch(ctx, "sort_two_level"));
+  unsigned int *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, nlarge, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned int nl = h[0];
+  if (nl) {
+    // skewed ranges, already in place in out: the LSD sort (it reuses
+    // scratch 4 and 5) on each, tmp's range as its second buffer
+    std::vector<unsigned long long> ranges(2 * (size_t)nl);
+    BYO_CU(ctx, cudaMemcpy(ranges.data(), large, 16ull * nl, cudaMemcpyDeviceToHost));
+    for (unsigned int q = 0; q < nl; q++) {
+      const uint64_t lo = ranges[2 * q], sz = ranges[2 * q + 1];
+      uint64_t *res = nullptr;
+      BYO_TRY(sort_u64(ctx, out + lo, tmp + lo, sz, sig_mask_for(n), &res));
+      if (res != out + lo) BYO_CU(ctx, cudaMemcpyAsync(out + lo, res, sz * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+  }
+  return check_launch(ctx, "sort_two_level");
+}
+
 int sort_bucketed(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t n, uint64_t *out, uint64_t *tmp) {
   if (count == 0) return BYO_OK;
+  if (count >= kTwoLevelMin) return sort_two_level(ctx, in, count, n, out, tmp);
   int lg = 0;
   while ((1ull << lg) < n) lg++;
   // about 24 keys per bucket: most buckets sort in one or two registers a lane

@@ -195,3 +195,37 @@ def test_large_batches(ctx, oracle_mod):
     assert G.insert_batch(skew) == st.insert_batch(skew)
     ro, rn = st.export_csr()
     _check_view(byo, O, G, ro, rn, (5,))
+
+
+@pytest.mark.gpu
+def test_two_level_sort_batches(ctx, oracle_mod):
+    """Batches of more than 2^21 keys take the two-level sort (coarse bins of
+    src, then a shared-memory sort per bin): a uniform batch, and a skewed one
+    with a bin above the shared-memory capacity and sources with more than 512
+    keys (both sorted afterwards on their ranges)."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 20
+    n = 1 << lg
+    G = byo.Graph.generate(ctx, "rmat", seed=8, lg_n=lg, draws=1 << 21, container="pma")
+    s, d = O.rmat_edges(8, lg, 1 << 21)
+    off, nb = O.build_csr(n, s, d)
+    st = O.Store(off, nb)
+    us, ud = O.uniform_pairs(301, n, 1_200_000)
+    keys = O.keys_from_pairs(us, ud)
+    assert len(keys) > (1 << 21)
+    assert G.insert_batch(keys) == st.insert_batch(keys)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (10,))
+    rng = np.random.default_rng(4)
+    # 16000 pairs with src < 4096 (one coarse bin) and two sources with 2000 keys each
+    ls = rng.integers(0, 4096, 16000)
+    ld = rng.integers(0, n, 16000)
+    hub = np.concatenate([np.full(2000, 7), np.full(2000, 3000)])
+    hd = np.concatenate([rng.choice(n, 2000, replace=False), rng.choice(n, 2000, replace=False)])
+    skew = O.keys_from_pairs(np.concatenate([us[:1_100_000], ls, hub]), np.concatenate([ud[:1_100_000], ld, hd]))
+    assert G.remove_batch(skew) == st.remove_batch(skew)
+    assert G.insert_batch(skew) == st.insert_batch(skew)
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (5,))
+    G.close()
