@@ -441,11 +441,11 @@ __device__ __forceinline__ void view_refresh_warp(const uint32_t *src, const uin
 
 // ---------------------------------------------------------------- optimistic merge
 // One warp per leaf with a batch segment.  The leaf (A) and, when short, the
-// segment (B) are staged in the warp's shared memory.  The merged sequence of
-// A and B (ties: A first) is cut into 32 equal diagonals (merge path, one
-// binary search per lane); each lane walks its diagonal twice: once to count
-// the elements it keeps, then -- after a warp scan -- to write them at their
-// final positions.
+// segment (B) are staged in the warp's shared memory.  The result's size is
+// counted first; then the merged sequence of A and B (ties: A first) is
+// produced 32 positions per round, a lane per position found on the merge
+// path, and the kept keys are packed by a ballot and written with
+// consecutive stores.
 //   insert keeps every A, and B[j] unless it equals the A element before it
 //   or the B element before it (B may hold duplicates: it is sorted, not
 //   deduplicated);
@@ -530,38 +530,23 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
     if (nb <= kOptSeg)
       for (uint32_t k = lane; k < nb; k += 32) Bsh[w][k] = keys[b0 + k];
     __syncwarp();
-    // this lane's diagonal [d0, d1) of the merged sequence
-    const uint64_t T = ca + nb, per = (T + 31) / 32;
-    const uint64_t d0 = lane * per < T ? lane * per : T, d1 = d0 + per < T ? d0 + per : T;
-    uint64_t lo = d0 > nb ? d0 - nb : 0, hi = d0 < ca ? d0 : ca;
-    while (lo < hi) {  // number of A elements among the first d0 merged
-      const uint64_t mid = (lo + hi) >> 1;
-      if (A[mid] <= bval(B, d0 - mid - 1)) lo = mid + 1; else hi = mid;
-    }
-    const uint64_t i0 = lo, j0 = d0 - lo;
-    // The walk along the diagonal band, without branches: each step takes
-    // the smaller head (A first on ties), and keeps it by the rule above;
-    // lastA / lastB are the A and B elements before the heads (~0: none, no
-    // key equals it).
-    const uint64_t lastA0 = i0 > 0 ? A[i0 - 1] : ~0ull, lastB0 = j0 > 0 ? bval(B, j0 - 1) : ~0ull;
-    // pass 1: count kept elements
-    uint32_t keep = 0;
-    {
-      uint64_t i = i0, k = j0, lastA = lastA0, lastB = lastB0;
-      for (uint64_t d = d0; d < d1; d++) {
-        const uint64_t a = i < ca ? A[i] : ~0ull, bk = k < nb ? bval(B, k) : ~0ull;
-        const bool takeA = i < ca && a <= bk;
-        const uint64_t x = takeA ? a : bk;
-        keep += insert ? (takeA || (x != lastA && x != lastB)) : (takeA && bk != a);
-        lastA = takeA ? a : lastA;
-        lastB = takeA ? lastB : bk;
-        i += takeA;
-        k += !takeA;
+    // The result's size first: the batch keys that are dropped (insert: equal
+    // to the key before them in B or present in A; remove: present in A,
+    // counted once) by one binary search of each batch key in A.
+    uint32_t drops = 0;
+    for (uint32_t t = lane; t < nb; t += 32) {
+      const uint64_t x = bval(B, t);
+      const bool dup = t > 0 && bval(B, t - 1) == x;
+      uint32_t l = 0, h = ca;
+      while (l < h) {
+        const uint32_t mid = (l + h) >> 1;
+        if (A[mid] < x) l = mid + 1; else h = mid;
       }
+      const bool found = l < ca && A[l] == x;
+      drops += insert ? (dup || found) : (!dup && found);
     }
-    const uint32_t incl = warp_inclusive_scan(keep);
-    const uint32_t r = s + __shfl_sync(kFull, incl, 31);
-    uint32_t pos = incl - keep;
+    drops = warp_sum(drops);
+    const uint32_t r = s + (insert ? ca + (uint32_t)nb - drops : ca - drops);
     uint32_t *osrc = nullptr, *odst = nullptr;
     uint64_t *ostage = nullptr;
     if (r <= kLeaf) {
@@ -578,30 +563,48 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       for (uint32_t e = lane; e < s; e += 32) ovf[at + e] = slot_key(src, dst, base + e);
       ostage = ovf + at + s;
     }
-    __syncwarp();  // every lane has read A before any in-place write
-    {
-      uint64_t i = i0, k = j0, lastA = lastA0, lastB = lastB0;
-      for (uint64_t d = d0; d < d1; d++) {
-        const uint64_t a = i < ca ? A[i] : ~0ull, bk = k < nb ? bval(B, k) : ~0ull;
+    // The merged sequence 32 positions at a time, a lane per position: the
+    // lane finds its position's split (i A and k B keys before it) on the
+    // merge path -- within 32 of its split one round earlier -- takes the
+    // smaller head (A first on ties) and keeps it by the rule above; a ballot
+    // then packs the kept keys, so the warp writes them with consecutive
+    // stores.  A and B are in shared memory, so writing the leaf in place is
+    // safe.
+    const uint32_t T = ca + (uint32_t)nb, nb32 = (uint32_t)nb;
+    uint32_t wpos = 0, split = 0;
+    for (uint32_t c0 = 0; c0 < T; c0 += 32) {
+      const uint32_t d = c0 + lane;
+      bool kept = false;
+      uint64_t x = 0;
+      if (d < T) {
+        uint32_t lo = d > nb32 ? d - nb32 : 0, hi = d < ca ? d : ca;
+        lo = lo > split ? lo : split;
+        hi = hi < split + 32 ? hi : split + 32;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (A[mid] <= bval(B, d - mid - 1)) lo = mid + 1; else hi = mid;
+        }
+        split = lo;
+        const uint32_t i = lo, k = d - lo;
+        const uint64_t a = i < ca ? A[i] : ~0ull, bk = k < nb32 ? bval(B, k) : ~0ull;
         const bool takeA = i < ca && a <= bk;
-        const uint64_t x = takeA ? a : bk;
-        const bool kept = insert ? (takeA || (x != lastA && x != lastB)) : (takeA && bk != a);
+        x = takeA ? a : bk;
+        const uint64_t lastA = i > 0 ? A[i - 1] : ~0ull, lastB = k > 0 ? bval(B, k - 1) : ~0ull;
+        kept = insert ? (takeA || (x != lastA && x != lastB)) : (takeA && bk != a);
         if (deg && takeA != kept)  // a key left (A dropped) or entered (B kept)
           atomicAdd(deg + (x >> 32), takeA ? 0xFFFFFFFFu : 1u);
-        lastA = takeA ? a : lastA;
-        lastB = takeA ? lastB : bk;
-        i += takeA;
-        k += !takeA;
-        if (kept) {
-          if (ostage) {
-            ostage[pos] = x;
-          } else {
-            osrc[pos] = (uint32_t)(x >> 32);
-            odst[pos] = (uint32_t)x;
-          }
-          pos++;
+      }
+      const unsigned m = __ballot_sync(kFull, kept);
+      const uint32_t p = wpos + __popc(m & lanemask_lt());
+      if (kept && s + p < r) {  // never past the counted size (the counts agree)
+        if (ostage) {
+          ostage[p] = x;
+        } else {
+          osrc[p] = (uint32_t)(x >> 32);
+          odst[p] = (uint32_t)x;
         }
       }
+      wpos += __popc(m);
     }
     if (!ostage) {
       for (uint32_t t = r + lane; t < c; t += 32) {
