@@ -65,6 +65,7 @@ struct Pma {
   DevBuf misc;            // flags / counters
   DevBuf epre;            // uint64[NL+1] element prefix for the view
   DevBuf ovf, ovf_off;    // overflow area of the optimistic merge, per-leaf offsets
+  DevBuf vrange, vchunks; // view rebuild: vertex range per leaf, chunks of the long ranges
   uint64_t rebuilds = 0, windows = 0;
 };
 
@@ -372,36 +373,14 @@ constexpr uint32_t kViewChunk = 1024, kViewThreads = 256, kViewWarpMax = 1u << 1
 
 __device__ __forceinline__ uint64_t ceil_src(uint64_t key) { return (key >> 32) + ((key & 0xFFFFFFFFull) != 0); }
 
-// The warp's part for merged leaf j (c keys now, old_last the src of its last
-// key before the merge or 0xFFFFFFFF if it was empty) and segment q.
-__device__ __forceinline__ void view_refresh_warp(const uint32_t *src, const uint64_t *__restrict__ sep, uint64_t NL,
-                                                  uint64_t n, uint64_t j, uint32_t c, uint32_t old_last,
-                                                  uint64_t smin, uint64_t smax, uint32_t *Y, uint64_t *off,
-                                                  uint64_t q, uint64_t *vrange, uint64_t *chunks,
-                                                  unsigned long long *nchunks) {
+// The offsets of vertices [a, e) of leaf j (c keys, src list ls): a warp
+// stages the src list in Y and fills the range as a merge of the vertex
+// sequence with it, each lane taking one diagonal band of the merge path.
+// off[v] = the leaf position of the first key with src >= v, or the next
+// leaf's start when there is none.
+__device__ __forceinline__ void leaf_fill_warp(const uint32_t *ls, uint32_t c, uint64_t a, uint64_t e, uint64_t j,
+                                               uint32_t *Y, uint64_t *off) {
   const unsigned lane = lane_id();
-  const uint32_t *ls = src + j * kLeaf;
-  const uint64_t vlo = j == 0 ? 0 : min(ceil_src(sep[j]), n + 1);
-  const uint64_t vhi = j + 1 == NL ? n + 1 : min(ceil_src(sep[j + 1]), n + 1);
-  const bool had = old_last != 0xFFFFFFFFu, has = c != 0;
-  const uint64_t new_last = has ? ls[c - 1] : 0;
-  // L + 1 and U + 1 with "no keys" as vlo - 1
-  const uint64_t l1 = !had || !has ? vlo : min((uint64_t)old_last, new_last) + 1;
-  uint64_t u1 = smax + 1;
-  if (had) u1 = max(u1, (uint64_t)old_last + 1);
-  if (has) u1 = max(u1, new_last + 1);
-  const uint64_t a = max(vlo, min(smin, l1)), e = max(a, min(vhi, u1));
-  if (e - a > kViewWarpMax) {
-    if (lane == 0) {
-      vrange[2 * q] = a;
-      vrange[2 * q + 1] = e;
-      const uint64_t nch = (e - a + kViewChunk - 1) / kViewChunk;
-      const uint64_t at = atomicAdd(nchunks, (unsigned long long)nch);
-      for (uint64_t t = 0; t < nch; t++) chunks[at + t] = q << 32 | t;
-    }
-    return;
-  }
-  if (e == a) return;
   for (uint32_t i = lane; i < c; i += 32) Y[i] = ls[i];
   __syncwarp();
   // keys with src in [a, e): positions [p0, p1)
@@ -438,6 +417,40 @@ __device__ __forceinline__ void view_refresh_warp(const uint32_t *src, const uin
     }
   }
 }
+
+// The warp's part for merged leaf j (c keys now, old_last the src of its last
+// key before the merge or 0xFFFFFFFF if it was empty) and segment q.
+__device__ __forceinline__ void view_refresh_warp(const uint32_t *src, const uint64_t *__restrict__ sep, uint64_t NL,
+                                                  uint64_t n, uint64_t j, uint32_t c, uint32_t old_last,
+                                                  uint64_t smin, uint64_t smax, uint32_t *Y, uint64_t *off,
+                                                  uint64_t q, uint64_t *vrange, uint64_t *chunks,
+                                                  unsigned long long *nchunks) {
+  const unsigned lane = lane_id();
+  const uint32_t *ls = src + j * kLeaf;
+  const uint64_t vlo = j == 0 ? 0 : min(ceil_src(sep[j]), n + 1);
+  const uint64_t vhi = j + 1 == NL ? n + 1 : min(ceil_src(sep[j + 1]), n + 1);
+  const bool had = old_last != 0xFFFFFFFFu, has = c != 0;
+  const uint64_t new_last = has ? ls[c - 1] : 0;
+  // L + 1 and U + 1 with "no keys" as vlo - 1
+  const uint64_t l1 = !had || !has ? vlo : min((uint64_t)old_last, new_last) + 1;
+  uint64_t u1 = smax + 1;
+  if (had) u1 = max(u1, (uint64_t)old_last + 1);
+  if (has) u1 = max(u1, new_last + 1);
+  const uint64_t a = max(vlo, min(smin, l1)), e = max(a, min(vhi, u1));
+  if (e - a > kViewWarpMax) {
+    if (lane == 0) {
+      vrange[2 * q] = a;
+      vrange[2 * q + 1] = e;
+      const uint64_t nch = (e - a + kViewChunk - 1) / kViewChunk;
+      const uint64_t at = atomicAdd(nchunks, (unsigned long long)nch);
+      for (uint64_t t = 0; t < nch; t++) chunks[at + t] = q << 32 | t;
+    }
+    return;
+  }
+  if (e == a) return;
+  leaf_fill_warp(ls, c, a, e, j, Y, off);
+}
+
 
 // ---------------------------------------------------------------- optimistic merge
 // One warp per leaf with a batch segment.  The leaf (A) and, when short, the
@@ -709,30 +722,6 @@ __global__ void __launch_bounds__(kPmaBlock) k_pma_spread(const uint64_t *__rest
 
 // ---------------------------------------------------------------- graph view
 
-// off[v] = slot of the first key >= (v,0) in the leaf (v,0) routes to, or the
-// start of the next leaf when that leaf has no such key; elem[v] = number of
-// keys < (v,0); for v in [0, n]
-__global__ void k_pma_view(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
-                           const uint64_t *__restrict__ sep, const uint64_t *__restrict__ epre, uint64_t NL,
-                           uint64_t n, uint64_t *off, uint64_t *elem) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v <= n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t key = v << 32;
-    const uint64_t i = route(sep, NL, key);
-    const uint32_t c = cnt[i];
-    uint32_t lo = 0, hi = c;
-    while (lo < hi) {
-      uint32_t mid = (lo + hi) >> 1;
-      if (src[i * kLeaf + mid] < (uint32_t)v) lo = mid + 1; else hi = mid;
-    }
-    // every key of leaf i is >= sep[i]; keys < (v,0) in leaf i are a prefix.
-    // A vertex past the leaf's last key starts at the next leaf: its (empty)
-    // range then does not depend on how many keys leaf i holds
-    off[v] = lo < c ? i * kLeaf + lo : (i + 1) * kLeaf;
-    elem[v] = epre[i] + lo;
-  }
-}
-
 __global__ void k_pma_deg(const uint64_t *__restrict__ elem, uint64_t n, uint32_t *deg) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x)
@@ -910,19 +899,22 @@ __global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict_
 // memory and each thread fills kViewChunk / kViewThreads vertices a block
 // width apart, each by its own binary search.  Nothing to do when a leaf
 // overflowed or the update shrinks: the windowed path rebuilds the whole view.
+// seg null: chunk q is of leaf q (the full view, which also writes
+// elem[v] = epre[leaf] + position); ctr null: no overflow check.
 __global__ void __launch_bounds__(kViewThreads)
     k_pma_view_chunks(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
                       const uint64_t *__restrict__ seg, const uint64_t *__restrict__ range,
                       const uint64_t *__restrict__ chunks, const unsigned long long *nchunks, uint64_t *off,
-                      const unsigned long long *ctr, uint64_t m_before, double shrink_below) {
+                      const unsigned long long *ctr, uint64_t m_before, double shrink_below,
+                      const uint64_t *__restrict__ epre, uint64_t *elem) {
   __shared__ uint32_t Y[kLeaf];
-  if (ctr[1] || (double)((long long)m_before + (long long)ctr[2]) < shrink_below) return;
+  if (ctr && (ctr[1] || (double)((long long)m_before + (long long)ctr[2]) < shrink_below)) return;
   const uint64_t nc = *nchunks;
   constexpr uint32_t kPer = kViewChunk / kViewThreads;
   for (uint64_t i = blockIdx.x; i < nc; i += gridDim.x) {
     const uint64_t ch = chunks[i];
     const uint64_t q = ch >> 32, t = ch & 0xFFFFFFFFull;
-    const uint64_t j = seg[2 * q] & 0xFFFFFFFFull;
+    const uint64_t j = seg ? seg[2 * q] & 0xFFFFFFFFull : q;
     const uint64_t e = range[2 * q + 1];
     const uint64_t v0 = range[2 * q] + t * kViewChunk + threadIdx.x;
     const uint32_t c = cnt[j];
@@ -939,6 +931,54 @@ __global__ void __launch_bounds__(kViewThreads)
         if (Y[mid] < v) lo = mid + 1; else hi = mid;
       }
       off[v] = lo < c ? j * kLeaf + lo : (j + 1) * kLeaf;
+      if (elem) elem[v] = epre[j] + lo;
+    }
+  }
+}
+
+// The whole view: a warp per leaf fills its vertex range [ceil(sep[j] /
+// 2^32), ceil(sep[j+1] / 2^32)) (the ranges of all leaves cover [0, n]),
+// 32 vertices per round, a lane per vertex with a binary search in the leaf
+// (its lines shared by the warp in L1) that starts where the lane's previous
+// vertex ended; ranges above kViewWarpMax vertices go to the chunk list.
+constexpr int kViewWarps = 8;
+__global__ void __launch_bounds__(32 * kViewWarps)
+    k_pma_view_leaves(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
+                      const uint64_t *__restrict__ sep, const uint64_t *__restrict__ epre, uint64_t NL, uint64_t n,
+                      uint64_t *off, uint64_t *elem, uint64_t *range, uint64_t *chunks,
+                      unsigned long long *nchunks) {
+  const unsigned lane = lane_id();
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    const uint64_t vlo = j == 0 ? 0 : min(ceil_src(sep[j]), n + 1);
+    const uint64_t vhi = j + 1 == NL ? n + 1 : min(ceil_src(sep[j + 1]), n + 1);
+    if (vhi - vlo > kViewWarpMax) {
+      if (lane == 0) {
+        range[2 * j] = vlo;
+        range[2 * j + 1] = vhi;
+        const uint64_t nch = (vhi - vlo + kViewChunk - 1) / kViewChunk;
+        const uint64_t at = atomicAdd(nchunks, (unsigned long long)nch);
+        for (uint64_t t = 0; t < nch; t++) chunks[at + t] = j << 32 | t;
+      }
+      continue;
+    }
+    if (vhi == vlo) continue;
+    const uint32_t c = cnt[j];
+    const uint32_t *ls = src + j * kLeaf;
+    const uint64_t eb = epre[j], base = j * kLeaf, next = (j + 1) * kLeaf;
+    uint32_t from = 0;
+    for (uint64_t v0 = vlo; v0 < vhi; v0 += 32) {
+      const uint64_t v = v0 + lane;
+      if (v >= vhi) break;
+      uint32_t lo = from, hi = c;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(ls + mid) < v) lo = mid + 1; else hi = mid;
+      }
+      from = lo;
+      off[v] = lo < c ? base + lo : next;
+      elem[v] = eb + lo;
     }
   }
 }
@@ -1015,14 +1055,26 @@ static int pma_view(byo_graph *g) {
   epre = (uint64_t *)p->epre.p;
   BYO_TRY(scan_u32_to_u64(ctx, p->cnt, p->NL, epre));
   BYO_TRY(ws(g, WS_SCAN, g->n + 2, &elem));
-  launch(ctx, k_pma_view, dim3(grid_for(ctx, g->n + 1, 256)), dim3(256), 0, (const uint32_t *)p->src,
-         (const uint32_t *)p->cnt, (const uint64_t *)p->sep, (const uint64_t *)epre, p->NL, g->n, g->d_off, elem);
-  launch(ctx, k_pma_deg, dim3(grid_for(ctx, g->n, 256)), dim3(256), 0, (const uint64_t *)elem, g->n, g->d_deg);
+  BYO_TRY(ensure(ctx, p->vrange, 2 * p->NL * 8));
+  BYO_TRY(ensure(ctx, p->vchunks, ((g->n + 1) / kViewChunk + p->NL + 1) * 8 + 8));
+  unsigned long long *nch = reinterpret_cast<unsigned long long *>(p->vchunks.p);
+  uint64_t *chunks = reinterpret_cast<uint64_t *>(p->vchunks.p) + 1;
+  BYO_CU(ctx, cudaMemsetAsync(nch, 0, 8, ctx->stream));
+  launch_t(ctx, "pma_view", k_pma_view_leaves, dim3(grid_for(ctx, p->NL * 32, 32 * kViewWarps, 8)), dim3(32 * kViewWarps), 0,
+         (const uint32_t *)p->src, (const uint32_t *)p->cnt, (const uint64_t *)p->sep, (const uint64_t *)epre, p->NL,
+         g->n, g->d_off, elem, (uint64_t *)p->vrange.p, chunks, nch);
   uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
   BYO_CU(ctx, cudaMemcpyAsync(h, epre + p->NL, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaMemcpyAsync(h + 1, nch, 8, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   g->m = h[0];
+  if (h[1])
+    launch_t(ctx, "pma_view", k_pma_view_chunks, dim3(grid_for(ctx, h[1], 1, 8)), dim3(kViewThreads), 0, (const uint32_t *)p->src,
+           (const uint32_t *)p->cnt, (const uint64_t *)nullptr, (const uint64_t *)p->vrange.p,
+           (const uint64_t *)chunks, (const unsigned long long *)nch, g->d_off, (const unsigned long long *)nullptr,
+           (uint64_t)0, 0.0, (const uint64_t *)epre, elem);
+  launch(ctx, k_pma_deg, dim3(grid_for(ctx, g->n, 256)), dim3(256), 0, (const uint64_t *)elem, g->n, g->d_deg);
   g->d_slots = p->dst;
   g->nslots = p->NL * kLeaf;
   return check_launch(ctx, "pma_view");
@@ -1063,7 +1115,7 @@ void pma_destroy(Pma *p) {
   if (!p) return;
   pma_free_arrays(p);
   for (DevBuf *b : {&p->keys_a, &p->keys_b, &p->bstart, &p->rcount, &p->rpre, &p->win, &p->marks, &p->staging,
-                    &p->misc, &p->epre, &p->ovf, &p->ovf_off})
+                    &p->misc, &p->epre, &p->ovf, &p->ovf_off, &p->vrange, &p->vchunks})
     free_buf(*b);
   delete p;
 }
@@ -1286,7 +1338,8 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
         launch(ctx, k_pma_view_chunks, dim3(grid_for(ctx, nch, 1, 8)), dim3(kViewThreads), 0,
                (const uint32_t *)p->src, (const uint32_t *)p->cnt, (const uint64_t *)bstart,
                (const uint64_t *)rpre, (const uint64_t *)p->win.p, (const unsigned long long *)(ctr + 4), g->d_off,
-               (const unsigned long long *)ctr, m_before, shrink_below);
+               (const unsigned long long *)ctr, m_before, shrink_below, (const uint64_t *)nullptr,
+               (uint64_t *)nullptr);
       g->m = total;
       return check_launch(ctx, "pma_update");
     }
