@@ -21,6 +21,8 @@ deduplicated, no self loops; the reference publishes no dataset for them):
   families learned policy vs m/20 on RMAT, ER, a grid and Chung-Lu.
   map      Test_Map and Test_Map_Remote (every remote width) on the dynamic
            workload's graph, CSR and PMA.
+  bytepd   the dynamic workload's graph in the byte-PD compressed format,
+           decoded into a CSR on the GPU.
 
 The metric is BASELINE's composite; `value` is the step's edge operations per
 second in G/s: BFS traversed edges (undirected, Graph500 convention) + CC
@@ -818,6 +820,74 @@ def map_cpu_sample():
                       "%d threads), %.1f s" % (passes, O.num_threads(), secs)}
 
 
+# ------------------------------------------------------------------ byte-PD graphs
+def run_bytepd(args, rank, world, local_rank):
+    """Compressed graphs (gbbs/encodings/byte_pd_amortized.h): the dynamic
+    workload's graph encoded on the GPU, then one step = decoding the byte-PD
+    arrays (host memory, as read from a file) into a CSR on the GPU."""
+    import torch
+    import byo_gb300 as byo
+    torch.cuda.set_device(local_rank)
+    ctx = byo.Context(local_rank)
+    G = byo.Graph.generate(ctx, "rmat", seed=SEED, lg_n=LG_N, draws=DRAWS)
+    n, m = G.N(), G.M()
+    ctx.kernel_timing("bytepd_encode")
+    bo, dg, data = G.to_bytepd(1000)
+    _, enc_ms = ctx.kernel_time("bytepd_encode")
+    ctx.kernel_timing(None)
+    enc_ms /= 2  # to_bytepd encodes twice (size query, then the bytes)
+    for _ in range(args.warmup):
+        byo.Graph.from_bytepd(ctx, bo, dg, data).close()
+    ctx.kernel_timing("bytepd_decode")
+    launches0 = ctx.launches
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    pushed = nvtx_push(torch, "timed")
+    t0 = time.time()
+    for _ in range(args.steps):
+        H = byo.Graph.from_bytepd(ctx, bo, dg, data)
+        H.close()
+    wall = (time.time() - t0) / args.steps
+    nvtx_pop(torch, pushed)
+    clk = clocks.stop()
+    kl, kms = ctx.kernel_time("bytepd_decode")
+    ctx.kernel_timing(None)
+    per = kms / args.steps  # the decode kernels of one step
+    peak, peak_kind = measured_peaks()
+    nbytes = len(data)
+    alg = nbytes + 4 * m + 8 * (n + 1) * 2 + 4 * n  # bytes read, ids written, offsets and degrees
+    res = {"metric": "byte-PD decode edges/s (compressed neighbour lists to CSR on the GPU)",
+           "value": m / (per / 1e3) / 1e9, "unit": "G edges/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": per, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "u8 varints -> u32 ids", "data": "synthetic (seeded RMAT)",
+           "config": {"workload": "byte-PD: RMAT 2^%d, %d draws, block 1000" % (LG_N, DRAWS), "n": n, "m": m,
+                      "compressed_bytes": nbytes, "bytes_per_edge": nbytes / max(m, 1),
+                      "encode_ms": enc_ms, "decode_ms": per,
+                      "note": "value: decode kernel time; e2e: host arrays to a finished CSR graph"},
+           "roofline": {"bound": "hbm", "kernel": "k_bpd_decode", "achieved": alg / (per / 1e3) / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": alg / (per / 1e3) / 1e9 / peak, "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": alg, "avg_launch_ms": per, "traffic": None},
+           "e2e": {"value": m / wall / 1e9, "unit": "G edges/s", "h2d_bytes_per_step": int(nbytes + bo.nbytes + dg.nbytes),
+                   "d2h_bytes_per_step": 0, "ms_per_step": wall * 1e3},
+           "gpu_launches": ctx.launches - launches0, "clocks": clk}
+    return res, ctx, G
+
+
+def bytepd_cpu_sample():
+    """The oracle's decode of the same arrays (OpenMP, all host threads)."""
+    O, off, nb, _ = cpu_setup(False)
+    bo, dg, data = O.bytepd_encode(off, nb, 1000)
+    passes, secs = 0, 0.0
+    while secs < 3.0:
+        t0 = time.time()
+        O.bytepd_decode(bo, dg, data, 1000)
+        secs += time.time() - t0
+        passes += 1
+    return {"value": len(nb) * passes / secs / 1e9, "unit": "G edges/s", "cores": O.num_threads(), "kind": "port",
+            "sample": "%d decodes of the same byte-PD arrays (oracle port, OpenMP, %d threads), %.1f s"
+                      % (passes, O.num_threads(), secs)}
+
+
 # ------------------------------------------------------------------ scale and graph families
 SCALE_GRAPHS = [
     ("rmat26", "RMAT 2^26, 2^30 draws (~2^31 directed)", dict(kind="rmat", seed=1, lg_n=26, draws=1 << 30)),
@@ -1168,7 +1238,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dynamic",
-                    choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map"])
+                    choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map", "bytepd"])
     ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
@@ -1195,12 +1265,14 @@ def main():
                               "e2e": {"value": cb["value"], "unit": MIXED_UNIT, "h2d_bytes_per_step": 0,
                                       "d2h_bytes_per_step": 0}}), flush=True)
             return 0
-        if args.workload == "map":
-            cb = map_cpu_sample()
-            print(json.dumps({"metric": "Test_Map + Test_Map_Remote edges/s (run_all's Map applications)",
+        if args.workload in ("map", "bytepd"):
+            cb = map_cpu_sample() if args.workload == "map" else bytepd_cpu_sample()
+            metric = ("Test_Map + Test_Map_Remote edges/s (run_all's Map applications)" if args.workload == "map"
+                      else "byte-PD decode edges/s (compressed neighbour lists to CSR on the GPU)")
+            print(json.dumps({"metric": metric,
                               "value": cb["value"], "unit": cb["unit"], "n_gpus": 0, "steps": args.steps,
                               "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
-                              "config": {"workload": "map (one pass per kind, CSR)"}, "cpu_baseline": cb,
+                              "config": {"workload": args.workload + " (bounded sample)"}, "cpu_baseline": cb,
                               "data": "synthetic (seeded RMAT)",
                               "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0,
                                       "d2h_bytes_per_step": 0}}), flush=True)
@@ -1223,6 +1295,11 @@ def main():
         res, ctx, G = run_map(args, rank, world, local_rank)
         if rank == 0 and not args.no_cpu_baseline:
             res["cpu_baseline"] = map_cpu_sample()
+        args.no_cpu_baseline = True
+    elif args.workload == "bytepd":
+        res, ctx, G = run_bytepd(args, rank, world, local_rank)
+        if rank == 0 and not args.no_cpu_baseline:
+            res["cpu_baseline"] = bytepd_cpu_sample()
         args.no_cpu_baseline = True
     elif args.workload in ("scale", "families"):
         fn = run_scale if args.workload == "scale" else run_families

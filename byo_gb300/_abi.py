@@ -126,6 +126,10 @@ SIGNATURES = {
     "byo_pagerank_delta_device": (_int, [_vp, _dbl, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
     "byo_triangle_count": (_int, [_vp, _P(_u64)]),
     "byo_map_sum": (_int, [_vp, _P(_u64)]),
+    "byo_graph_from_bytepd": (_int, [_vp, _u64, _vp, _vp, _vp, _u64, _u32, _int, _P(_vp)]),
+    "byo_graph_read_bytepd": (_int, [_vp, ctypes.c_char_p, _u32, _int, _P(_vp)]),
+    "byo_graph_write_bytepd": (_int, [_vp, ctypes.c_char_p, _u32]),
+    "byo_graph_encode_bytepd": (_int, [_vp, _u32, _vp, _vp, _vp, _P(_u64)]),
     "byo_map_remote": (_int, [_vp, _vp, _u32, _P(_u64)]),
     "byo_map_remote_device": (_int, [_vp, _vp, _u32, _P(_u64)]),
     "byo_functor_bfs_create": (_int, [_vp, _u32, _P(_vp)]),

@@ -126,6 +126,34 @@ int byo_graph_read_adj(byo_ctx *ctx, const char *path, int binary, int container
   return graph_from_host_csr(ctx, container, n, m, off.data(), nb.data(), out);
 }
 
+int byo_graph_from_bytepd(byo_ctx *ctx, uint64_t n, const uint64_t *byte_offsets, const uint32_t *degrees,
+                          const uint8_t *bytes, uint64_t nbytes, uint32_t block, int container, byo_graph **out) {
+  if (!ctx || !out) return BYO_EINVAL;
+  *out = nullptr;
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+    return set_error(ctx, BYO_EINVAL, "unknown container");
+  return graph_from_bytepd_host(ctx, n, byte_offsets, degrees, bytes, nbytes, block ? block : 1000, container, out);
+}
+
+int byo_graph_read_bytepd(byo_ctx *ctx, const char *path, uint32_t block, int container, byo_graph **out) {
+  if (!ctx || !path || !out) return BYO_EINVAL;
+  *out = nullptr;
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+    return set_error(ctx, BYO_EINVAL, "unknown container");
+  return bytepd_read_file(ctx, path, block ? block : 1000, container, out);
+}
+
+int byo_graph_write_bytepd(byo_graph *g, const char *path, uint32_t block) {
+  if (!g || !path) return BYO_EINVAL;
+  return bytepd_write_file(g, path, block ? block : 1000);
+}
+
+int byo_graph_encode_bytepd(byo_graph *g, uint32_t block, uint64_t *byte_offsets, uint32_t *degrees, uint8_t *bytes,
+                            uint64_t *nbytes) {
+  if (!g || !nbytes) return BYO_EINVAL;
+  return bytepd_encode_host(g, block ? block : 1000, byte_offsets, degrees, bytes, nbytes);
+}
+
 int byo_graph_write_adj(byo_graph *g, const char *path, int binary) {
   if (!g || !path) return BYO_EINVAL;
   std::vector<uint64_t> off(g->n + 1);

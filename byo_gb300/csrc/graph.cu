@@ -234,43 +234,51 @@ int graph_from_sorted_keys(byo_ctx *ctx, int container, uint64_t n, const uint64
   return BYO_OK;
 }
 
+// A graph from a CSR already on the device (validated: sorted, duplicate-free,
+// ids < n); the arrays stay the caller's.
+int graph_from_device_csr(byo_ctx *ctx, int container, uint64_t n, uint64_t m, const uint64_t *d_off,
+                          const uint32_t *d_nbrs, byo_graph **out) {
+  uint64_t *keys = nullptr;
+  unsigned int *d_bad = nullptr;
+  int rc = BYO_OK;
+  cudaError_t e = cudaMalloc(&keys, (m ? m : 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&d_bad, 4);
+  if (e != cudaSuccess) rc = set_error(ctx, BYO_ENOMEM, "cudaMalloc", e);
+  if (rc == BYO_OK) {
+    cudaMemsetAsync(d_bad, 0, 4, ctx->stream);
+    launch(ctx, k_check_csr, dim3(grid_for(ctx, n, 256)), dim3(256), 0, d_off, d_nbrs, n, d_bad);
+    unsigned int bad = 0;
+    cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) rc = set_error(ctx, BYO_EDEVICE, "check CSR", e);
+    else if (bad) rc = set_error(ctx, BYO_EINVAL, "adjacency must be sorted, duplicate-free and < n");
+  }
+  if (rc == BYO_OK) {
+    launch(ctx, k_keys_from_csr, dim3(grid_for(ctx, n * 32, 256, 16)), dim3(256), 0, d_off, d_nbrs, n, keys);
+    rc = graph_from_sorted_keys(ctx, container, n, keys, m, out);
+  }
+  if (keys) cudaFree(keys);
+  if (d_bad) cudaFree(d_bad);
+  return rc;
+}
+
 int graph_from_host_csr(byo_ctx *ctx, int container, uint64_t n, uint64_t m, const uint64_t *h_off,
                         const uint32_t *h_nbrs, byo_graph **out) {
   if (n >= 0xFFFFFFFFull) return set_error(ctx, BYO_EINVAL, "n must be < 2^32 - 1");
   if (!h_off || (m && !h_nbrs)) return set_error(ctx, BYO_EINVAL, "null CSR array");
   if (h_off[0] != 0 || h_off[n] != m) return set_error(ctx, BYO_EINVAL, "offsets[0] != 0 or offsets[n] != m");
-  uint64_t *d_off = nullptr, *keys = nullptr;
+  uint64_t *d_off = nullptr;
   uint32_t *d_nbrs = nullptr;
-  unsigned int *d_bad = nullptr;
   int rc = BYO_OK;
-  auto fail = [&](int code, const char *what, cudaError_t e) {
-    rc = set_error(ctx, code, what, e);
-  };
-  cudaError_t e;
-  if ((e = cudaMalloc(&d_off, (n + 1) * 8)) != cudaSuccess) fail(BYO_ENOMEM, "cudaMalloc", e);
-  if (rc == BYO_OK && (e = cudaMalloc(&d_nbrs, (m ? m : 1) * 4)) != cudaSuccess) fail(BYO_ENOMEM, "cudaMalloc", e);
-  if (rc == BYO_OK && (e = cudaMalloc(&keys, (m ? m : 1) * 8)) != cudaSuccess) fail(BYO_ENOMEM, "cudaMalloc", e);
-  if (rc == BYO_OK && (e = cudaMalloc(&d_bad, 4)) != cudaSuccess) fail(BYO_ENOMEM, "cudaMalloc", e);
+  cudaError_t e = cudaMalloc(&d_off, (n + 1) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&d_nbrs, (m ? m : 1) * 4);
+  if (e != cudaSuccess) rc = set_error(ctx, BYO_ENOMEM, "cudaMalloc", e);
   if (rc == BYO_OK) {
     cudaMemcpyAsync(d_off, h_off, (n + 1) * 8, cudaMemcpyHostToDevice, ctx->stream);
     if (m) cudaMemcpyAsync(d_nbrs, h_nbrs, m * 4, cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemsetAsync(d_bad, 0, 4, ctx->stream);
-    launch(ctx, k_check_csr, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint64_t *)d_off,
-           (const uint32_t *)d_nbrs, n, d_bad);
-    unsigned int bad = 0;
-    cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, ctx->stream);
-    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) fail(BYO_EDEVICE, "upload CSR", e);
-    else if (bad) fail(BYO_EINVAL, "adjacency must be sorted, duplicate-free and < n", cudaSuccess);
-  }
-  if (rc == BYO_OK) {
-    launch(ctx, k_keys_from_csr, dim3(grid_for(ctx, n * 32, 256, 16)), dim3(256), 0, (const uint64_t *)d_off,
-           (const uint32_t *)d_nbrs, n, keys);
-    rc = graph_from_sorted_keys(ctx, container, n, keys, m, out);
+    rc = graph_from_device_csr(ctx, container, n, m, d_off, d_nbrs, out);
   }
   if (d_off) cudaFree(d_off);
   if (d_nbrs) cudaFree(d_nbrs);
-  if (keys) cudaFree(keys);
-  if (d_bad) cudaFree(d_bad);
   return rc;
 }
 

@@ -230,6 +230,15 @@ int pagerank_run(byo_graph *g, double eps, uint32_t max_iters, int precision, do
                  uint32_t *iters, double *l1);
 int tc_run(byo_graph *g, uint64_t *count);
 int map_run(byo_graph *g, int width, const void *d_remote, uint64_t *sum);
+int graph_from_device_csr(byo_ctx *ctx, int container, uint64_t n, uint64_t m, const uint64_t *d_off,
+                          const uint32_t *d_nbrs, byo_graph **out);
+int graph_from_bytepd_host(byo_ctx *ctx, uint64_t n, const uint64_t *h_bo, const uint32_t *h_deg,
+                           const unsigned char *h_bytes, uint64_t nbytes, uint32_t P, int container,
+                           byo_graph **out);
+int bytepd_read_file(byo_ctx *ctx, const char *path, uint32_t P, int container, byo_graph **out);
+int bytepd_write_file(byo_graph *g, const char *path, uint32_t P);
+int bytepd_encode_host(byo_graph *g, uint32_t P, uint64_t *h_bo, uint32_t *h_deg, unsigned char *h_bytes,
+                       uint64_t *nbytes);
 uint64_t map_remote_bytes(uint64_t n, uint32_t width);
 
 // ---------------------------------------------------------------- PMA (pma.cu)

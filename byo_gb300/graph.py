@@ -231,6 +231,42 @@ class Graph:
         check(lib().byo_graph_read_adj(ctx.h, os.fsencode(path), int(binary), cont, ctypes.byref(h)), ctx.h)
         return cls(ctx, h)
 
+    @classmethod
+    def read_bytepd(cls, ctx, path, block=1000, container="csr"):
+        """read_compressed_symmetric_graph (graph_io.h:351-390): a byte-PD file,
+        decoded on the GPU."""
+        h = ctypes.c_void_p()
+        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        check(lib().byo_graph_read_bytepd(ctx.h, os.fsencode(path), block, cont, ctypes.byref(h)), ctx.h)
+        return cls(ctx, h)
+
+    @classmethod
+    def from_bytepd(cls, ctx, byte_offsets, degrees, data, block=1000, container="csr"):
+        """A graph from byte-PD arrays (byte offsets [n+1], degrees [n], bytes)."""
+        bo = np.ascontiguousarray(byte_offsets, np.uint64)
+        dg = np.ascontiguousarray(degrees, np.uint32)
+        by = np.ascontiguousarray(data, np.uint8)
+        h = ctypes.c_void_p()
+        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        check(lib().byo_graph_from_bytepd(ctx.h, len(dg), bo.ctypes.data, dg.ctypes.data, by.ctypes.data, len(by),
+                                          block, cont, ctypes.byref(h)), ctx.h)
+        return cls(ctx, h)
+
+    def to_bytepd(self, block=1000):
+        """(byte offsets, degrees, bytes) of the byte-PD encoding, made on the GPU."""
+        n = self.N()
+        bo = np.empty(n + 1, np.uint64)
+        dg = np.empty(max(n, 1), np.uint32)
+        size = ctypes.c_uint64(0)
+        check(lib().byo_graph_encode_bytepd(self.h, block, None, None, None, ctypes.byref(size)), self.ctx.h)
+        by = np.empty(max(size.value, 1), np.uint8)
+        check(lib().byo_graph_encode_bytepd(self.h, block, bo.ctypes.data, dg.ctypes.data, by.ctypes.data,
+                                            ctypes.byref(size)), self.ctx.h)
+        return bo, dg[:n], by[:size.value]
+
+    def write_bytepd(self, path, block=1000):
+        check(lib().byo_graph_write_bytepd(self.h, os.fsencode(path), block), self.ctx.h)
+
     @staticmethod
     def _keys(batch):
         a = np.asarray(batch)

@@ -263,6 +263,26 @@ int byo_pagerank_delta_device(byo_graph *g, double eps, double local_eps, uint32
  * (benchmarks/TriangleCounting/ShunTangwongsan15/Triangle.h:167-204). */
 int byo_triangle_count(byo_graph *g, uint64_t *count);
 
+/* ------------------------------------------------------------------ byte-PD graphs
+ * The reference's compressed graphs: neighbour lists in the bytepd_amortized
+ * encoding (gbbs/encodings/byte_pd_amortized.h:1100-1155,
+ * byte_pd_amortized.cc:7-55) and its file (gbbs/graph_io.h:351-390: int64 n,
+ * m, total bytes; uint64 byte offsets[n+1]; uint32 degrees[n]; the bytes).
+ * `block` is the encoder's block size, the reader's PARALLEL_DEGREE
+ * (gbbs/macros.h:83); 0 = 1000.  Decoding and encoding run on the GPU; the
+ * graph is held decoded (CSR or PMA container).  Malformed data, or lists
+ * that are not strictly increasing, give BYO_EINVAL. */
+int byo_graph_from_bytepd(byo_ctx *ctx, uint64_t n, const uint64_t *byte_offsets, const uint32_t *degrees,
+                          const uint8_t *bytes, uint64_t nbytes, uint32_t block, int container, byo_graph **out);
+int byo_graph_read_bytepd(byo_ctx *ctx, const char *path, uint32_t block, int container, byo_graph **out);
+int byo_graph_write_bytepd(byo_graph *g, const char *path, uint32_t block);
+/* Encodes g into host arrays: byte_offsets[n+1], degrees[n], bytes[*nbytes].
+ * *nbytes is the capacity of `bytes` on entry and the size on return; with
+ * bytes NULL only the size (and the offsets and degrees, when given) are
+ * returned. */
+int byo_graph_encode_bytepd(byo_graph *g, uint32_t block, uint64_t *byte_offsets, uint32_t *degrees, uint8_t *bytes,
+                            uint64_t *nbytes);
+
 /* ------------------------------------------------------------------ neighbour maps
  * Test_Map (benchmarks/Map/Base/Map.h:8-18): the sum over every edge (u, v)
  * of v, by one scan of the container's own slots (a PMA's leaves as they lie,

@@ -566,6 +566,146 @@ void orc_pagerank_delta(uint64_t n, const uint64_t *offsets, const uint32_t *nbr
   free(next);
 }
 
+/* byte-PD (see oracle.h): byte_pd_amortized.cc:7-55 and
+ * byte_pd_amortized.h:1100-1155 restated. */
+static uint64_t varint_len(uint64_t v) { /* 7 bits per byte, at least 0 bytes for 0 */
+  uint64_t k = 0;
+  while (v) {
+    k++;
+    v >>= 7;
+  }
+  return k;
+}
+
+static uint64_t first_len(int64_t diff) {
+  uint64_t a = (uint64_t)(diff < 0 ? -diff : diff);
+  return 1 + varint_len(a >> 6);
+}
+
+static uint64_t vertex_bytes(const uint32_t *nb, uint64_t d, uint32_t src, uint32_t P) {
+  if (!d) return 0;
+  const uint64_t nbk = 1 + (d - 1) / P;
+  uint64_t bytes = 4 + 4 * (nbk - 1) + 4 * nbk;
+  for (uint64_t e = 0; e < d; e++)
+    bytes += (e % P == 0) ? first_len((int64_t)nb[e] - (int64_t)src) : varint_len((uint64_t)(nb[e] - nb[e - 1]));
+  return bytes;
+}
+
+uint64_t orc_bytepd_sizes(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, uint32_t P, uint64_t *sizes) {
+  uint64_t total = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : total)
+  for (int64_t v = 0; v < (int64_t)n; v++) {
+    sizes[v] = vertex_bytes(nbrs + offsets[v], offsets[v + 1] - offsets[v], (uint32_t)v, P);
+    total += sizes[v];
+  }
+  return total;
+}
+
+static void put_u32(unsigned char *p, uint32_t x) { memcpy(p, &x, 4); }
+static uint32_t get_u32(const unsigned char *p) {
+  uint32_t x;
+  memcpy(&x, p, 4);
+  return x;
+}
+
+static unsigned char *put_first(unsigned char *p, int64_t diff) {
+  uint64_t a = (uint64_t)(diff < 0 ? -diff : diff);
+  unsigned char b = (unsigned char)(a & 0x3f);
+  if (diff < 0) b |= 0x40;
+  a >>= 6;
+  if (a) b |= 0x80;
+  *p++ = b;
+  while (a) {
+    unsigned char c = (unsigned char)(a & 0x7f);
+    a >>= 7;
+    if (a) c |= 0x80;
+    *p++ = c;
+  }
+  return p;
+}
+
+static unsigned char *put_diff(unsigned char *p, uint64_t a) {
+  while (a) {
+    unsigned char c = (unsigned char)(a & 0x7f);
+    a >>= 7;
+    if (a) c |= 0x80;
+    *p++ = c;
+  }
+  return p;
+}
+
+void orc_bytepd_encode(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, uint32_t P,
+                       const uint64_t *byte_offsets, unsigned char *bytes) {
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t v = 0; v < (int64_t)n; v++) {
+    const uint64_t d = offsets[v + 1] - offsets[v];
+    if (!d) continue;
+    const uint32_t *nb = nbrs + offsets[v];
+    unsigned char *base = bytes + byte_offsets[v];
+    const uint64_t nbk = 1 + (d - 1) / P;
+    put_u32(base, (uint32_t)d);
+    unsigned char *p = base + 4 + 4 * (nbk - 1);
+    for (uint64_t i = 0; i < nbk; i++) {
+      if (i > 0) put_u32(base + 4 + 4 * (i - 1), (uint32_t)(p - base));
+      put_u32(p, (uint32_t)(i * P));
+      p += 4;
+      const uint64_t e0 = i * P, e1 = e0 + P < d ? e0 + P : d;
+      p = put_first(p, (int64_t)nb[e0] - (int64_t)v);
+      for (uint64_t e = e0 + 1; e < e1; e++) p = put_diff(p, (uint64_t)(nb[e] - nb[e - 1]));
+    }
+  }
+}
+
+int orc_bytepd_decode(uint64_t n, const uint64_t *byte_offsets, const uint32_t *degrees, const unsigned char *bytes,
+                      uint64_t nbytes, uint32_t P, uint64_t *offsets, uint32_t *nbrs) {
+  offsets[0] = 0;
+  for (uint64_t v = 0; v < n; v++) offsets[v + 1] = offsets[v] + degrees[v];
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : bad)
+  for (int64_t v = 0; v < (int64_t)n; v++) {
+    const uint64_t d = degrees[v];
+    if (!d) continue;
+    const unsigned char *base = bytes + byte_offsets[v], *end = bytes + byte_offsets[v + 1];
+    if (byte_offsets[v + 1] > nbytes || base + 4 > end || get_u32(base) != d) {
+      bad = 1;
+      continue;
+    }
+    const uint64_t nbk = 1 + (d - 1) / P;
+    uint32_t *out = nbrs + offsets[v];
+    for (uint64_t i = 0; i < nbk && !bad; i++) {
+      const unsigned char *p = i == 0 ? base + 4 + 4 * (nbk - 1) : base + get_u32(base + 4 + 4 * (i - 1));
+      const uint64_t e0 = get_u32(p), e1 = i + 1 == nbk ? d : get_u32(base + get_u32(base + 4 + 4 * i));
+      p += 4;
+      int64_t last = 0;
+      for (uint64_t e = e0; e < e1; e++) {
+        uint64_t a = 0;
+        int shift, neg = 0;
+        if (p >= end) {
+          bad = 1;
+          break;
+        }
+        unsigned char b = *p++;
+        if (e == e0) {
+          a = b & 0x3f;
+          neg = (b & 0x40) != 0;
+          shift = 6;
+        } else {
+          a = b & 0x7f;
+          shift = 7;
+        }
+        while ((b & 0x80) && p < end && shift < 64) {
+          b = *p++;
+          a |= (uint64_t)(b & 0x7f) << shift;
+          shift += 7;
+        }
+        last = e == e0 ? (neg ? (int64_t)v - (int64_t)a : (int64_t)v + (int64_t)a) : last + (int64_t)a;
+        out[e] = (uint32_t)last;
+      }
+    }
+  }
+  return bad ? -1 : 0;
+}
+
 /* Map.h:8-18 and RemoteRead/Map.h:21-33: a parallel_for over vertices, each
  * summing over its neighbours, combined by a Reducer_sum<size_t>. */
 uint64_t orc_map_sum(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs) {

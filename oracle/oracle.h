@@ -125,6 +125,33 @@ void orc_pagerank(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, dou
 void orc_pagerank_delta(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, double eps, double local_eps,
                         uint32_t max_iters, double *p, uint32_t *rounds_out, double *l1_out);
 
+/* ---------------------------------------------------------------- byte-PD
+ * The bytepd_amortized encoding of neighbour lists
+ * (gbbs/encodings/byte_pd_amortized.h:1100-1155 sequentialCompressEdgeSet,
+ * byte_pd_amortized.cc:7-55 compressFirstEdge / compressEdge, the reader
+ * iter at byte_pd_amortized.h:180-260) and the compressed graph file
+ * (gbbs/graph_io.h:351-390; utils/converter.h:671-760 writes it):
+ *   file: int64 n, m, total bytes; uint64 byte offsets[n + 1]; uint32
+ *   degrees[n]; the bytes.  A vertex of degree d > 0 starts with uint32 d,
+ *   then uint32 byte offsets (from the vertex start) of blocks 1 .. nb-1,
+ *   nb = 1 + (d-1)/P; block i holds uint32 i*P and then up to P neighbours:
+ *   the first as (neighbour - source): byte 0 = bit 7 "more bytes", bit 6
+ *   sign, bits 0-5 the low six bits of |difference|, further bytes 7 bits
+ *   each (bit 7 "more"); the others as the positive difference to the
+ *   previous neighbour, 7 bits per byte, bit 7 "more".  The reader uses
+ *   P = PARALLEL_DEGREE = 1000 (gbbs/macros.h:83).  Neighbour lists must be
+ *   strictly increasing (a zero difference has no encoding).
+ * orc_bytepd_sizes: per-vertex byte counts into sizes[n]; returns the total.
+ * orc_bytepd_encode: writes every vertex at byte_offsets[v] (exclusive prefix
+ * of the sizes, byte_offsets[n] = total) into bytes.
+ * orc_bytepd_decode: the CSR back (offsets from the degrees); returns 0, or -1
+ * on a malformed run. */
+uint64_t orc_bytepd_sizes(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, uint32_t P, uint64_t *sizes);
+void orc_bytepd_encode(uint64_t n, const uint64_t *offsets, const uint32_t *nbrs, uint32_t P,
+                       const uint64_t *byte_offsets, unsigned char *bytes);
+int orc_bytepd_decode(uint64_t n, const uint64_t *byte_offsets, const uint32_t *degrees, const unsigned char *bytes,
+                      uint64_t nbytes, uint32_t P, uint64_t *offsets, uint32_t *nbrs);
+
 /* Test_Map (benchmarks/Map/Base/Map.h:8-18): sum over every edge of its
  * destination id.  Test_Map_Remote (benchmarks/Map/RemoteRead/Map.h:21-33):
  * sum over every edge (u, v) of remote[v], remote an n-entry array of

@@ -63,6 +63,10 @@ def lib():
                                           _f64p, _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_double)]),
             "orc_triangle_count": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p]),
             "orc_map_sum": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p]),
+            "orc_bytepd_sizes": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p, _c.c_uint32, _u64p]),
+            "orc_bytepd_encode": (None, [_c.c_uint64, _u64p, _u32p, _c.c_uint32, _u64p, _c.c_void_p]),
+            "orc_bytepd_decode": (_c.c_int, [_c.c_uint64, _u64p, _u32p, _c.c_void_p, _c.c_uint64, _c.c_uint32,
+                                             _u64p, _u32p]),
             "orc_map_remote": (_c.c_uint64, [_c.c_uint64, _u64p, _u32p, _c.c_void_p, _c.c_uint32]),
             "orc_store_create": (_c.c_void_p, [_c.c_uint64, _u64p, _u32p]),
             "orc_store_destroy": (None, [_c.c_void_p]),
@@ -189,6 +193,31 @@ def pagerank_delta(offsets, nbrs, eps=1e-6, local_eps=0.01, max_iters=100):
     lib().orc_pagerank_delta(n, _u64(offsets), _u32(nbrs), eps, local_eps, max_iters, p, ctypes.byref(r),
                              ctypes.byref(l1))
     return p, r.value, l1.value
+
+
+def bytepd_encode(offsets, nbrs, P=1000):
+    """byte-PD amortized encoding: (byte_offsets[n+1], degrees[n], bytes)."""
+    n = len(offsets) - 1
+    off, nb = _u64(offsets), _u32(nbrs)
+    sizes = np.zeros(max(n, 1), np.uint64)
+    total = lib().orc_bytepd_sizes(n, off, nb, P, sizes)
+    bo = np.zeros(n + 1, np.uint64)
+    bo[1:] = np.cumsum(sizes[:n])
+    out = np.zeros(max(total, 1), np.uint8)
+    lib().orc_bytepd_encode(n, off, nb, P, bo, out.ctypes.data_as(ctypes.c_void_p))
+    return bo, np.diff(off).astype(np.uint32), out[:total]
+
+
+def bytepd_decode(byte_offsets, degrees, data, P=1000):
+    n = len(degrees)
+    off = np.zeros(n + 1, np.uint64)
+    nb = np.zeros(max(int(np.sum(degrees, dtype=np.uint64)), 1), np.uint32)
+    buf = np.ascontiguousarray(data, np.uint8)
+    rc = lib().orc_bytepd_decode(n, _u64(byte_offsets), _u32(degrees), buf.ctypes.data_as(ctypes.c_void_p),
+                                 len(buf), P, off, nb)
+    if rc != 0:
+        raise ValueError("malformed byte-PD data")
+    return off, nb[:off[-1]]
 
 
 def map_sum(offsets, nbrs):

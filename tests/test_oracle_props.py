@@ -192,3 +192,29 @@ def test_map_restatement(oracle_mod):
             r = np.full((n, w // 8), 7, np.uint64)
             r[:, 0] = rng.integers(0, 1000, size=n)
             assert O.map_remote(off, nb, r, w) == int(r[nb, 0].sum())
+
+
+def test_bytepd_golden_and_round_trip(oracle_mod):
+    """The byte-PD amortized layout, byte for byte on a hand-encoded vertex
+    (byte_pd_amortized.cc:7-55: first neighbour as a signed difference from
+    the source with 6 bits in its first byte, then 7-bit differences), and
+    encode -> decode round trips for several block sizes."""
+    O = oracle_mod
+    # vertex 5 with neighbours 3, 7, 200 (others empty), one block
+    off = np.array([0, 0, 0, 0, 0, 0, 3, 3], np.uint64)
+    nb = np.array([3, 7, 200], np.uint32)
+    bo, deg, data = O.bytepd_encode(off, nb, 1000)
+    exp = bytes([3, 0, 0, 0,  0, 0, 0, 0,  0x42, 0x04, 0xC1, 0x01])
+    assert bytes(data) == exp and bo.tolist() == [0] * 6 + [12, 12] and deg.tolist() == [0] * 5 + [3, 0]
+    # two blocks of 2: block offsets, block start indices, the first edge of
+    # block 1 again relative to the source (200 - 5 = 195 = 0b11 000011)
+    off2 = np.array([0, 0, 0, 0, 0, 0, 3], np.uint64)
+    bo, deg, data = O.bytepd_encode(off2, nb, 2)
+    exp = bytes([3, 0, 0, 0,  14, 0, 0, 0,  0, 0, 0, 0,  0x42, 0x04,  2, 0, 0, 0,  0x83, 0x03])
+    assert bytes(data) == exp
+    for P in (1000, 256, 7, 1):
+        s, d = O.rmat_edges(11, 12, 1 << 16)
+        o, n_ = O.build_csr(1 << 12, s, d)
+        bo, deg, data = O.bytepd_encode(o, n_, P)
+        o2, n2 = O.bytepd_decode(bo, deg, data, P)
+        assert np.array_equal(o2, o) and np.array_equal(n2, n_)
