@@ -126,6 +126,8 @@ SIGNATURES = {
     "byo_pagerank_delta_device": (_int, [_vp, _dbl, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
     "byo_triangle_count": (_int, [_vp, _P(_u64)]),
     "byo_map_sum": (_int, [_vp, _P(_u64)]),
+    "byo_graph_update_stream": (_int, [_vp, _vp, _vp, _vp, _u64, _vp]),
+    "byo_graph_update_stream_device": (_int, [_vp, _vp, _vp, _vp, _u64, _vp]),
     "byo_graph_from_bytepd": (_int, [_vp, _u64, _vp, _vp, _vp, _u64, _u32, _int, _P(_vp)]),
     "byo_graph_read_bytepd": (_int, [_vp, ctypes.c_char_p, _u32, _int, _P(_vp)]),
     "byo_graph_write_bytepd": (_int, [_vp, ctypes.c_char_p, _u32]),

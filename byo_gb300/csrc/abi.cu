@@ -270,6 +270,47 @@ static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int
   return pma_update(g, d, count, sorted, insert, changed);
 }
 
+static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, const uint64_t *h_offsets,
+                                const uint8_t *h_ops, uint64_t nbatch, uint64_t *changed) {
+  if (!g || (nbatch && (!keys || !h_offsets || !h_ops))) return BYO_EINVAL;
+  byo_ctx *ctx = g->ctx;
+  if (g->container != BYO_CONTAINER_PMA)
+    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA container");
+  if (!nbatch) return BYO_OK;
+  if (h_offsets[0] != 0) return set_error(ctx, BYO_EINVAL, "update stream: offsets[0] != 0");
+  for (uint64_t b = 0; b < nbatch; b++)
+    if (h_offsets[b + 1] < h_offsets[b]) return set_error(ctx, BYO_EINVAL, "update stream: offsets decrease");
+  const uint64_t total = h_offsets[nbatch];
+  const uint64_t *d = keys;
+  if (host) {
+    uint64_t *buf = nullptr;
+    BYO_TRY(ws(g, WS_TC_OFF, total ? total : 1, &buf));
+    if (total) BYO_CU(ctx, cudaMemcpyAsync(buf, keys, total * 8, cudaMemcpyHostToDevice, ctx->stream));
+    d = buf;
+  }
+  uint64_t *sb = nullptr;
+  BYO_TRY(ws(g, WS_STREAM, (nbatch + 1) + (nbatch + 7) / 8, &sb));
+  BYO_CU(ctx, cudaMemcpyAsync(sb, h_offsets, (nbatch + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
+  unsigned char *d_ops = reinterpret_cast<unsigned char *>(sb + nbatch + 1);
+  std::vector<unsigned char> ops(nbatch);
+  for (uint64_t b = 0; b < nbatch; b++) ops[b] = h_ops[b] ? 1 : 0;
+  BYO_CU(ctx, cudaMemcpyAsync(d_ops, ops.data(), nbatch, cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<long long> ch(nbatch);
+  const int rc = pma_update_stream(g, d, sb, h_offsets, d_ops, ops.data(), nbatch, ch.data());
+  if (changed)
+    for (uint64_t b = 0; b < nbatch; b++) changed[b] = (uint64_t)ch[b];
+  return rc;
+}
+
+int byo_graph_update_stream(byo_graph *g, const uint64_t *h_keys, const uint64_t *offsets, const uint8_t *ops,
+                            uint64_t nbatch, uint64_t *changed) {
+  return update_stream_common(g, h_keys, 1, offsets, ops, nbatch, changed);
+}
+int byo_graph_update_stream_device(byo_graph *g, const uint64_t *d_keys, const uint64_t *offsets, const uint8_t *ops,
+                                   uint64_t nbatch, uint64_t *changed) {
+  return update_stream_common(g, d_keys, 0, offsets, ops, nbatch, changed);
+}
+
 int byo_graph_insert_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
                            uint64_t *changed) {
   return update_common(g, h_keys, count, sorted, 1, 1, changed);

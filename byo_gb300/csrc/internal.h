@@ -99,6 +99,7 @@ enum Ws {
   WS_TC_CNT,
   WS_BUCKETS,
   WS_MISC,
+  WS_STREAM,        // update stream: batch offsets and operations
   WS_COUNT
 };
 
@@ -243,6 +244,8 @@ uint64_t map_remote_bytes(uint64_t n, uint32_t width);
 
 // ---------------------------------------------------------------- PMA (pma.cu)
 int pma_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);
+int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_boff, const uint64_t *h_boff,
+                      const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed);
 int pma_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert,
                uint64_t *changed);
 int pma_export_keys(byo_graph *g, uint64_t *d_keys_out);

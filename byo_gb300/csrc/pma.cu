@@ -34,9 +34,11 @@
 // every leaf touched (read + write of src and dst), twice for windowed leaves.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "device.cuh"
+#include "gridsync.cuh"
 #include "internal.h"
 #include "scan.cuh"
 
@@ -483,22 +485,18 @@ struct ViewOut {
   unsigned long long *nchunks;
 };
 
+// One leaf (work item q) merged by the calling warp, with Aw / Bw its staging
+// in shared memory (kLeaf and kOptSeg keys); returns the change of the leaf's
+// key count.
 template <bool kList>
-__global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
-    uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
-    const uint64_t *__restrict__ bstart, uint64_t *seg, const unsigned long long *nseg,
-    int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
-    unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta, uint32_t *deg,
-    ViewOut view) {
-  __shared__ uint64_t As[kOptWarps][kLeaf];
-  __shared__ uint64_t Bsh[kOptWarps][kOptSeg];
-  const unsigned w = threadIdx.x >> 5, lane = lane_id();
-  const uint64_t *A = As[w];
-  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  long long dsum = 0;
-  const uint64_t nwork = kList ? *nseg : NL;
-  for (uint64_t q = gw; q < nwork; q += nw) {
+__device__ __forceinline__ long long merge_leaf(uint64_t q, uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL,
+                                                const uint64_t *__restrict__ keys, const uint64_t *__restrict__ bstart,
+                                                uint64_t *seg, int insert, uint32_t *rcount, uint64_t *ovf,
+                                                uint64_t *ovf_off, unsigned long long *ctr, uint32_t *deg,
+                                                const ViewOut &view, uint64_t *Aw, uint64_t *Bw) {
+  const unsigned lane = lane_id();
+  const uint64_t *A = Aw;
+  {
     uint64_t j, b0, b1;
     if (kList) {
       j = seg[2 * q] & 0xFFFFFFFFull;
@@ -517,10 +515,10 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
         if (kList) seg[2 * q] = j | (uint64_t)c << 32;
         else rcount[j] = c;
       }
-      continue;
+      return 0;
     }
     const uint64_t nb = b1 - b0;
-    const uint64_t *B = nb <= kOptSeg ? Bsh[w] : keys + b0;
+    const uint64_t *B = nb <= kOptSeg ? Bw : keys + b0;
     const uint64_t base = j * kLeaf;
     // The s leaf keys below the first batch key keep their slots: the merge
     // reads and writes only the rest.  s by two rounds of lane-parallel
@@ -539,9 +537,9 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
       }
     }
     const uint32_t ca = c - s;  // the leaf keys that take part in the merge
-    for (uint32_t e = lane; e < ca; e += 32) As[w][e] = slot_key(src, dst, base + s + e);
+    for (uint32_t e = lane; e < ca; e += 32) Aw[e] = slot_key(src, dst, base + s + e);
     if (nb <= kOptSeg)
-      for (uint32_t k = lane; k < nb; k += 32) Bsh[w][k] = keys[b0 + k];
+      for (uint32_t k = lane; k < nb; k += 32) Bw[k] = keys[b0 + k];
     __syncwarp();
     // The result's size first: the batch keys that are dropped (insert: equal
     // to the key before them in B or present in A; remove: present in A,
@@ -629,15 +627,34 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
     if (lane == 0) {
       if (kList) seg[2 * q] = j | (uint64_t)r << 32;
       else rcount[j] = r;
-      dsum += (long long)r - (long long)c;
     }
     __syncwarp();  // the leaf's new contents (and A's last reads) are done warp-wide
     if (kList && view.off && !ostage)
       view_refresh_warp(src, view.sep, NL, view.n, j, r, old_last, keys[b0] >> 32, keys[b1 - 1] >> 32,
-                        reinterpret_cast<uint32_t *>(As[w]), view.off, q, view.range, view.chunks, view.nchunks);
+                        reinterpret_cast<uint32_t *>(Aw), view.off, q, view.range, view.chunks, view.nchunks);
     __syncwarp();
+    return (long long)r - (long long)c;
   }
-  if (lane == 0 && dsum) atomicAdd((unsigned long long *)delta, (unsigned long long)dsum);
+}
+
+template <bool kList>
+__global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
+    uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
+    const uint64_t *__restrict__ bstart, uint64_t *seg, const unsigned long long *nseg,
+    int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
+    unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta, uint32_t *deg,
+    ViewOut view) {
+  __shared__ uint64_t As[kOptWarps][kLeaf];
+  __shared__ uint64_t Bsh[kOptWarps][kOptSeg];
+  const unsigned w = threadIdx.x >> 5;
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  long long dsum = 0;
+  const uint64_t nwork = kList ? *nseg : NL;
+  for (uint64_t q = gw; q < nwork; q += nw)
+    dsum += merge_leaf<kList>(q, src, dst, cnt, NL, keys, bstart, seg, insert, rcount, ovf, ovf_off, ctr, deg, view,
+                              As[w], Bsh[w]);
+  if (lane_id() == 0 && dsum) atomicAdd((unsigned long long *)delta, (unsigned long long)dsum);
 }
 
 // Copies the current contents of every leaf in a window (all leaves when
@@ -744,13 +761,13 @@ __global__ void k_pma_export(const uint32_t *__restrict__ src, const uint32_t *_
 // With `bounds` set (a batch not yet validated on the host), a batch with a
 // src or dst >= n or flagged unsorted yields no segments, so the merge after
 // it changes nothing and the host reports the error once it reads the flags.
-__global__ void k_pma_segments(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
-                               uint64_t b, uint64_t *seg, unsigned long long *nseg,
-                               const unsigned long long *bounds, uint64_t n, const unsigned int *unsorted) {
-  if (bounds && (bounds[0] >= n || bounds[1] >= n || *unsorted)) return;
+// The segment list, warps striding over the keys (first key tid0 & ~31,
+// stride `stride` threads).
+__device__ __forceinline__ void segments_range(const uint64_t *__restrict__ sep, uint64_t NL,
+                                               const uint64_t *__restrict__ keys, uint64_t b, uint64_t *seg,
+                                               unsigned long long *nseg, uint64_t tid0, uint64_t stride) {
   const unsigned lane = lane_id();
-  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < b;
-       base += (uint64_t)gridDim.x * blockDim.x) {
+  for (uint64_t base = tid0 & ~31ull; base < b; base += stride) {
     const uint64_t q = base + lane;
     // the leaf of key q, and lane 0 also that of key base - 1, in one search
     // loop whose trip count depends only on NL (the two searches overlap)
@@ -790,6 +807,14 @@ __global__ void k_pma_segments(const uint64_t *__restrict__ sep, uint64_t NL, co
   }
 }
 
+__global__ void k_pma_segments(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
+                               uint64_t b, uint64_t *seg, unsigned long long *nseg,
+                               const unsigned long long *bounds, uint64_t n, const unsigned int *unsorted) {
+  if (bounds && (bounds[0] >= n || bounds[1] >= n || *unsorted)) return;
+  segments_range(sep, NL, keys, b, seg, nseg, blockIdx.x * (uint64_t)blockDim.x + threadIdx.x,
+                 (uint64_t)gridDim.x * blockDim.x);
+}
+
 // One block of 1024 threads sorts up to kSmallSort keys (a bitonic network
 // over P = 1024 K keys, padded with ~0) and reports the largest src and dst
 // in bounds[0], bounds[1].  The keys live in registers: lane l of warp w holds
@@ -812,12 +837,12 @@ __device__ __forceinline__ void sort_regs_cx(uint64_t (&x)[K], uint32_t ibase, u
   }
 }
 
+// The sort by a block of 1024 threads with s (1024 K keys) and red (64 words)
+// in shared memory.
 template <int K>
-__global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict__ in, uint32_t count, uint64_t *out,
-                                                     unsigned long long *bounds) {
+__device__ __forceinline__ void sort_small_block(const uint64_t *__restrict__ in, uint32_t count, uint64_t *out,
+                                                 unsigned long long *bounds, uint64_t *s, uint64_t (*red)[32]) {
   constexpr uint32_t P = 1024u * K, kWarpSpan = 32u * K;
-  __shared__ uint64_t s[P];
-  __shared__ uint64_t red[2][32];
   const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
   const uint32_t ibase = w * kWarpSpan + lane;
   uint64_t x[K];
@@ -892,6 +917,14 @@ __global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict_
     bounds[0] = ms;
     bounds[1] = md;
   }
+}
+
+template <int K>
+__global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict__ in, uint32_t count, uint64_t *out,
+                                                     unsigned long long *bounds) {
+  __shared__ uint64_t s[1024u * K];
+  __shared__ uint64_t red[2][32];
+  sort_small_block<K>(in, count, out, bounds, s, red);
 }
 
 
@@ -1197,6 +1230,64 @@ int traversal_view(byo_graph *g, byo_graph **out) {
   return BYO_OK;
 }
 
+// After a merge that left overflowing leaves (or a remove that shrinks the
+// array): rcount from the merge (for a segment-list merge, cnt with the merged
+// leaves' counts from seg), then the windows over the counts are gathered and
+// spread, or the whole array is rebuilt; the view is rebuilt either way.
+static int pma_finish_windowed(byo_graph *g, bool list, const uint64_t *bstart, const unsigned long long *d_nseg,
+                               uint64_t b, uint64_t total, bool shrink) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  const uint64_t NL = p->NL;
+  const double cap = (double)NL * kLeaf;
+  BYO_TRY(ensure(ctx, p->rcount, NL * 4));
+  BYO_TRY(ensure(ctx, p->rpre, (NL + 1) * 8));
+  uint32_t *rcount = (uint32_t *)p->rcount.p;
+  uint64_t *rpre = (uint64_t *)p->rpre.p;
+  unsigned int *flags = (unsigned int *)((unsigned long long *)p->misc.p + 2);
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  if (list) {
+    BYO_CU(ctx, cudaMemcpyAsync(rcount, p->cnt, NL * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    launch(ctx, k_pma_seg_counts, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)bstart,
+           d_nseg, rcount);
+  }
+  BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
+  BYO_TRY(ensure(ctx, p->win, NL * 4));
+  uint32_t *win = (uint32_t *)p->win.p;
+  bool rebuild = shrink || (double)total > kRootMax * cap;
+  if (!rebuild) {
+    BYO_TRY(ensure(ctx, p->marks, (uint64_t)(p->H + 1) * NL));
+    uint8_t *marks = (uint8_t *)p->marks.p;
+    BYO_CU(ctx, cudaMemsetAsync(marks, 0, (uint64_t)(p->H + 1) * NL, ctx->stream));
+    BYO_CU(ctx, cudaMemsetAsync(flags + 1, 0, 8, ctx->stream));
+    launch(ctx, k_pma_windows, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint32_t *)rcount,
+           (const uint64_t *)rpre, NL, p->H, marks, flags + 1, flags + 2);
+    BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+    rebuild = ((const unsigned int *)h)[1] != 0;
+    if (!rebuild) launch(ctx, k_pma_cover, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint8_t *)marks, NL,
+                         p->H, win);
+  }
+  BYO_TRY(ensure(ctx, p->staging, (total ? total : 1) * 8));
+  uint64_t *stg = (uint64_t *)p->staging.p;
+  launch(ctx, k_pma_gather, dim3(grid_for(ctx, NL * 32, 256, 16)), dim3(256), 0, (const uint32_t *)p->src,
+         (const uint32_t *)p->dst, (const uint32_t *)rcount, (const uint32_t *)p->cnt, NL, (const uint32_t *)win,
+         rebuild ? 1 : 0, (const uint64_t *)rpre, (const uint64_t *)p->ovf.p, (const uint64_t *)p->ovf_off.p, stg);
+  BYO_TRY(check_launch(ctx, "pma_gather"));
+  if (rebuild) {
+    ctx->last_update_strategy = 1;
+    p->rebuilds++;
+    return pma_layout(g, stg, total, leaves_for(total));
+  }
+  p->windows++;
+  launch_t(ctx, "pma_redistribute", k_pma_spread, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0,
+           (const uint64_t *)stg, (const uint64_t *)rpre, (const uint32_t *)win, NL, p->src, p->dst, p->cnt, p->sep,
+           NL, 0, (const uint64_t *)p->sep);
+  BYO_TRY(check_launch(ctx, "pma_update"));
+  return pma_view(g);
+}
+
 int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sorted, int insert,
                uint64_t *changed) {
   byo_ctx *ctx = g->ctx;
@@ -1347,45 +1438,222 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     return pma_view(g);
   }
   // 4. overflow (or shrink): windows over the counts after the merge
-  if (list) {
-    BYO_CU(ctx, cudaMemcpyAsync(rcount, p->cnt, NL * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-    launch(ctx, k_pma_seg_counts, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)bstart,
-           (const unsigned long long *)(ctr + 3), rcount);
+  return pma_finish_windowed(g, list, bstart, (const unsigned long long *)(ctr + 3), b, total, shrink);
+}
+
+// ---------------------------------------------------------------- update stream
+// A run of small batches (each <= kSmallSort keys and at most NL/2 of them, so
+// that the segment-list merge applies) drained by one persistent cooperative
+// kernel: per batch, CTA 0 sorts the keys in registers; the grid finds the
+// segments, merges the leaves (refreshing the offsets around them), and fills
+// long offset ranges, with a bounded grid barrier between the phases.  A batch
+// whose merge overflows a leaf or shrinks the array stops the kernel after its
+// merge; the host finishes that batch with the windowed path and relaunches
+// from the next one.  A batch with a key >= n stops it before its merge.
+constexpr int kStreamThreads = 1024, kStreamWarps = kStreamThreads / 32;
+constexpr size_t kStreamSmem = (size_t)kStreamWarps * (kLeaf + kOptSeg) * 8;
+
+struct StreamCtl {
+  GridBar bar;
+  unsigned long long bounds[2];
+  unsigned long long ctr[6];  // [0] overflow cursor [1] overflowing leaves [2] delta [3] segments [4] view chunks
+  long long m;                // keys in the container
+  unsigned int stop, reason;  // batch index + 1 where the kernel stopped; 1 overflow or shrink, 2 invalid keys
+};
+
+struct StreamArgs {
+  uint32_t *src, *dst, *cnt;
+  const uint64_t *sep;
+  uint64_t NL, n;
+  uint64_t *off;
+  uint32_t *deg;
+  const uint64_t *keys, *boff;
+  const unsigned char *ops;
+  uint64_t first, nbatch;
+  uint64_t *sorted, *seg, *vrange, *chunks, *ovf, *ovf_off;
+  double shrink_below;  // a remove that leaves fewer keys rebuilds the array
+  long long *changed;
+  StreamCtl *ctl;
+};
+
+// One chunk of a long offset range, by the whole CTA (Y: the leaf's src list).
+__device__ __forceinline__ void view_chunk_block(const uint32_t *__restrict__ src, const uint32_t *__restrict__ cnt,
+                                                 const uint64_t *__restrict__ seg, const uint64_t *__restrict__ range,
+                                                 uint64_t ch, uint64_t *off, uint32_t *Y) {
+  const uint64_t q = ch >> 32, t = ch & 0xFFFFFFFFull;
+  const uint64_t j = seg[2 * q] & 0xFFFFFFFFull;
+  const uint64_t a = range[2 * q] + t * kViewChunk, e0 = range[2 * q + 1];
+  const uint64_t e = a + kViewChunk < e0 ? a + kViewChunk : e0;
+  const uint32_t c = cnt[j];
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < c; k += blockDim.x) Y[k] = src[j * kLeaf + k];
+  __syncthreads();
+  for (uint64_t v = a + threadIdx.x; v < e; v += blockDim.x) {
+    uint32_t lo = 0, hi = c;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (Y[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    off[v] = lo < c ? j * kLeaf + lo : (j + 1) * kLeaf;
   }
-  BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
-  BYO_TRY(ensure(ctx, p->win, NL * 4));
-  uint32_t *win = (uint32_t *)p->win.p;
-  bool rebuild = shrink || (double)total > kRootMax * cap;
-  if (!rebuild) {
-    BYO_TRY(ensure(ctx, p->marks, (uint64_t)(p->H + 1) * NL));
-    uint8_t *marks = (uint8_t *)p->marks.p;
-    BYO_CU(ctx, cudaMemsetAsync(marks, 0, (uint64_t)(p->H + 1) * NL, ctx->stream));
-    BYO_CU(ctx, cudaMemsetAsync(flags + 1, 0, 8, ctx->stream));
-    launch(ctx, k_pma_windows, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint32_t *)rcount,
-           (const uint64_t *)rpre, NL, p->H, marks, flags + 1, flags + 2);
-    BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+__global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
+  extern __shared__ unsigned long long stream_smem[];
+  uint64_t *As = reinterpret_cast<uint64_t *>(stream_smem);  // [kStreamWarps][kLeaf]
+  uint64_t *Bs = As + (size_t)kStreamWarps * kLeaf;           // [kStreamWarps][kOptSeg]
+  StreamCtl *c = a.ctl;
+  const unsigned nb = gridDim.x, w = threadIdx.x >> 5;
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nthr = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t gw = tid >> 5, nw = nthr >> 5;
+  const ViewOut view{a.sep, a.n, a.off, a.vrange, a.chunks, &c->ctr[4]};
+  for (uint64_t bi = a.first; bi < a.nbatch; bi++) {
+    const uint64_t k0 = a.boff[bi], count = a.boff[bi + 1] - k0;
+    const int insert = a.ops[bi];
+    if (blockIdx.x == 0) {
+      if (threadIdx.x < 6) c->ctr[threadIdx.x] = 0;
+      uint64_t(*red)[32] = reinterpret_cast<uint64_t(*)[32]>(As + 4096);
+      if (count <= 1024) sort_small_block<1>(a.keys + k0, (uint32_t)count, a.sorted, c->bounds, As, red);
+      else if (count <= 2048) sort_small_block<2>(a.keys + k0, (uint32_t)count, a.sorted, c->bounds, As, red);
+      else sort_small_block<4>(a.keys + k0, (uint32_t)count, a.sorted, c->bounds, As, red);
+    }
+    if (!grid_sync(&c->bar, nb)) return;
+    if (c->bounds[0] >= a.n || c->bounds[1] >= a.n) {
+      if (tid == 0) {
+        c->stop = (unsigned int)bi + 1;
+        c->reason = 2;
+      }
+      return;
+    }
+    segments_range(a.sep, a.NL, a.sorted, count, a.seg, &c->ctr[3], tid, nthr);
+    if (!grid_sync(&c->bar, nb)) return;
+    const uint64_t ns = *(volatile unsigned long long *)&c->ctr[3];
+    long long dsum = 0;
+    for (uint64_t q = gw; q < ns; q += nw)
+      dsum += merge_leaf<true>(q, a.src, a.dst, a.cnt, a.NL, a.sorted, nullptr, a.seg, insert, nullptr, a.ovf,
+                               a.ovf_off, c->ctr, a.deg, view, As + (size_t)w * kLeaf, Bs + (size_t)w * kOptSeg);
+    if (lane_id() == 0 && dsum) atomicAdd(&c->ctr[2], (unsigned long long)dsum);
+    if (!grid_sync(&c->bar, nb)) return;
+    const long long delta = (long long)*(volatile unsigned long long *)&c->ctr[2];
+    const long long total = c->m + delta;
+    if (*(volatile unsigned long long *)&c->ctr[1] || (!insert && (double)total < a.shrink_below)) {
+      if (tid == 0) {
+        c->stop = (unsigned int)bi + 1;
+        c->reason = 1;
+      }
+      return;
+    }
+    const uint64_t nch = *(volatile unsigned long long *)&c->ctr[4];
+    for (uint64_t t = blockIdx.x; t < nch; t += gridDim.x)
+      view_chunk_block(a.src, a.cnt, a.seg, a.vrange, a.chunks[t], a.off, reinterpret_cast<uint32_t *>(As));
+    if (tid == 0) {
+      a.changed[bi] = delta;
+      c->m = total;
+    }
+    if (!grid_sync(&c->bar, nb)) return;
+  }
+}
+
+int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_boff, const uint64_t *h_boff,
+                      const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed) {
+  byo_ctx *ctx = g->ctx;
+  Pma *p = g->pma;
+  if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PMA container");
+  for (uint64_t bi = 0; bi < nbatch; bi++) h_changed[bi] = 0;
+  if (!nbatch) return BYO_OK;
+  g->version++;
+  StreamCtl *c = nullptr;
+  long long *d_changed = nullptr;
+  BYO_TRY(ensure(ctx, p->misc, 128 + sizeof(StreamCtl) + 8 * nbatch));
+  c = reinterpret_cast<StreamCtl *>((char *)p->misc.p + 128);
+  d_changed = reinterpret_cast<long long *>(c + 1);
+  BYO_CU(ctx, cudaFuncSetAttribute(k_pma_stream, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStreamSmem));
+  int per_sm = 0;
+  BYO_CU(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pma_stream, kStreamThreads, kStreamSmem));
+  if (per_sm < 1) return set_error(ctx, BYO_EDEVICE, "update stream: persistent kernel cannot be resident");
+  StreamCtl *hc = nullptr;
+  BYO_TRY(pinned(ctx, std::max<size_t>(sizeof(StreamCtl), 4096), (void **)&hc));
+  uint64_t bi = 0;
+  while (bi < nbatch) {
+    const uint64_t NL = p->NL;
+    const uint64_t cnt_b = h_boff[bi + 1] - h_boff[bi];
+    if (cnt_b == 0) {
+      bi++;
+      continue;
+    }
+    if (cnt_b > kSmallSort || 2 * cnt_b > NL) {  // not a small batch: the ordinary update
+      uint64_t ch = 0;
+      BYO_TRY(pma_update(g, d_keys + h_boff[bi], cnt_b, 0, h_ops[bi], &ch));
+      h_changed[bi] = (long long)ch;
+      bi++;
+      continue;
+    }
+    // the run of small batches from bi
+    uint64_t be = bi;
+    while (be < nbatch && h_boff[be + 1] - h_boff[be] <= kSmallSort && 2 * (h_boff[be + 1] - h_boff[be]) <= NL) be++;
+    BYO_TRY(ensure(ctx, p->keys_a, kSmallSort * 8));
+    BYO_TRY(ensure(ctx, p->bstart, std::max<uint64_t>(NL + 1, 2 * kSmallSort) * 8));
+    BYO_TRY(ensure(ctx, p->rpre, std::max<uint64_t>(NL + 1, 2 * kSmallSort) * 8));
+    BYO_TRY(ensure(ctx, p->win, ((g->n + 1) / kViewChunk + kSmallSort + 64) * 8));
+    BYO_TRY(ensure(ctx, p->ovf, (NL * kLeaf + kSmallSort + 1) * 8));
+    BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
+    std::memset(hc, 0, sizeof(StreamCtl));
+    hc->m = (long long)g->m;
+    BYO_CU(ctx, cudaMemcpyAsync(c, hc, sizeof(StreamCtl), cudaMemcpyHostToDevice, ctx->stream));
+    StreamArgs a;
+    a.src = p->src;
+    a.dst = p->dst;
+    a.cnt = p->cnt;
+    a.sep = p->sep;
+    a.NL = NL;
+    a.n = g->n;
+    a.off = g->d_off;
+    a.deg = g->d_deg;
+    a.keys = d_keys;
+    a.boff = d_boff;
+    a.ops = d_ops;
+    a.first = bi;
+    a.nbatch = be;
+    a.sorted = (uint64_t *)p->keys_a.p;
+    a.seg = (uint64_t *)p->bstart.p;
+    a.vrange = (uint64_t *)p->rpre.p;
+    a.chunks = (uint64_t *)p->win.p;
+    a.ovf = (uint64_t *)p->ovf.p;
+    a.ovf_off = (uint64_t *)p->ovf_off.p;
+    a.shrink_below = NL > 1 ? kRootMin * (double)NL * kLeaf : -1.0;
+    a.changed = d_changed;
+    a.ctl = c;
+    void *args[] = {(void *)&a};
+    BYO_CU(ctx, cudaLaunchCooperativeKernel((const void *)k_pma_stream, dim3(ctx->num_sms * per_sm),
+                                            dim3(kStreamThreads), args, kStreamSmem, ctx->stream));
+    ctx->launches++;
+    BYO_CU(ctx, cudaMemcpyAsync(hc, c, sizeof(StreamCtl), cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaMemcpyAsync(h_changed + bi, d_changed + bi, 8 * (be - bi), cudaMemcpyDeviceToHost,
+                                ctx->stream));
     BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-    rebuild = ((const unsigned int *)h)[1] != 0;
-    if (!rebuild) launch(ctx, k_pma_cover, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint8_t *)marks, NL,
-                         p->H, win);
+    if (hc->bar.err) return set_error(ctx, BYO_ETIMEDOUT, "update stream: grid barrier timed out");
+    BYO_TRY(check_launch(ctx, "pma_stream"));
+    const uint64_t done_to = hc->stop ? hc->stop - 1 : be;  // batches [bi, done_to) are complete
+    for (uint64_t k = bi; k < done_to; k++) h_changed[k] = h_changed[k] < 0 ? -h_changed[k] : h_changed[k];
+    g->m = (uint64_t)hc->m;
+    if (!hc->stop) {
+      bi = be;
+      continue;
+    }
+    if (hc->reason == 2) {
+      for (uint64_t k = done_to; k < nbatch; k++) h_changed[k] = 0;
+      return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+    }
+    // batch done_to merged with overflowing leaves (or shrinking): finish it
+    const long long delta = (long long)hc->ctr[2];
+    const uint64_t total = (uint64_t)((long long)g->m + delta);
+    const bool shrink = !h_ops[done_to] && (double)total < a.shrink_below;
+    h_changed[done_to] = delta < 0 ? -delta : delta;
+    const unsigned long long *d_nseg = &c->ctr[3];
+    BYO_TRY(pma_finish_windowed(g, true, a.seg, d_nseg, h_boff[done_to + 1] - h_boff[done_to], total, shrink));
+    bi = done_to + 1;
   }
-  BYO_TRY(ensure(ctx, p->staging, (total ? total : 1) * 8));
-  uint64_t *stg = (uint64_t *)p->staging.p;
-  launch(ctx, k_pma_gather, dim3(grid_for(ctx, NL * 32, 256, 16)), dim3(256), 0, (const uint32_t *)p->src,
-         (const uint32_t *)p->dst, (const uint32_t *)rcount, (const uint32_t *)p->cnt, NL, (const uint32_t *)win,
-         rebuild ? 1 : 0, (const uint64_t *)rpre, (const uint64_t *)p->ovf.p, (const uint64_t *)p->ovf_off.p, stg);
-  BYO_TRY(check_launch(ctx, "pma_gather"));
-  if (rebuild) {
-    ctx->last_update_strategy = 1;
-    p->rebuilds++;
-    return pma_layout(g, stg, total, leaves_for(total));
-  }
-  p->windows++;
-  launch_t(ctx, "pma_redistribute", k_pma_spread, dim3(grid_for(ctx, NL, 1, 16)), dim3(kPmaBlock), 0,
-           (const uint64_t *)stg, (const uint64_t *)rpre, (const uint32_t *)win, NL, p->src, p->dst, p->cnt, p->sep,
-           NL, 0, (const uint64_t *)p->sep);
-  BYO_TRY(check_launch(ctx, "pma_update"));
-  return pma_view(g);
+  return BYO_OK;
 }
 
 }  // namespace byo

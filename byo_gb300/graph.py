@@ -274,6 +274,20 @@ class Graph:
             a = (a[:, 0].astype(np.uint64) << np.uint64(32)) | a[:, 1].astype(np.uint64)
         return np.ascontiguousarray(a, np.uint64)
 
+    def update_stream(self, batches, ops):
+        """Applies update batches in order (ops[b]: True insert, False remove)
+        through byo_graph_update_stream; returns each batch's changed count."""
+        ks = [self._keys(b) for b in batches]
+        off = np.zeros(len(ks) + 1, np.uint64)
+        off[1:] = np.cumsum([len(k) for k in ks])
+        keys = np.concatenate(ks) if ks else np.zeros(0, np.uint64)
+        keys = np.ascontiguousarray(keys, np.uint64)
+        o = np.ascontiguousarray([1 if x else 0 for x in ops], np.uint8)
+        ch = np.zeros(max(len(ks), 1), np.uint64)
+        check(lib().byo_graph_update_stream(self.h, keys.ctypes.data, off.ctypes.data, o.ctypes.data, len(ks),
+                                            ch.ctypes.data), self.ctx.h)
+        return ch[:len(ks)].astype(np.int64)
+
     def insert_batch(self, batch, sorted=False):
         k = self._keys(batch)
         ch = ctypes.c_uint64(0)

@@ -263,6 +263,25 @@ int byo_pagerank_delta_device(byo_graph *g, double eps, double local_eps, uint32
  * (benchmarks/TriangleCounting/ShunTangwongsan15/Triangle.h:167-204). */
 int byo_triangle_count(byo_graph *g, uint64_t *count);
 
+/* A stream of update batches (Batch_insert_runner's loop,
+ * benchmarks/run_unweighted.h:781-893, as one call): batch b is keys
+ * [offsets[b], offsets[b+1]) (src << 32 | dst, unsorted, duplicates allowed),
+ * inserted when ops[b] != 0 and removed otherwise, in order.  Runs of small
+ * batches (at most 4096 keys and at most half as many as the container has
+ * leaves) are drained by one persistent kernel -- sort, segment search,
+ * merge and offset refresh per batch between grid barriers, one host
+ * synchronisation for the run; a batch that overflows a leaf stops the
+ * kernel, is finished on the windowed path and the run resumes after it;
+ * larger batches take byo_graph_insert/remove_batch.  changed[b] (may be NULL)
+ * receives each batch's count of keys inserted or removed.  A key with src or
+ * dst >= n gives BYO_EINVAL with the batches before it applied.  offsets and
+ * ops are host arrays; keys are host (byo_graph_update_stream) or device
+ * (_device) memory. */
+int byo_graph_update_stream(byo_graph *g, const uint64_t *h_keys, const uint64_t *offsets, const uint8_t *ops,
+                            uint64_t nbatch, uint64_t *changed);
+int byo_graph_update_stream_device(byo_graph *g, const uint64_t *d_keys, const uint64_t *offsets, const uint8_t *ops,
+                                   uint64_t nbatch, uint64_t *changed);
+
 /* ------------------------------------------------------------------ byte-PD graphs
  * The reference's compressed graphs: neighbour lists in the bytepd_amortized
  * encoding (gbbs/encodings/byte_pd_amortized.h:1100-1155,

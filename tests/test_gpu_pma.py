@@ -229,3 +229,85 @@ def test_two_level_sort_batches(ctx, oracle_mod):
     ro, rn = st.export_csr()
     _check_view(byo, O, G, ro, rn, (5,))
     G.close()
+
+
+def _stream_batches(O, rng, n, sizes, halves=False):
+    """Symmetrised batches of `sizes` random pairs (and of the first half of
+    each batch's pairs, so that removing them keeps the graph undirected)."""
+    out, half = [], []
+    for k in sizes:
+        pairs = rng.integers(0, n, size=(k, 2))
+        out.append(O.keys_from_pairs(pairs[:, 0], pairs[:, 1]))
+        half.append(O.keys_from_pairs(pairs[: k // 2, 0], pairs[: k // 2, 1]))
+    return (out, half) if halves else out
+
+
+@pytest.mark.gpu
+def test_update_stream_matches_batch_by_batch(ctx, oracle_mod):
+    """byo_graph_update_stream: runs of small batches in one persistent
+    kernel give the oracle's per-batch changed counts and contents; a batch
+    of more than 4096 keys in between takes the ordinary update."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 1 << 15
+    G = byo.Graph.generate(ctx, "rmat", seed=61, lg_n=15, draws=1 << 19, container="pma")
+    s, d = O.rmat_edges(61, 15, 1 << 19)
+    off, nb = O.build_csr(n, s, d)
+    st = O.Store(off, nb)
+    rng = np.random.default_rng(7)
+    sizes = [1, 3, 40, 700, 1, 2000, 9000, 64, 5, 300]
+    ins, halves = _stream_batches(O, rng, n, sizes, halves=True)
+    batches = ins + [ins[i] for i in (3, 0, 6, 9)] + [halves[5]]
+    ops = [True] * len(ins) + [False] * 5
+    exp = [st.insert_batch(b) if op else st.remove_batch(b) for b, op in zip(batches, ops)]
+    got = G.update_stream(batches, ops)
+    assert got.tolist() == exp
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (0, 3))
+    G.close()
+
+
+@pytest.mark.gpu
+def test_update_stream_overflow_shrink_invalid(ctx, oracle_mod):
+    """A batch that overflows a leaf stops the persistent kernel, is finished
+    on the windowed path, and the stream resumes; removes that shrink the
+    array rebuild it; a key >= n stops the stream with the batches before it
+    applied."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 1 << 12
+    G = byo.Graph.generate(ctx, "rmat", seed=62, lg_n=12, draws=1 << 15, container="pma")
+    s, d = O.rmat_edges(62, 12, 1 << 15)
+    off, nb = O.build_csr(n, s, d)
+    st = O.Store(off, nb)
+    rng = np.random.default_rng(8)
+    # 600 new neighbours of one vertex overflow its leaf
+    hub = O.keys_from_pairs(np.full(600, 77), rng.choice(n, 600, replace=False))
+    small = _stream_batches(O, rng, n, [50, 20, 5])
+    batches = [small[0], hub, small[1], small[2]]
+    ops = [True, True, True, True]
+    exp = [st.insert_batch(b) for b in batches]
+    assert G.update_stream(batches, ops).tolist() == exp
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (77,))
+    # remove nearly everything in small batches: the array shrinks (rebuilds) on the way
+    src = np.repeat(np.arange(n, dtype=np.uint64), np.diff(ro).astype(np.int64))
+    und = src < rn.astype(np.uint64)  # each undirected edge once; its batch removes both directions
+    us, ud = src[und], rn[und].astype(np.uint64)
+    chunks = [O.keys_from_pairs(us[i:i + 1500], ud[i:i + 1500]) for i in range(0, len(us) - 1500, 1500)]
+    exp = [st.remove_batch(c) for c in chunks]
+    assert G.update_stream(chunks, [False] * len(chunks)).tolist() == exp
+    ro, rn = st.export_csr()
+    _check_view(byo, O, G, ro, rn, (0,))
+    # an invalid key in the third batch: the first two are applied
+    good = _stream_batches(O, rng, n, [10, 10])
+    bad = np.array([(5 << 32) | n], np.uint64)
+    with pytest.raises(byo.ByoError) as e:
+        G.update_stream(good + [bad, good[0]], [True, True, True, True])
+    assert e.value.code == byo._abi.BYO_EINVAL
+    for b in good:
+        st.insert_batch(b)
+    ro, rn = st.export_csr()
+    o2, n2 = G.export_csr()
+    assert np.array_equal(o2, ro) and np.array_equal(n2, rn)
+    G.close()
