@@ -23,6 +23,9 @@ deduplicated, no self loops; the reference publishes no dataset for them):
            workload's graph, CSR and PMA.
   bytepd   the dynamic workload's graph in the byte-PD compressed format,
            decoded into a CSR on the GPU.
+  stream   200 small update batches inserted then removed on the mixed
+           workload's PMA through byo_graph_update_stream, against one call
+           per batch.
 
 The metric is BASELINE's composite; `value` is the step's edge operations per
 second in G/s: BFS traversed edges (undirected, Graph500 convention) + CC
@@ -820,6 +823,101 @@ def map_cpu_sample():
                       "%d threads), %.1f s" % (passes, O.num_threads(), secs)}
 
 
+# ------------------------------------------------------------------ update stream
+STREAM_BATCHES, STREAM_SEED = 200, 4242
+
+
+def stream_batches(n, seed):
+    """STREAM_BATCHES symmetrised uniform batches of 10-2000 pairs
+    (log-uniform), as Batch_insert_runner's small sizes produce them."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(10), np.log(2000), STREAM_BATCHES)).astype(np.int64)
+    out = []
+    for k in sizes:
+        pairs = rng.integers(0, n, size=(int(k), 2), dtype=np.uint64)
+        keys = np.concatenate([(pairs[:, 0] << np.uint64(32)) | pairs[:, 1],
+                               (pairs[:, 1] << np.uint64(32)) | pairs[:, 0]])
+        out.append(keys[(keys >> np.uint64(32)) != (keys & np.uint64(0xFFFFFFFF))])
+    return out
+
+
+def run_stream(args, rank, world, local_rank):
+    """Small update batches, one step = the 200 batches inserted and then
+    removed on the mixed workload's PMA (RMAT 2^24): through
+    byo_graph_update_stream (one persistent kernel per run of small batches)
+    and, for comparison, one byo_graph_insert/remove_batch_device call per
+    batch."""
+    import torch
+    import byo_gb300 as byo
+    from byo_gb300 import _abi
+    L = _abi.lib()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = byo.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    lg = args.lg or MIXED_LG
+    G = byo.Graph.generate(ctx, "rmat", seed=MIXED_SEED, lg_n=lg, draws=8 << lg, container="pma")
+    n, m0 = G.N(), G.M()
+    bs = stream_batches(n, STREAM_SEED)
+    nb = len(bs)
+    keys = np.concatenate(bs + bs)
+    offs = np.zeros(2 * nb + 1, np.uint64)
+    offs[1:] = np.cumsum([len(b) for b in bs + bs])
+    ops = np.array([1] * nb + [0] * nb, np.uint8)
+    d_keys = torch.from_numpy(keys.view(np.int64)).to(dev)
+    changed = np.zeros(2 * nb, np.uint64)
+    total_keys = int(offs[-1])
+
+    def stream_step():
+        _abi.check(L.byo_graph_update_stream_device(G.h, d_keys.data_ptr(), offs.ctypes.data, ops.ctypes.data,
+                                                    2 * nb, changed.ctypes.data), ctx.h)
+
+    ch = ctypes.c_uint64(0)
+
+    def batch_step():
+        for i in range(2 * nb):
+            f = L.byo_graph_insert_batch_device if ops[i] else L.byo_graph_remove_batch_device
+            _abi.check(f(G.h, d_keys.data_ptr() + 8 * int(offs[i]), int(offs[i + 1] - offs[i]), 0, ctypes.byref(ch)),
+                       ctx.h)
+
+    for _ in range(args.warmup):
+        stream_step()
+        batch_step()
+    assert G.M() == m0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    launches0 = ctx.launches
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    pushed = nvtx_push(torch, "timed")
+    ms_stream = timed(stream_step)
+    nvtx_pop(torch, pushed)
+    clk = clocks.stop()
+    launches = ctx.launches - launches0
+    ms_batch = timed(batch_step)
+    assert G.M() == m0
+    res = {"metric": "small update batches, keys applied per second (insert then remove, 10-2000 pairs each)",
+           "value": total_keys / (ms_stream / 1e3) / 1e9, "unit": "G keys/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_stream, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "u64 keys", "data": "synthetic (seeded RMAT, uniform update pairs)",
+           "config": {"workload": "stream: RMAT 2^%d PMA, %d batches of 10-2000 pairs, inserted then removed"
+                                  % (lg, nb), "n": n, "m": m0, "keys_per_step": total_keys,
+                      "us_per_batch_stream": ms_stream * 1e3 / (2 * nb),
+                      "us_per_batch_calls": ms_batch * 1e3 / (2 * nb),
+                      "speedup_vs_calls": ms_batch / ms_stream},
+           "gpu_launches": launches // max(args.steps, 1), "clocks": clk}
+    return res, ctx, G
+
+
 # ------------------------------------------------------------------ byte-PD graphs
 def run_bytepd(args, rank, world, local_rank):
     """Compressed graphs (gbbs/encodings/byte_pd_amortized.h): the dynamic
@@ -1238,7 +1336,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dynamic",
-                    choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map", "bytepd"])
+                    choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map", "bytepd",
+                             "stream"])
     ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
@@ -1295,6 +1394,9 @@ def main():
         res, ctx, G = run_map(args, rank, world, local_rank)
         if rank == 0 and not args.no_cpu_baseline:
             res["cpu_baseline"] = map_cpu_sample()
+        args.no_cpu_baseline = True
+    elif args.workload == "stream":
+        res, ctx, G = run_stream(args, rank, world, local_rank)
         args.no_cpu_baseline = True
     elif args.workload == "bytepd":
         res, ctx, G = run_bytepd(args, rank, world, local_rank)

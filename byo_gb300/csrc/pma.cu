@@ -1455,12 +1455,16 @@ constexpr size_t kStreamSmem = (size_t)kStreamWarps * (kLeaf + kOptSeg) * 8;
 
 struct StreamCtl {
   GridBar bar;
-  unsigned long long bounds[2];
-  unsigned long long ctr[6];  // [0] overflow cursor [1] overflowing leaves [2] delta [3] segments [4] view chunks
-  long long m;                // keys in the container
-  unsigned int stop, reason;  // batch index + 1 where the kernel stopped; 1 overflow or shrink, 2 invalid keys
+  unsigned long long bounds[2][2];
+  unsigned long long ctr[2][6];  // per buffer: [0] overflow cursor [1] overflowing leaves [2] delta [3] segments
+                                 // [4] view chunks
+  long long m;                   // keys in the container
+  unsigned int stop, reason;     // batch index + 1 where the kernel stopped; 1 overflow or shrink, 2 invalid keys
 };
 
+// Batch b uses buffer b & 1 of the sorted keys, segment list, offset ranges
+// and chunk list, so that the next batch can be sorted and its segments found
+// while this one is merged and its long ranges filled.
 struct StreamArgs {
   uint32_t *src, *dst, *cnt;
   const uint64_t *sep;
@@ -1471,7 +1475,8 @@ struct StreamArgs {
   const unsigned char *ops;
   uint64_t first, nbatch;
   uint64_t *sorted, *seg, *vrange, *chunks, *ovf, *ovf_off;
-  double shrink_below;  // a remove that leaves fewer keys rebuilds the array
+  uint64_t chunk_words;  // per buffer
+  double shrink_below;   // a remove that leaves fewer keys rebuilds the array
   long long *changed;
   StreamCtl *ctl;
 };
@@ -1498,6 +1503,22 @@ __device__ __forceinline__ void view_chunk_block(const uint32_t *__restrict__ sr
   }
 }
 
+__device__ __forceinline__ void stream_sort(const StreamArgs &a, uint64_t bi, uint64_t *As) {
+  StreamCtl *c = a.ctl;
+  const int buf = (int)(bi & 1);
+  if (threadIdx.x < 6) c->ctr[buf][threadIdx.x] = 0;
+  const uint64_t k0 = a.boff[bi], count = a.boff[bi + 1] - k0;
+  uint64_t *out = a.sorted + (size_t)buf * kSmallSort;
+  uint64_t(*red)[32] = reinterpret_cast<uint64_t(*)[32]>(As + kSmallSort);
+  if (count <= 1024) sort_small_block<1>(a.keys + k0, (uint32_t)count, out, c->bounds[buf], As, red);
+  else if (count <= 2048) sort_small_block<2>(a.keys + k0, (uint32_t)count, out, c->bounds[buf], As, red);
+  else sort_small_block<4>(a.keys + k0, (uint32_t)count, out, c->bounds[buf], As, red);
+}
+
+// Per batch bi, two phases between grid barriers:
+//   1. the long offset ranges of batch bi-1 (its merge is done), and the
+//      segments of batch bi (its keys were sorted during phase 2 of bi-1);
+//   2. the merge of batch bi by CTAs 1.., while CTA 0 sorts batch bi+1.
 __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
   extern __shared__ unsigned long long stream_smem[];
   uint64_t *As = reinterpret_cast<uint64_t *>(stream_smem);  // [kStreamWarps][kLeaf]
@@ -1505,52 +1526,69 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
   StreamCtl *c = a.ctl;
   const unsigned nb = gridDim.x, w = threadIdx.x >> 5;
   const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nthr = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t gw = tid >> 5, nw = nthr >> 5;
-  const ViewOut view{a.sep, a.n, a.off, a.vrange, a.chunks, &c->ctr[4]};
-  for (uint64_t bi = a.first; bi < a.nbatch; bi++) {
-    const uint64_t k0 = a.boff[bi], count = a.boff[bi + 1] - k0;
-    const int insert = a.ops[bi];
-    if (blockIdx.x == 0) {
-      if (threadIdx.x < 6) c->ctr[threadIdx.x] = 0;
-      uint64_t(*red)[32] = reinterpret_cast<uint64_t(*)[32]>(As + 4096);
-      if (count <= 1024) sort_small_block<1>(a.keys + k0, (uint32_t)count, a.sorted, c->bounds, As, red);
-      else if (count <= 2048) sort_small_block<2>(a.keys + k0, (uint32_t)count, a.sorted, c->bounds, As, red);
-      else sort_small_block<4>(a.keys + k0, (uint32_t)count, a.sorted, c->bounds, As, red);
+  // warps that merge: those of CTAs 1.. (all of them on a one-CTA grid)
+  const bool solo = nb == 1;
+  const uint64_t mw0 = solo ? 0 : 32, nmw = (nthr >> 5) - mw0, gw = (tid >> 5) - (solo ? 0 : 32);
+  if (blockIdx.x == 0) stream_sort(a, a.first, As);
+  if (!grid_sync(&c->bar, nb)) return;
+  for (uint64_t bi = a.first;; bi++) {
+    const int cur = (int)(bi & 1), prv = cur ^ 1;
+    const bool has = bi < a.nbatch;
+    const bool valid = has && c->bounds[cur][0] < a.n && c->bounds[cur][1] < a.n;
+    // phase 1
+    if (bi > a.first) {
+      const uint64_t nch = *(volatile unsigned long long *)&c->ctr[prv][4];
+      const uint64_t *chk = a.chunks + (size_t)prv * a.chunk_words;
+      for (uint64_t t = blockIdx.x; t < nch; t += gridDim.x)
+        view_chunk_block(a.src, a.cnt, a.seg + (size_t)prv * 2 * kSmallSort,
+                         a.vrange + (size_t)prv * 2 * kSmallSort, chk[t], a.off, reinterpret_cast<uint32_t *>(As));
+      if (tid == 0) {
+        const long long d = (long long)c->ctr[prv][2];
+        a.changed[bi - 1] = d;
+        c->m += d;
+      }
     }
+    const uint64_t count = has ? a.boff[bi + 1] - a.boff[bi] : 0;
+    if (valid)
+      segments_range(a.sep, a.NL, a.sorted + (size_t)cur * kSmallSort, count,
+                     a.seg + (size_t)cur * 2 * kSmallSort, &c->ctr[cur][3], tid, nthr);
     if (!grid_sync(&c->bar, nb)) return;
-    if (c->bounds[0] >= a.n || c->bounds[1] >= a.n) {
+    if (!has) return;
+    if (!valid) {
       if (tid == 0) {
         c->stop = (unsigned int)bi + 1;
         c->reason = 2;
       }
       return;
     }
-    segments_range(a.sep, a.NL, a.sorted, count, a.seg, &c->ctr[3], tid, nthr);
+    // phase 2
+    const int insert = a.ops[bi];
+    if (!solo && blockIdx.x == 0) {
+      if (bi + 1 < a.nbatch) stream_sort(a, bi + 1, As);
+    } else {
+      const ViewOut view{a.sep, a.n, a.off, a.vrange + (size_t)cur * 2 * kSmallSort,
+                         a.chunks + (size_t)cur * a.chunk_words, &c->ctr[cur][4]};
+      const uint64_t ns = *(volatile unsigned long long *)&c->ctr[cur][3];
+      long long dsum = 0;
+      for (uint64_t q = gw; q < ns; q += nmw)
+        dsum += merge_leaf<true>(q, a.src, a.dst, a.cnt, a.NL, a.sorted + (size_t)cur * kSmallSort, nullptr,
+                                 a.seg + (size_t)cur * 2 * kSmallSort, insert, nullptr, a.ovf, a.ovf_off, c->ctr[cur],
+                                 a.deg, view, As + (size_t)w * kLeaf, Bs + (size_t)w * kOptSeg);
+      if (lane_id() == 0 && dsum) atomicAdd(&c->ctr[cur][2], (unsigned long long)dsum);
+      if (solo) {
+        __syncthreads();
+        if (bi + 1 < a.nbatch) stream_sort(a, bi + 1, As);
+      }
+    }
     if (!grid_sync(&c->bar, nb)) return;
-    const uint64_t ns = *(volatile unsigned long long *)&c->ctr[3];
-    long long dsum = 0;
-    for (uint64_t q = gw; q < ns; q += nw)
-      dsum += merge_leaf<true>(q, a.src, a.dst, a.cnt, a.NL, a.sorted, nullptr, a.seg, insert, nullptr, a.ovf,
-                               a.ovf_off, c->ctr, a.deg, view, As + (size_t)w * kLeaf, Bs + (size_t)w * kOptSeg);
-    if (lane_id() == 0 && dsum) atomicAdd(&c->ctr[2], (unsigned long long)dsum);
-    if (!grid_sync(&c->bar, nb)) return;
-    const long long delta = (long long)*(volatile unsigned long long *)&c->ctr[2];
-    const long long total = c->m + delta;
-    if (*(volatile unsigned long long *)&c->ctr[1] || (!insert && (double)total < a.shrink_below)) {
+    const long long total = c->m + (long long)*(volatile unsigned long long *)&c->ctr[cur][2];
+    if (*(volatile unsigned long long *)&c->ctr[cur][1] || (!insert && (double)total < a.shrink_below)) {
       if (tid == 0) {
         c->stop = (unsigned int)bi + 1;
         c->reason = 1;
       }
       return;
     }
-    const uint64_t nch = *(volatile unsigned long long *)&c->ctr[4];
-    for (uint64_t t = blockIdx.x; t < nch; t += gridDim.x)
-      view_chunk_block(a.src, a.cnt, a.seg, a.vrange, a.chunks[t], a.off, reinterpret_cast<uint32_t *>(As));
-    if (tid == 0) {
-      a.changed[bi] = delta;
-      c->m = total;
-    }
-    if (!grid_sync(&c->bar, nb)) return;
   }
 }
 
@@ -1591,10 +1629,11 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
     // the run of small batches from bi
     uint64_t be = bi;
     while (be < nbatch && h_boff[be + 1] - h_boff[be] <= kSmallSort && 2 * (h_boff[be + 1] - h_boff[be]) <= NL) be++;
-    BYO_TRY(ensure(ctx, p->keys_a, kSmallSort * 8));
-    BYO_TRY(ensure(ctx, p->bstart, std::max<uint64_t>(NL + 1, 2 * kSmallSort) * 8));
-    BYO_TRY(ensure(ctx, p->rpre, std::max<uint64_t>(NL + 1, 2 * kSmallSort) * 8));
-    BYO_TRY(ensure(ctx, p->win, ((g->n + 1) / kViewChunk + kSmallSort + 64) * 8));
+    const uint64_t chunk_words = (g->n + 1) / kViewChunk + kSmallSort + 64;
+    BYO_TRY(ensure(ctx, p->keys_a, 2 * kSmallSort * 8));
+    BYO_TRY(ensure(ctx, p->bstart, std::max<uint64_t>(NL + 1, 4 * kSmallSort) * 8));
+    BYO_TRY(ensure(ctx, p->rpre, std::max<uint64_t>(NL + 1, 4 * kSmallSort) * 8));
+    BYO_TRY(ensure(ctx, p->win, 2 * chunk_words * 8));
     BYO_TRY(ensure(ctx, p->ovf, (NL * kLeaf + kSmallSort + 1) * 8));
     BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
     std::memset(hc, 0, sizeof(StreamCtl));
@@ -1620,6 +1659,7 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
     a.chunks = (uint64_t *)p->win.p;
     a.ovf = (uint64_t *)p->ovf.p;
     a.ovf_off = (uint64_t *)p->ovf_off.p;
+    a.chunk_words = chunk_words;
     a.shrink_below = NL > 1 ? kRootMin * (double)NL * kLeaf : -1.0;
     a.changed = d_changed;
     a.ctl = c;
@@ -1645,12 +1685,14 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
       return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
     }
     // batch done_to merged with overflowing leaves (or shrinking): finish it
-    const long long delta = (long long)hc->ctr[2];
+    const int buf = (int)(done_to & 1);
+    const long long delta = (long long)hc->ctr[buf][2];
     const uint64_t total = (uint64_t)((long long)g->m + delta);
     const bool shrink = !h_ops[done_to] && (double)total < a.shrink_below;
     h_changed[done_to] = delta < 0 ? -delta : delta;
-    const unsigned long long *d_nseg = &c->ctr[3];
-    BYO_TRY(pma_finish_windowed(g, true, a.seg, d_nseg, h_boff[done_to + 1] - h_boff[done_to], total, shrink));
+    const unsigned long long *d_nseg = &c->ctr[buf][3];
+    BYO_TRY(pma_finish_windowed(g, true, a.seg + (size_t)buf * 2 * kSmallSort, d_nseg,
+                                h_boff[done_to + 1] - h_boff[done_to], total, shrink));
     bi = done_to + 1;
   }
   return BYO_OK;
