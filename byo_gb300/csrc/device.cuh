@@ -96,4 +96,42 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// Bitonic sort of R*32 keys held by a warp in registers: element r*32 + lane
+// lives in register r of that lane; strides below 32 exchange through
+// shuffles, larger strides swap registers inside a lane.
+template <int R>
+__device__ __forceinline__ void warp_bitonic(uint64_t (&v)[R]) {
+  const unsigned lane = lane_id();
+#pragma unroll
+  for (int size = 2; size <= R * 32; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride >= 32) {
+        const int rs = stride / 32;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          if ((r & rs) == 0) {
+            const bool up = ((r * 32) & size) == 0;
+            const uint64_t x = v[r], y = v[r ^ rs];
+            if ((x > y) == up) {
+              v[r] = y;
+              v[r ^ rs] = x;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const unsigned i = r * 32 + lane;
+          const uint64_t x = v[r];
+          const uint64_t y = __shfl_xor_sync(kFull, x, stride);
+          const bool up = (i & size) == 0, lower = (lane & stride) == 0;
+          const uint64_t lo = x < y ? x : y, hi = x < y ? y : x;
+          v[r] = (lower == up) ? lo : hi;
+        }
+      }
+    }
+  }
+}
+
 }  // namespace byo

@@ -291,48 +291,12 @@ __global__ void k_bucket_scatter(const uint64_t *__restrict__ keys, uint64_t cou
   }
 }
 
-// One warp per bucket: bitonic network in registers.  Element r*32 + lane
-// lives in register r of that lane: strides below 32 exchange through
-// shuffles, larger strides swap registers inside a lane, so the sort touches
-// no shared memory.  Buckets are padded with ~0 to R*32 keys; buckets above
-// kWarpBucket keys are listed for the LSD fallback.
+// One warp per bucket: warp_bitonic (device.cuh).  Buckets are padded with
+// ~0 to R*32 keys; buckets above kWarpBucket keys are listed for the LSD
+// fallback.
 constexpr uint32_t kWarpBucket = 512;
 constexpr uint64_t kTwoLevelMin = 1ull << 21;  // batches from this size take the two-level sort
 
-template <int R>
-__device__ __forceinline__ void warp_bitonic(uint64_t (&v)[R]) {
-  const unsigned lane = lane_id();
-#pragma unroll
-  for (int size = 2; size <= R * 32; size <<= 1) {
-#pragma unroll
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      if (stride >= 32) {
-        const int rs = stride / 32;
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-          if ((r & rs) == 0) {
-            const bool up = ((r * 32) & size) == 0;
-            const uint64_t x = v[r], y = v[r ^ rs];
-            if ((x > y) == up) {
-              v[r] = y;
-              v[r ^ rs] = x;
-            }
-          }
-        }
-      } else {
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-          const unsigned i = r * 32 + lane;
-          const uint64_t x = v[r];
-          const uint64_t y = __shfl_xor_sync(kFull, x, stride);
-          const bool up = (i & size) == 0, lower = (lane & stride) == 0;
-          const uint64_t lo = x < y ? x : y, hi = x < y ? y : x;
-          v[r] = (lower == up) ? lo : hi;
-        }
-      }
-    }
-  }
-}
 
 template <int R>
 __device__ __forceinline__ void bucket_sort_regs(const uint64_t *__restrict__ in, uint64_t *out, uint64_t lo,
