@@ -22,6 +22,7 @@ NONE = 0xFFFFFFFF
 
 CONTAINER_CSR = 0
 CONTAINER_PMA = 1
+CONTAINER_VOS = 2
 
 GEN_RMAT, GEN_ER, GEN_GRID, GEN_CHUNG_LU = 0, 1, 2, 3
 
@@ -126,6 +127,7 @@ SIGNATURES = {
     "byo_pagerank_delta_device": (_int, [_vp, _dbl, _dbl, _u32, _vp, _P(_u32), _P(_dbl)]),
     "byo_triangle_count": (_int, [_vp, _P(_u64)]),
     "byo_map_sum": (_int, [_vp, _P(_u64)]),
+    "byo_graph_create": (_int, [_vp, _int, _u64, _u64, _vp, _vp, _P(_vp)]),
     "byo_graph_update_stream": (_int, [_vp, _vp, _vp, _vp, _u64, _vp]),
     "byo_graph_update_stream_device": (_int, [_vp, _vp, _vp, _vp, _u64, _vp]),
     "byo_graph_from_bytepd": (_int, [_vp, _u64, _vp, _vp, _vp, _u64, _u32, _int, _P(_vp)]),

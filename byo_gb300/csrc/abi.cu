@@ -108,6 +108,15 @@ int byo_graph_create_pma(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h
   return graph_from_host_csr(ctx, BYO_CONTAINER_PMA, n, m, h_offsets, h_nbrs, out);
 }
 
+int byo_graph_create(byo_ctx *ctx, int container, uint64_t n, uint64_t m, const uint64_t *h_offsets,
+                     const uint32_t *h_nbrs, byo_graph **out) {
+  if (!ctx || !out) return BYO_EINVAL;
+  *out = nullptr;
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
+    return set_error(ctx, BYO_EINVAL, "unknown container");
+  return graph_from_host_csr(ctx, container, n, m, h_offsets, h_nbrs, out);
+}
+
 int byo_adj_read(const char *path, int binary, uint64_t *n, uint64_t *m, uint64_t *offsets, uint32_t *nbrs) {
   if (!path || !n || !m || (offsets && !nbrs && *m)) return BYO_EINVAL;
   return adj_read_host(nullptr, path, binary, n, m, offsets, nbrs);
@@ -116,7 +125,7 @@ int byo_adj_read(const char *path, int binary, uint64_t *n, uint64_t *m, uint64_
 int byo_graph_read_adj(byo_ctx *ctx, const char *path, int binary, int container, byo_graph **out) {
   if (!ctx || !path || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
     return set_error(ctx, BYO_EINVAL, "unknown container");
   uint64_t n = 0, m = 0;
   BYO_TRY(adj_read_host(ctx, path, binary, &n, &m, nullptr, nullptr));
@@ -130,7 +139,7 @@ int byo_graph_from_bytepd(byo_ctx *ctx, uint64_t n, const uint64_t *byte_offsets
                           const uint8_t *bytes, uint64_t nbytes, uint32_t block, int container, byo_graph **out) {
   if (!ctx || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
     return set_error(ctx, BYO_EINVAL, "unknown container");
   return graph_from_bytepd_host(ctx, n, byte_offsets, degrees, bytes, nbytes, block ? block : 1000, container, out);
 }
@@ -138,7 +147,7 @@ int byo_graph_from_bytepd(byo_ctx *ctx, uint64_t n, const uint64_t *byte_offsets
 int byo_graph_read_bytepd(byo_ctx *ctx, const char *path, uint32_t block, int container, byo_graph **out) {
   if (!ctx || !path || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
     return set_error(ctx, BYO_EINVAL, "unknown container");
   return bytepd_read_file(ctx, path, block ? block : 1000, container, out);
 }
@@ -165,7 +174,7 @@ int byo_graph_write_adj(byo_graph *g, const char *path, int binary) {
 int byo_graph_generate(byo_ctx *ctx, int container, const byo_gen_spec *spec, byo_graph **out) {
   if (!ctx || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA)
+  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
     return set_error(ctx, BYO_EINVAL, "unknown container");
   return graph_generate(ctx, container, spec, out);
 }
@@ -181,6 +190,7 @@ void byo_graph_destroy(byo_graph *g) {
   for (auto &b : g->ws) free_buf(b);
   if (g->pma) pma_destroy(g->pma);
   else if (g->d_slots) cudaFree(g->d_slots);
+  if (g->vos) vos_destroy(g->vos);
   if (g->d_off) cudaFree(g->d_off);
   if (g->d_deg) cudaFree(g->d_deg);
   delete g;
@@ -256,8 +266,8 @@ static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int
   if (!g) return BYO_EINVAL;
   byo_ctx *ctx = g->ctx;
   if (changed) *changed = 0;
-  if (g->container != BYO_CONTAINER_PMA)
-    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA container");
+  if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS)
+    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA or VOS container");
   if (count == 0) return BYO_OK;
   if (!keys) return set_error(ctx, BYO_EINVAL, "null keys");
   const uint64_t *d = keys;
@@ -267,6 +277,7 @@ static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int
     BYO_CU(ctx, cudaMemcpyAsync(buf, keys, count * 8, cudaMemcpyHostToDevice, ctx->stream));
     d = buf;
   }
+  if (g->container == BYO_CONTAINER_VOS) return vos_update(g, d, count, sorted, insert, changed);
   return pma_update(g, d, count, sorted, insert, changed);
 }
 
@@ -274,8 +285,8 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
                                 const uint8_t *h_ops, uint64_t nbatch, uint64_t *changed) {
   if (!g || (nbatch && (!keys || !h_offsets || !h_ops))) return BYO_EINVAL;
   byo_ctx *ctx = g->ctx;
-  if (g->container != BYO_CONTAINER_PMA)
-    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA container");
+  if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS)
+    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA or VOS container");
   if (!nbatch) return BYO_OK;
   if (h_offsets[0] != 0) return set_error(ctx, BYO_EINVAL, "update stream: offsets[0] != 0");
   for (uint64_t b = 0; b < nbatch; b++)
@@ -296,7 +307,17 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
   for (uint64_t b = 0; b < nbatch; b++) ops[b] = h_ops[b] ? 1 : 0;
   BYO_CU(ctx, cudaMemcpyAsync(d_ops, ops.data(), nbatch, cudaMemcpyHostToDevice, ctx->stream));
   std::vector<long long> ch(nbatch);
-  const int rc = pma_update_stream(g, d, sb, h_offsets, d_ops, ops.data(), nbatch, ch.data());
+  int rc = BYO_OK;
+  if (g->container == BYO_CONTAINER_VOS) {  // one update per batch
+    for (uint64_t b = 0; b < nbatch && rc == BYO_OK; b++) {
+      uint64_t c = 0;
+      if (h_offsets[b + 1] > h_offsets[b])
+        rc = vos_update(g, d + h_offsets[b], h_offsets[b + 1] - h_offsets[b], 0, ops[b], &c);
+      ch[b] = (long long)c;
+    }
+  } else {
+    rc = pma_update_stream(g, d, sb, h_offsets, d_ops, ops.data(), nbatch, ch.data());
+  }
   if (changed)
     for (uint64_t b = 0; b < nbatch; b++) changed[b] = (uint64_t)ch[b];
   return rc;

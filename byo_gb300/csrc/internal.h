@@ -30,6 +30,7 @@ struct DevBuf {
 };
 
 struct Pma;  // pma.cu
+struct Vos;  // vos.cu
 struct Mlp;  // mlp.cu
 
 }  // namespace byo
@@ -66,6 +67,7 @@ struct byo_graph {
   uint64_t nslots = 0;
   uint32_t *d_deg = nullptr;
   byo::Pma *pma = nullptr;
+  byo::Vos *vos = nullptr;  // vector of per-vertex runs (BYO_CONTAINER_VOS)
   byo::DevBuf ws[24];  // per-graph workspaces, indexed by the Ws enum
   byo_tuning tune = {};  // launch shapes set by the caller or the autotuner (0 = automatic)
   // A PMA keeps a compact CSR snapshot of its contents for the read-only
@@ -244,6 +246,10 @@ uint64_t map_remote_bytes(uint64_t n, uint32_t width);
 
 // ---------------------------------------------------------------- PMA (pma.cu)
 int pma_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);
+int vos_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);
+int vos_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert, uint64_t *changed);
+int vos_compact(byo_graph *g, const uint64_t *offc, uint32_t *out);
+void vos_destroy(Vos *v);
 int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_boff, const uint64_t *h_boff,
                       const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed);
 int pma_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert,

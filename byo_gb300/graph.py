@@ -106,6 +106,15 @@ class Context:
                      unvisited=r.unvisited, ms=r.ms, features=list(r.features)) for r in arr[:n.value]]
 
 
+def _container(name):
+    """csr (static), pma (packed-memory array, CPMA / PMA_graph) or vos (vector
+    of per-vertex sorted runs, the vector-of-sets containers)."""
+    table = {"csr": _abi.CONTAINER_CSR, "pma": _abi.CONTAINER_PMA, "vos": _abi.CONTAINER_VOS}
+    if name not in table:
+        raise ValueError("container must be csr, pma or vos")
+    return table[name]
+
+
 class Graph:
     """gbbs::Graph<Rep, symmetric=true, full_api> over a device container."""
 
@@ -121,8 +130,8 @@ class Graph:
         nb = np.ascontiguousarray(nbrs, np.uint32)
         n = len(off) - 1
         h = ctypes.c_void_p()
-        fn = lib().byo_graph_create_pma if container == "pma" else lib().byo_graph_create_csr
-        check(fn(ctx.h, n, len(nb), _ptr(off), _ptr(nb), ctypes.byref(h)), ctx.h)
+        check(lib().byo_graph_create(ctx.h, _container(container), n, len(nb), _ptr(off), _ptr(nb), ctypes.byref(h)),
+              ctx.h)
         return cls(ctx, h)
 
     @classmethod
@@ -132,7 +141,7 @@ class Graph:
                  "chung_lu": _abi.GEN_CHUNG_LU}
         spec = _abi.GenSpec(kinds[kind], seed, lg_n, n, draws, a, b, c, exponent)
         h = ctypes.c_void_p()
-        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        cont = _container(container)
         check(lib().byo_graph_generate(ctx.h, cont, ctypes.byref(spec), ctypes.byref(h)), ctx.h)
         return cls(ctx, h)
 
@@ -182,7 +191,7 @@ class Graph:
 
     @property
     def container(self):
-        return "pma" if lib().byo_graph_container(self.h) == _abi.CONTAINER_PMA else "csr"
+        return {_abi.CONTAINER_PMA: "pma", _abi.CONTAINER_VOS: "vos"}.get(lib().byo_graph_container(self.h), "csr")
 
     def degrees(self):
         out = np.empty(self.N(), np.uint32)
@@ -227,7 +236,7 @@ class Graph:
     def read_adj(cls, ctx, path, binary=False, container="csr"):
         """read_unweighted_symmetric_graph (graph_io.h:98-124) into a container."""
         h = ctypes.c_void_p()
-        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        cont = _container(container)
         check(lib().byo_graph_read_adj(ctx.h, os.fsencode(path), int(binary), cont, ctypes.byref(h)), ctx.h)
         return cls(ctx, h)
 
@@ -236,7 +245,7 @@ class Graph:
         """read_compressed_symmetric_graph (graph_io.h:351-390): a byte-PD file,
         decoded on the GPU."""
         h = ctypes.c_void_p()
-        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        cont = _container(container)
         check(lib().byo_graph_read_bytepd(ctx.h, os.fsencode(path), block, cont, ctypes.byref(h)), ctx.h)
         return cls(ctx, h)
 
@@ -247,7 +256,7 @@ class Graph:
         dg = np.ascontiguousarray(degrees, np.uint32)
         by = np.ascontiguousarray(data, np.uint8)
         h = ctypes.c_void_p()
-        cont = _abi.CONTAINER_PMA if container == "pma" else _abi.CONTAINER_CSR
+        cont = _container(container)
         check(lib().byo_graph_from_bytepd(ctx.h, len(dg), bo.ctypes.data, dg.ctypes.data, by.ctypes.data, len(by),
                                           block, cont, ctypes.byref(h)), ctx.h)
         return cls(ctx, h)

@@ -69,12 +69,19 @@ const char *byo_version(void);
  * CSR (graph_io.h:117-123 builds it; run_csr.cc:87-106 and
  * run_single_pma.cc:75-89 consume it): offsets[n+1] and nbrs[m], sorted and
  * duplicate-free per vertex.  The arrays are copied; the caller keeps them. */
-enum byo_container { BYO_CONTAINER_CSR = 0, BYO_CONTAINER_PMA = 1 };
+/* CSR (static), PMA (one packed-memory array of src << 32 | dst keys, the
+ * CPMA / PMA_graph counterpart) and VOS (a vector of per-vertex sorted runs
+ * with slack, the counterpart of the vector-of-sets containers,
+ * run_vector_pma.cc / run_vector_vector.cc).  PMA and VOS take updates. */
+enum byo_container { BYO_CONTAINER_CSR = 0, BYO_CONTAINER_PMA = 1, BYO_CONTAINER_VOS = 2 };
 
 int byo_graph_create_csr(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h_offsets,
                          const uint32_t *h_nbrs, byo_graph **out);
 int byo_graph_create_pma(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h_offsets,
                          const uint32_t *h_nbrs, byo_graph **out);
+/* Either container from a CSR (sorted, duplicate-free lists, copied in). */
+int byo_graph_create(byo_ctx *ctx, int container, uint64_t n, uint64_t m, const uint64_t *h_offsets,
+                     const uint32_t *h_nbrs, byo_graph **out);
 void byo_graph_destroy(byo_graph *g);
 int byo_graph_container(const byo_graph *g);
 /* G.N() / num_vertices() (graph.h:2627; run_csr.cc:31) */
