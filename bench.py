@@ -27,7 +27,7 @@ deduplicated, no self loops; the reference publishes no dataset for them):
            workload's PMA through byo_graph_update_stream, against one call
            per batch.
 
-The metric is BASELINE's composite; `value` is the step's edge operations per
+The metric is the composite of BFS, CC, PageRank and update rates; `value` is the step's edge operations per
 second in G/s: BFS traversed edges (undirected, Graph500 convention) + CC
 edges (undirected) + PageRank directed edges x iterations + inserted and
 removed directed keys.  The per-component rates are in `components`.
@@ -37,7 +37,7 @@ API, CUDA events on the library's stream); `e2e` runs the same step through
 the public host API with the batch in pinned host memory and every result
 (parents, labels, ranks) copied back to the host inside the timed region.
 Under torchrun (N > 1) every rank runs an independent replica (the path does
-not shard in this build): weak scaling, value = all ranks' work / max time.
+not shard): weak scaling, value = all ranks' work / max time.
 """
 import argparse
 import ctypes
@@ -189,7 +189,7 @@ def run_ours(args, rank, world, local_rank):
     ctx = byo.Context(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
     dynamic = args.workload == "dynamic"
-    container = "pma" if dynamic else "csr"
+    container = args.container if dynamic else "csr"
     t0 = time.time()
     G = byo.Graph.generate(ctx, "rmat", seed=SEED, lg_n=LG_N, draws=DRAWS, container=container)
     n, m0 = G.N(), G.M()
@@ -353,7 +353,7 @@ def run_ours(args, rank, world, local_rank):
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 ids / fp32-kahan pagerank (fp64 residual)",
         "data": "synthetic (seeded RMAT, no dataset)",
-        "config": {"workload": "config[1] dynamic PMA: RMAT 2^22, 2^26 draws, batch 1e7 pairs" if dynamic
+        "config": {"workload": "dynamic %s: RMAT 2^22, 2^26 draws, batch 1e7 pairs" % container.upper() if dynamic
                    else "static CSR: RMAT 2^22, 2^26 draws",
                    "n": n, "m": m_trav, "batch_pairs": BATCH if dynamic else 0, "bfs_src": SRC,
                    "pr_eps": PR_EPS, "pr_max_iters": PR_ITERS, "policy": args.policy,
@@ -1309,7 +1309,7 @@ def run_reference(args, dynamic):
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps, "higher_is_better": True,
             "impl": "reference",
-            "config": {"workload": "config[1] dynamic PMA: RMAT 2^22, 2^26 draws, batch 1e7 pairs" if dynamic
+            "config": {"workload": "dynamic PMA: RMAT 2^22, 2^26 draws, batch 1e7 pairs" if dynamic
                        else "static CSR: RMAT 2^22, 2^26 draws"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
@@ -1339,6 +1339,8 @@ def main():
                     choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map", "bytepd",
                              "stream"])
     ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
+    ap.add_argument("--container", default="pma", choices=["pma", "vos"],
+                    help="dynamic: the container updated (pma: packed-memory array; vos: vector of per-vertex runs)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
                     help="auto: the committed learned network if present, else m20")

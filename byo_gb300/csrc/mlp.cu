@@ -3,8 +3,8 @@
 //   0 push, 1 pull, 2 blocked      (per edgeMap round, from frontier statistics)
 //   3 in-place merge, 4 rebuild    (per container update, from batch statistics)
 // The choice never changes a result, only speed.  GBBS's m/20 rule stays the
-// fallback (no trained network) and the judge: the network's pick replaces the
-// rule's only when it predicts a gain of more than kJudgeMargin.
+// fallback (no trained network) and the arbiter: the network's pick replaces the
+// rule's only when it predicts a gain of more than kArbiterMargin.
 //
 // Training is on the device with the kernels below: one CTA runs Adam over
 // minibatches of kMb samples; activations of a minibatch sit in shared memory,
@@ -313,7 +313,7 @@ int update_strategy(byo_ctx *ctx, uint64_t batch, uint64_t m, uint64_t slots, in
   float x[kIn], y[kOut];
   update_features(batch, m, slots, sorted, insert, x);
   forward_host(ctx->policy->h_params, x, y);
-  return (y[3] - y[4] > kJudgeMargin) ? 1 : 0;
+  return (y[3] - y[4] > kArbiterMargin) ? 1 : 0;
 }
 
 }  // namespace byo

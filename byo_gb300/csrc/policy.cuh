@@ -4,8 +4,8 @@
 // five actions: 0 push, 1 pull, 2 blocked (per edgeMap round), 3 in-place
 // merge, 4 rebuild (per container update).  Parameters are packed as W1 [32x16],
 // b1, W2 [32x32], b2, W3 [5x32], b3.  GBBS's m/20 rule
-// (edge_map_data.h:254-307) is the fallback and the judge: the network's pick
-// replaces the rule's only when it predicts a gain above kJudgeMargin.
+// (edge_map_data.h:254-307) is the fallback and the arbiter: the network's pick
+// replaces the rule's only when it predicts a gain above kArbiterMargin.
 #pragma once
 
 #include <cuda_pipeline.h>
@@ -20,7 +20,7 @@ constexpr int kW1 = 0, kB1 = kW1 + kH * kIn, kW2 = kB1 + kH, kB2 = kW2 + kH * kH
               kB3 = kW3 + kOut * kH, kParams = kB3 + kOut;  // 1765
 // The network must predict a gain of more than 2^(16*margin) - 1 (about 7%)
 // over the rule's choice before it overrides it.
-constexpr float kJudgeMargin = 0.006f;
+constexpr float kArbiterMargin = 0.006f;
 
 // The network is consulted when the frontier's size plus out-degree is within
 // kGateFactor of the m/20 threshold, when the round before was dense, or when
@@ -91,8 +91,8 @@ __device__ __forceinline__ void round_policy_warp(const float *P, RoundStats *st
     int best = 0;
     for (int o = 1; o < 3; o++)
       if (y[o] < y[best]) best = o;
-    // the m/20 rule judges: keep its choice unless the predicted gain is clear
-    if (y[fallback] - y[best] <= kJudgeMargin) best = fallback;
+    // the m/20 rule arbitrates: keep its choice unless the predicted gain is clear
+    if (y[fallback] - y[best] <= kArbiterMargin) best = fallback;
     st->mode = (unsigned long long)best;
   }
 }

@@ -11,7 +11,7 @@ as rebuild (byo_update_sample).
 
 Targets are log2(1 + microseconds) / 16.  A trained network is installed with
 install(); BFS(..., policy=POLICY_LEARNED) and update policy UPDATE_LEARNED use
-it, and the m/20 rule stays the fallback and the judge inside the engine.
+it, and the m/20 rule stays the fallback and the arbiter inside the engine.
 """
 import argparse
 import ctypes
@@ -133,20 +133,20 @@ def loss_grad(ctx, params, X, Y, M):
     return float(loss.value), g
 
 
-JUDGE_MARGIN = 0.006  # the engine's kJudgeMargin (a predicted gain of about 7%)
+ARBITER_MARGIN = 0.006  # the engine's kArbiterMargin (a predicted gain of about 7%)
 GATE_FACTOR = 64      # the engine's kGateFactor
 GATE_HUB_BIN = 5      # the engine's kGateHubBin (degree >= 4^5)
 
 
 def round_choices(ctx, params, X, fallback):
     """The engine's decision rule applied to predictions: argmin over the
-    three directions unless the rule's choice is within the judge margin, and
+    three directions unless the rule's choice is within the arbiter margin, and
     the rule alone for frontiers far below its threshold without a hub
     (feature 14 is (|F| + outdeg) / (m/20), features 6..13 the degree
     histogram by powers of 4)."""
     P = forward(ctx, params, X)[:, :3]
     best = P.argmin(1)
-    keep = P[np.arange(len(P)), fallback] - P[np.arange(len(P)), best] <= JUDGE_MARGIN
+    keep = P[np.arange(len(P)), fallback] - P[np.arange(len(P)), best] <= ARBITER_MARGIN
     hub = (X[:, 6 + GATE_HUB_BIN:14] > 0).any(1)
     keep |= (X[:, 14] * GATE_FACTOR <= 1.0) & ~hub
     return np.where(keep, fallback, best)
@@ -242,7 +242,7 @@ def main():
                         "best_us": round_cost(Yt, Yt[:, :3].argmin(1))}
     pu = forward(ctx, params, ux)
     upd = {"samples": int(len(ux)), "merge_us": float(micros(uy[:, 3]).sum()),
-           "learned_us": float(micros(np.where(pu[:, 3] - pu[:, 4] > JUDGE_MARGIN, uy[:, 4], uy[:, 3])).sum()),
+           "learned_us": float(micros(np.where(pu[:, 3] - pu[:, 4] > ARBITER_MARGIN, uy[:, 4], uy[:, 3])).sum()),
            "best_us": float(micros(uy[:, 3:5].min(1)).sum())}
     np.save(args.out, params)
     meta = {"train_samples": int(len(X)), "epochs": args.epochs, "loss_first": float(losses[0]),

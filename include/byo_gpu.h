@@ -390,7 +390,7 @@ int byo_ctx_kernel_time(byo_ctx *ctx, const char *tag, uint64_t *launches, doubl
  * own kernels on samples the engine logs (round logs with round timing on,
  * byo_update_sample).  BYO_POLICY_LEARNED rounds and BYO_UPDATE_LEARNED
  * batches use it; the m/20 rule (edge_map_data.h:254-307) and in-place merge
- * remain the fallback and judge.  No counterpart in the reference beyond the
+ * remain the fallback and arbiter.  No counterpart in the reference beyond the
  * rule it learns around. */
 #define BYO_POLICY_NFEATURES 16
 #define BYO_POLICY_NOUTPUTS 5
