@@ -220,35 +220,59 @@ __device__ __forceinline__ uint64_t seg_of(const uint64_t *pre, uint64_t nseg, u
 }
 
 // the old keys of the touched runs, flattened: each moves to its place in the
-// staging copy of its run
-__global__ void k_vos_shift(const uint64_t *__restrict__ keys, uint64_t cnt, const uint64_t *__restrict__ segs,
-                            uint64_t nseg, const uint64_t *__restrict__ abase, uint64_t total_a,
-                            const uint64_t *__restrict__ tbase, const uint32_t *__restrict__ rk,
-                            const uint32_t *__restrict__ kflag, const uint64_t *__restrict__ kscan,
-                            const uint64_t *__restrict__ base, const uint32_t *__restrict__ slots, int insert,
-                            uint32_t *temp) {
-  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total_a;
-       t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t s = seg_of(abase, nseg, t);
-    const uint64_t b0 = segs[s], b1 = s + 1 < nseg ? segs[s + 1] : cnt;
-    const uint64_t v = keys[b0] >> 32;
-    const uint32_t i = (uint32_t)(t - abase[s]);
-    const uint32_t x = slots[base[v] + i];
-    uint64_t l = b0, h = b1;
-    if (insert) {  // batch keys with rank <= i go before A[i]
-      while (l < h) {
-        const uint64_t mid = (l + h) >> 1;
-        if (rk[mid] <= i) l = mid + 1; else h = mid;
+// staging copy of its run.  A CTA takes 256 consecutive keys per round; its
+// first key's segment is found once, the following segment starts are read
+// into shared memory, and every thread searches there.
+constexpr int kShiftThreads = 256;
+__global__ void __launch_bounds__(kShiftThreads)
+    k_vos_shift(const uint64_t *__restrict__ keys, uint64_t cnt, const uint64_t *__restrict__ segs, uint64_t nseg,
+                const uint64_t *__restrict__ abase, uint64_t total_a, const uint64_t *__restrict__ tbase,
+                const uint32_t *__restrict__ rk, const uint32_t *__restrict__ kflag,
+                const uint64_t *__restrict__ kscan, const uint64_t *__restrict__ base,
+                const uint32_t *__restrict__ slots, int insert, uint32_t *temp) {
+  __shared__ uint64_t sa[kShiftThreads + 2];
+  __shared__ uint64_t s0sh;
+  for (uint64_t t0 = blockIdx.x * (uint64_t)kShiftThreads; t0 < total_a; t0 += (uint64_t)gridDim.x * kShiftThreads) {
+    if (threadIdx.x == 0) s0sh = seg_of(abase, nseg, t0);
+    __syncthreads();
+    const uint64_t s0 = s0sh;
+    // 256 keys span at most 257 segments: their starts, and the end
+    for (uint32_t k = threadIdx.x; k < kShiftThreads + 2; k += kShiftThreads)
+      sa[k] = s0 + k <= nseg ? abase[s0 + k] : ~0ull;
+    __syncthreads();
+    const uint64_t t = t0 + threadIdx.x;
+    if (t < total_a) {
+      uint64_t s;
+      if (sa[kShiftThreads] <= t) {  // past the window (runs of segments with no old keys): search it all
+        s = seg_of(abase, nseg, t);
+      } else {
+        uint32_t lo = 0, hi = kShiftThreads;  // last k with sa[k] <= t
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (sa[mid] <= t) lo = mid; else hi = mid;
+        }
+        s = s0 + lo;
       }
-      temp[tbase[s] + i + (kscan[l] - kscan[b0])] = x;
-    } else {  // the first batch key with rank >= i removes A[i] when it is kept
-      while (l < h) {
-        const uint64_t mid = (l + h) >> 1;
-        if (rk[mid] < i) l = mid + 1; else h = mid;
+      const uint64_t b0 = segs[s], b1 = s + 1 < nseg ? segs[s + 1] : cnt;
+      const uint64_t v = keys[b0] >> 32;
+      const uint32_t i = (uint32_t)(t - abase[s]);
+      const uint32_t x = slots[base[v] + i];
+      uint64_t l = b0, h = b1;
+      if (insert) {  // batch keys with rank <= i go before A[i]
+        while (l < h) {
+          const uint64_t mid = (l + h) >> 1;
+          if (rk[mid] <= i) l = mid + 1; else h = mid;
+        }
+        temp[tbase[s] + i + (kscan[l] - kscan[b0])] = x;
+      } else {  // the first batch key with rank >= i removes A[i] when it is kept
+        while (l < h) {
+          const uint64_t mid = (l + h) >> 1;
+          if (rk[mid] < i) l = mid + 1; else h = mid;
+        }
+        if (!(l < b1 && rk[l] == i && kflag[l])) temp[tbase[s] + i - (kscan[l] - kscan[b0])] = x;
       }
-      if (l < b1 && rk[l] == i && kflag[l]) continue;
-      temp[tbase[s] + i - (kscan[l] - kscan[b0])] = x;
     }
+    __syncthreads();
   }
 }
 
@@ -358,7 +382,8 @@ int vos_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   BYO_TRY(ensure(ctx, V->temp, (total_t + 1) * 4));
   uint32_t *temp = (uint32_t *)V->temp.p;
   // 4. merged runs into the staging area, back into their regions
-  launch(ctx, k_vos_shift, dim3(grid_for(ctx, total_a, 256, 16)), dim3(256), 0, keys, count, (const uint64_t *)segs,
+  launch(ctx, k_vos_shift, dim3(grid_for(ctx, total_a, kShiftThreads, 8)), dim3(kShiftThreads), 0, keys, count,
+         (const uint64_t *)segs,
          nseg, (const uint64_t *)abase, total_a, (const uint64_t *)tbase, (const uint32_t *)rk,
          (const uint32_t *)kflag, (const uint64_t *)kscan, (const uint64_t *)g->d_off,
          (const uint32_t *)g->d_slots, insert, temp);
