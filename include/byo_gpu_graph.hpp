@@ -71,9 +71,7 @@ class DeviceGraph {
   DeviceGraph() = default;
   DeviceGraph(int container, const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m) {
     Context &c = Context::get();
-    int rc = container == BYO_CONTAINER_PMA ? byo_graph_create_pma(c.h(), n, m, off, nbrs, &g_)
-                                            : byo_graph_create_csr(c.h(), n, m, off, nbrs, &g_);
-    c.check(rc, "create graph");
+    c.check(byo_graph_create(c.h(), container, n, m, off, nbrs, &g_), "create graph");
     refresh();
   }
   DeviceGraph(const DeviceGraph &) = delete;
@@ -171,14 +169,25 @@ class GPU_PMA_graph : public detail::DeviceGraph {
   GPU_PMA_graph(const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m)
       : DeviceGraph(BYO_CONTAINER_PMA, off, nbrs, n, m) {}
   template <class VData, class Edge>
-  GPU_PMA_graph(VData *v_data, size_t n, size_t, std::function<void()> deletion_fn, Edge *e0,
-                vertex_weight_type * = nullptr) {
+  GPU_PMA_graph(VData *v_data, size_t n, size_t m, std::function<void()> deletion_fn, Edge *e0,
+                vertex_weight_type *w = nullptr)
+      : GPU_PMA_graph(BYO_CONTAINER_PMA, v_data, n, m, deletion_fn, e0, w) {}
+
+ protected:
+  // the same loader path into another updatable container (GPU_VOS_graph)
+  template <class VData, class Edge>
+  GPU_PMA_graph(int container, VData *v_data, size_t n, size_t, std::function<void()> deletion_fn, Edge *e0,
+                vertex_weight_type *) {
     std::vector<uint64_t> off;
     std::vector<uint32_t> nbrs;
     detail::loader_csr(v_data, n, e0, off, nbrs);
-    static_cast<DeviceGraph &>(*this) = DeviceGraph(BYO_CONTAINER_PMA, off.data(), nbrs.data(), n, nbrs.size());
+    static_cast<DeviceGraph &>(*this) = DeviceGraph(container, off.data(), nbrs.data(), n, nbrs.size());
     if (deletion_fn) deletion_fn();
   }
+  GPU_PMA_graph(int container, const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m)
+      : DeviceGraph(container, off, nbrs, n, m) {}
+
+ public:
 
   // PMA_graph::insert_sorted_batch / remove_sorted_batch: the tuple array is
   // read as uint64 (src << 32 | dst) keys, as the reference bit_casts it.
@@ -208,6 +217,22 @@ class GPU_PMA_graph : public detail::DeviceGraph {
     Context::get().check(rc, ins ? "insert_batch" : "remove_batch");
     refresh();
   }
+};
+
+// Vector of per-vertex sorted sets on the GPU (run_vector_pma.cc,
+// run_vector_vector.cc: gbbs::symmetric_set_graph over one set per vertex):
+// the same interface as GPU_PMA_graph over BYO_CONTAINER_VOS.
+template <class W>
+class GPU_VOS_graph : public GPU_PMA_graph<W> {
+ public:
+  using typename GPU_PMA_graph<W>::vertex_weight_type;
+  GPU_VOS_graph() = default;
+  GPU_VOS_graph(const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m)
+      : GPU_PMA_graph<W>(BYO_CONTAINER_VOS, off, nbrs, n, m) {}
+  template <class VData, class Edge>
+  GPU_VOS_graph(VData *v_data, size_t n, size_t m, std::function<void()> deletion_fn, Edge *e0,
+                vertex_weight_type *w = nullptr)
+      : GPU_PMA_graph<W>(BYO_CONTAINER_VOS, v_data, n, m, deletion_fn, e0, w) {}
 };
 
 // ---------------------------------------------------------------- GPU algorithms

@@ -79,6 +79,16 @@ int main() {
   CHECK(pma.num_edges() == 14 && pma.degree(6) == 1);
   lab = byo::gpu_cc(pma);
   CHECK((lab == std::vector<uint32_t>{0, 0, 0, 0, 0, 0, 0}));
+
+  // the vector-of-sets container answers the same calls
+  byo::GPU_VOS_graph<int> vos(vd.data(), n, edges.size(), nullptr, edges.data());
+  CHECK(vos.num_edges() == 12);
+  vos.insert_batch(batch.data(), batch.size());
+  CHECK(vos.num_edges() == 16 && vos.degree(1) == 2 && vos.degree(6) == 2);
+  CHECK((byo::gpu_bfs(vos, 0) == std::vector<uint32_t>{0, 0, 1, 2, 5, 6, 0}));
+  vos.remove_sorted_batch(sorted.data(), sorted.size());
+  CHECK(vos.num_edges() == 14 && vos.degree(6) == 1);
+  CHECK((vos.offsets() == pma.offsets()) && (vos.edges() == pma.edges()));
   std::printf("adapter ok\n");
   return 0;
 }
