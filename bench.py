@@ -148,6 +148,21 @@ def nvtx_pop(torch, pushed):
         torch.cuda.nvtx.range_pop()
 
 
+class nvtx_range:
+    """A named range inside the timed region, one per component of a step
+    (ncu --nvtx --nvtx-include "timed/pagerank/" captures PageRank's launches)."""
+
+    def __init__(self, torch, name, on=True):
+        self.torch, self.name, self.on, self.pushed = torch, name, on, False
+
+    def __enter__(self):
+        if self.on:
+            self.pushed = nvtx_push(self.torch, self.name)
+
+    def __exit__(self, *exc):
+        nvtx_pop(self.torch, self.pushed)
+
+
 # ------------------------------------------------------------------ peaks
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -221,24 +236,29 @@ def run_ours(args, rank, world, local_rank):
             if record:
                 ev[0].record(stream)
             if dynamic:
-                _abi.check(L.byo_graph_insert_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)),
-                           ctx.h)
+                with nvtx_range(torch, "insert", record):
+                    _abi.check(L.byo_graph_insert_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)),
+                               ctx.h)
             if record:
                 ev[1].record(stream)
-            _abi.check(L.byo_bfs_device(G.h, SRC, parent.data_ptr(), None, policy, ctypes.byref(rounds)),
-                       ctx.h)
+            with nvtx_range(torch, "bfs", record):
+                _abi.check(L.byo_bfs_device(G.h, SRC, parent.data_ptr(), None, policy, ctypes.byref(rounds)),
+                           ctx.h)
             if record:
                 ev[2].record(stream)
-            _abi.check(L.byo_cc_device(G.h, label.data_ptr()), ctx.h)
+            with nvtx_range(torch, "cc", record):
+                _abi.check(L.byo_cc_device(G.h, label.data_ptr()), ctx.h)
             if record:
                 ev[3].record(stream)
-            _abi.check(L.byo_pagerank_device(G.h, PR_EPS, PR_ITERS, 0, pr.data_ptr(), ctypes.byref(it),
-                                             ctypes.byref(l1)), ctx.h)
+            with nvtx_range(torch, "pagerank", record):
+                _abi.check(L.byo_pagerank_device(G.h, PR_EPS, PR_ITERS, 0, pr.data_ptr(), ctypes.byref(it),
+                                                 ctypes.byref(l1)), ctx.h)
             if record:
                 ev[4].record(stream)
             if dynamic:
-                _abi.check(L.byo_graph_remove_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)),
-                           ctx.h)
+                with nvtx_range(torch, "remove", record):
+                    _abi.check(L.byo_graph_remove_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)),
+                               ctx.h)
             if record:
                 ev[5].record(stream)
 

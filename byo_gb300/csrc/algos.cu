@@ -21,7 +21,6 @@
 // is the same).
 #include <algorithm>
 #include <cmath>
-#include <unordered_map>
 #include <vector>
 
 #include "device.cuh"
@@ -70,17 +69,21 @@ __global__ void k_cc_init(uint32_t *p, uint64_t n) {
 }
 
 // Link the first kSample neighbours of every vertex (one thread per vertex).
+// Sampling round r (Afforest): every vertex links to its r-th neighbour;
+// a compress between rounds keeps the trees flat for the next round's finds.
 __global__ void k_cc_sample(const uint64_t *__restrict__ off, const uint32_t *__restrict__ slots,
-                            uint32_t *p, uint64_t n) {
+                            uint32_t *p, uint64_t n, int round) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t b = off[v], e = off[v + 1];
     int taken = 0;
-    for (uint64_t j = b; j < e && taken < kSample; j++) {
-      uint32_t u = slots[j];
+    for (uint64_t j = b; j < e; j++) {
+      const uint32_t u = slots[j];
       if (u == kSentinel) continue;
-      taken++;
-      cc_link(p, (uint32_t)v, u);
+      if (taken++ == round) {
+        cc_link(p, (uint32_t)v, u);
+        break;
+      }
     }
   }
 }
@@ -97,7 +100,8 @@ __global__ void k_cc_compress(uint32_t *p, uint64_t n) {
 template <int GS>
 __global__ void __launch_bounds__(256) k_cc_finish(const uint64_t *__restrict__ off,
                                                    const uint32_t *__restrict__ slots, uint32_t *p,
-                                                   uint64_t n, uint32_t giant) {
+                                                   uint64_t n, const uint32_t *__restrict__ giant_root) {
+  const uint32_t giant = *giant_root;
   const unsigned gl = threadIdx.x % GS;
   const uint64_t gid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / GS;
   const uint64_t ng = ((uint64_t)gridDim.x * blockDim.x) / GS;
@@ -116,15 +120,46 @@ __global__ void __launch_bounds__(256) k_cc_finish(const uint64_t *__restrict__ 
   }
 }
 
-__global__ void k_gather_u32(const uint32_t *__restrict__ src, uint64_t n, uint64_t seed, uint32_t cnt,
-                             uint32_t *out) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-    uint64_t z = seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    z ^= z >> 31;
-    out[i] = src[(uint32_t)(((z & 0xFFFFFFFFull) * n) >> 32)];
+// The most frequent root among kCcProbe vertices drawn by a fixed hash (the
+// giant component, skipped by k_cc_finish): one CTA sorts the roots in
+// shared memory and keeps the longest run (ties: the smallest root).
+constexpr uint32_t kCcProbe = 1024;
+__global__ void __launch_bounds__(kCcProbe) k_cc_giant(const uint32_t *__restrict__ p, uint64_t n, uint64_t seed,
+                                                       uint32_t *giant) {
+  __shared__ uint32_t s[kCcProbe], st[kCcProbe];
+  __shared__ unsigned long long best;
+  const uint32_t t = threadIdx.x;
+  uint64_t z = seed + (uint64_t)(t + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  s[t] = __ldcg(p + (uint32_t)(((z & 0xFFFFFFFFull) * n) >> 32));
+  if (t == 0) best = 0;
+  __syncthreads();
+  for (uint32_t k = 2; k <= kCcProbe; k <<= 1)
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      const uint32_t x = t ^ j;
+      if (x > t) {
+        const uint32_t a = s[t], b = s[x];
+        if ((a > b) == ((t & k) == 0)) {
+          s[t] = b;
+          s[x] = a;
+        }
+      }
+      __syncthreads();
+    }
+  st[t] = (t == 0 || s[t] != s[t - 1]) ? t : 0;  // start of t's run after a max-scan
+  __syncthreads();
+  for (uint32_t d = 1; d < kCcProbe; d <<= 1) {
+    const uint32_t v = t >= d ? st[t - d] : 0;
+    __syncthreads();
+    if (v > st[t]) st[t] = v;
+    __syncthreads();
   }
+  if (t == kCcProbe - 1 || s[t] != s[t + 1])
+    atomicMax(&best, ((unsigned long long)(t - st[t] + 1) << 32) | (0xFFFFFFFFu - s[t]));
+  __syncthreads();
+  if (t == 0) *giant = 0xFFFFFFFFu - (uint32_t)best;
 }
 
 int cc_run(byo_graph *g, uint32_t *d_label) {
@@ -133,40 +168,26 @@ int cc_run(byo_graph *g, uint32_t *d_label) {
   if (n == 0) return BYO_OK;
   uint32_t *p = d_label;
   launch(ctx, k_cc_init, dim3(grid_for(ctx, n, 256)), dim3(256), 0, p, n);
-  launch(ctx, k_cc_sample, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint64_t *)g->d_off,
-         (const uint32_t *)g->d_slots, p, n);
-  launch(ctx, k_cc_compress, dim3(grid_for(ctx, n, 256)), dim3(256), 0, p, n);
-  // most frequent root among 1024 sampled vertices
-  constexpr uint32_t kProbe = 1024;
-  uint32_t *probe = nullptr;
-  BYO_TRY(ws(g, WS_MISC, kProbe, &probe));
-  launch(ctx, k_gather_u32, dim3(4), dim3(256), 0, (const uint32_t *)p, n, (uint64_t)0x5EEDull, kProbe,
-         probe);
-  uint32_t *h = nullptr;
-  BYO_TRY(pinned(ctx, 4096 + kProbe * 4, (void **)&h));
-  BYO_CU(ctx, cudaMemcpyAsync(h, probe, kProbe * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  std::unordered_map<uint32_t, uint32_t> freq;
-  uint32_t giant = h[0], best = 0;
-  for (uint32_t i = 0; i < kProbe; i++) {
-    uint32_t c = ++freq[h[i]];
-    if (c > best) {
-      best = c;
-      giant = h[i];
-    }
+  for (int r = 0; r < kSample; r++) {
+    launch(ctx, k_cc_sample, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint64_t *)g->d_off,
+           (const uint32_t *)g->d_slots, p, n, r);
+    launch(ctx, k_cc_compress, dim3(grid_for(ctx, n, 256)), dim3(256), 0, p, n);
   }
+  uint32_t *giant = nullptr;
+  BYO_TRY(ws(g, WS_MISC, 4, &giant));
+  launch(ctx, k_cc_giant, dim3(1), dim3(kCcProbe), 0, (const uint32_t *)p, n, (uint64_t)0x5EEDull, giant);
   const double avg = (double)g->m / (double)n;
   const int GS = avg >= 24 ? 16 : avg >= 8 ? 8 : 4;
   const int grid = grid_for(ctx, n * GS, 256, 16);
   if (GS == 16)
     launch_t(ctx, "cc_finish", k_cc_finish<16>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
-           (const uint32_t *)g->d_slots, p, n, giant);
+           (const uint32_t *)g->d_slots, p, n, (const uint32_t *)giant);
   else if (GS == 8)
     launch_t(ctx, "cc_finish", k_cc_finish<8>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
-           (const uint32_t *)g->d_slots, p, n, giant);
+           (const uint32_t *)g->d_slots, p, n, (const uint32_t *)giant);
   else
     launch_t(ctx, "cc_finish", k_cc_finish<4>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
-           (const uint32_t *)g->d_slots, p, n, giant);
+           (const uint32_t *)g->d_slots, p, n, (const uint32_t *)giant);
   launch(ctx, k_cc_compress, dim3(grid_for(ctx, n, 256)), dim3(256), 0, p, n);
   return check_launch(ctx, "cc");
 }
