@@ -508,8 +508,11 @@ __device__ __forceinline__ void pr_finish(uint64_t v, T tot, const uint32_t *__r
 // One warp per unit, no block-wide barriers: the warp gathers p_div of the
 // unit's slots (16 independent loads per lane in flight) into its own stage in
 // shared memory, then reduces.  Light tile: runs of <= 32 one lane each, longer
-// runs (found by ballot) one warp each.  Heavy chunk: warp partial to part[].
-template <bool kComp, typename T>
+// runs (found by ballot) one warp each.  Heavy chunk: warp partial to part[];
+// with kDirectHeavy (FP64) each lane sums its gathered slots lane, lane+32, ...
+// in registers without the stage, in the same order: measured at RMAT 2^22,
+// 20 FP64 iterations 34.0 -> 28.8 ms, while FP32 runs 1% faster staged.
+template <bool kComp, typename T, bool kDirectHeavy>
 __global__ void __launch_bounds__(kPrBlock) k_pr_units(const uint64_t *__restrict__ off,
                                                        const uint32_t *__restrict__ slots,
                                                        const uint32_t *__restrict__ deg,
@@ -528,6 +531,26 @@ __global__ void __launch_bounds__(kPrBlock) k_pr_units(const uint64_t *__restric
     const PrDesc d = desc[t];
     const uint32_t len = (uint32_t)(d.s1 - d.s0);
     const uint32_t *id = slots + d.s0;
+    if (d.v1 == kNoVertex && kDirectHeavy) {
+      T s = T(0), c = T(0);
+      for (uint32_t i = lane; i < len; i += 32 * 16) {
+        uint32_t u[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) u[q] = i + 32 * q < len ? __ldcs(id + i + 32 * q) : kSentinel;
+        T g[16];
+#pragma unroll
+        for (int q = 0; q < 16; q++) g[q] = u[q] != kSentinel ? __ldg(pdiv_in + u[q]) : T(0);
+#pragma unroll
+        for (int q = 0; q < 16; q++)
+          if (i + 32 * q < len) acc_add<kComp>(s, c, g[q]);
+      }
+      T tot = group_total<kComp, T, 32>(s, c);
+      if (lane == 0) {
+        part[2 * (uint64_t)d.chunk] = tot;
+        part[2 * (uint64_t)d.chunk + 1] = T(0);
+      }
+      continue;
+    }
     for (uint32_t i = lane; i < len; i += 32 * 16) {
       uint32_t u[16];
 #pragma unroll
@@ -761,7 +784,7 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
       void *ua[] = {(void *)&off_, (void *)&slots_, (void *)&deg_, (void *)&desc_, (void *)&nunits_,
                     (void *)&pdiv_in[h], (void *)&pcur[h], (void *)&pnext[h], (void *)&pdiv_out[h], (void *)&part,
                     (void *)&damping_, (void *)&added_, (void *)&l1_};
-      kp.func = (void *)k_pr_units<kComp, T>;
+      kp.func = (void *)k_pr_units<kComp, T, sizeof(T) == 8>;
       kp.gridDim = dim3(grid_u);
       kp.blockDim = dim3(kPrBlock);
       kp.kernelParams = ua;

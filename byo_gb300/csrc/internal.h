@@ -102,6 +102,7 @@ enum Ws {
   WS_BUCKETS,
   WS_MISC,
   WS_STREAM,        // update stream: batch offsets and operations
+  WS_MS_LEVELS,     // uint64[16][n] 64-source BFS: bit b of each pair's level
   WS_COUNT
 };
 

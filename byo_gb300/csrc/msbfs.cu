@@ -25,9 +25,14 @@
 // A push round needs the list of its input frontier: it has one when the
 // previous round was a push, otherwise it first collects it from F.  It also
 // needs N free of the entries of two rounds before, which it clears from that
-// round's list, or wholesale when that round was a pull.  Levels go straight
-// to the output (source-major, one store per (source, vertex) pair); pairs
-// never reached get BYO_NONE in a last pass.  Rounds are separated by a grid
+// round's list, or wholesale when that round was a pull.  Levels are kept as
+// bit planes: when round r reaches sources `got` at v, got is ORed into
+// plane b of v for every bit b of r (16 planes, rounds below 2^16; later
+// rounds write their levels straight to the output).  A last kernel turns
+// each vertex's planes into its 64 levels and writes them source-major, a
+// warp storing 32 consecutive words per source, with BYO_NONE for pairs never
+// reached; the traversal itself makes no scattered output stores.  Rounds are
+// separated by a grid
 // barrier of the project's own whose wait is bounded in time: a barrier that
 // does not complete sets an error flag and every block leaves.
 #include <algorithm>
@@ -40,6 +45,7 @@
 namespace byo {
 
 constexpr int kMsBlock = 256;
+constexpr int kLevelBits = 16;                   // bit planes of the levels (rounds < 2^16)
 constexpr int kMsLog = 64;                       // rounds recorded for byo_last_rounds
 
 struct MsCtl {
@@ -68,6 +74,7 @@ struct MsArgs {
   uint64_t ccap;           // capacity of each chunk list
   uint32_t *T, *H;         // touched list; heavy list (warp vertices front, hubs back)
   uint32_t *levels;        // [k][n]
+  uint64_t *planes;        // [kLevelBits][n]: bit b of the level of each (source, vertex)
   const uint32_t *srcs;
   uint32_t k;
   MsCtl *ctl;
@@ -90,10 +97,18 @@ __device__ __forceinline__ uint64_t warp_or64(uint64_t x) {
   return (uint64_t)hi << 32 | lo;
 }
 
-// Writes the levels of the lanes' newly reached (source, vertex) pairs: one
-// store instruction per source bit present in the warp, so lanes holding
-// consecutive vertices write consecutive words.  Warp-uniform call.
+// Records round r as the level of the lanes' newly reached (source, vertex)
+// pairs: ORs `got` into v's plane b for each bit b of r.  From round 2^16 on,
+// one store per pair straight to the output, one store instruction per
+// source bit present in the warp.  Warp-uniform call (r is uniform).
 __device__ __forceinline__ void ms_levels(const MsArgs &a, uint32_t v, uint64_t got, uint32_t r) {
+  if (r < (1u << kLevelBits)) {
+    if (got)
+      for (uint32_t m = r; m; m &= m - 1)
+        atomicOr((unsigned long long *)a.planes + (uint64_t)(__ffs((int)m) - 1) * a.n + v,
+                 (unsigned long long)got);
+    return;
+  }
   uint64_t any = warp_or64(got);
   while (any) {
     const int s = __ffsll((long long)any) - 1;
@@ -190,6 +205,7 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
     stm(a.A, i, 0);
     stm(a.B, i, 0);
     stm(a.X, i, 0);
+    stm(a.planes, i, 0);  // plane 0; plane b is cleared before round 2^b
   }
   for (uint64_t base = warp * 32; base < n; base += nwarps * 32) {
     const uint64_t v = base + lane;
@@ -229,7 +245,6 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
       }
       stm(a.A, v, ldm(a.A, v) | 1ull << s);
       stm(a.seen, v, ldm(a.seen, v) | 1ull << s);
-      a.levels[(uint64_t)s * n + v] = 0;
     }
     c->lvalid[0] = 1;
     c->lvalid[2] = 1;  // an empty list: round 1 has nothing to clear
@@ -447,6 +462,11 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
       }
       ms_count(c, cur, my_cnt, my_deg);
     }
+    // the plane that round r + 1 is the first to use
+    if (((r + 1) & r) == 0 && r + 1 < (1u << kLevelBits)) {
+      uint64_t *pl = a.planes + (uint64_t)(__ffs((int)(r + 1)) - 1) * n;
+      for (uint64_t i = tid; i < n; i += nthr) stm(pl, i, 0);
+    }
     if (!grid_sync(&c->bar, nb)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0 && r <= kMsLog) {
       c->rlog[r - 1][0] = globaltimer_ns();
@@ -458,18 +478,42 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
     F = N;
     N = t;
   }
-  // (source, vertex) pairs never reached
-  for (uint64_t base = warp * 32; base < n; base += nwarps * 32) {
-    const uint64_t v = base + lane;
-    const uint64_t miss = v < n ? a.full & ~ldm(a.seen, v) : 0;
-    uint64_t any = warp_or64(miss);
-    while (any) {
-      const int s = __ffsll((long long)any) - 1;
-      any &= any - 1;
-      if ((miss >> s) & 1) __stcs(a.levels + (uint64_t)s * n + v, kSentinel);
+  if (blockIdx.x == 0 && threadIdx.x == 0) c->rounds = r - 1;
+}
+
+// The levels from the bit planes, a thread per vertex: level of (s, v) =
+// sum over planes b of bit s of plane b, << b.  A zero level is the source
+// itself, a pair reached from round 2^16 on (already written), or a pair
+// never reached (BYO_NONE).  Per source a warp stores 32 consecutive words.
+__global__ void __launch_bounds__(256) k_ms_levels(const MsArgs a) {
+  if (a.ctl->bar.err) return;
+  const uint32_t last = a.ctl->rounds;
+  const int used = last ? min(32 - __clz((int)last), kLevelBits) : 0;
+  const uint64_t n = a.n;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t lv[64];
+#pragma unroll
+    for (int s = 0; s < 64; s++) lv[s] = 0;
+    for (int b = 0; b < used; b++) {
+      const uint64_t pl = __ldcs(a.planes + (uint64_t)b * n + v);
+      if (!pl) continue;
+#pragma unroll
+      for (int s = 0; s < 64; s++) lv[s] |= (uint32_t)((pl >> s) & 1) << b;
+    }
+    const uint64_t sv = __ldcs(a.seen + v);
+#pragma unroll
+    for (int s = 0; s < 64; s++) {
+      if ((uint32_t)s >= a.k) break;
+      uint32_t out = lv[s];
+      if (!out) {
+        if (__ldg(a.srcs + s) == (uint32_t)v) out = 0;
+        else if ((sv >> s) & 1) continue;  // reached after round 2^16 - 1: written by the traversal
+        else out = kSentinel;
+      }
+      __stcs(a.levels + (uint64_t)s * n + v, out);
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) c->rounds = r - 1;
 }
 
 int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint32_t *rounds) {
@@ -517,6 +561,7 @@ int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_
   a.srcs = misc;
   a.ctl = (MsCtl *)(misc + 64);
   a.levels = d_levels;
+  BYO_TRY(ws(g, WS_MS_LEVELS, (size_t)kLevelBits * n, &a.planes));
   BYO_CU(ctx, cudaMemcpyAsync(misc, h_srcs, k * 4, cudaMemcpyHostToDevice, ctx->stream));
   BYO_CU(ctx, cudaMemsetAsync(a.ctl, 0, sizeof(MsCtl), ctx->stream));
   // co-resident grid for the cooperative launch
@@ -528,6 +573,7 @@ int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_
   void *args[] = {(void *)&a};
   const bool timed = !ctx->ktag.empty() && ktimer_begin(ctx, "bfs_multi");
   BYO_CU(ctx, cudaLaunchCooperativeKernel((const void *)k_ms_bfs, dim3(grid), dim3(kMsBlock), args, 0, ctx->stream));
+  launch(ctx, k_ms_levels, dim3(grid_for(ctx, n, 256)), dim3(256), 0, a);
   ctx->launches++;
   if (timed) ktimer_end(ctx);
   MsCtl *h = nullptr;

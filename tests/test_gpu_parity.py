@@ -215,6 +215,24 @@ def _sym_csr(n, pairs):
 
 
 @pytest.mark.gpu
+def test_bfs_multi_deep_levels(ctx):
+    """Levels from 2^16 on (a path of 70000 vertices) are stored by the
+    traversal itself, the lower ones come from the bit planes; an isolated
+    vertex stays unreached."""
+    import byo_gb300 as byo
+    n = 70000
+    off, nb = _sym_csr(n + 1, [(i, i + 1) for i in range(n - 1)])
+    G = byo.Graph.from_csr(ctx, off, nb)
+    srcs = [0, n - 1, 1234]
+    lev = byo.BFS_multi(G, srcs)
+    for i, s in enumerate(srcs):
+        want = np.abs(np.arange(n + 1, dtype=np.int64) - s).astype(np.uint32)
+        want[n] = 0xFFFFFFFF
+        assert np.array_equal(lev[i], want), i
+    G.close()
+
+
+@pytest.mark.gpu
 def test_bfs_multi_launch_shapes(ctx, oracle_mod):
     """Every direction and degree-bucket path of the 64-source kernel (forced
     push, forced pull, warp-per-vertex pull, hub chunks) gives the levels of
