@@ -29,7 +29,7 @@ namespace byo {
 
 struct Vos {
   DevBuf keys_a, keys_b, misc;
-  DevBuf rk, kflag, kscan, segid, segs, tbase, abase, rnew, temp, ovt;
+  DevBuf rk, kflag, kscan, segid, segs, tbase, abase, rnew, temp, ovt, chunks;
 };
 
 __host__ __device__ __forceinline__ uint64_t vos_cap(uint64_t d) {
@@ -107,27 +107,106 @@ int vos_build(byo_graph *g, const uint64_t *d_keys, uint64_t m) {
 void vos_destroy(Vos *v) {
   if (!v) return;
   for (DevBuf *b : {&v->keys_a, &v->keys_b, &v->misc, &v->rk, &v->kflag, &v->kscan, &v->segid, &v->segs, &v->tbase,
-                    &v->abase, &v->rnew, &v->temp, &v->ovt})
+                    &v->abase, &v->rnew, &v->temp, &v->ovt, &v->chunks})
     free_buf(*b);
   delete v;
 }
 
 // The compact CSR of the runs (for the read-only algorithms' snapshot):
 // out[offc[v] ..] = the first deg[v] slots of v's region.
-__global__ void k_vos_compact(const uint64_t *__restrict__ base, const uint32_t *__restrict__ slots,
-                              const uint32_t *__restrict__ deg, const uint64_t *__restrict__ offc, uint64_t n,
-                              uint32_t *out) {
+// The element ranges of units (vertices, touched runs) are walked in chunks
+// of kChunk consecutive positions, a warp per chunk, so a hub's run is spread
+// over many warps and no warp's work depends on the degrees.  For each chunk
+// the warp loads the starts and metadata of up to 32 consecutive units (from
+// first[c], the unit holding the chunk's first position) into shared memory,
+// lane j unit j, handles the chunk's positions inside them -- each lane finds
+// its position's unit by a binary search over the 32 starts -- and moves on
+// to the next 32 units until the chunk ends.
+constexpr int kVosBlock = 256;
+constexpr int kVosWarps = kVosBlock / 32;
+constexpr uint64_t kChunk = 2048;
+
+// first[c] = the unit whose range [ust[u], ust[u+1]) holds position c * kChunk
+__global__ void k_chunk_first(const uint64_t *__restrict__ ust, uint64_t nunits, uint32_t *first) {
+  for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < nunits;
+       u += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t a = ust[u], b = ust[u + 1];
+    for (uint64_t c = (a + kChunk - 1) / kChunk; c * kChunk < b; c++) first[c] = (uint32_t)u;
+  }
+}
+
+static int chunk_first(byo_ctx *ctx, DevBuf &buf, const uint64_t *ust, uint64_t nunits, uint64_t total,
+                       uint32_t **first, uint64_t *nchunks) {
+  *nchunks = (total + kChunk - 1) / kChunk;
+  BYO_TRY(ensure(ctx, buf, (*nchunks + 1) * 4));
+  *first = (uint32_t *)buf.p;
+  if (nunits)
+    launch(ctx, k_chunk_first, dim3(grid_for(ctx, nunits, 256)), dim3(256), 0, ust, nunits, *first);
+  return BYO_OK;
+}
+
+// last j in [0, nu) with st[j] <= p (st[nu] is the window's end)
+__device__ __forceinline__ int unit_of(const uint64_t *st, int nu, uint64_t p) {
+  int lo = 0, hi = nu;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (st[mid] <= p) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kVosBlock) k_vos_compact(const uint64_t *__restrict__ base,
+                                                           const uint32_t *__restrict__ slots,
+                                                           const uint64_t *__restrict__ offc, uint64_t n,
+                                                           const uint32_t *__restrict__ first, uint64_t nchunks,
+                                                           uint32_t *out) {
+  __shared__ uint64_t st[kVosWarps][33], sb[kVosWarps][32];
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t v = gw; v < n; v += nw) {
-    const uint32_t d = deg[v];
-    for (uint32_t i = lane_id(); i < d; i += 32) out[offc[v] + i] = slots[base[v] + i];
+  const uint64_t total = offc[n];
+  for (uint64_t c = gw; c < nchunks; c += nw) {
+    const uint64_t c0 = c * kChunk, c1 = min(c0 + kChunk, total);
+    uint64_t u = first[c];
+    for (;;) {
+      const int nu = (int)min((uint64_t)32, n - u);
+      if ((int)lane < nu) {
+        st[w][lane] = offc[u + lane];
+        sb[w][lane] = base[u + lane];
+      }
+      if (lane == 0) st[w][nu] = offc[u + nu];
+      __syncwarp();
+      const uint64_t lo = max(c0, st[w][0]), hi = min(c1, st[w][nu]);
+      for (uint64_t p = lo + lane; p < hi; p += 128) {
+        uint32_t x[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const uint64_t pp = p + 32 * q;
+          if (pp < hi) {
+            const int j = unit_of(st[w], nu, pp);
+            x[q] = slots[sb[w][j] + (pp - st[w][j])];
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (p + 32 * q < hi) out[p + 32 * q] = x[q];
+      }
+      const bool more = st[w][nu] < c1;
+      __syncwarp();
+      if (!more) break;
+      u += nu;
+    }
   }
 }
 
 int vos_compact(byo_graph *g, const uint64_t *offc, uint32_t *out) {
-  launch(g->ctx, k_vos_compact, dim3(grid_for(g->ctx, g->n * 32, 256, 8)), dim3(256), 0, (const uint64_t *)g->d_off,
-         (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg, offc, g->n, out);
+  uint32_t *first = nullptr;
+  uint64_t nchunks = 0;
+  BYO_TRY(chunk_first(g->ctx, g->vos->chunks, offc, g->n, g->m, &first, &nchunks));
+  if (nchunks)
+    launch(g->ctx, k_vos_compact, dim3(grid_for(g->ctx, nchunks * 32, kVosBlock, 8)), dim3(kVosBlock), 0,
+           (const uint64_t *)g->d_off, (const uint32_t *)g->d_slots, offc, g->n, (const uint32_t *)first, nchunks,
+           out);
   return check_launch(g->ctx, "vos_compact");
 }
 
@@ -219,60 +298,96 @@ __device__ __forceinline__ uint64_t seg_of(const uint64_t *pre, uint64_t nseg, u
   return lo;
 }
 
-// the old keys of the touched runs, flattened: each moves to its place in the
-// staging copy of its run.  A CTA takes 256 consecutive keys per round; its
-// first key's segment is found once, the following segment starts are read
-// into shared memory, and every thread searches there.
-constexpr int kShiftThreads = 256;
-__global__ void __launch_bounds__(kShiftThreads)
+// The old keys of the touched runs, in chunks over their concatenation
+// (abase): each key moves to its place in the staging copy of its run,
+// shifted by the kept batch keys of its run that go before it (insert:
+// rank <= i; remove: rank < i, and a kept batch key of rank i removes it).
+// The ranks and kept-key prefix of a window's batch keys are staged in shared
+// memory when they fit.
+constexpr int kShiftStage = 256;
+__global__ void __launch_bounds__(kVosBlock)
     k_vos_shift(const uint64_t *__restrict__ keys, uint64_t cnt, const uint64_t *__restrict__ segs, uint64_t nseg,
-                const uint64_t *__restrict__ abase, uint64_t total_a, const uint64_t *__restrict__ tbase,
+                const uint64_t *__restrict__ abase, const uint64_t *__restrict__ tbase,
                 const uint32_t *__restrict__ rk, const uint32_t *__restrict__ kflag,
                 const uint64_t *__restrict__ kscan, const uint64_t *__restrict__ base,
-                const uint32_t *__restrict__ slots, int insert, uint32_t *temp) {
-  __shared__ uint64_t sa[kShiftThreads + 2];
-  __shared__ uint64_t s0sh;
-  for (uint64_t t0 = blockIdx.x * (uint64_t)kShiftThreads; t0 < total_a; t0 += (uint64_t)gridDim.x * kShiftThreads) {
-    if (threadIdx.x == 0) s0sh = seg_of(abase, nseg, t0);
-    __syncthreads();
-    const uint64_t s0 = s0sh;
-    // 256 keys span at most 257 segments: their starts, and the end
-    for (uint32_t k = threadIdx.x; k < kShiftThreads + 2; k += kShiftThreads)
-      sa[k] = s0 + k <= nseg ? abase[s0 + k] : ~0ull;
-    __syncthreads();
-    const uint64_t t = t0 + threadIdx.x;
-    if (t < total_a) {
-      uint64_t s;
-      if (sa[kShiftThreads] <= t) {  // past the window (runs of segments with no old keys): search it all
-        s = seg_of(abase, nseg, t);
-      } else {
-        uint32_t lo = 0, hi = kShiftThreads;  // last k with sa[k] <= t
-        while (hi - lo > 1) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (sa[mid] <= t) lo = mid; else hi = mid;
-        }
-        s = s0 + lo;
+                const uint32_t *__restrict__ slots, int insert, const uint32_t *__restrict__ first,
+                uint64_t nchunks, uint32_t *temp) {
+  __shared__ uint64_t st[kVosWarps][33], stb[kVosWarps][32], sbs[kVosWarps][32];
+  __shared__ uint32_t kb[kVosWarps][33];  // batch key range of each run, relative to the window's first
+  __shared__ uint32_t srk[kVosWarps][kShiftStage];
+  __shared__ uint32_t sks[kVosWarps][kShiftStage + 1];  // kept prefix relative to the window's first key
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t total = abase[nseg];
+  for (uint64_t c = gw; c < nchunks; c += nw) {
+    const uint64_t c0 = c * kChunk, c1 = min(c0 + kChunk, total);
+    uint64_t s0 = first[c];
+    for (;;) {
+      const int nu = (int)min((uint64_t)32, nseg - s0);
+      const uint64_t sg = s0 + lane;
+      const uint64_t g0 = segs[s0], g1 = s0 + nu < nseg ? segs[s0 + nu] : cnt;
+      if ((int)lane < nu) {
+        const uint64_t b0 = segs[sg];
+        st[w][lane] = abase[sg];
+        stb[w][lane] = tbase[sg];
+        sbs[w][lane] = base[keys[b0] >> 32];
+        kb[w][lane] = (uint32_t)(b0 - g0);
       }
-      const uint64_t b0 = segs[s], b1 = s + 1 < nseg ? segs[s + 1] : cnt;
-      const uint64_t v = keys[b0] >> 32;
-      const uint32_t i = (uint32_t)(t - abase[s]);
-      const uint32_t x = slots[base[v] + i];
-      uint64_t l = b0, h = b1;
-      if (insert) {  // batch keys with rank <= i go before A[i]
-        while (l < h) {
-          const uint64_t mid = (l + h) >> 1;
-          if (rk[mid] <= i) l = mid + 1; else h = mid;
-        }
-        temp[tbase[s] + i + (kscan[l] - kscan[b0])] = x;
-      } else {  // the first batch key with rank >= i removes A[i] when it is kept
-        while (l < h) {
-          const uint64_t mid = (l + h) >> 1;
-          if (rk[mid] < i) l = mid + 1; else h = mid;
-        }
-        if (!(l < b1 && rk[l] == i && kflag[l])) temp[tbase[s] + i - (kscan[l] - kscan[b0])] = x;
+      if (lane == 0) {
+        st[w][nu] = abase[s0 + nu];
+        kb[w][nu] = (uint32_t)(g1 - g0);
       }
+      const uint32_t K = (uint32_t)(g1 - g0);
+      const bool staged = K <= kShiftStage;
+      if (staged) {
+        const uint64_t ks0 = kscan[g0];
+        for (uint32_t k = lane; k < K; k += 32) srk[w][k] = rk[g0 + k];
+        for (uint32_t k = lane; k <= K; k += 32) sks[w][k] = (uint32_t)(kscan[g0 + k] - ks0);
+      }
+      __syncwarp();
+      const uint64_t lo = max(c0, st[w][0]), hi = min(c1, st[w][nu]);
+      for (uint64_t p0 = lo + lane; p0 < hi; p0 += 128) {
+        int jq[4];
+        uint32_t xq[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const uint64_t p = p0 + 32 * q;
+          jq[q] = p < hi ? unit_of(st[w], nu, p) : -1;
+          if (jq[q] >= 0) xq[q] = slots[sbs[w][jq[q]] + (p - st[w][jq[q]])];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (jq[q] < 0) continue;
+          const int j = jq[q];
+          const uint32_t i = (uint32_t)(p0 + 32 * q - st[w][j]);
+          uint32_t l = kb[w][j], h = kb[w][j + 1];
+          const uint32_t lb = l, e = h;
+          if (insert) {  // batch keys with rank <= i go before A[i]
+            while (l < h) {
+              const uint32_t mid = (l + h) >> 1;
+              if ((staged ? srk[w][mid] : rk[g0 + mid]) <= i) l = mid + 1; else h = mid;
+            }
+          } else {  // the first batch key with rank >= i removes A[i] when it is kept
+            while (l < h) {
+              const uint32_t mid = (l + h) >> 1;
+              if ((staged ? srk[w][mid] : rk[g0 + mid]) < i) l = mid + 1; else h = mid;
+            }
+          }
+          const uint32_t before = staged ? sks[w][l] - sks[w][lb] : (uint32_t)(kscan[g0 + l] - kscan[g0 + lb]);
+          if (insert) {
+            temp[stb[w][j] + i + before] = xq[q];
+          } else {
+            const bool gone = l < e && (staged ? srk[w][l] : rk[g0 + l]) == i && kflag[g0 + l];
+            if (!gone) temp[stb[w][j] + i - before] = xq[q];
+          }
+        }
+      }
+      const bool more = st[w][nu] < c1;
+      __syncwarp();
+      if (!more) break;
+      s0 += nu;
     }
-    __syncthreads();
   }
 }
 
@@ -287,30 +402,111 @@ __global__ void k_vos_insert_new(const uint64_t *__restrict__ keys, uint64_t cnt
   }
 }
 
-// runs that still fit go back into their regions (sentinels after them);
-// degrees updated; outgrown runs counted and remembered (ovt[v] = staging start)
-__global__ void k_vos_back(const uint64_t *__restrict__ keys, uint64_t cnt, const uint64_t *__restrict__ segs,
-                           uint64_t nseg, const uint64_t *__restrict__ tbase, const uint64_t *__restrict__ base,
-                           const uint32_t *__restrict__ temp, uint32_t *slots, uint32_t *deg, uint64_t *ovt,
-                           unsigned long long *ctr /* [0] outgrown runs, [1] delta */) {
+// Runs that still fit go back into their regions: chunks over the staging
+// area (tbase), a run that outgrew its region skipped.
+__global__ void __launch_bounds__(kVosBlock) k_vos_back(const uint64_t *__restrict__ keys,
+                                                        const uint64_t *__restrict__ segs, uint64_t nseg,
+                                                        const uint64_t *__restrict__ tbase,
+                                                        const uint64_t *__restrict__ base,
+                                                        const uint32_t *__restrict__ temp,
+                                                        const uint32_t *__restrict__ first, uint64_t nchunks,
+                                                        uint32_t *slots) {
+  __shared__ uint64_t st[kVosWarps][33], sbs[kVosWarps][32];
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t s = gw; s < nseg; s += nw) {
-    const uint64_t v = keys[segs[s]] >> 32;
-    const uint64_t r = tbase[s + 1] - tbase[s], d = deg[v], cap = base[v + 1] - base[v];
-    if (r > cap) {
-      if (lane_id() == 0) {
-        ovt[v] = tbase[s];
-        atomicAdd(&ctr[0], 1ull);
+  const uint64_t total = tbase[nseg];
+  for (uint64_t c = gw; c < nchunks; c += nw) {
+    const uint64_t c0 = c * kChunk, c1 = min(c0 + kChunk, total);
+    uint64_t s0 = first[c];
+    for (;;) {
+      const int nu = (int)min((uint64_t)32, nseg - s0);
+      const uint64_t sg = s0 + lane;
+      if ((int)lane < nu) {
+        const uint64_t v = keys[segs[sg]] >> 32;
+        const uint64_t t = tbase[sg], b = base[v];
+        st[w][lane] = t;
+        sbs[w][lane] = tbase[sg + 1] - t <= base[v + 1] - b ? b : ~0ull;
       }
-    } else {
-      for (uint64_t i = lane_id(); i < r; i += 32) slots[base[v] + i] = temp[tbase[s] + i];
-      for (uint64_t i = r + lane_id(); i < d; i += 32) slots[base[v] + i] = kSentinel;
+      if (lane == 0) st[w][nu] = tbase[s0 + nu];
+      __syncwarp();
+      const uint64_t lo = max(c0, st[w][0]), hi = min(c1, st[w][nu]);
+      for (uint64_t p = lo + lane; p < hi; p += 128) {
+        uint32_t x[4];
+        int jj[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const uint64_t pp = p + 32 * q;
+          jj[q] = pp < hi ? unit_of(st[w], nu, pp) : -1;
+          if (jj[q] >= 0) x[q] = temp[pp];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          if (jj[q] >= 0 && sbs[w][jj[q]] != ~0ull) slots[sbs[w][jj[q]] + (p + 32 * q - st[w][jj[q]])] = x[q];
+      }
+      const bool more = st[w][nu] < c1;
+      __syncwarp();
+      if (!more) break;
+      s0 += nu;
     }
-    if (lane_id() == 0) {
+  }
+}
+
+// Per touched run, a lane each: its degree; outgrown runs counted and
+// remembered (ovt[v] = staging start); a run that shrank gets sentinels after
+// its new end (the warp fills each such tail).  Counts reduced per block.
+__global__ void __launch_bounds__(kVosBlock) k_vos_runs(const uint64_t *__restrict__ keys,
+                                                        const uint64_t *__restrict__ segs, uint64_t nseg,
+                                                        const uint64_t *__restrict__ tbase,
+                                                        const uint64_t *__restrict__ base, uint32_t *slots,
+                                                        uint32_t *deg, uint64_t *ovt,
+                                                        unsigned long long *ctr /* [0] outgrown runs, [1] delta */) {
+  __shared__ long long red[2][kVosWarps];
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  long long delta = 0, outgrown = 0;
+  for (uint64_t s0 = gw * 32; s0 < nseg; s0 += nw * 32) {
+    const uint64_t sg = s0 + lane;
+    uint64_t b = 0, r = 0, d = 0;
+    bool fits = false;
+    if (sg < nseg) {
+      const uint64_t v = keys[segs[sg]] >> 32;
+      const uint64_t t = tbase[sg];
+      b = base[v];
+      r = tbase[sg + 1] - t;
+      d = deg[v];
+      fits = r <= base[v + 1] - b;
+      if (!fits) {
+        ovt[v] = t;
+        outgrown++;
+      }
       deg[v] = (uint32_t)r;
-      atomicAdd(&ctr[1], (unsigned long long)((long long)r - (long long)d));
+      delta += (long long)r - (long long)d;
     }
+    unsigned m = __ballot_sync(kFull, fits && d > r);
+    while (m) {
+      const int j = __ffs(m) - 1;
+      m &= m - 1;
+      const uint64_t bj = __shfl_sync(kFull, b, j), rj = __shfl_sync(kFull, r, j), dj = __shfl_sync(kFull, d, j);
+      for (uint64_t i = rj + lane; i < dj; i += 32) slots[bj + i] = kSentinel;
+    }
+  }
+  delta = warp_sum(delta);
+  outgrown = warp_sum(outgrown);
+  if (lane == 0) {
+    red[0][w] = delta;
+    red[1][w] = outgrown;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long a = 0, o = 0;
+    for (int i = 0; i < kVosWarps; i++) {
+      a += red[0][i];
+      o += red[1][i];
+    }
+    if (o) atomicAdd(&ctr[0], (unsigned long long)o);
+    if (a) atomicAdd(&ctr[1], (unsigned long long)a);
   }
 }
 
@@ -382,11 +578,17 @@ int vos_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   BYO_TRY(ensure(ctx, V->temp, (total_t + 1) * 4));
   uint32_t *temp = (uint32_t *)V->temp.p;
   // 4. merged runs into the staging area, back into their regions
-  launch(ctx, k_vos_shift, dim3(grid_for(ctx, total_a, kShiftThreads, 8)), dim3(kShiftThreads), 0, keys, count,
-         (const uint64_t *)segs,
-         nseg, (const uint64_t *)abase, total_a, (const uint64_t *)tbase, (const uint32_t *)rk,
-         (const uint32_t *)kflag, (const uint64_t *)kscan, (const uint64_t *)g->d_off,
-         (const uint32_t *)g->d_slots, insert, temp);
+  // chunk tables for the shift (over the old keys) and the copy back (over
+  // the staging area), sized once: the buffer must not move between the two
+  BYO_TRY(ensure(ctx, V->chunks, ((total_a > total_t ? total_a : total_t) / kChunk + 2) * 4));
+  uint32_t *first = nullptr;
+  uint64_t nchunks = 0;
+  BYO_TRY(chunk_first(ctx, V->chunks, abase, nseg, total_a, &first, &nchunks));
+  if (nchunks)
+    launch(ctx, k_vos_shift, dim3(grid_for(ctx, nchunks * 32, kVosBlock, 8)), dim3(kVosBlock), 0, keys, count,
+           (const uint64_t *)segs, nseg, (const uint64_t *)abase, (const uint64_t *)tbase, (const uint32_t *)rk,
+           (const uint32_t *)kflag, (const uint64_t *)kscan, (const uint64_t *)g->d_off,
+           (const uint32_t *)g->d_slots, insert, (const uint32_t *)first, nchunks, temp);
   if (insert)
     launch(ctx, k_vos_insert_new, dim3(grid_for(ctx, count, 256)), dim3(256), 0, keys, count,
            (const uint32_t *)segid, (const uint64_t *)segs, (const uint64_t *)tbase, (const uint32_t *)rk,
@@ -394,9 +596,14 @@ int vos_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   BYO_TRY(ensure(ctx, V->ovt, g->n * 8));
   uint64_t *ovt = (uint64_t *)V->ovt.p;
   BYO_CU(ctx, cudaMemsetAsync(ovt, 0xFF, g->n * 8, ctx->stream));
-  launch_t(ctx, "vos_merge", k_vos_back, dim3(grid_for(ctx, nseg * 32, 256, 8)), dim3(256), 0, keys, count,
-           (const uint64_t *)segs, nseg, (const uint64_t *)tbase, (const uint64_t *)g->d_off,
-           (const uint32_t *)temp, g->d_slots, g->d_deg, ovt, ctr + 2);
+  BYO_TRY(chunk_first(ctx, V->chunks, tbase, nseg, total_t, &first, &nchunks));
+  if (nchunks)
+    launch_t(ctx, "vos_merge", k_vos_back, dim3(grid_for(ctx, nchunks * 32, kVosBlock, 8)), dim3(kVosBlock), 0,
+             keys, (const uint64_t *)segs, nseg, (const uint64_t *)tbase, (const uint64_t *)g->d_off,
+             (const uint32_t *)temp, (const uint32_t *)first, nchunks, g->d_slots);
+  launch(ctx, k_vos_runs, dim3(grid_for(ctx, (nseg + 31) / 32 * 32, kVosBlock, 8)), dim3(kVosBlock), 0, keys,
+         (const uint64_t *)segs, nseg, (const uint64_t *)tbase, (const uint64_t *)g->d_off, g->d_slots, g->d_deg,
+         ovt, ctr + 2);
   BYO_CU(ctx, cudaMemcpyAsync(h, ctr + 2, 16, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   const uint64_t outgrown = h[0];
