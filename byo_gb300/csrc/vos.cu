@@ -120,8 +120,9 @@ void vos_destroy(Vos *v) {
 // the warp loads the starts and metadata of up to 32 consecutive units (from
 // first[c], the unit holding the chunk's first position) into shared memory,
 // lane j unit j, handles the chunk's positions inside them -- each lane finds
-// its position's unit by a binary search over the 32 starts -- and moves on
-// to the next 32 units until the chunk ends.
+// its first position's unit by a binary search over the 32 starts and then
+// steps forward with its positions -- and moves on to the next 32 units until
+// the chunk ends.
 constexpr int kVosBlock = 256;
 constexpr int kVosWarps = kVosBlock / 32;
 constexpr uint64_t kChunk = 2048;
@@ -154,6 +155,12 @@ __device__ __forceinline__ int unit_of(const uint64_t *st, int nu, uint64_t p) {
   }
   return lo;
 }
+// From the unit j of an earlier position to the unit of p: a lane's positions
+// rise by 32 per step and runs hold ~30 keys, so this is about one compare.
+__device__ __forceinline__ int unit_next(const uint64_t *st, int nu, int j, uint64_t p) {
+  while (j + 1 < nu && st[j + 1] <= p) j++;
+  return j;
+}
 
 __global__ void __launch_bounds__(kVosBlock) k_vos_compact(const uint64_t *__restrict__ base,
                                                            const uint32_t *__restrict__ slots,
@@ -177,13 +184,14 @@ __global__ void __launch_bounds__(kVosBlock) k_vos_compact(const uint64_t *__res
       if (lane == 0) st[w][nu] = offc[u + nu];
       __syncwarp();
       const uint64_t lo = max(c0, st[w][0]), hi = min(c1, st[w][nu]);
+      int j = lo + lane < hi ? unit_of(st[w], nu, lo + lane) : 0;
       for (uint64_t p = lo + lane; p < hi; p += 128) {
         uint32_t x[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           const uint64_t pp = p + 32 * q;
           if (pp < hi) {
-            const int j = unit_of(st[w], nu, pp);
+            j = unit_next(st[w], nu, j, pp);
             x[q] = slots[sb[w][j] + (pp - st[w][j])];
           }
         }
@@ -347,14 +355,19 @@ __global__ void __launch_bounds__(kVosBlock)
       }
       __syncwarp();
       const uint64_t lo = max(c0, st[w][0]), hi = min(c1, st[w][nu]);
+      int jc = lo + lane < hi ? unit_of(st[w], nu, lo + lane) : 0;
       for (uint64_t p0 = lo + lane; p0 < hi; p0 += 128) {
         int jq[4];
         uint32_t xq[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           const uint64_t p = p0 + 32 * q;
-          jq[q] = p < hi ? unit_of(st[w], nu, p) : -1;
-          if (jq[q] >= 0) xq[q] = slots[sbs[w][jq[q]] + (p - st[w][jq[q]])];
+          jq[q] = -1;
+          if (p < hi) {
+            jc = unit_next(st[w], nu, jc, p);
+            jq[q] = jc;
+            xq[q] = slots[sbs[w][jc] + (p - st[w][jc])];
+          }
         }
 #pragma unroll
         for (int q = 0; q < 4; q++) {
@@ -431,14 +444,19 @@ __global__ void __launch_bounds__(kVosBlock) k_vos_back(const uint64_t *__restri
       if (lane == 0) st[w][nu] = tbase[s0 + nu];
       __syncwarp();
       const uint64_t lo = max(c0, st[w][0]), hi = min(c1, st[w][nu]);
+      int jc = lo + lane < hi ? unit_of(st[w], nu, lo + lane) : 0;
       for (uint64_t p = lo + lane; p < hi; p += 128) {
         uint32_t x[4];
         int jj[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
           const uint64_t pp = p + 32 * q;
-          jj[q] = pp < hi ? unit_of(st[w], nu, pp) : -1;
-          if (jj[q] >= 0) x[q] = temp[pp];
+          jj[q] = -1;
+          if (pp < hi) {
+            jc = unit_next(st[w], nu, jc, pp);
+            jj[q] = jc;
+            x[q] = temp[pp];
+          }
         }
 #pragma unroll
         for (int q = 0; q < 4; q++)
