@@ -235,6 +235,14 @@ class GPU_VOS_graph : public GPU_PMA_graph<W> {
       : GPU_PMA_graph<W>(BYO_CONTAINER_VOS, v_data, n, m, deletion_fn, e0, w) {}
 };
 
+// The PCSR target (run_pcsr.cc:24-99, symmetric_PCSR_graph): one packed
+// array of a graph's edges in (source, destination) order with gaps, and a
+// per-vertex index into it -- the layout the PMA container keeps (leaves of
+// sorted keys with slack, the view's per-vertex offsets).  The target takes
+// the PMA container under its own name.
+template <class W>
+using GPU_PCSR_graph = GPU_PMA_graph<W>;
+
 // ---------------------------------------------------------------- GPU algorithms
 // BFS (BFS.h:47-64): Parents with UINT_E_MAX for unreached, parent[src] = src.
 inline std::vector<uint32_t> gpu_bfs(const detail::DeviceGraph &G, uint32_t src, int policy = BYO_POLICY_M20) {

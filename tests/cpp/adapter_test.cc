@@ -89,6 +89,9 @@ int main() {
   vos.remove_sorted_batch(sorted.data(), sorted.size());
   CHECK(vos.num_edges() == 14 && vos.degree(6) == 1);
   CHECK((vos.offsets() == pma.offsets()) && (vos.edges() == pma.edges()));
+  byo::GPU_PCSR_graph<int> pcsr(vd.data(), n, edges.size(), nullptr, edges.data());
+  pcsr.insert_batch(batch.data(), batch.size());
+  CHECK(pcsr.num_edges() == 16 && pcsr.degree(1) == 2 && pcsr.degree(6) == 2);
   std::printf("adapter ok\n");
   return 0;
 }
