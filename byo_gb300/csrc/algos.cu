@@ -934,11 +934,36 @@ __device__ __forceinline__ bool tc_member(const uint32_t *A, uint32_t na, uint32
   return lo < na && A[lo] == x;
 }
 
-// Wedges of the v's at positions c, c + stride, ... (chunks of 32) of A.
-// Warp-collective; pre/bas are this warp's 32-entry scratch.
+// N+(u) as a sorted array (binary search) or as an open-addressing hash set
+// in shared memory (linear probing, load <= 1/2: about two probes a lookup
+// against log2 |N+(u)| steps).
+struct TcSorted {
+  const uint32_t *A;
+  uint32_t na;
+  __device__ __forceinline__ bool has(uint32_t x) const { return tc_member(A, na, x); }
+};
+struct TcHash {
+  const uint32_t *t;
+  uint32_t mask, shift;
+  __device__ __forceinline__ bool has(uint32_t x) const {
+    uint32_t h = (x * 0x9E3779B1u) >> shift;
+    for (;;) {
+      const uint32_t y = t[h];
+      if (y == x) return true;
+      if (y == kSentinel) return false;
+      h = (h + 1) & mask;
+    }
+  }
+};
+constexpr uint32_t kTcHash = 2 * kTcWarpCap;  // table entries per warp
+
+// Wedges of the v's at positions c, c + stride, ... (chunks of 32) of V =
+// N+(u), each w of N+(v) looked up in S.  Warp-collective; pre/bas are this
+// warp's 32-entry scratch.
+template <class Set>
 __device__ __forceinline__ uint64_t tc_wedges(const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dn,
                                               const uint32_t *A, uint32_t na, uint32_t c0, uint32_t stride,
-                                              uint32_t *pre, uint64_t *bas) {
+                                              uint32_t *pre, uint64_t *bas, const Set &S) {
   const unsigned lane = lane_id();
   uint64_t cnt = 0;
   for (uint32_t c = c0; c < na; c += stride) {
@@ -955,39 +980,54 @@ __device__ __forceinline__ uint64_t tc_wedges(const uint64_t *__restrict__ doff,
     bas[lane] = b;
     __syncwarp();
     const uint32_t total = __shfl_sync(kFull, incl, 31);
-    for (uint32_t t = lane; t < total; t += 32) {
-      uint32_t lo = 0, hi = 31;  // first lane whose inclusive prefix exceeds t
+    uint32_t lo = 0;  // first lane whose inclusive prefix exceeds t: a binary search for
+    if (lane < total) {  // the lane's first t, then a forward walk as t rises by 32
+      uint32_t hi = 31;
       while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (pre[mid] <= t) lo = mid + 1; else hi = mid;
+        if (pre[mid] <= lane) lo = mid + 1; else hi = mid;
       }
+    }
+    for (uint32_t t = lane; t < total; t += 32) {
+      while (pre[lo] <= t) lo++;
       const uint32_t start = lo ? pre[lo - 1] : 0;
       const uint32_t w = dn[bas[lo] + (t - start)];
-      cnt += tc_member(A, na, w);
+      cnt += S.has(w);
     }
     __syncwarp();
   }
   return cnt;
 }
 
-// A warp per vertex with 2 <= |N+(u)| <= kTcWarpCap.
+// A warp per vertex with 2 <= |N+(u)| <= kTcWarpCap: N+(u) goes into a hash
+// set of the next power of two >= 2 |N+(u)| entries (at least 64) in the
+// warp's shared memory; the v's are read from the list itself.
 __global__ void __launch_bounds__(256) k_tc_warp(const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dn,
                                                  uint64_t n, unsigned long long *total) {
-  __shared__ uint32_t As[8][kTcWarpCap];
+  __shared__ uint32_t Ht[8][kTcHash];
   __shared__ uint32_t pre[8][32];
   __shared__ uint64_t bas[8][32];
   __shared__ unsigned long long sm[9];
   const unsigned w = threadIdx.x >> 5, lane = lane_id();
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint32_t *tab = Ht[w];
   uint64_t cnt = 0;
   for (uint64_t u = gw; u < n; u += nw) {
     const uint64_t ab = doff[u];
     const uint32_t na = (uint32_t)(doff[u + 1] - ab);
     if (na < 2 || na > kTcWarpCap) continue;
-    for (uint32_t i = lane; i < na; i += 32) As[w][i] = dn[ab + i];
+    const uint32_t lg = max(6, 32 - __clz((int)(2 * na - 1)));  // 2^lg >= 2 na
+    const uint32_t size = 1u << lg, mask = size - 1, shift = 32 - lg;
+    for (uint32_t i = lane; i < size; i += 32) tab[i] = kSentinel;
     __syncwarp();
-    cnt += tc_wedges(doff, dn, As[w], na, 0, 32, pre[w], bas[w]);
+    for (uint32_t i = lane; i < na; i += 32) {
+      const uint32_t x = dn[ab + i];
+      uint32_t h = (x * 0x9E3779B1u) >> shift;
+      while (atomicCAS(tab + h, kSentinel, x) != kSentinel) h = (h + 1) & mask;
+    }
+    __syncwarp();
+    cnt += tc_wedges(doff, dn, dn + ab, na, 0, 32, pre[w], bas[w], TcHash{tab, mask, shift});
     __syncwarp();
   }
   const unsigned long long tot = block_sum((unsigned long long)cnt, sm);
@@ -1017,7 +1057,7 @@ __global__ void __launch_bounds__(256) k_tc_block(const uint64_t *__restrict__ d
       A = Ablk;
     }
     __syncthreads();
-    cnt += tc_wedges(doff, dn, A, na, w * 32, nwb * 32, pre[w], bas[w]);
+    cnt += tc_wedges(doff, dn, A, na, w * 32, nwb * 32, pre[w], bas[w], TcSorted{A, na});
     __syncthreads();
   }
   const unsigned long long tot = block_sum((unsigned long long)cnt, sm);
