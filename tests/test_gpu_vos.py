@@ -86,3 +86,35 @@ def test_vos_generate_and_empty(ctx, oracle_mod):
     assert G.insert_batch(allk) == len(rn)
     _check(byo, O, G, ro, rn, (10,))
     G.close()
+
+
+def test_vos_large_batch_matches_pma(ctx, oracle_mod):
+    """A batch past the two-level sort's threshold (2^21 keys), runs that span
+    many key chunks, and an empty batch: the VOS container keeps the oracle's
+    contents, the same as the PMA's."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 18
+    n = 1 << lg
+    G = byo.Graph.generate(ctx, "rmat", seed=73, lg_n=lg, draws=1 << 22, container="vos")
+    P = byo.Graph.generate(ctx, "rmat", seed=73, lg_n=lg, draws=1 << 22, container="pma")
+    s, d = O.rmat_edges(73, lg, 1 << 22)
+    ro, rn = O.build_csr(n, s, d)
+    st = O.Store(ro, rn)
+    rng = np.random.default_rng(74)
+    pairs = rng.integers(0, n, size=(1200000, 2))
+    keys = O.keys_from_pairs(pairs[:, 0], pairs[:, 1])
+    assert len(keys) >= 1 << 21
+    exp = st.insert_batch(keys)
+    assert G.insert_batch(keys) == exp and P.insert_batch(keys) == exp
+    ro, rn = st.export_csr()
+    _check(byo, O, G, ro, rn, (10,))
+    po, pn = P.export_csr()
+    assert np.array_equal(po, ro) and np.array_equal(pn, rn)
+    assert G.insert_batch(np.zeros(0, np.uint64)) == 0
+    exp = st.remove_batch(keys)
+    assert G.remove_batch(keys) == exp
+    ro, rn = st.export_csr()
+    _check(byo, O, G, ro, rn, (10,))
+    G.close()
+    P.close()
