@@ -476,8 +476,11 @@ struct OutLightTile {
   }
 };
 
+// heavy chunks after the light tiles (their count read on the device)
 __global__ void k_pr_desc_chunks(const uint64_t *__restrict__ off, const uint32_t *__restrict__ heavy,
-                                 const uint64_t *__restrict__ cbase, uint64_t nheavy, uint64_t base, PrDesc *desc) {
+                                 const uint64_t *__restrict__ cbase, uint64_t nheavy,
+                                 const uint64_t *__restrict__ nlight, PrDesc *desc) {
+  const uint64_t base = *nlight;
   for (uint64_t h = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; h < nheavy;
        h += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t v = heavy[h];
@@ -516,12 +519,14 @@ template <bool kComp, typename T, bool kDirectHeavy>
 __global__ void __launch_bounds__(kPrBlock) k_pr_units(const uint64_t *__restrict__ off,
                                                        const uint32_t *__restrict__ slots,
                                                        const uint32_t *__restrict__ deg,
-                                                       const PrDesc *__restrict__ desc, uint64_t nunits,
+                                                       const PrDesc *__restrict__ desc,
+                                                       const uint64_t *__restrict__ counts,
                                                        const T *__restrict__ pdiv_in, const T *__restrict__ p_curr,
                                                        T *__restrict__ p_next, T *__restrict__ pdiv_out,
                                                        T *__restrict__ part, T damping, T added, double *l1) {
   __shared__ T stage[kPrBlock / 32][kPrStage];
   __shared__ double sm[kPrBlock / 32 + 1];
+  const uint64_t nunits = counts[0] + counts[1];  // light tiles + heavy chunks
   const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
   T *buf = stage[warp];
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
@@ -686,7 +691,8 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   BYO_TRY(ws(g, WS_BUCKETS, 2 * n + 8, &lists));
   uint32_t *tstart = lists, *heavy = lists + (n + 4);
   double *d_l1 = nullptr;
-  BYO_TRY(ws(g, WS_MISC, 4, (uint32_t **)&d_l1));
+  BYO_TRY(ws(g, WS_MISC, 8, (uint32_t **)&d_l1));
+  uint64_t *counts = reinterpret_cast<uint64_t *>(d_l1 + 2);  // [0] light tiles, [1] heavy chunks
   uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
   const uint64_t *tot = nullptr;
@@ -697,32 +703,33 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   BYO_CU(ctx, cudaMemcpyAsync(h + 1, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   const uint64_t ntiles = h[0], nheavy = h[1];
+  // From here the plan stays on the device: the counts of light tiles and
+  // heavy chunks go to `counts`, which k_pr_desc_chunks and k_pr_units read,
+  // and the buffers and grid are sized by upper bounds (a heavy vertex of d
+  // slots makes ceil(d / kPrTile) chunks), so the host builds the graph
+  // below while the GPU finishes the plan.
   BYO_TRY(scan_apply(ctx, nheavy, InChunks{g->d_off, heavy}, OutPrefix{cbase}, &tot));
   BYO_CU(ctx, cudaMemcpyAsync(cbase + nheavy, tot, 8, cudaMemcpyDeviceToDevice, ctx->stream));
-  BYO_CU(ctx, cudaMemcpyAsync(h + 2, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  h[3] = n;
+  BYO_CU(ctx, cudaMemcpyAsync(counts + 1, tot, 8, cudaMemcpyDeviceToDevice, ctx->stream));
+  h[3] = n;  // h[3] is not written again before the next synchronisation
   BYO_CU(ctx, cudaMemcpyAsync(tstart + ntiles, h + 3, 4, cudaMemcpyHostToDevice, ctx->stream));
   launch(ctx, k_pr_init<T>, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint32_t *)g->d_deg, n, pa, da,
          (T)(1.0 / (double)n));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const uint64_t nchunks = h[2];
+  const uint64_t max_chunks = g->nslots / kPrTile + nheavy + 1;
   // descriptors: compacted light tiles, then heavy chunks
   PrDesc *desc = nullptr;
-  BYO_TRY(ws(g, WS_TC_NBR, (ntiles + nchunks + 1) * sizeof(PrDesc) / 4, (uint32_t **)&desc));
+  BYO_TRY(ws(g, WS_TC_NBR, (ntiles + max_chunks + 1) * sizeof(PrDesc) / 4, (uint32_t **)&desc));
   BYO_TRY(scan_apply(ctx, ntiles, InLightTile{g->d_off, tstart}, OutLightTile{g->d_off, tstart, desc}, &tot));
-  BYO_CU(ctx, cudaMemcpyAsync(h + 4, tot, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const uint64_t nlight = h[4];
+  BYO_CU(ctx, cudaMemcpyAsync(counts, tot, 8, cudaMemcpyDeviceToDevice, ctx->stream));
   if (nheavy)
     launch(ctx, k_pr_desc_chunks, dim3(grid_for(ctx, nheavy, 256)), dim3(256), 0, (const uint64_t *)g->d_off,
-           (const uint32_t *)heavy, (const uint64_t *)cbase, nheavy, nlight, desc);
-  const uint64_t nunits = nlight + nchunks;
+           (const uint32_t *)heavy, (const uint64_t *)cbase, nheavy, (const uint64_t *)counts, desc);
   T *part = nullptr;
-  BYO_TRY(ws(g, WS_TC_CNT, 2 * nchunks + 2, &part));
+  BYO_TRY(ws(g, WS_TC_CNT, 2 * max_chunks + 2, &part));
   const T damping = (T)0.85;
   const T added = (T)((1 - 0.85) * (1 / (double)n));
   const int grid_c = grid_for(ctx, nheavy * 32, 256, 8);
-  const int grid_u = grid_for(ctx, nunits * 32, kPrBlock, sizeof(T) == 4 ? 5 : 3);
+  const int grid_u = grid_for(ctx, (ntiles + max_chunks) * 32, kPrBlock, sizeof(T) == 4 ? 5 : 3);
   // The iterations run as one CUDA graph: a WHILE node whose body holds two
   // iterations (pa -> pb, then under an IF node pb -> pa), each ending in
   // k_pr_check, which sets the conditions from the L1 norm on the device.
@@ -767,13 +774,14 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
     const uint32_t *slots_ = g->d_slots, *deg_ = g->d_deg, *heavy_ = heavy;
     const uint64_t *cbase_ = cbase;
     const PrDesc *desc_ = desc;
+    const uint64_t *counts_ = counts;
     T *pa_ = pa, *pb_ = pb, *da_ = da, *db_ = db;
     double *l1_ = d_l1;
     PrLoop *loop_ = loop;
     const double eps_ = eps;
     const uint32_t maxit_ = max_iters;
     T damping_ = damping, added_ = added;
-    uint64_t nunits_ = nunits, nheavy_ = nheavy;
+    uint64_t nheavy_ = nheavy;
     int half0 = 0, half1 = 1;
     const T *pdiv_in[2] = {da_, db_}, *pcur[2] = {pa_, pb_};
     T *pnext[2] = {pb_, pa_}, *pdiv_out[2] = {db_, da_};
@@ -781,7 +789,7 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
       if (rc != BYO_OK) return;
       cudaKernelNodeParams kp = {};
       cudaGraphNode_t nu = nullptr, nc = nullptr, nk = nullptr;
-      void *ua[] = {(void *)&off_, (void *)&slots_, (void *)&deg_, (void *)&desc_, (void *)&nunits_,
+      void *ua[] = {(void *)&off_, (void *)&slots_, (void *)&deg_, (void *)&desc_, (void *)&counts_,
                     (void *)&pdiv_in[h], (void *)&pcur[h], (void *)&pnext[h], (void *)&pdiv_out[h], (void *)&part,
                     (void *)&damping_, (void *)&added_, (void *)&l1_};
       kp.func = (void *)k_pr_units<kComp, T, sizeof(T) == 8>;
