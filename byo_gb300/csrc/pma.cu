@@ -95,11 +95,17 @@ __device__ __forceinline__ uint64_t route(const uint64_t *sep, uint64_t NL, uint
 
 __global__ void k_key_bounds(const uint64_t *__restrict__ keys, uint64_t cnt, unsigned long long *out) {
   uint64_t ms = 0, md = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t k = keys[i];
-    ms = ms > (k >> 32) ? ms : (k >> 32);
-    md = md > (k & 0xFFFFFFFFull) ? md : (k & 0xFFFFFFFFull);
+  const uint64_t nthr = (uint64_t)gridDim.x * blockDim.x;
+  // four loads per thread in flight
+  for (uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i0 < cnt; i0 += 4 * nthr) {
+    uint64_t k[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) k[q] = i0 + q * nthr < cnt ? keys[i0 + q * nthr] : 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      ms = ms > (k[q] >> 32) ? ms : (k[q] >> 32);
+      md = md > (k[q] & 0xFFFFFFFFull) ? md : (k[q] & 0xFFFFFFFFull);
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -1034,7 +1040,16 @@ __global__ void k_pma_compact(const uint32_t *__restrict__ dst, const uint32_t *
   for (uint64_t i = gw; i < NL; i += nw) {
     const uint32_t c = cnt[i];
     const uint64_t o = epre[i];
-    for (uint32_t e = lane_id(); e < c; e += 32) out[o + e] = __ldcs(dst + i * kLeaf + e);
+    // eight loads per lane in flight before the stores
+    for (uint32_t e0 = lane_id(); e0 < c; e0 += 256) {
+      uint32_t x[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (e0 + 32 * q < c) x[q] = __ldcs(dst + i * kLeaf + e0 + 32 * q);
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (e0 + 32 * q < c) out[o + e0 + 32 * q] = x[q];
+    }
   }
 }
 
