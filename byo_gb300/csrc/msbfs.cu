@@ -481,37 +481,58 @@ __global__ void __launch_bounds__(kMsBlock, 5) k_ms_bfs(MsArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) c->rounds = r - 1;
 }
 
+// Bits 0..7 of x spread to the low bit of bytes 0..7 (SWAR: the byte is
+// copied into every byte lane, lane i keeps bit i, and a carry-free add
+// turns each lane's kept bit into its top bit, shifted down to bit 0).
+__device__ __forceinline__ uint64_t spread8(uint64_t x) {
+  const uint64_t t = ((x & 0xFFull) * 0x0101010101010101ull) & 0x8040201008040201ull;
+  return ((t + 0x7F7F7F7F7F7F7F7Full) >> 7) & 0x0101010101010101ull;
+}
+
+// One (source, vertex) level: a zero level is the source itself, a pair
+// reached from round 2^16 on (already written) or a pair never reached.
+__device__ __forceinline__ void ms_store_level(const MsArgs &a, uint32_t s, uint64_t v, uint32_t lv,
+                                               uint64_t sv) {
+  if (!lv) {
+    if (__ldg(a.srcs + s) == (uint32_t)v) lv = 0;
+    else if ((sv >> s) & 1) return;  // reached after round 2^16 - 1: written by the traversal
+    else lv = kSentinel;
+  }
+  __stcs(a.levels + (uint64_t)s * a.n + v, lv);
+}
+
 // The levels from the bit planes, a thread per vertex: level of (s, v) =
-// sum over planes b of bit s of plane b, << b.  A zero level is the source
-// itself, a pair reached from round 2^16 on (already written), or a pair
-// never reached (BYO_NONE).  Per source a warp stores 32 consecutive words.
+// sum over planes b of bit s of plane b, << b.  Up to 8 planes (levels below
+// 256) the levels of 8 sources at a time are assembled as bytes of one word,
+// a spread8 per plane; deeper traversals take them bit by bit.  Per source a
+// warp stores 32 consecutive words.
 __global__ void __launch_bounds__(256) k_ms_levels(const MsArgs a) {
   if (a.ctl->bar.err) return;
   const uint32_t last = a.ctl->rounds;
   const int used = last ? min(32 - __clz((int)last), kLevelBits) : 0;
   const uint64_t n = a.n;
+  const uint32_t k = a.k;
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t lv[64];
-#pragma unroll
-    for (int s = 0; s < 64; s++) lv[s] = 0;
-    for (int b = 0; b < used; b++) {
-      const uint64_t pl = __ldcs(a.planes + (uint64_t)b * n + v);
-      if (!pl) continue;
-#pragma unroll
-      for (int s = 0; s < 64; s++) lv[s] |= (uint32_t)((pl >> s) & 1) << b;
-    }
     const uint64_t sv = __ldcs(a.seen + v);
+    if (used <= 8) {
+      uint64_t pl[8];
 #pragma unroll
-    for (int s = 0; s < 64; s++) {
-      if ((uint32_t)s >= a.k) break;
-      uint32_t out = lv[s];
-      if (!out) {
-        if (__ldg(a.srcs + s) == (uint32_t)v) out = 0;
-        else if ((sv >> s) & 1) continue;  // reached after round 2^16 - 1: written by the traversal
-        else out = kSentinel;
+      for (int b = 0; b < 8; b++) pl[b] = b < used ? __ldcs(a.planes + (uint64_t)b * n + v) : 0;
+      for (uint32_t s0 = 0; s0 < k; s0 += 8) {
+        uint64_t packed = 0;
+#pragma unroll
+        for (int b = 0; b < 8; b++) packed |= spread8(pl[b] >> s0) << b;
+#pragma unroll
+        for (uint32_t i = 0; i < 8; i++)
+          if (s0 + i < k) ms_store_level(a, s0 + i, v, (uint32_t)(packed >> (8 * i)) & 0xFFu, sv);
       }
-      __stcs(a.levels + (uint64_t)s * n + v, out);
+    } else {
+      for (uint32_t s = 0; s < k; s++) {
+        uint32_t lv = 0;
+        for (int b = 0; b < used; b++) lv |= (uint32_t)((__ldg(a.planes + (uint64_t)b * n + v) >> s) & 1) << b;
+        ms_store_level(a, s, v, lv, sv);
+      }
     }
   }
 }
