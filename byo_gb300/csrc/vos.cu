@@ -311,7 +311,8 @@ __device__ __forceinline__ uint64_t seg_of(const uint64_t *pre, uint64_t nseg, u
 // shifted by the kept batch keys of its run that go before it (insert:
 // rank <= i; remove: rank < i, and a kept batch key of rank i removes it).
 // The ranks and kept-key prefix of a window's batch keys are staged in shared
-// memory when they fit.
+// memory when they fit; each lane walks a pointer forward through its run's
+// batch keys as its keys rise.
 constexpr int kShiftStage = 256;
 __global__ void __launch_bounds__(kVosBlock)
     k_vos_shift(const uint64_t *__restrict__ keys, uint64_t cnt, const uint64_t *__restrict__ segs, uint64_t nseg,
@@ -356,6 +357,8 @@ __global__ void __launch_bounds__(kVosBlock)
       __syncwarp();
       const uint64_t lo = max(c0, st[w][0]), hi = min(c1, st[w][nu]);
       int jc = lo + lane < hi ? unit_of(st[w], nu, lo + lane) : 0;
+      int bj = -1;      // run of the lane's batch-key pointer
+      uint32_t bl = 0;  // first batch key of run bj not yet before the lane's key
       for (uint64_t p0 = lo + lane; p0 < hi; p0 += 128) {
         int jq[4];
         uint32_t xq[4];
@@ -374,19 +377,18 @@ __global__ void __launch_bounds__(kVosBlock)
           if (jq[q] < 0) continue;
           const int j = jq[q];
           const uint32_t i = (uint32_t)(p0 + 32 * q - st[w][j]);
-          uint32_t l = kb[w][j], h = kb[w][j + 1];
-          const uint32_t lb = l, e = h;
-          if (insert) {  // batch keys with rank <= i go before A[i]
-            while (l < h) {
-              const uint32_t mid = (l + h) >> 1;
-              if ((staged ? srk[w][mid] : rk[g0 + mid]) <= i) l = mid + 1; else h = mid;
-            }
-          } else {  // the first batch key with rank >= i removes A[i] when it is kept
-            while (l < h) {
-              const uint32_t mid = (l + h) >> 1;
-              if ((staged ? srk[w][mid] : rk[g0 + mid]) < i) l = mid + 1; else h = mid;
-            }
+          const uint32_t lb = kb[w][j], e = kb[w][j + 1];
+          // the lane's keys rise within a run, so its pointer into the run's
+          // batch keys (sorted by rank) only moves forward
+          if (j != bj) {
+            bj = j;
+            bl = lb;
           }
+          if (insert)  // batch keys with rank <= i go before A[i]
+            while (bl < e && (staged ? srk[w][bl] : rk[g0 + bl]) <= i) bl++;
+          else  // the first batch key with rank >= i removes A[i] when it is kept
+            while (bl < e && (staged ? srk[w][bl] : rk[g0 + bl]) < i) bl++;
+          const uint32_t l = bl;
           const uint32_t before = staged ? sks[w][l] - sks[w][lb] : (uint32_t)(kscan[g0 + l] - kscan[g0 + lb]);
           if (insert) {
             temp[stb[w][j] + i + before] = xq[q];
