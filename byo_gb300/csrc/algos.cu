@@ -94,19 +94,37 @@ __global__ void k_cc_compress(uint32_t *p, uint64_t n) {
     p[v] = cc_find(p, (uint32_t)v);
 }
 
-// Remaining edges of vertices outside the giant component; GS lanes per
-// vertex.  A vertex inside the giant component is skipped entirely: each of
-// its neighbours outside it will link the edge from its own side.
+// The vertices whose remaining edges must be linked: more than kSample
+// neighbours (the first kSample are linked by the sampling rounds) and a root
+// other than the giant component's, a thread per vertex, appended to `list`.
+// A vertex inside the giant component is skipped entirely: each of its
+// neighbours outside it will link the edge from its own side, and roots only
+// merge, so a vertex found inside stays inside.
+__global__ void __launch_bounds__(256) k_cc_outside(const uint32_t *__restrict__ deg, uint32_t *p, uint64_t n,
+                                                    const uint32_t *__restrict__ giant_root, uint32_t *list,
+                                                    unsigned long long *count) {
+  const uint32_t giant = *giant_root;
+  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+       base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v = base + lane_id();
+    const bool keep = v < n && deg[v] > (uint32_t)kSample && cc_find(p, (uint32_t)v) != giant;
+    const uint64_t at = warp_append(keep, count);
+    if (keep) list[at] = (uint32_t)v;
+  }
+}
+
+// Remaining edges of the listed vertices, GS lanes per vertex.
 template <int GS>
 __global__ void __launch_bounds__(256) k_cc_finish(const uint64_t *__restrict__ off,
                                                    const uint32_t *__restrict__ slots, uint32_t *p,
-                                                   uint64_t n, const uint32_t *__restrict__ giant_root) {
-  const uint32_t giant = *giant_root;
+                                                   const uint32_t *__restrict__ list,
+                                                   const unsigned long long *__restrict__ count) {
+  const uint64_t nl = *count;
   const unsigned gl = threadIdx.x % GS;
   const uint64_t gid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / GS;
   const uint64_t ng = ((uint64_t)gridDim.x * blockDim.x) / GS;
-  for (uint64_t v = gid; v < n; v += ng) {
-    if (cc_find(p, (uint32_t)v) == giant) continue;
+  for (uint64_t t = gid; t < nl; t += ng) {
+    const uint32_t v = list[t];
     const uint64_t b = off[v], e = off[v + 1];
     // skip the first kSample non-gap neighbours: already linked
     uint64_t start = b;
@@ -115,7 +133,7 @@ __global__ void __launch_bounds__(256) k_cc_finish(const uint64_t *__restrict__ 
     for (uint64_t j = start + gl; j < e; j += GS) {
       uint32_t u = slots[j];
       if (u == kSentinel) continue;
-      cc_link(p, (uint32_t)v, u);
+      cc_link(p, v, u);
     }
   }
 }
@@ -173,21 +191,26 @@ int cc_run(byo_graph *g, uint32_t *d_label) {
            (const uint32_t *)g->d_slots, p, n, r);
     launch(ctx, k_cc_compress, dim3(grid_for(ctx, n, 256)), dim3(256), 0, p, n);
   }
-  uint32_t *giant = nullptr;
-  BYO_TRY(ws(g, WS_MISC, 4, &giant));
+  uint32_t *giant = nullptr, *list = nullptr;
+  BYO_TRY(ws(g, WS_MISC, 4, &giant));  // [0] giant root, [2..3] count of listed vertices
+  BYO_TRY(ws(g, WS_FRONT_LIST_A, n, &list));
+  unsigned long long *count = reinterpret_cast<unsigned long long *>(giant + 2);
+  BYO_CU(ctx, cudaMemsetAsync(count, 0, 8, ctx->stream));
   launch(ctx, k_cc_giant, dim3(1), dim3(kCcProbe), 0, (const uint32_t *)p, n, (uint64_t)0x5EEDull, giant);
+  launch(ctx, k_cc_outside, dim3(grid_for(ctx, n, 256)), dim3(256), 0, (const uint32_t *)g->d_deg, p, n,
+         (const uint32_t *)giant, list, count);
   const double avg = (double)g->m / (double)n;
   const int GS = avg >= 24 ? 16 : avg >= 8 ? 8 : 4;
   const int grid = grid_for(ctx, n * GS, 256, 16);
   if (GS == 16)
     launch_t(ctx, "cc_finish", k_cc_finish<16>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
-           (const uint32_t *)g->d_slots, p, n, (const uint32_t *)giant);
+             (const uint32_t *)g->d_slots, p, (const uint32_t *)list, (const unsigned long long *)count);
   else if (GS == 8)
     launch_t(ctx, "cc_finish", k_cc_finish<8>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
-           (const uint32_t *)g->d_slots, p, n, (const uint32_t *)giant);
+             (const uint32_t *)g->d_slots, p, (const uint32_t *)list, (const unsigned long long *)count);
   else
     launch_t(ctx, "cc_finish", k_cc_finish<4>, dim3(grid), dim3(256), 0, (const uint64_t *)g->d_off,
-           (const uint32_t *)g->d_slots, p, n, (const uint32_t *)giant);
+             (const uint32_t *)g->d_slots, p, (const uint32_t *)list, (const unsigned long long *)count);
   launch(ctx, k_cc_compress, dim3(grid_for(ctx, n, 256)), dim3(256), 0, p, n);
   return check_launch(ctx, "cc");
 }
