@@ -843,6 +843,104 @@ def map_cpu_sample():
                       "%d threads), %.1f s" % (passes, O.num_threads(), secs)}
 
 
+# ------------------------------------------------------------------ triangle counting
+def tc_dag_bytes(off, nb):
+    """Algorithmic bytes of one degree-ordered TC (4 per id of both out-lists
+    per DAG edge, Triangle.h:167-204 with intersect.h:72-151), from the CSR on
+    the host: rank by (degree, id), DAG edges point to the higher rank."""
+    n = len(off) - 1
+    deg = np.diff(off.astype(np.int64))
+    order = np.lexsort((np.arange(n), deg))
+    rank = np.empty(n, np.int64)
+    rank[order] = np.arange(n)
+    src = np.repeat(np.arange(n, dtype=np.int64), deg)
+    up = rank[nb.astype(np.int64)] > rank[src]
+    s, d = src[up], nb.astype(np.int64)[up]
+    dplus = np.bincount(s, minlength=n)
+    return int(4 * (dplus[s].sum() + dplus[d].sum())), int(len(s))
+
+
+def run_tc(args, rank, world, local_rank):
+    """TriangleCounting (Triangle_degree_ordering) on RMAT 2^22 with average
+    degree 32 (the scale workload's TC graph), CSR: one step = one count."""
+    import torch
+    import byo_gb300 as byo
+    from byo_gb300 import _abi
+    L = _abi.lib()
+    torch.cuda.set_device(local_rank)
+    ctx = byo.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    name, desc, spec = TC_GRAPH
+    spec = dict(spec)
+    kind = spec.pop("kind")
+    G = byo.Graph.generate(ctx, kind, container="csr", **spec)
+    n, m = G.N(), G.M()
+    off, nb = G.export_csr()
+    alg_bytes, dag_edges = tc_dag_bytes(off, nb)
+    del off, nb
+    cnt = ctypes.c_uint64(0)
+    for _ in range(args.warmup):
+        _abi.check(L.byo_triangle_count(G.h, ctypes.byref(cnt)), ctx.h)
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pushed = nvtx_push(torch, "timed")
+    e0.record(stream)
+    for _ in range(args.steps):
+        _abi.check(L.byo_triangle_count(G.h, ctypes.byref(cnt)), ctx.h)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    nvtx_pop(torch, pushed)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = ctx.launches - launches0
+    # end to end: the host API from a host CSR (graph upload included)
+    offh, nbh = G.export_csr()
+    t0 = time.perf_counter()
+    H = byo.Graph.from_csr(ctx, offh, nbh)
+    c2 = byo.Triangle_degree_ordering(H)
+    e2e_s = time.perf_counter() - t0
+    H.close()
+    assert c2 == cnt.value
+    peak, peak_kind = measured_peaks()
+    res = {"metric": "TriangleCounting (degree-ordered) edges/s on RMAT 2^22, average degree 32",
+           "value": m / (ms / 1e3) / 1e9, "unit": "G edges/s (directed edges of the graph per count)",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 ids, u64 count",
+           "data": "synthetic (seeded RMAT)",
+           "config": {"workload": "tc: %s, CSR" % desc, "n": n, "m": m, "dag_edges": dag_edges,
+                      "triangles": int(cnt.value), "l2": "graph 513 MB > L2"},
+           "roofline": {"bound": "hbm", "kernel": "k_tc_warp + k_tc_block (one count)",
+                        "achieved": alg_bytes / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": alg_bytes / (ms / 1e3) / 1e9 / peak, "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": ms, "traffic": None},
+           "e2e": {"value": m / e2e_s / 1e9, "unit": "G edges/s (directed edges of the graph per count)",
+                   "h2d_bytes_per_step": int(offh.nbytes + nbh.nbytes), "d2h_bytes_per_step": 8},
+           "gpu_launches": launches, "clocks": clk}
+    return res, ctx, G
+
+
+def tc_cpu_sample():
+    """The oracle's degree-ordered TC (OpenMP, all host threads) on RMAT 2^18
+    with average degree 32 (2^22 draws): a bounded sample of the workload."""
+    from oracle import oracle as O
+    O.build()
+    s, d = O.rmat_edges(1, 18, 1 << 22)
+    off, nb = O.build_csr(1 << 18, s, d)
+    runs, secs = 0, 0.0
+    while secs < 3.0:
+        t0 = time.time()
+        O.triangle_count(off, nb)
+        secs += time.time() - t0
+        runs += 1
+    return {"value": len(nb) * runs / secs / 1e9, "unit": "G edges/s (directed edges of the graph per count)",
+            "cores": O.num_threads(), "kind": "port",
+            "sample": "%d counts on RMAT 2^18, 2^22 draws (oracle port, OpenMP, %d threads), %.1f s"
+                      % (runs, O.num_threads(), secs)}
+
+
 # ------------------------------------------------------------------ update stream
 STREAM_BATCHES, STREAM_SEED = 200, 4242
 
@@ -1357,7 +1455,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dynamic",
                     choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map", "bytepd",
-                             "stream"])
+                             "stream", "tc"])
     ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
     ap.add_argument("--container", default="pma", choices=["pma", "vos"],
                     help="dynamic: the container updated (pma: packed-memory array; vos: vector of per-vertex runs)")
@@ -1386,10 +1484,11 @@ def main():
                               "e2e": {"value": cb["value"], "unit": MIXED_UNIT, "h2d_bytes_per_step": 0,
                                       "d2h_bytes_per_step": 0}}), flush=True)
             return 0
-        if args.workload in ("map", "bytepd"):
-            cb = map_cpu_sample() if args.workload == "map" else bytepd_cpu_sample()
-            metric = ("Test_Map + Test_Map_Remote edges/s (run_all's Map applications)" if args.workload == "map"
-                      else "byte-PD decode edges/s (compressed neighbour lists to CSR on the GPU)")
+        if args.workload in ("map", "bytepd", "tc"):
+            cb = {"map": map_cpu_sample, "bytepd": bytepd_cpu_sample, "tc": tc_cpu_sample}[args.workload]()
+            metric = {"map": "Test_Map + Test_Map_Remote edges/s (run_all's Map applications)",
+                      "bytepd": "byte-PD decode edges/s (compressed neighbour lists to CSR on the GPU)",
+                      "tc": "TriangleCounting (degree-ordered) edges/s on RMAT 2^22, average degree 32"}[args.workload]
             print(json.dumps({"metric": metric,
                               "value": cb["value"], "unit": cb["unit"], "n_gpus": 0, "steps": args.steps,
                               "warmup": args.warmup, "higher_is_better": True, "impl": "reference",
@@ -1419,6 +1518,11 @@ def main():
         args.no_cpu_baseline = True
     elif args.workload == "stream":
         res, ctx, G = run_stream(args, rank, world, local_rank)
+        args.no_cpu_baseline = True
+    elif args.workload == "tc":
+        res, ctx, G = run_tc(args, rank, world, local_rank)
+        if rank == 0 and not args.no_cpu_baseline:
+            res["cpu_baseline"] = tc_cpu_sample()
         args.no_cpu_baseline = True
     elif args.workload == "bytepd":
         res, ctx, G = run_bytepd(args, rank, world, local_rank)
