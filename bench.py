@@ -2,8 +2,8 @@
 """Benchmark of the BYO hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dynamic|static|mixed|multi|scale|families|map]
-                    [--policy m20|learned|...]
+                    [--workload dynamic|static|mixed|multi|scale|families|map|bytepd|stream|tc]
+                    [--container pma|vos] [--policy m20|learned|...]
 
 Workloads (synthetic: seeded RMAT a=.57 b=.19 c=.19 d=.05, symmetrised,
 deduplicated, no self loops; the reference publishes no dataset for them):
@@ -26,6 +26,9 @@ deduplicated, no self loops; the reference publishes no dataset for them):
   stream   200 small update batches inserted then removed on the mixed
            workload's PMA through byo_graph_update_stream, against one call
            per batch.
+  tc       triangle counting (degree ordered) on RMAT n=2^22, average degree
+           32, CSR: one count per step.
+--container vos runs the dynamic step on the vector of per-vertex runs.
 
 The metric is the composite of BFS, CC, PageRank and update rates; `value` is the step's edge operations per
 second in G/s: BFS traversed edges (undirected, Graph500 convention) + CC
