@@ -1031,8 +1031,8 @@ __device__ __forceinline__ uint64_t tc_wedges(const uint64_t *__restrict__ doff,
 }
 
 // A warp per vertex with 2 <= |N+(u)| <= kTcWarpCap: N+(u) goes into a hash
-// set of the next power of two >= 2 |N+(u)| entries (at least 64) in the
-// warp's shared memory; the v's are read from the list itself.
+// set of the next power of two >= 4 |N+(u)| entries (at least 64, at most
+// kTcHash) in the warp's shared memory; the v's are read from the list itself.
 __global__ void __launch_bounds__(256) k_tc_warp(const uint64_t *__restrict__ doff, const uint32_t *__restrict__ dn,
                                                  uint64_t n, unsigned long long *total) {
   __shared__ uint32_t Ht[8][kTcHash];
@@ -1048,7 +1048,9 @@ __global__ void __launch_bounds__(256) k_tc_warp(const uint64_t *__restrict__ do
     const uint64_t ab = doff[u];
     const uint32_t na = (uint32_t)(doff[u + 1] - ab);
     if (na < 2 || na > kTcWarpCap) continue;
-    const uint32_t lg = max(6, 32 - __clz((int)(2 * na - 1)));  // 2^lg >= 2 na
+    // 2^lg >= 4 na up to the table's kTcHash entries (>= 2 na): load <= 1/4
+    // for most vertices, so a miss (most lookups) ends after ~1.4 probes
+    const uint32_t lg = min(31 - __clz((int)kTcHash), max(6, 32 - __clz((int)(4 * na - 1))));
     const uint32_t size = 1u << lg, mask = size - 1, shift = 32 - lg;
     for (uint32_t i = lane; i < size; i += 32) tab[i] = kSentinel;
     __syncwarp();
