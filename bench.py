@@ -197,6 +197,147 @@ def bfs_bytes(n, reached_deg_sum, reached):
     return 4 * reached_deg_sum + 8 * (n + 1) + 8 * reached + 4 * n
 
 
+def cc_bytes(n, m):
+    # one pass over the edges (ids), offsets once, labels read + written once
+    return 4 * m + 8 * (n + 1) + 8 * n
+
+
+def update_bytes(B, touched_entries):
+    # 8-byte keys read + written once for the sort, and the 4-byte entries of
+    # every leaf the merge touches read + written once
+    return 16 * B + 8 * touched_entries
+
+
+def dynamic_config(dynamic, container, n, m):
+    """The workload description both arms print (same keys and values)."""
+    return {"workload": ("dynamic %s: RMAT 2^22, 2^26 draws, batch 1e7 pairs" % container.upper()) if dynamic
+            else "static CSR: RMAT 2^22, 2^26 draws",
+            "n": int(n), "m": int(m), "batch_pairs": BATCH if dynamic else 0, "bfs_src": SRC,
+            "pr_eps": PR_EPS, "pr_max_iters": PR_ITERS, "rmat": [0.57, 0.19, 0.19], "seed": SEED,
+            "batch_seed": BATCH_SEED if dynamic else None,
+            "l2": "inputs larger than L2 (RMAT 2^22 graph > 126 MB)"}
+
+
+# ------------------------------------------------------------------ parity against the oracle
+def parity_selfcheck(byo, L, _abi, ctx, G, keys, B, policy, dynamic, O, off0, nb0, okeys):
+    """The headline workload's outputs against the oracle, on the state the
+    timed steps see (before the timed region): container contents before the
+    batch, after the insert and after the remove; BFS parents and levels and
+    CC labels bit for bit; PageRank (FP32-Kahan) L1 against the FP64 oracle.
+    Returns the parity block and the oracle's sorted-set store holding the
+    contents after the remove (the batch's pairs that were already edges are
+    gone then, in both), for the batch sweep."""
+    ch = ctypes.c_uint64(0)
+    go, gn = G.export_csr()
+    contents = bool(np.array_equal(go, off0) and np.array_equal(gn, nb0))
+    so, sn = off0, nb0
+    st = None
+    if dynamic:
+        st = O.Store(off0, nb0)
+        _abi.check(L.byo_graph_insert_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+        contents &= int(ch.value) == st.insert_batch(okeys)
+        so, sn = st.export_csr()
+        go, gn = G.export_csr()
+        contents &= bool(np.array_equal(go, so) and np.array_equal(gn, sn))
+    par, lev = byo.BFS(G, SRC, policy=policy, levels=True)
+    opar, olev = O.bfs(so, sn, SRC)
+    bfs_ok = bool(np.array_equal(par, opar) and np.array_equal(lev, olev))
+    lab = byo.SimpleUnionAsync(G)
+    cc_ok = bool(np.array_equal(lab, O.cc(so, sn)))
+    p, it, _ = byo.PageRank(G, PR_EPS, PR_ITERS, info=True)
+    op, oit, _ = O.pagerank(so, sn, PR_EPS, PR_ITERS)
+    l1 = float(np.abs(p - op).sum())
+    del so, sn
+    if dynamic:
+        _abi.check(L.byo_graph_remove_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+        contents &= int(ch.value) == st.remove_batch(okeys)
+        so, sn = st.export_csr()
+        go, gn = G.export_csr()
+        contents &= bool(np.array_equal(go, so) and np.array_equal(gn, sn))
+    block = {"contents": contents, "bfs": bfs_ok, "cc": cc_ok, "pr_l1": l1, "pr_l1_bound": 1e-6,
+             "pr_iters": [int(it), int(oit)],
+             "checked": "before the timed region, on the state the timed steps see: contents (sorted adjacency) "
+                        "before the batch, after the insert and after the remove, and the changed-key counts; "
+                        "BFS(%d) parents + levels and CC labels after the insert, bit-exact; PageRank "
+                        "FP32-Kahan vs the FP64 oracle, L1 over all vertices" % SRC}
+    block["ok"] = bool(contents and bfs_ok and cc_ok and l1 <= 1e-6)
+    return block, st
+
+
+SWEEP_SIZES = (1_000, 100_000, 10_000_000)
+SWEEP_ROUNDS = 10
+
+
+def batch_sweep(byo, L, _abi, ctx, G, torch, stream, dev, n, policy, O, st):
+    """BASELINE's dynamic-container schedule (Batch_insert_runner,
+    benchmarks/run_unweighted.h:781-893): for each batch size b in 1e3, 1e5,
+    1e7 pairs, rounds 0..10 (round 0 untimed), each inserting a fresh batch
+    of b uniform pairs, symmetrised (2b directed keys, unsorted), then
+    removing it.  Insert and remove are timed on the device (CUDA events on
+    the library's stream around the device-API call); after every batch,
+    outside the timing, the contents and changed-key count are compared with
+    the oracle's sorted-set store `st` (which holds the container's contents
+    on entry) and BFS(10) parents and CC labels with the oracle's answers on
+    those contents."""
+    ch = ctypes.c_uint64(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out, checks, failures = {}, 0, []
+    kbuf = torch.empty(2 * max(SWEEP_SIZES), dtype=torch.int64, device=dev)
+    t_verify = 0.0
+    for b in SWEEP_SIZES:
+        tag = "1e%d" % (len(str(b)) - 1)
+        ins_ms, rem_ms, upd_bytes = [], [], [0.0, 0.0]
+        for r in range(SWEEP_ROUNDS + 1):
+            seed = 50_000 + 1000 * len(str(b)) + r
+            _abi.check(L.byo_gen_uniform_keys_device(ctx.h, seed, n, b, kbuf.data_ptr()), ctx.h)
+            us, ud = O.uniform_pairs(seed, n, b)
+            okeys = O.keys_from_pairs(us, ud)
+            for phase in (1, 0):
+                ctx.synchronize()
+                with torch.cuda.stream(stream):
+                    e0.record(stream)
+                    fn = L.byo_graph_insert_batch_device if phase else L.byo_graph_remove_batch_device
+                    _abi.check(fn(G.h, kbuf.data_ptr(), 2 * b, 0, ctypes.byref(ch)), ctx.h)
+                    e1.record(stream)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1)
+                if r > 0:
+                    (ins_ms if phase else rem_ms).append(ms)
+                    upd_bytes[1 - phase] += update_bytes(2 * b, G.last_update_stats()["touched_entries"])
+                # verification, outside the timing
+                tv = time.perf_counter()
+                ok = int(ch.value) == (st.insert_batch(okeys) if phase else st.remove_batch(okeys))
+                so, sn = st.export_csr()
+                go, gn = G.export_csr()
+                ok &= bool(np.array_equal(go, so) and np.array_equal(gn, sn))
+                del go, gn
+                opar, _ = O.bfs(so, sn, SRC)
+                ok &= bool(np.array_equal(byo.BFS(G, SRC, policy=policy), opar))
+                ok &= bool(np.array_equal(byo.SimpleUnionAsync(G), O.cc(so, sn)))
+                del so, sn
+                checks += 1
+                if not ok:
+                    failures.append("%s %s round %d" % ("insert" if phase else "remove", tag, r))
+                t_verify += time.perf_counter() - tv
+        ti, tr = float(np.mean(ins_ms)), float(np.mean(rem_ms))
+        out["insert_edges_per_s_" + tag] = 2 * b / (ti / 1e3)
+        out["remove_edges_per_s_" + tag] = 2 * b / (tr / 1e3)
+        out["insert_ms_" + tag] = ti
+        out["remove_ms_" + tag] = tr
+        out["insert_hbm_gbs_" + tag] = upd_bytes[0] / (sum(ins_ms) / 1e3) / 1e9
+        out["remove_hbm_gbs_" + tag] = upd_bytes[1] / (sum(rem_ms) / 1e3) / 1e9
+    out["verified_batches"] = checks
+    out["verify_failures"] = failures
+    out["verified"] = not failures
+    out["how"] = ("%d rounds (+1 untimed) per size, a fresh seeded batch of uniform pairs each round, symmetrised, "
+                  "insert then remove; edges/s = directed keys (2 x pairs) / device time of the call (sort + merge + "
+                  "view upkeep, as the reference times insert_batch, run_unweighted.h:832-835); every batch, timed "
+                  "and untimed, verified against the oracle outside the timing: contents, changed count, BFS(%d) "
+                  "parents, CC labels (%.1f s of checking); hbm_gbs = (16 B per key + 8 B per entry of every "
+                  "touched leaf) / time" % (SWEEP_ROUNDS, SRC, t_verify))
+    return out
+
+
 # ------------------------------------------------------------------ our arm
 def run_ours(args, rank, world, local_rank):
     import torch
@@ -228,6 +369,15 @@ def run_ours(args, rank, world, local_rank):
     label = torch.empty(n, dtype=torch.int32, device=dev)
     pr = torch.empty(n, dtype=torch.float64, device=dev)
     ctx.synchronize()
+    # parity of this exact workload against the oracle, before any timing
+    parity, ostore, O = None, None, None
+    if rank == 0 and not args.no_parity:
+        t0 = time.time()
+        O, off0, nb0, okeys = cpu_setup(dynamic)
+        parity, ostore = parity_selfcheck(byo, L, _abi, ctx, G, keys, B, policy, dynamic, O, off0, nb0, okeys)
+        del off0, nb0, okeys
+        parity["seconds"] = round(time.time() - t0, 1)
+        log("parity vs oracle: %s" % json.dumps(parity))
     ch = ctypes.c_uint64(0)
     rounds = ctypes.c_uint32(0)
     it = ctypes.c_uint32(0)
@@ -285,6 +435,13 @@ def run_ours(args, rank, world, local_rank):
     reached_mask = (parent.cpu() != -1)
     reached = int(reached_mask.sum())
     bfs_edges = int(deg_t[reached_mask].sum())
+    upd_stats = {}
+    if dynamic:  # leaves the merge touches (the state repeats every step)
+        _abi.check(L.byo_graph_insert_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+        upd_stats["insert"] = G.last_update_stats()
+        _abi.check(L.byo_graph_remove_batch_device(G.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+        upd_stats["remove"] = G.last_update_stats()
+        ctx.synchronize()
     pr_iters = it.value or PR_ITERS
     units = {"bfs": bfs_edges / 2, "cc": m_trav / 2, "pr": m_trav * pr_iters,
              "insert": B if dynamic else 0, "remove": B if dynamic else 0}
@@ -363,6 +520,26 @@ def run_ours(args, rank, world, local_rank):
         components.update({"insert_edges_per_s": B / (comp[0] / 1e3), "remove_edges_per_s": B / (comp[4] / 1e3),
                            "insert_ms": comp[0], "remove_ms": comp[4]})
 
+    # a roofline fraction per component, from each phase's device time
+    # (CUDA events around the call) and its algorithmic bytes
+    def frac(byts, ms):
+        gbs = byts / (ms / 1e3) / 1e9
+        return {"achieved_gbs": gbs, "frac": gbs / peak, "algorithmic_bytes": byts, "ms": ms}
+    per = {"bfs": frac(bfs_bytes(n, bfs_edges, reached), comp[1]),
+           "cc": frac(cc_bytes(n, m_trav), comp[2]),
+           "pr": frac(pr_iteration_bytes(n, m_trav, nslots) * pr_iters, comp[3])}
+    if dynamic:
+        per["insert"] = frac(update_bytes(B, upd_stats["insert"]["touched_entries"]), comp[0])
+        per["remove"] = frac(update_bytes(B, upd_stats["remove"]["touched_entries"]), comp[4])
+        per["insert"]["touched_leaves"] = upd_stats["insert"]["touched_leaves"]
+        per["insert"]["touched_entries"] = upd_stats["insert"]["touched_entries"]
+        per["remove"]["touched_leaves"] = upd_stats["remove"]["touched_leaves"]
+        per["remove"]["touched_entries"] = upd_stats["remove"]["touched_entries"]
+    roof["per_component"] = per
+    roof["per_component_bytes"] = ("bfs 4*sum(deg of reached) + 8(n+1) + 8*reached + 4n (includes the PMA snapshot "
+                                   "rebuild in its time); cc one pass 4m + 8(n+1) + 8n; pr per iteration 4m + 4m + "
+                                   "8(n+1) + 16n; insert/remove 16 B per key + 8 B per entry of every touched leaf")
+
     # the learned policy against the m/20 rule (and in-place merge) on the
     # same state, same GPU: BFS and the update pair, median of 5
     if have_net:
@@ -371,17 +548,20 @@ def run_ours(args, rank, world, local_rank):
     # end to end through the public host API
     e2e = run_e2e(args, byo, G, ctx, torch, dynamic, keys, B, n, policy, total_units, world, dev)
 
+    # BASELINE's batch-size sweep with verification after every batch
+    if dynamic and ostore is not None and not args.no_sweep:
+        t0 = time.time()
+        components["batch_sweep"] = batch_sweep(byo, L, _abi, ctx, G, torch, stream, dev, n, policy, O, ostore)
+        log("batch sweep: %.1f s" % (time.time() - t0))
+
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 ids / fp32-kahan pagerank (fp64 residual)",
         "data": "synthetic (seeded RMAT, no dataset)",
-        "config": {"workload": "dynamic %s: RMAT 2^22, 2^26 draws, batch 1e7 pairs" % container.upper() if dynamic
-                   else "static CSR: RMAT 2^22, 2^26 draws",
-                   "n": n, "m": m_trav, "batch_pairs": BATCH if dynamic else 0, "bfs_src": SRC,
-                   "pr_eps": PR_EPS, "pr_max_iters": PR_ITERS, "policy": args.policy,
-                   "parallelism": "replicas x%d" % world,
-                   "l2": "inputs larger than L2 (graph %.0f MB > 126 MB)" % ((8 * n + 4 * nslots) / 1e6)},
+        "config": dynamic_config(dynamic, container, n, m_trav),
+        "policy": args.policy, "parallelism": "replicas x%d" % world,
+        "parity": parity,
         "components": components, "roofline": roof, "e2e": e2e, "gpu_launches": launches,
         "clocks": clk,
     }
@@ -1378,7 +1558,17 @@ def mixed_cpu_sample(steps=None):
 
 
 # ------------------------------------------------------------------ CPU (oracle) legs
+_CPU_SETUP = {}
+
+
 def cpu_setup(dynamic):
+    if dynamic in _CPU_SETUP:
+        return _CPU_SETUP[dynamic]
+    _CPU_SETUP[dynamic] = _cpu_setup(dynamic)
+    return _CPU_SETUP[dynamic]
+
+
+def _cpu_setup(dynamic):
     from oracle import oracle as O
     O.build()
     s, d = O.rmat_edges(SEED, LG_N, DRAWS)
@@ -1392,10 +1582,16 @@ def cpu_setup(dynamic):
 
 
 def cpu_step(O, off, nb, keys, store):
-    """One step of the workload on the CPU restatement; returns (units, ms per phase)."""
+    """One step of the workload on the CPU restatement; returns (units, ms per
+    phase, edges after the insert).  Phases: insert into the sorted-set store,
+    export of its contents as the CSR the traversals read (the counterpart of
+    the GPU container's compact snapshot, which the GPU arm rebuilds inside
+    its BFS phase), BFS, CC, PageRank, remove."""
     t = [time.perf_counter()]
     if keys is not None:
         store.insert_batch(keys)
+    t.append(time.perf_counter())
+    if keys is not None:
         off, nb = store.export_csr()
     t.append(time.perf_counter())
     par, _ = O.bfs(off, nb, SRC)
@@ -1411,7 +1607,10 @@ def cpu_step(O, off, nb, keys, store):
     deg = np.diff(off.astype(np.int64))
     reached = par != O.NONE
     units = deg[reached].sum() / 2 + m / 2 + m * iters + (2 * len(keys) if keys is not None else 0)
-    return float(units), np.diff(t) * 1e3
+    return float(units), np.diff(t) * 1e3, m
+
+
+CPU_PHASES = ["insert", "export", "bfs", "cc", "pr", "remove"]
 
 
 def run_reference(args, dynamic):
@@ -1421,19 +1620,24 @@ def run_reference(args, dynamic):
     for _ in range(args.warmup):
         cpu_step(O, off, nb, keys, store)
     tot_units, tot_s = 0.0, 0.0
+    ph_tot = np.zeros(len(CPU_PHASES))
+    m_trav = len(nb)
     for _ in range(args.steps):
-        u, ph = cpu_step(O, off, nb, keys, store)
+        u, ph, m_trav = cpu_step(O, off, nb, keys, store)
         tot_units += u
         tot_s += ph.sum() / 1e3
+        ph_tot += ph
     value = tot_units / tot_s / 1e9
-    sample = "full steps of the workload on the oracle port (OpenMP), %d threads" % threads
+    sample = ("full steps of the workload on the oracle port (OpenMP), %d threads; each step's time includes "
+              "the export of the store's contents as a CSR for the traversals (phase 'export', the counterpart "
+              "of the GPU container's snapshot, which the GPU arm rebuilds inside its BFS phase)" % threads)
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps, "higher_is_better": True,
             "impl": "reference",
-            "config": {"workload": "dynamic PMA: RMAT 2^22, 2^26 draws, batch 1e7 pairs" if dynamic
-                       else "static CSR: RMAT 2^22, 2^26 draws"},
+            "config": dynamic_config(dynamic, "pma", 1 << LG_N, m_trav),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample,
+                             "phase_ms": {k: float(v) / args.steps for k, v in zip(CPU_PHASES, ph_tot)}},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "data": "synthetic (seeded RMAT, no dataset)"}
 
@@ -1441,12 +1645,12 @@ def run_reference(args, dynamic):
 def cpu_baseline_sample(dynamic):
     O, off, nb, keys = cpu_setup(dynamic)
     store = O.Store(off, nb) if dynamic else None
-    u, ph = cpu_step(O, off, nb, keys, store)
+    u, ph, _ = cpu_step(O, off, nb, keys, store)
     secs = ph.sum() / 1e3
     return {"value": u / secs / 1e9, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
-            "sample": "one full step of the same workload on the oracle port (OpenMP, %d threads), %.1f s"
-                      % (O.num_threads(), secs),
-            "phase_ms": {k: float(v) for k, v in zip(["insert", "bfs", "cc", "pr", "remove"], ph)}}
+            "sample": "one full step of the same workload on the oracle port (OpenMP, %d threads), %.1f s, "
+                      "including the export of the store as a CSR for the traversals" % (O.num_threads(), secs),
+            "phase_ms": {k: float(v) for k, v in zip(CPU_PHASES, ph)}}
 
 
 # ------------------------------------------------------------------ main
@@ -1466,6 +1670,8 @@ def main():
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
                     help="auto: the committed learned network if present, else m20")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="dynamic/static: skip the oracle check before timing")
+    ap.add_argument("--no-sweep", action="store_true", help="dynamic: skip the 1e3/1e5/1e7 batch-size sweep")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps")

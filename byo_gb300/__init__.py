@@ -8,8 +8,8 @@ by byo_gb300.build); this package is the Python view of that ABI.
 """
 from . import _abi  # noqa: F401
 from ._abi import ByoError  # noqa: F401
-from .graph import (BFS, BFS_F, BFS_multi, Context, Graph, PageRank, PageRank_edgeMap, PageRankDelta,  # noqa: F401
-                    SimpleUnionAsync, Test_Map, Test_Map_Remote, Triangle_degree_ordering, UINT_E_MAX, bfs_cc,
-                    edgeMap, vertexSubset)
+from .graph import (BFS, BFS_ComponentLabel_F, BFS_F, BFS_multi, Context, Graph, PR_Delta_F, PR_F,  # noqa: F401
+                    PageRank, PageRank_edgeMap, PageRankDelta, SimpleUnionAsync, Test_Map, Test_Map_Remote,
+                    Triangle_degree_ordering, UINT_E_MAX, bfs_cc, edgeMap, vertexFilter, vertexMap, vertexSubset)
 
 __version__ = "0.1.0"

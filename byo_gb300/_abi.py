@@ -77,6 +77,22 @@ class RoundLog(ctypes.Structure):
                 ("unvisited", _u64), ("ms", ctypes.c_float), ("features", ctypes.c_float * 16)]
 
 
+F_BFS, F_BFS_LABEL, F_PR, F_PR_DELTA = 0, 1, 2, 3
+VOP_PR_UPDATE, VOP_ZERO, VOP_PR_DELTA_FIRST, VOP_PR_DELTA = 0, 1, 2, 3
+
+
+class VertexOp(ctypes.Structure):
+    _fields_ = [("kind", _int), ("d_a", _vp), ("d_b", _vp), ("d_c", _vp), ("damping", _dbl), ("eps2", _dbl)]
+
+
+class UpdateStats(ctypes.Structure):
+    _fields_ = [("keys", _u64), ("changed", _u64), ("touched_leaves", _u64), ("touched_entries", _u64),
+                ("leaf_slots", _u64), ("path", _u32), ("reserved", _u32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "byo_version": (ctypes.c_char_p, []),
@@ -87,6 +103,7 @@ SIGNATURES = {
     "byo_ctx_launches": (_u64, [_vp]),
     "byo_ctx_synchronize": (_int, [_vp]),
     "byo_ctx_set_round_timing": (_int, [_vp, _int]),
+    "byo_ctx_set_barrier_test": (_int, [_vp, _u32, _u32]),
     "byo_ctx_kernel_timing": (_int, [_vp, ctypes.c_char_p]),
     "byo_ctx_kernel_time": (_int, [_vp, ctypes.c_char_p, _P(_u64), _P(_dbl)]),
     "byo_graph_create_csr": (_int, [_vp, _u64, _u64, _vp, _vp, _P(_vp)]),
@@ -104,6 +121,7 @@ SIGNATURES = {
     "byo_graph_remove_batch": (_int, [_vp, _vp, _u64, _int, _P(_u64)]),
     "byo_graph_insert_batch_device": (_int, [_vp, _vp, _u64, _int, _P(_u64)]),
     "byo_graph_remove_batch_device": (_int, [_vp, _vp, _u64, _int, _P(_u64)]),
+    "byo_graph_last_update_stats": (_int, [_vp, _P(UpdateStats)]),
     "byo_gen_rmat_pairs_device": (_int, [_vp, _u64, _u32, _dbl, _dbl, _dbl, _u64, _u64, _vp, _vp]),
     "byo_gen_uniform_pairs_device": (_int, [_vp, _u64, _u64, _u64, _u64, _vp, _vp]),
     "byo_gen_uniform_keys_device": (_int, [_vp, _u64, _u64, _u64, _vp]),
@@ -139,6 +157,14 @@ SIGNATURES = {
     "byo_functor_bfs_create": (_int, [_vp, _u32, _P(_vp)]),
     "byo_functor_bfs_parents": (_int, [_vp, _vp]),
     "byo_functor_destroy": (None, [_vp]),
+    "byo_functor_bfs_label_create": (_int, [_vp, _u32, _vp, _P(_vp)]),
+    "byo_functor_pr_create": (_int, [_vp, _vp, _vp, _P(_vp)]),
+    "byo_functor_pr_delta_create": (_int, [_vp, _vp, _vp, _P(_vp)]),
+    "byo_functor_kind": (_int, [_vp]),
+    "byo_vs_create_bitmap": (_int, [_vp, _vp, _P(_vp)]),
+    "byo_vs_create_all": (_int, [_vp, _P(_vp)]),
+    "byo_vertex_map": (_int, [_vp, _P(VertexOp)]),
+    "byo_vertex_filter": (_int, [_vp, _P(VertexOp), _P(_vp)]),
     "byo_vs_create_single": (_int, [_vp, _u32, _P(_vp)]),
     "byo_vs_create_list": (_int, [_vp, _vp, _u64, _P(_vp)]),
     "byo_vs_destroy": (None, [_vp]),

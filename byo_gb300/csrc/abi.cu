@@ -36,8 +36,10 @@ int copy_to_host(byo_ctx *ctx, void *h, const void *d, size_t bytes) {
 
 struct byo_functor {
   byo_graph *g = nullptr;
-  TravState st;
+  int kind = BYO_F_BFS;
+  TravState st;  // BFS_F
   DevBuf lp, visited;
+  FunctorArgs fa;  // the other kinds
 };
 
 struct byo_vertex_subset {
@@ -268,6 +270,7 @@ static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int
   if (changed) *changed = 0;
   if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS)
     return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA or VOS container");
+  g->upd = UpdateStats{};
   if (count == 0) return BYO_OK;
   if (!keys) return set_error(ctx, BYO_EINVAL, "null keys");
   const uint64_t *d = keys;
@@ -330,6 +333,18 @@ int byo_graph_update_stream(byo_graph *g, const uint64_t *h_keys, const uint64_t
 int byo_graph_update_stream_device(byo_graph *g, const uint64_t *d_keys, const uint64_t *offsets, const uint8_t *ops,
                                    uint64_t nbatch, uint64_t *changed) {
   return update_stream_common(g, d_keys, 0, offsets, ops, nbatch, changed);
+}
+
+int byo_graph_last_update_stats(const byo_graph *g, byo_update_stats *out) {
+  if (!g || !out) return BYO_EINVAL;
+  *out = byo_update_stats{};
+  out->keys = g->upd.keys;
+  out->changed = g->upd.changed;
+  out->touched_leaves = g->upd.leaves;
+  out->touched_entries = g->upd.entries;
+  out->leaf_slots = g->container == BYO_CONTAINER_PMA ? pma_leaf_slots() : 0;
+  out->path = g->upd.path;
+  return BYO_OK;
 }
 
 int byo_graph_insert_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
@@ -465,7 +480,12 @@ int byo_pagerank_device(byo_graph *g, double eps, uint32_t max_iters, int precis
 
 int byo_pagerank_edgemap(byo_graph *g, double eps, uint32_t max_iters, double *h_p, uint32_t *iters,
                          double *l1) {
-  return byo_pagerank(g, eps, max_iters, BYO_PR_FP64, h_p, iters, l1);
+  if (!g || !h_p) return BYO_EINVAL;
+  if (g->n == 0) return BYO_OK;
+  double *d = nullptr;
+  BYO_TRY(host_out_buffer(g, g->n, &d));
+  BYO_TRY(pagerank_edgemap_run(g, eps, max_iters, d, iters, l1));
+  return copy_to_host(g->ctx, h_p, d, g->n * 8);
 }
 
 int byo_pagerank_delta_device(byo_graph *g, double eps, double local_eps, uint32_t max_iters, double *d_p,
@@ -562,6 +582,49 @@ int byo_functor_bfs_parents(byo_functor *f, uint32_t *h_parents) {
   return copy_to_host(g->ctx, h_parents, d, g->n * 4);
 }
 
+static int functor_new(byo_graph *g, const FunctorArgs &fa, byo_functor **out) {
+  byo_functor *f = new (std::nothrow) byo_functor();
+  if (!f) return set_error(g->ctx, BYO_ENOMEM, "functor");
+  f->g = g;
+  f->kind = fa.kind;
+  f->fa = fa;
+  *out = f;
+  return BYO_OK;
+}
+
+int byo_functor_bfs_label_create(byo_graph *g, uint32_t src, uint32_t *d_parents, byo_functor **out) {
+  if (!g || !out || !d_parents) return BYO_EINVAL;
+  *out = nullptr;
+  if (src >= g->n) return set_error(g->ctx, BYO_EINVAL, "src >= n");
+  FunctorArgs fa;
+  fa.kind = BYO_F_BFS_LABEL;
+  fa.parents = d_parents;
+  fa.src = src;
+  return functor_new(g, fa, out);
+}
+
+int byo_functor_pr_create(byo_graph *g, const double *d_p_curr, double *d_p_next, byo_functor **out) {
+  if (!g || !out || !d_p_curr || !d_p_next) return BYO_EINVAL;
+  *out = nullptr;
+  FunctorArgs fa;
+  fa.kind = BYO_F_PR;
+  fa.p_curr = d_p_curr;
+  fa.p_next = d_p_next;
+  return functor_new(g, fa, out);
+}
+
+int byo_functor_pr_delta_create(byo_graph *g, const double *d_delta, double *d_ngh_sum, byo_functor **out) {
+  if (!g || !out || !d_delta || !d_ngh_sum) return BYO_EINVAL;
+  *out = nullptr;
+  FunctorArgs fa;
+  fa.kind = BYO_F_PR_DELTA;
+  fa.delta = d_delta;
+  fa.ngh = d_ngh_sum;
+  return functor_new(g, fa, out);
+}
+
+int byo_functor_kind(const byo_functor *f) { return f ? f->kind : BYO_EINVAL; }
+
 void byo_functor_destroy(byo_functor *f) {
   if (!f) return;
   if (f->g && f->g->ctx) cudaStreamSynchronize(f->g->ctx->stream);
@@ -640,6 +703,22 @@ int byo_vs_create_single(byo_graph *g, uint32_t v, byo_vertex_subset **out) {
   return byo_vs_create_list(g, &v, 1, out);
 }
 
+int byo_vs_create_bitmap(byo_graph *g, const uint32_t *d_bits, byo_vertex_subset **out) {
+  if (!g || !out) return BYO_EINVAL;
+  *out = nullptr;
+  byo_vertex_subset *vs = nullptr;
+  BYO_TRY(vs_alloc(g, &vs));
+  int rc = frontier_from_bits(g, d_bits, vs->f);
+  if (rc != BYO_OK) {
+    byo_vs_destroy(vs);
+    return rc;
+  }
+  *out = vs;
+  return BYO_OK;
+}
+
+int byo_vs_create_all(byo_graph *g, byo_vertex_subset **out) { return byo_vs_create_bitmap(g, nullptr, out); }
+
 void byo_vs_destroy(byo_vertex_subset *vs) {
   if (!vs) return;
   if (vs->g && vs->g->ctx) cudaStreamSynchronize(vs->g->ctx->stream);
@@ -696,8 +775,12 @@ int byo_edge_map(byo_graph *g, byo_vertex_subset *vs, byo_functor *f, int64_t th
     }
   }
   if (rc == BYO_OK && !empty) {
-    EngineTuning tune = default_tuning(g);
-    rc = edge_map_round(g, f->st, vs->f, o->f, mode, tune);
+    if (f->kind == BYO_F_BFS) {
+      EngineTuning tune = default_tuning(g);
+      rc = edge_map_round(g, f->st, vs->f, o->f, mode, tune);
+    } else {
+      rc = generic_edge_map(g, f->fa, vs->f, o->f, mode, !(flags & BYO_FL_NO_OUTPUT));
+    }
   } else if (rc == BYO_OK) {
     o->f.size = 0;
     o->f.has_list = o->f.has_bits = true;
@@ -710,6 +793,49 @@ int byo_edge_map(byo_graph *g, byo_vertex_subset *vs, byo_functor *f, int64_t th
   if (flags & BYO_FL_NO_OUTPUT) {
     o->f.size = 0;
     o->f.outdeg = 0;
+  }
+  *out = o;
+  return BYO_OK;
+}
+
+static int vop_args(byo_vertex_subset *vs, const byo_vertex_op *op, VertexOpArgs *a) {
+  byo_ctx *ctx = vs->g->ctx;
+  switch (op->kind) {
+    case BYO_VOP_PR_UPDATE:
+    case BYO_VOP_ZERO:
+      if (!op->d_a) return set_error(ctx, BYO_EINVAL, "vertex op: d_a is null");
+      break;
+    case BYO_VOP_PR_DELTA_FIRST:
+    case BYO_VOP_PR_DELTA:
+      if (!op->d_a || !op->d_b || !op->d_c) return set_error(ctx, BYO_EINVAL, "vertex op: null array");
+      break;
+    default:
+      return set_error(ctx, BYO_EINVAL, "vertex op: unknown kind");
+  }
+  *a = VertexOpArgs{op->kind, op->d_a, op->d_b, op->d_c, op->damping, op->eps2};
+  return BYO_OK;
+}
+
+int byo_vertex_map(byo_vertex_subset *vs, const byo_vertex_op *op) {
+  if (!vs || !op) return BYO_EINVAL;
+  VertexOpArgs a;
+  BYO_TRY(vop_args(vs, op, &a));
+  return vertex_op_run(vs->g, a, vs->f, nullptr);
+}
+
+int byo_vertex_filter(byo_vertex_subset *vs, const byo_vertex_op *op, byo_vertex_subset **out) {
+  if (!vs || !op || !out) return BYO_EINVAL;
+  *out = nullptr;
+  byo_graph *g = vs->g;
+  VertexOpArgs a;
+  BYO_TRY(vop_args(vs, op, &a));
+  byo_vertex_subset *o = nullptr;
+  BYO_TRY(vs_alloc(g, &o));
+  int rc = memset_async(g->ctx, o->f.bits, 0, (g->n + 31) / 32 * 4);
+  if (rc == BYO_OK) rc = vertex_op_run(g, a, vs->f, &o->f);
+  if (rc != BYO_OK) {
+    byo_vs_destroy(o);
+    return rc;
   }
   *out = o;
   return BYO_OK;
@@ -796,6 +922,15 @@ int byo_update_sample(byo_graph *g, const uint64_t *h_keys, uint64_t count, floa
 }
 
 int byo_ctx_last_update_strategy(const byo_ctx *ctx) { return ctx ? ctx->last_update_strategy : BYO_EINVAL; }
+
+int byo_ctx_set_barrier_test(byo_ctx *ctx, uint32_t limit_ms, uint32_t extra_blocks) {
+  if (!ctx) return BYO_EINVAL;
+  if (limit_ms > 4000 || extra_blocks > 1)
+    return set_error(ctx, BYO_EINVAL, "barrier test: limit_ms <= 4000 and extra_blocks <= 1");
+  ctx->bar_limit_ms = limit_ms;
+  ctx->bar_extra = extra_blocks;
+  return BYO_OK;
+}
 
 int byo_ctx_set_round_timing(byo_ctx *ctx, int on) {
   if (!ctx) return BYO_EINVAL;

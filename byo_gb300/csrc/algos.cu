@@ -9,7 +9,7 @@
 // then link the remaining edges of vertices outside that component only.  The
 // final labels do not depend on the order of links.
 //
-// PageRank (PageRank.h:125-193): Jacobi pull with lane groups per vertex,
+// PageRank (PageRank.h:125-193): Jacobi pull over warp-sized work units,
 // FP32 state with compensated (TwoSum) per-vertex sums, FP64 L1 residual.
 // Bytes per iteration: 4 B per slot (ids) + 4 B per slot (p_div gather) +
 // 16 B offsets/degrees + 12 B state per vertex.
@@ -366,9 +366,9 @@ __device__ __forceinline__ T group_total(T s, T c) {
 //   heavy chunk  kPrTile consecutive slots of one heavier vertex; its
 //                compensated partial goes to part[chunk] and k_pr_combine sums
 //                a vertex's chunks in order
-// A unit's p_div values are gathered into shared memory with 4/8-byte
-// cp.async copies (no registers held per gather), double-buffered so the next
-// unit's gathers are in flight while this one is reduced.
+// A warp gathers a unit's p_div values with plain loads, 16 independent
+// loads per lane in flight, into its own stage in shared memory, then reduces
+// from the stage (k_pr_units).
 constexpr int kPrTile = 512;            // slots per warp tile / heavy chunk
 constexpr uint32_t kPrLightMax = 128;   // longest run of a light vertex
 constexpr int kPrBlock = 256;
@@ -420,49 +420,6 @@ struct InChunks {
     return (off[v + 1] - off[v] + kPrTile - 1) / kPrTile;
   }
 };
-
-template <typename T>
-__device__ __forceinline__ void cp_async_gather(T *dst_smem, const T *src) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(dst_smem);
-  if constexpr (sizeof(T) == 4)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src));
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-// ---- TMA bulk copy of a unit's slot ids into shared memory (mbarrier
-// completion); waits are bounded and report through *err.
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)));
-  asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
-}
-__device__ __forceinline__ void tma_ids(uint32_t *dst, const uint32_t *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile("fence.proxy.async.shared::cta;\n" ::);
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes));
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-// true when the phase completed within the spin budget
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
-  const unsigned a = smem_u32(bar);
-  for (uint32_t it = 0; it < (1u << 24); it++) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(phase)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
 
 // Unit descriptor (built once per PageRank call): slot range and either a
 // light tile's vertices [v0, v1) or a heavy chunk (v1 == kNoVertex).

@@ -148,6 +148,8 @@ int bfs_small_rounds(byo_graph *g, TravState &st, Frontier *&cur, Frontier *&nxt
   std::memset(h, 0, sizeof(SmallCtl));
   h->cnt[0] = cur->size;
   h->outdeg[0] = cur->outdeg;
+  h->bar.limit_ms = ctx->bar_limit_ms;
+  h->bar.extra = ctx->bar_extra;
   BYO_CU(ctx, cudaMemcpyAsync(c, h, sizeof(SmallCtl), cudaMemcpyHostToDevice, ctx->stream));
   SmallArgs a;
   a.off = g->d_off;

@@ -85,6 +85,32 @@ EngineTuning default_tuning(const byo_graph *g);
 int bfs_small_rounds(byo_graph *g, TravState &st, Frontier *&cur, Frontier *&nxt, uint64_t limit, bool gate_hub,
                      RoundStats *d_st, uint32_t *rounds_run);
 
+// ---- the edgeMap functors other than BFS_F, vertexMap / vertexFilter (edgemap.cu)
+struct FunctorArgs {
+  int kind = 0;                   // BYO_F_BFS_LABEL, BYO_F_PR, BYO_F_PR_DELTA
+  uint32_t *parents = nullptr;    // BFS_LABEL: Parents
+  uint32_t src = 0;               // BFS_LABEL: the label written
+  const double *p_curr = nullptr; // PR
+  double *p_next = nullptr;
+  const double *delta = nullptr;  // PR_DELTA: [2n] delta, delta / degree
+  double *ngh = nullptr;          // PR_DELTA: nghSum
+};
+struct VertexOpArgs {
+  int kind;           // BYO_VOP_*
+  double *a, *b, *c;  // per kind (include/byo_gpu.h)
+  double damping, eps2;
+};
+// One edgeMap round of a generic functor: reads `in`, writes `out` (out.bits
+// all zero, list capacity n) unless !output.
+int generic_edge_map(byo_graph *g, const FunctorArgs &f, Frontier &in, Frontier &out, int mode, bool output);
+// vertexMap (out == nullptr) or vertexFilter (out: bits all zero) over `in`.
+int vertex_op_run(byo_graph *g, const VertexOpArgs &op, Frontier &in, Frontier *out);
+// Builds f.list (and size, outdeg) from f.bits when only the bitmap is held.
+int ensure_list(byo_graph *g, Frontier &f);
+// f.bits = d_bits (every vertex when null), then its list, size and outdeg.
+int frontier_from_bits(byo_graph *g, const uint32_t *d_bits, Frontier &f);
+int pagerank_edgemap_run(byo_graph *g, double eps, uint32_t max_iters, double *d_p, uint32_t *iters, double *l1);
+
 // Arguments of the policy epilogue fused into a round's last kernel
 // (policy.cuh); on == 0 disables it.
 struct PolicyTail {

@@ -56,6 +56,17 @@ struct byo_ctx {
   size_t kev_used = 0;
   int update_policy = BYO_UPDATE_MERGE;  // container update strategy
   int last_update_strategy = 0;          // 0 merge, 1 rebuild (last batch)
+  // grid-barrier test hook (byo_ctx_set_barrier_test): limit in ms (0 = the
+  // default) and arrivals awaited beyond the launched blocks
+  uint32_t bar_limit_ms = 0, bar_extra = 0;
+};
+
+// What the last batch update did (PMA): batch keys, keys changed, leaves the
+// merge rewrote and the keys they held before it; path 0 merge, 1 rebuild,
+// 2 merge then window redistribution.
+struct UpdateStats {
+  uint64_t keys = 0, changed = 0, leaves = 0, entries = 0;
+  uint32_t path = 0;
 };
 
 struct byo_graph {
@@ -76,6 +87,7 @@ struct byo_graph {
   byo_graph *snap = nullptr;
   uint64_t snap_version = 0;
   uint64_t slots_cap = 0;  // snapshot: capacity of d_slots
+  UpdateStats upd;         // the last batch update (PMA)
 };
 
 namespace byo {
@@ -253,6 +265,7 @@ int vos_compact(byo_graph *g, const uint64_t *offc, uint32_t *out);
 void vos_destroy(Vos *v);
 int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_boff, const uint64_t *h_boff,
                       const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed);
+uint64_t pma_leaf_slots();
 int pma_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert,
                uint64_t *changed);
 int pma_export_keys(byo_graph *g, uint64_t *d_keys_out);

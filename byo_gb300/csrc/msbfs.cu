@@ -585,6 +585,11 @@ int bfs_multi_run(byo_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_
   BYO_TRY(ws(g, WS_MS_LEVELS, (size_t)kLevelBits * n, &a.planes));
   BYO_CU(ctx, cudaMemcpyAsync(misc, h_srcs, k * 4, cudaMemcpyHostToDevice, ctx->stream));
   BYO_CU(ctx, cudaMemsetAsync(a.ctl, 0, sizeof(MsCtl), ctx->stream));
+  if (ctx->bar_limit_ms || ctx->bar_extra) {  // the barrier test hook
+    const unsigned int hb[2] = {ctx->bar_limit_ms, ctx->bar_extra};
+    BYO_CU(ctx, cudaMemcpyAsync(&a.ctl->bar.limit_ms, hb, sizeof(hb), cudaMemcpyHostToDevice, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));  // hb is on the stack
+  }
   // co-resident grid for the cooperative launch
   int per_sm = 0;
   BYO_CU(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ms_bfs, kMsBlock, 0));

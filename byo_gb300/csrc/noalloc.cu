@@ -2,21 +2,27 @@
 //
 // Some callers cannot let a library allocate device memory: hosts whose memory
 // manager reserves the whole GPU up front and hands out sub-ranges itself (a
-// database buffer pool, a JVM or Go runtime that owns one big device arena),
-// and code that issues work while a CUDA stream is being captured, where
-// cudaMalloc is not permitted.  For them byo_bfs_csr_noalloc runs the same
-// direction-optimising BFS as byo_bfs (same parents and levels) with every
-// piece of traversal state in one file-scope device array, g_bfs_scratch, of
-// fixed size: room for BYO_NOALLOC_MAX_VERTICES (2^20) vertices at 16.4 bytes
-// per vertex (16.4 MiB).  Every GPU that loads this library keeps that
-// array until the process exits.
+// database buffer pool, a JVM or Go runtime that owns one big device arena).
+// A cudaMalloc from inside the library would either fail (the arena already
+// holds the memory) or take memory the host's manager does not know about.
+// For them byo_bfs_csr_noalloc runs the same direction-optimising BFS as
+// byo_bfs (same parents and levels) with every piece of traversal state in one
+// file-scope device array, g_bfs_scratch, of fixed size: room for
+// BYO_NOALLOC_MAX_VERTICES (2^20) vertices at 16.4 bytes per vertex
+// (16.4 MiB).  Every GPU that loads this library keeps that array until the
+// process exits.
+//
+// The call is host-synchronous: after each round it copies the next
+// frontier's size back to pageable host memory and synchronises the caller's
+// stream, and it returns when the result is in the output arrays.
 //
 // The array is shared by every call on a device and keeps what the last call
 // left in it; each call re-initialises what must start at zero.  Calls that
 // overlap on the GPU (two streams, or two host threads) race on it and give
 // wrong results; callers must serialise them.  The first call on a device
 // looks the array's device address up (cudaGetSymbolAddress) with that device
-// current; make that first call before any stream capture begins.
+// current and caches it per (device, CUDA context); a context created after a
+// cudaDeviceReset is a new key, so the address is looked up again there.
 #include <mutex>
 
 #include "../../include/byo_gpu.h"
@@ -185,13 +191,43 @@ __global__ void k_na_extract(const uint64_t *__restrict__ lp, uint64_t n, uint32
 // ---------------------------------------------------------------- set-up
 
 std::mutex g_mu;
-void *g_addr[256];  // device address of g_bfs_scratch, per device ordinal
+// Device address of g_bfs_scratch per device ordinal, valid for the CUDA
+// context current when it was looked up (a reset destroys the context and
+// reloads the module, so the address is looked up again for a new context).
+void *g_addr[256];
+void *g_addr_ctx[256];
+
+typedef int (*CtxGetCurrentFn)(void **);
+
+// The current CUDA context (driver handle), or null when the driver entry
+// point is unavailable (then the cache is keyed on the device alone).
+void *current_context() {
+  static CtxGetCurrentFn fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      f = nullptr;
+    }
+    return reinterpret_cast<CtxGetCurrentFn>(f);
+  }();
+  void *c = nullptr;
+  if (fn && fn(&c) != 0) c = nullptr;
+  return c;
+}
 
 int scratch_for_current_device(void **out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return BYO_EDEVICE;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    cudaGetLastError();
+    return BYO_EDEVICE;
+  }
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  void *cx = current_context();
+  if (!g_addr[dev] || !cx || g_addr_ctx[dev] != cx) {
+    // The runtime makes the device's primary context current here if no
+    // context is current yet; the key is read again afterwards.
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_bfs_scratch);
     if (e != cudaSuccess || !p) {
@@ -199,6 +235,7 @@ int scratch_for_current_device(void **out) {
       return BYO_EDEVICE;
     }
     g_addr[dev] = p;
+    g_addr_ctx[dev] = current_context();
   }
   *out = g_addr[dev];
   return BYO_OK;
@@ -226,6 +263,7 @@ extern "C" int byo_bfs_csr_noalloc(const uint64_t *d_offsets, const uint32_t *d_
   uint64_t consumed = 0;  // size of the frontier whose bits sit in the next bitmap
   uint64_t deg_src[2] = {0, 0};
   k_na_init<<<grid_of(n, 256), 256, 0, st>>>(s.lp, s.visited, s.bits[0], s.bits[1], s.list[0], s.stats, n, src);
+  if (cudaGetLastError() != cudaSuccess) return BYO_EDEVICE;
   if (cudaMemcpyAsync(deg_src, d_offsets + src, 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) {
     cudaGetLastError();
@@ -244,7 +282,10 @@ extern "C" int byo_bfs_csr_noalloc(const uint64_t *d_offsets, const uint32_t *d_
     const int nxt = cur ^ 1;
     // the next bitmap still holds the frontier before `cur`
     if (nr > 0) k_na_clear<<<grid_of(consumed + 1, 256), 256, 0, st>>>(s.list[nxt], consumed, s.bits[nxt]);
-    cudaMemsetAsync(s.stats, 0, 16, st);
+    if (cudaMemsetAsync(s.stats, 0, 16, st) != cudaSuccess) {
+      cudaGetLastError();
+      return BYO_EDEVICE;
+    }
     const uint64_t lvl = (uint64_t)r << 32;
     if (pull) {
       k_na_pull<<<grid_of(W * 32, 256), 256, 0, st>>>(d_offsets, d_nbrs, s.bits[cur], n, s.lp, s.visited,
@@ -255,6 +296,9 @@ extern "C" int byo_bfs_csr_noalloc(const uint64_t *d_offsets, const uint32_t *d_
       k_na_mark<<<grid_of(outdeg + 1, 256), 256, 0, st>>>(s.list[nxt], s.stats, s.visited);
     }
     consumed = fsize;
+    // a launch that failed to start leaves no sticky error: catch it here,
+    // before the round's counts are read back
+    if (cudaGetLastError() != cudaSuccess) return BYO_EDEVICE;
     unsigned long long got[2] = {0, 0};
     if (cudaMemcpyAsync(got, s.stats, 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess) {

@@ -499,7 +499,8 @@ __device__ __forceinline__ long long merge_leaf(uint64_t q, uint32_t *src, uint3
                                                 const uint64_t *__restrict__ keys, const uint64_t *__restrict__ bstart,
                                                 uint64_t *seg, int insert, uint32_t *rcount, uint64_t *ovf,
                                                 uint64_t *ovf_off, unsigned long long *ctr, uint32_t *deg,
-                                                const ViewOut &view, uint64_t *Aw, uint64_t *Bw) {
+                                                const ViewOut &view, uint64_t *Aw, uint64_t *Bw, uint64_t &tleaves,
+                                                uint64_t &tentries) {
   const unsigned lane = lane_id();
   const uint64_t *A = Aw;
   {
@@ -524,6 +525,8 @@ __device__ __forceinline__ long long merge_leaf(uint64_t q, uint32_t *src, uint3
       return 0;
     }
     const uint64_t nb = b1 - b0;
+    tleaves += 1;  // a leaf the merge rewrites, and the keys it held
+    tentries += c;
     const uint64_t *B = nb <= kOptSeg ? Bw : keys + b0;
     const uint64_t base = j * kLeaf;
     // The s leaf keys below the first batch key keep their slots: the merge
@@ -656,11 +659,16 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   long long dsum = 0;
+  uint64_t tleaves = 0, tentries = 0;
   const uint64_t nwork = kList ? *nseg : NL;
   for (uint64_t q = gw; q < nwork; q += nw)
     dsum += merge_leaf<kList>(q, src, dst, cnt, NL, keys, bstart, seg, insert, rcount, ovf, ovf_off, ctr, deg, view,
-                              As[w], Bsh[w]);
+                              As[w], Bsh[w], tleaves, tentries);
   if (lane_id() == 0 && dsum) atomicAdd((unsigned long long *)delta, (unsigned long long)dsum);
+  if (lane_id() == 0 && tleaves) {  // ctr[5], ctr[6]: touched leaves and the keys they held
+    atomicAdd(&ctr[5], (unsigned long long)tleaves);
+    atomicAdd(&ctr[6], (unsigned long long)tentries);
+  }
 }
 
 // Copies the current contents of every leaf in a window (all leaves when
@@ -1304,6 +1312,8 @@ static int pma_finish_windowed(byo_graph *g, bool list, const uint64_t *bstart, 
   return pma_view(g);
 }
 
+uint64_t pma_leaf_slots() { return kLeaf; }
+
 int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sorted, int insert,
                uint64_t *changed) {
   byo_ctx *ctx = g->ctx;
@@ -1389,6 +1399,7 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
     const uint64_t total = h[0];
     if (changed) *changed = insert ? total - m_before : m_before - total;
+    g->upd = UpdateStats{b, insert ? total - m_before : m_before - total, NL, m_before, 1u};
     if (total == m_before) return BYO_OK;
     return pma_rebuild(g, batch, bstart, rpre, total, insert);
   }
@@ -1399,7 +1410,8 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   BYO_TRY(ensure(ctx, p->ovf, (NL * kLeaf + b + 1) * 8));
   BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
   // counters, cleared with the rest of misc: [0] cursor, [1] overflowing
-  // leaves, [2] delta, [3] segments, [4] view chunks
+  // leaves, [2] delta, [3] segments, [4] view chunks, [5] leaves merged,
+  // [6] keys those leaves held before the merge
   unsigned long long *ctr = (unsigned long long *)(flags + 4);
   const double cap = (double)NL * kLeaf;
   const double shrink_below = !insert && NL > 1 ? kRootMin * cap : -1.0;
@@ -1425,7 +1437,7 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
              rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2),
              (uint32_t *)nullptr, ViewOut{});
   }
-  BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 72, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 88, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   if (defer) {
     if (h[0] >= g->n || h[1] >= g->n) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
@@ -1437,6 +1449,8 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   const uint64_t total = (uint64_t)((long long)m_before + delta);
   if (changed) *changed = insert ? total - m_before : m_before - total;
   const bool shrink = (double)total < shrink_below;
+  g->upd = UpdateStats{b, insert ? total - m_before : m_before - total, hc[5], hc[6],
+                       (novf || shrink) ? 2u : 0u};
   if (novf == 0 && !shrink) {
     if (list) {
       // long ranges left by the merge (rare: keys far past a leaf's last key)
@@ -1586,10 +1600,11 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
                          a.chunks + (size_t)cur * a.chunk_words, &c->ctr[cur][4]};
       const uint64_t ns = *(volatile unsigned long long *)&c->ctr[cur][3];
       long long dsum = 0;
+      uint64_t tleaves = 0, tentries = 0;  // not reported by the stream
       for (uint64_t q = gw; q < ns; q += nmw)
         dsum += merge_leaf<true>(q, a.src, a.dst, a.cnt, a.NL, a.sorted + (size_t)cur * kSmallSort, nullptr,
                                  a.seg + (size_t)cur * 2 * kSmallSort, insert, nullptr, a.ovf, a.ovf_off, c->ctr[cur],
-                                 a.deg, view, As + (size_t)w * kLeaf, Bs + (size_t)w * kOptSeg);
+                                 a.deg, view, As + (size_t)w * kLeaf, Bs + (size_t)w * kOptSeg, tleaves, tentries);
       if (lane_id() == 0 && dsum) atomicAdd(&c->ctr[cur][2], (unsigned long long)dsum);
       if (solo) {
         __syncthreads();
@@ -1654,6 +1669,8 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
     BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
     std::memset(hc, 0, sizeof(StreamCtl));
     hc->m = (long long)g->m;
+    hc->bar.limit_ms = ctx->bar_limit_ms;
+    hc->bar.extra = ctx->bar_extra;
     BYO_CU(ctx, cudaMemcpyAsync(c, hc, sizeof(StreamCtl), cudaMemcpyHostToDevice, ctx->stream));
     StreamArgs a;
     a.src = p->src;

@@ -314,6 +314,13 @@ class Graph:
     insert_sorted_batch = insert_batch
     remove_sorted_batch = remove_batch
 
+    def last_update_stats(self):
+        """What the last insert/remove batch did: keys, changed, touched_leaves,
+        touched_entries (keys those leaves held), leaf_slots, path."""
+        st = _abi.UpdateStats()
+        check(lib().byo_graph_last_update_stats(self.h, ctypes.byref(st)), self.ctx.h)
+        return st.as_dict()
+
 
 # ------------------------------------------------------------ vertexSubset / edgeMap
 
@@ -342,6 +349,22 @@ class vertexSubset:
 
     def __del__(self):
         self.close()
+
+    @classmethod
+    def from_bitmap(cls, G, bits):
+        """vertexSubset(n, m, BitArray&&) (vertex_subset.h:263-270): members are
+        the set bits of `bits`, a device array of ceil(n/32) uint32 words
+        (anything with data_ptr(), e.g. a CUDA tensor); None: every vertex."""
+        h = ctypes.c_void_p()
+        if bits is None:
+            check(lib().byo_vs_create_all(G.h, ctypes.byref(h)), G.ctx.h)
+        else:
+            check(lib().byo_vs_create_bitmap(G.h, bits.data_ptr(), ctypes.byref(h)), G.ctx.h)
+        return cls(G, _handle=h)
+
+    @classmethod
+    def all(cls, G):
+        return cls.from_bitmap(G, None)
 
     def size(self):
         return int(lib().byo_vs_size(self.h))
@@ -382,6 +405,70 @@ class BFS_F:
         out = np.empty(self.G.N(), np.uint32)
         check(lib().byo_functor_bfs_parents(self.h, _ptr(out)), self.G.ctx.h)
         return out
+
+
+class _DeviceFunctor:
+    """A device functor over caller arrays (CUDA tensors, kept alive here)."""
+
+    def __init__(self, G, create, *args):
+        self.G = G
+        self._keep = [a for a in args if hasattr(a, "data_ptr")]
+        h = ctypes.c_void_p()
+        conv = [a.data_ptr() if hasattr(a, "data_ptr") else a for a in args]
+        check(create(G.h, *conv, ctypes.byref(h)), G.ctx.h)
+        self.h = h
+        G.ctx._adopt(self)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().byo_functor_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class BFS_ComponentLabel_F(_DeviceFunctor):
+    """BFS_ComponentLabel_F (benchmarks/Connectivity/BFSCC/Connectivity.h:31-50)
+    over a device Parents array of n uint32 (int32 tensor)."""
+
+    def __init__(self, G, parents, src):
+        super().__init__(G, lib().byo_functor_bfs_label_create, int(src), parents)
+
+
+class PR_F(_DeviceFunctor):
+    """PR_F (benchmarks/PageRank/PageRank.h:33-50) over device float64 arrays."""
+
+    def __init__(self, G, p_curr, p_next):
+        super().__init__(G, lib().byo_functor_pr_create, p_curr, p_next)
+
+
+class PR_Delta_F(_DeviceFunctor):
+    """delta::PR_Delta_F (benchmarks/PageRank/PageRank.h:200-226): delta is a
+    device float64 array of n {delta, delta / degree} pairs, ngh_sum n float64."""
+
+    def __init__(self, G, delta, ngh_sum):
+        super().__init__(G, lib().byo_functor_pr_delta_create, delta, ngh_sum)
+
+
+def _vop(kind, a=None, b=None, c=None, damping=0.85, eps2=0.0):
+    ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    return _abi.VertexOp(kind, ptr(a), ptr(b), ptr(c), damping, eps2)
+
+
+def vertexMap(vs, kind, a=None, b=None, c=None, damping=0.85, eps2=0.0):
+    """vertexMap (vertex_subset.h:382-398) with a vertex function of the
+    reference (_abi.VOP_*; arrays as include/byo_gpu.h byo_vertex_op says)."""
+    op = _vop(kind, a, b, c, damping, eps2)
+    check(lib().byo_vertex_map(vs.h, ctypes.byref(op)), vs.G.ctx.h)
+
+
+def vertexFilter(vs, kind, a=None, b=None, c=None, damping=0.85, eps2=0.0):
+    """vertexFilter (vertex_subset.h:441-485): the members the function keeps."""
+    op = _vop(kind, a, b, c, damping, eps2)
+    h = ctypes.c_void_p()
+    check(lib().byo_vertex_filter(vs.h, ctypes.byref(op), ctypes.byref(h)), vs.G.ctx.h)
+    return vertexSubset(vs.G, _handle=h)
 
 
 def edgeMap(G, vs, F, threshold=-1, flags=0):

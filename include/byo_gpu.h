@@ -116,6 +116,25 @@ int byo_graph_insert_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t
 int byo_graph_remove_batch_device(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted,
                                   uint64_t *changed);
 
+/* What the last insert/remove batch on g did, for the update path's byte
+ * accounting (the reference's Batch_insert_runner times the batch,
+ * benchmarks/run_unweighted.h:832-873; it reports no byte counts).  keys: the
+ * batch's keys (duplicates included); changed: keys inserted or removed;
+ * touched_leaves: PMA leaves the merge rewrote; touched_entries: keys those
+ * leaves held before the merge; leaf_slots: slots per PMA leaf (0 for other
+ * containers); path: 0 in-place merge, 1 rebuild, 2 merge then window
+ * redistribution of overflowing leaves (whose extra traffic is not counted). */
+typedef struct byo_update_stats {
+  uint64_t keys;
+  uint64_t changed;
+  uint64_t touched_leaves;
+  uint64_t touched_entries;
+  uint64_t leaf_slots;
+  uint32_t path;
+  uint32_t reserved;
+} byo_update_stats;
+int byo_graph_last_update_stats(const byo_graph *g, byo_update_stats *out);
+
 /* ------------------------------------------------------------------ graph files
  * The reference's input formats (gbbs/graph_io.cc:35-95, read by
  * read_unweighted_symmetric_graph, gbbs/graph_io.h:98-124):
@@ -246,10 +265,10 @@ int byo_pagerank(byo_graph *g, double eps, uint32_t max_iters, int precision, do
 int byo_pagerank_device(byo_graph *g, double eps, uint32_t max_iters, int precision, double *d_p,
                         uint32_t *iters, double *l1);
 
-/* PageRank_edgeMap (benchmarks/PageRank/PageRank.h:80-123): its edgeMap runs
- * with threshold 0 over the all-vertex frontier, which takes edgeMapDense, so
- * it computes PageRank's recurrence; this runs the FP64 pull (precision
- * BYO_PR_FP64 of byo_pagerank) and returns the last iterate. */
+/* PageRank_edgeMap (benchmarks/PageRank/PageRank.h:80-123), its loop through
+ * the edgeMap API: frontier = every vertex; per iteration edgeMap(PR_F,
+ * threshold 0, no_output) (always the dense round), vertexMap(PR_Vertex_F),
+ * the L1 change, reset and swap; FP64.  Returns the last computed iterate. */
 int byo_pagerank_edgemap(byo_graph *g, double eps, uint32_t max_iters, double *h_p, uint32_t *iters,
                          double *l1);
 
@@ -325,12 +344,22 @@ int byo_map_remote(byo_graph *g, const void *h_remote, uint32_t width, uint64_t 
 int byo_map_remote_device(byo_graph *g, const void *d_remote, uint32_t width, uint64_t *sum);
 
 /* ------------------------------------------------------------------ edgeMap API
- * vertexSubset (gbbs/vertex_subset.h:202-371) and edgeMap
- * (gbbs/edge_map_data.h:254-315) over device functors.  The functor set is
- * closed (a device kernel cannot call a host lambda); each mirrors a GBBS
- * functor struct {update, updateAtomic, cond}. */
+ * vertexSubset (gbbs/vertex_subset.h:202-371), edgeMap
+ * (gbbs/edge_map_data.h:254-315), vertexMap and vertexFilter
+ * (gbbs/vertex_subset.h:382-485) over device functors.  A device kernel cannot
+ * call a host lambda, so the functor set is closed; each kind mirrors one GBBS
+ * functor struct {update, updateAtomic, cond} over arrays the caller owns
+ * (d_*: device memory of the graph's context, n entries unless stated). */
 enum byo_functor_kind {
-  BYO_F_BFS = 0 /* BFS_F, BFS.h:30-45, over a parents array owned by the functor */
+  BYO_F_BFS = 0,       /* BFS_F, BFS.h:30-45, over a parents array owned by the functor */
+  BYO_F_BFS_LABEL = 1, /* BFS_ComponentLabel_F, benchmarks/Connectivity/BFSCC/Connectivity.h:31-50:
+                          cond(d) = Parents[d] == BYO_NONE; update writes src into Parents[d]
+                          (returns 1 if it changed); updateAtomic = CAS(BYO_NONE -> src) */
+  BYO_F_PR = 2,        /* PR_F, benchmarks/PageRank/PageRank.h:33-50: p_next[d] += p_curr[s] /
+                          degree(s); cond true; updateAtomic adds atomically */
+  BYO_F_PR_DELTA = 3   /* delta::PR_Delta_F, PageRank.h:200-226: nghSum[d] += delta_over_degree[s],
+                          returns whether nghSum[d] was 0 before; d_delta holds n pairs
+                          {delta, delta / degree} (struct delta_and_degree) */
 };
 /* edgeMap flags, values as gbbs/flags.h:8-19 */
 enum byo_edge_map_flags {
@@ -345,20 +374,65 @@ typedef struct byo_functor byo_functor;
 /* BFS_F over a fresh Parents array (all BYO_NONE but Parents[src] = src). */
 int byo_functor_bfs_create(byo_graph *g, uint32_t src, byo_functor **out);
 int byo_functor_bfs_parents(byo_functor *f, uint32_t *h_parents);
+/* The functors over caller arrays (kept by pointer; they must outlive it). */
+int byo_functor_bfs_label_create(byo_graph *g, uint32_t src, uint32_t *d_parents, byo_functor **out);
+int byo_functor_pr_create(byo_graph *g, const double *d_p_curr, double *d_p_next, byo_functor **out);
+int byo_functor_pr_delta_create(byo_graph *g, const double *d_delta, double *d_ngh_sum, byo_functor **out);
+int byo_functor_kind(const byo_functor *f);
 void byo_functor_destroy(byo_functor *f);
 
 /* vertexSubset(n, v) and vertexSubset(n, list) (vertex_subset.h:240-262). */
 int byo_vs_create_single(byo_graph *g, uint32_t v, byo_vertex_subset **out);
 int byo_vs_create_list(byo_graph *g, const uint32_t *h_ids, uint64_t count,
                        byo_vertex_subset **out);
+/* vertexSubset(n, m, BitArray&&) (vertex_subset.h:263-270): the members are
+ * the set bits of d_bits (ceil(n/32) words, bit v of word v/32; bits of ids
+ * >= n ignored), copied in.  _all: BitArray(n, true), every vertex. */
+int byo_vs_create_bitmap(byo_graph *g, const uint32_t *d_bits, byo_vertex_subset **out);
+int byo_vs_create_all(byo_graph *g, byo_vertex_subset **out);
 void byo_vs_destroy(byo_vertex_subset *vs);
 uint64_t byo_vs_size(const byo_vertex_subset *vs);
 int byo_vs_is_dense(const byo_vertex_subset *vs);
 /* Members in increasing id order (toSparse + sort). */
 int byo_vs_to_list(byo_vertex_subset *vs, uint32_t *h_out, uint64_t cap);
-/* edgeMap(G, vs, F, threshold, flags): threshold -1 => M/20. */
+/* edgeMap(G, vs, F, threshold, flags): threshold -1 => M/20.  Direction as
+ * edgeMapData (edge_map_data.h:254-307); sparse and blocked rounds apply cond
+ * and updateAtomic from the members, dense rounds apply update to each vertex
+ * whose cond holds, neighbours in increasing id order, until cond fails.  The
+ * output holds each vertex once (as with gbbs's remove_duplicates flag);
+ * BYO_FL_NO_OUTPUT gives an empty subset. */
 int byo_edge_map(byo_graph *g, byo_vertex_subset *vs, byo_functor *f, int64_t threshold,
                  uint32_t flags, byo_vertex_subset **out);
+
+/* vertexMap / vertexFilter (vertex_subset.h:382-485) with one of the
+ * reference's vertex functions, applied to every member i:
+ *   BYO_VOP_PR_UPDATE      PR_Vertex_F (PageRank.h:53-68):
+ *                          d_a[i] = damping * d_a[i] + (1 - damping) / n
+ *   BYO_VOP_ZERO           PR_Vertex_Reset (PageRank.h:71-78): d_a[i] = 0
+ *   BYO_VOP_PR_DELTA_FIRST delta::PR_Vertex_F_FirstRound (PageRank.h:252-281):
+ *                          pre = damping * d_c[i] + (1 - damping) / n;
+ *                          d_a[i] += pre; delta = pre - 1/n; d_b[2i] = delta,
+ *                          d_b[2i+1] = delta / degree(i); keeps i when
+ *                          delta > eps2 * d_a[i]
+ *   BYO_VOP_PR_DELTA       delta::PR_Vertex_F (PageRank.h:294-318):
+ *                          delta = d_c[i] * damping; d_b[2i], d_b[2i+1] as
+ *                          above; when |delta| > eps2 * d_a[i], d_a[i] +=
+ *                          delta and i is kept
+ * (d_a: p, d_b: the delta pairs, d_c: nghSum).  vertexMap ignores the
+ * results; vertexFilter returns the members kept. */
+enum byo_vertex_op_kind {
+  BYO_VOP_PR_UPDATE = 0,
+  BYO_VOP_ZERO = 1,
+  BYO_VOP_PR_DELTA_FIRST = 2,
+  BYO_VOP_PR_DELTA = 3
+};
+typedef struct byo_vertex_op {
+  int kind;
+  double *d_a, *d_b, *d_c;
+  double damping, eps2;
+} byo_vertex_op;
+int byo_vertex_map(byo_vertex_subset *vs, const byo_vertex_op *op);
+int byo_vertex_filter(byo_vertex_subset *vs, const byo_vertex_op *op, byo_vertex_subset **out);
 
 /* ------------------------------------------------------------------ statistics
  * Per-round log of the last traversal (the learned policy's training data). */
@@ -374,6 +448,15 @@ typedef struct byo_round_log {
 int byo_last_rounds(byo_ctx *ctx, byo_round_log *out, uint64_t cap, uint64_t *count);
 /* Times every round with CUDA events (adds one host wait per round). */
 int byo_ctx_set_round_timing(byo_ctx *ctx, int on);
+/* Test hook for the bounded device waits: the grid barriers of the persistent
+ * kernels (small BFS rounds, 64-source BFS, the update stream) give up after
+ * limit_ms (<= 4000; 0 = the default 4 s) and wait for extra_blocks (0 or 1)
+ * more arrivals than blocks launched.  With extra_blocks = 1 no barrier can
+ * complete: the kernel's blocks leave after limit_ms and the call returns
+ * BYO_ETIMEDOUT with the context still usable.  (0, 0) restores the default.
+ * No reference counterpart (the reference's waits are host-side, in
+ * parlaylib's scheduler). */
+int byo_ctx_set_barrier_test(byo_ctx *ctx, uint32_t limit_ms, uint32_t extra_blocks);
 /* Brackets every launch of the kernels tagged `tag` ("*": all tags, NULL: off)
  * with CUDA events on the context's stream; byo_ctx_kernel_time sums the
  * launches of one tag (NULL: all) since the last byo_ctx_kernel_timing call.
@@ -422,19 +505,22 @@ int byo_update_sample(byo_graph *g, const uint64_t *h_keys, uint64_t count, floa
 
 /* ------------------------------------------------------------------ allocation-free BFS
  * No counterpart in the reference.  For callers that cannot let a library
- * allocate device memory: hosts whose memory manager owns the whole GPU and
- * hands out sub-ranges itself, and code issuing work while a CUDA stream is
- * being captured, where cudaMalloc is not allowed.  BFS from src over the
+ * allocate device memory: hosts whose memory manager reserves the whole GPU
+ * up front and hands out sub-ranges itself (a buffer pool, a managed runtime
+ * that owns one device arena), where a cudaMalloc inside the library would
+ * fail or take memory the manager does not track.  BFS from src over the
  * caller's device CSR (d_offsets[n+1], d_nbrs[m], symmetric, sorted), on the
  * caller's stream (cudaStream_t, NULL = default) of the current device,
  * writing the same parents and levels as byo_bfs into the caller's device
  * arrays (either may be NULL, not both).  Calls no cudaMalloc / cudaFree:
  * the traversal state lives in one static device array sized for
  * BYO_NOALLOC_MAX_VERTICES vertices (16.4 MiB per GPU, held until exit);
- * n above that returns BYO_EINVAL.  The array is shared by all calls: calls
- * that overlap on the GPU race and must be serialised by the caller.  The
- * first call on a device looks the array up and should come before any
- * stream capture starts.  Returns when the result is in the output arrays. */
+ * n above that, src >= n or n == 0 return BYO_EINVAL.  The array is shared
+ * by all calls: calls that overlap on the GPU race and must be serialised by
+ * the caller.  The call is host-synchronous: it reads each round's frontier
+ * size back and synchronises `stream` every round, and returns when the
+ * result is in the output arrays.  The array's device address is looked up
+ * on the first call in each CUDA context of a device and cached. */
 #define BYO_NOALLOC_MAX_VERTICES (1u << 20)
 int byo_bfs_csr_noalloc(const uint64_t *d_offsets, const uint32_t *d_nbrs, uint64_t n, uint64_t m,
                         uint32_t src, uint32_t *d_parent, uint32_t *d_level, void *stream,

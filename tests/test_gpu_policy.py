@@ -114,3 +114,33 @@ def test_update_policy_samples_and_parity(ctx, oracle_mod):
         assert np.array_equal(go, ro) and np.array_equal(gn, rn)
     _abi.check(_abi.lib().byo_ctx_set_update_policy(ctx.h, _abi.UPDATE_MERGE), ctx.h)
     G.close()
+
+
+def test_committed_policy_gains_on_held_out_graphs(ctx):
+    """The committed network (trained on other seeds) against the m/20 rule on
+    rounds of graphs it never saw: RMAT 2^20 and Chung-Lu 2^20 (exponent 2.1),
+    six seeded sources each, every round timed under push, pull and blocked.
+    The summed round time under the network's choices must be at least 3%
+    below the rule's on each family."""
+    import byo_gb300 as byo
+    from byo_gb300 import policy as P
+    assert P.load_default(ctx), "no committed policy network"
+    params = P.get_params(ctx)
+    fams = {"rmat": byo.Graph.generate(ctx, "rmat", seed=977, lg_n=20, draws=1 << 24),
+            "chung-lu": byo.Graph.generate(ctx, "chung_lu", seed=978, n=1 << 20, draws=1 << 23, exponent=2.1)}
+    try:
+        for name, G in fams.items():
+            deg = G.degrees()
+            rng = np.random.default_rng(4242 + G.N())
+            srcs = rng.choice(np.nonzero(deg)[0], 6, replace=False)
+            X, Y, M, C = P.collect_round_samples(G, srcs)
+            ch = P.round_choices(ctx, params, X, C)
+            t_m20, t_learned = P.round_cost(Y, C), P.round_cost(Y, ch)
+            t_best = P.round_cost(Y, Y[:, :3].argmin(1))
+            print("%s held-out rounds %d: m/20 %.0f us, learned %.0f us (%.2fx), best %.0f us"
+                  % (name, len(X), t_m20, t_learned, t_m20 / t_learned, t_best))
+            assert t_learned < 0.97 * t_m20, name
+    finally:
+        P.clear(ctx)
+        for G in fams.values():
+            G.close()
