@@ -347,6 +347,8 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     ctx = byo.Context(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
+    if args.pr_launches == "stream":
+        _abi.check(L.byo_ctx_set_pagerank_graphs(ctx.h, 0), ctx.h)
     dynamic = args.workload == "dynamic"
     container = args.container if dynamic else "csr"
     t0 = time.time()
@@ -502,6 +504,17 @@ def run_ours(args, rank, world, local_rank):
         roof.update({"achieved": achieved, "frac": achieved / peak, "kernel": "bfs (push+pull+blocked)"})
     else:
         roof.update({"achieved": None, "frac": None})
+    if dom == "pr_pull":
+        # second roof: the device's random one-word gather rate from a table
+        # the size of PageRank's FP32 p/deg array (L2-resident)
+        gr = ctypes.c_double(0)
+        _abi.check(L.byo_gather_roof(ctx.h, 4 * n, ctypes.byref(gr)), ctx.h)
+        got = m_trav * pr_iters * args.steps / (ktimes[dom][1] / 1e3)
+        roof["gather_roof"] = {"unit": "G gathers/s", "peak": gr.value / 1e9, "achieved": got / 1e9,
+                               "frac": got / gr.value if gr.value else None, "table_bytes": 4 * n,
+                               "how": "byo_gather_roof: uniform random 4-byte loads from a table of 4n bytes, "
+                                      "16 in flight per thread, best of 5 launches (CUDA events); achieved = "
+                                      "directed edges x iterations / PageRank kernel time"}
     tr = traffic_table().get(dom)
     roof["traffic"] = tr.get("bytes_per_launch") if tr else None
     roof["kernel_ms_share"] = {t: round(ktimes[t][1] / max(elapsed_ms, 1e-9), 4) for t in tags if ktimes[t][0]}
@@ -1672,6 +1685,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="dynamic/static: skip the oracle check before timing")
     ap.add_argument("--no-sweep", action="store_true", help="dynamic: skip the 1e3/1e5/1e7 batch-size sweep")
+    ap.add_argument("--pr-launches", default="graph", choices=["graph", "stream"],
+                    help="PageRank iterations as one CUDA graph (default) or one stream launch per kernel "
+                         "(for per-kernel profiles)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 steps")

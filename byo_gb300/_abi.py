@@ -104,6 +104,8 @@ SIGNATURES = {
     "byo_ctx_synchronize": (_int, [_vp]),
     "byo_ctx_set_round_timing": (_int, [_vp, _int]),
     "byo_ctx_set_barrier_test": (_int, [_vp, _u32, _u32]),
+    "byo_ctx_set_pagerank_graphs": (_int, [_vp, _int]),
+    "byo_gather_roof": (_int, [_vp, _u64, _P(_dbl)]),
     "byo_ctx_kernel_timing": (_int, [_vp, ctypes.c_char_p]),
     "byo_ctx_kernel_time": (_int, [_vp, ctypes.c_char_p, _P(_u64), _P(_dbl)]),
     "byo_graph_create_csr": (_int, [_vp, _u64, _u64, _vp, _vp, _P(_vp)]),

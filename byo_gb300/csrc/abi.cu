@@ -932,6 +932,18 @@ int byo_ctx_set_barrier_test(byo_ctx *ctx, uint32_t limit_ms, uint32_t extra_blo
   return BYO_OK;
 }
 
+int byo_ctx_set_pagerank_graphs(byo_ctx *ctx, int on) {
+  if (!ctx) return BYO_EINVAL;
+  ctx->pr_graphs = on != 0;
+  return BYO_OK;
+}
+
+int byo_gather_roof(byo_ctx *ctx, uint64_t table_bytes, double *gathers_per_s) {
+  if (!ctx || !gathers_per_s) return BYO_EINVAL;
+  *gathers_per_s = 0.0;
+  return gather_roof(ctx, table_bytes, gathers_per_s);
+}
+
 int byo_ctx_set_round_timing(byo_ctx *ctx, int on) {
   if (!ctx) return BYO_EINVAL;
   ctx->time_rounds = on != 0;

@@ -368,7 +368,7 @@ __device__ __forceinline__ T group_total(T s, T c) {
 //                a vertex's chunks in order
 // A warp gathers a unit's p_div values with plain loads, 16 independent
 // loads per lane in flight, into its own stage in shared memory, then reduces
-// from the stage (k_pr_units).
+// from the stage (k_pr_units; light tiles by pr_light_tile).
 constexpr int kPrTile = 512;            // slots per warp tile / heavy chunk
 constexpr uint32_t kPrLightMax = 128;   // longest run of a light vertex
 constexpr int kPrBlock = 256;
@@ -488,6 +488,117 @@ __device__ __forceinline__ void pr_finish(uint64_t v, T tot, const uint32_t *__r
   l1loc += fabs((double)p_curr[v] - (double)p);
 }
 
+// (s, c) += (s2, c2), compensated when kComp (TwoSum of the sums, errors added)
+template <bool kComp, typename T>
+__device__ __forceinline__ void acc_merge(T &s, T &c, T s2, T c2) {
+  if constexpr (kComp) {
+    T t = s + s2;
+    T bb = t - s;
+    T e = (s - (t - bb)) + (s2 - bb);
+    s = t;
+    c = c + c2 + e;
+  } else {
+    s += s2;
+  }
+}
+
+// Per-warp scratch of a light tile beside its stage: a head flag for the first
+// slot of every non-empty run.
+constexpr uint32_t kPrFlagWords = (kPrStage + 31) / 32;
+template <typename T>
+constexpr size_t pr_warp_smem() {
+  return (size_t)kPrStage * sizeof(T) + kPrFlagWords * 4;
+}
+
+// Position of the last head flag below pos (there is one: slot 0 is a head).
+__device__ __forceinline__ uint32_t last_head_below(const uint32_t *flags, uint32_t pos) {
+  for (int w = (int)((pos - 1) >> 5); w >= 0; w--) {
+    uint32_t word = flags[w];
+    const uint32_t lim = pos - 32u * (uint32_t)w;  // bits below pos in this word
+    if (lim < 32) word &= (1u << lim) - 1u;
+    if (word) return 32u * (uint32_t)w + 31u - __clz(word);
+  }
+  return 0;
+}
+
+// Sums of a light tile's runs from the staged values buf[0, len).  Each lane
+// takes an odd-length chunk of consecutive slots (odd, so the lanes' reads
+// fall in different banks) and sums it in order; the partial of a run that
+// crosses chunk boundaries is carried by an inclusive segmented warp scan (a
+// lane holding a head starts a new segment) and the run open at a lane's
+// start is completed by the lane that holds its end.  Each run's total is
+// written over the staged value of its first slot, and a last pass finishes
+// the tile's vertices a lane each (consecutive vertices, coalesced).  One
+// fixed order per graph, so results are deterministic.
+template <bool kComp, typename T>
+__device__ __forceinline__ void pr_light_tile(const PrDesc &d, uint32_t len, T *buf, uint32_t *flags,
+                                              const uint64_t *__restrict__ off, const uint32_t *__restrict__ deg,
+                                              const T *__restrict__ p_curr, T *__restrict__ p_next,
+                                              T *__restrict__ pdiv_out, T damping, T added, double &l1loc) {
+  const unsigned lane = lane_id();
+  for (uint32_t w = lane; w < kPrFlagWords; w += 32) flags[w] = 0;
+  __syncwarp();
+  for (uint32_t x = d.v0 + lane; x < d.v1; x += 32) {
+    const uint64_t a = off[x], b = off[x + 1];
+    if (b > a) {
+      const uint32_t r0 = (uint32_t)(a - d.s0);
+      atomicOr(flags + (r0 >> 5), 1u << (r0 & 31));
+    }
+  }
+  __syncwarp();
+  const uint32_t C = ((len + 31) >> 5) | 1u;
+  const uint32_t lo = min(lane * C, len), hi = min(lo + C, len);
+  T s = T(0), c = T(0), hs = T(0), hc = T(0);
+  bool head = false;
+  uint32_t hpos = 0, fw = 0;
+  for (uint32_t r = lo; r < hi; r++) {
+    if (r == lo || (r & 31) == 0) fw = flags[r >> 5];
+    if ((fw >> (r & 31)) & 1u) {
+      if (!head) {
+        hs = s;
+        hc = c;
+        head = true;
+      } else {
+        buf[hpos] = kComp ? s + c : s;  // a run inside this chunk
+      }
+      s = T(0);
+      c = T(0);
+      hpos = r;
+    }
+    acc_add<kComp>(s, c, buf[r]);
+  }
+  T ss = s, sc = c;
+  int f = head ? 1 : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T ps = __shfl_up_sync(kFull, ss, o), pc = __shfl_up_sync(kFull, sc, o);
+    const int pf = __shfl_up_sync(kFull, f, o);
+    if ((int)lane >= o) {
+      if (!f) {
+        T ts = ps, tc = pc;
+        acc_merge<kComp>(ts, tc, ss, sc);
+        ss = ts;
+        sc = tc;
+      }
+      f |= pf;
+    }
+  }
+  T cs = __shfl_up_sync(kFull, ss, 1), cc = __shfl_up_sync(kFull, sc, 1);
+  __syncwarp();  // every lane's reads of the stage are done
+  if (head && lo > 0) {  // the run open at lo ends in this chunk
+    acc_merge<kComp>(cs, cc, hs, hc);
+    buf[last_head_below(flags, lo)] = kComp ? cs + cc : cs;
+  }
+  if (lane == 31 && len)  // the run open at the tile's end
+    buf[last_head_below(flags, len)] = kComp ? ss + sc : ss;
+  __syncwarp();
+  for (uint32_t x = d.v0 + lane; x < d.v1; x += 32) {
+    const uint64_t a = off[x], b = off[x + 1];
+    pr_finish<kComp, T>(x, b > a ? buf[a - d.s0] : T(0), deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+  }
+  __syncwarp();
+}
+
 // One warp per unit, no block-wide barriers: the warp gathers p_div of the
 // unit's slots (16 independent loads per lane in flight) into its own stage in
 // shared memory, then reduces.  Light tile: runs of <= 32 one lane each, longer
@@ -496,7 +607,7 @@ __device__ __forceinline__ void pr_finish(uint64_t v, T tot, const uint32_t *__r
 // in registers without the stage, in the same order: measured at RMAT 2^22,
 // 20 FP64 iterations 34.0 -> 28.8 ms, while FP32 runs 1% faster staged.
 template <bool kComp, typename T, bool kDirectHeavy>
-__global__ void __launch_bounds__(kPrBlock) k_pr_units(const uint64_t *__restrict__ off,
+__global__ void __launch_bounds__(kPrBlock, 5) k_pr_units(const uint64_t *__restrict__ off,
                                                        const uint32_t *__restrict__ slots,
                                                        const uint32_t *__restrict__ deg,
                                                        const PrDesc *__restrict__ desc,
@@ -504,11 +615,13 @@ __global__ void __launch_bounds__(kPrBlock) k_pr_units(const uint64_t *__restric
                                                        const T *__restrict__ pdiv_in, const T *__restrict__ p_curr,
                                                        T *__restrict__ p_next, T *__restrict__ pdiv_out,
                                                        T *__restrict__ part, T damping, T added, double *l1) {
-  __shared__ T stage[kPrBlock / 32][kPrStage];
+  extern __shared__ __align__(16) unsigned char pr_smem[];
   __shared__ double sm[kPrBlock / 32 + 1];
   const uint64_t nunits = counts[0] + counts[1];  // light tiles + heavy chunks
   const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
-  T *buf = stage[warp];
+  T *buf = reinterpret_cast<T *>(pr_smem) + (size_t)warp * kPrStage;
+  uint32_t *flags = reinterpret_cast<uint32_t *>(reinterpret_cast<T *>(pr_smem) + (size_t)(kPrBlock / 32) * kPrStage) +
+                    (size_t)warp * kPrFlagWords;
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   double l1loc = 0.0;
@@ -546,30 +659,7 @@ __global__ void __launch_bounds__(kPrBlock) k_pr_units(const uint64_t *__restric
     }
     __syncwarp();
     if (d.v1 != kNoVertex) {
-      for (uint32_t x0 = d.v0; x0 < d.v1; x0 += 32) {
-        const uint32_t x = x0 + lane;
-        uint32_t r0 = 0, r1 = 0;
-        if (x < d.v1) {
-          r0 = (uint32_t)(off[x] - d.s0);
-          r1 = (uint32_t)(off[x + 1] - d.s0);
-        }
-        const bool lng = r1 - r0 > 32;
-        if (x < d.v1 && !lng) {
-          T s = T(0), c = T(0);
-          for (uint32_t r = r0; r < r1; r++) acc_add<kComp>(s, c, buf[r]);
-          pr_finish<kComp, T>(x, kComp ? s + c : s, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
-        }
-        unsigned m = __ballot_sync(kFull, lng);
-        while (m) {
-          const int src = __ffs(m) - 1;
-          m &= m - 1;
-          const uint32_t q0 = __shfl_sync(kFull, r0, src), q1 = __shfl_sync(kFull, r1, src);
-          T s = T(0), c = T(0);
-          for (uint32_t r = q0 + lane; r < q1; r += 32) acc_add<kComp>(s, c, buf[r]);
-          T tot = group_total<kComp, T, 32>(s, c);
-          if (lane == 0) pr_finish<kComp, T>(x0 + src, tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
-        }
-      }
+      pr_light_tile<kComp, T>(d, len, buf, flags, off, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
     } else {
       T s = T(0), c = T(0);
       for (uint32_t r = lane; r < len; r += 32) acc_add<kComp>(s, c, buf[r]);
@@ -646,6 +736,17 @@ __global__ void k_pr_check(double *d_l1, double eps, uint32_t max_iters, PrLoop 
   cudaGraphSetConditional(h_while, cont);
 }
 
+// k_pr_check for stream launches: records the iteration's L1 and clears the
+// accumulators; the host reads the state and decides.
+__global__ void k_pr_check_plain(double *d_l1, PrLoop *st, int half) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  ++st->iters;
+  st->l1 = d_l1[0];
+  st->last = half;
+  d_l1[0] = 0.0;
+  d_l1[1] = 0.0;
+}
+
 template <typename T>
 __global__ void k_to_f64(const T *__restrict__ in, uint64_t n, double *out) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
@@ -709,7 +810,13 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   const T damping = (T)0.85;
   const T added = (T)((1 - 0.85) * (1 / (double)n));
   const int grid_c = grid_for(ctx, nheavy * 32, 256, 8);
-  const int grid_u = grid_for(ctx, (ntiles + max_chunks) * 32, kPrBlock, sizeof(T) == 4 ? 5 : 3);
+  const size_t units_smem = (size_t)(kPrBlock / 32) * pr_warp_smem<T>();
+  BYO_CU(ctx, cudaFuncSetAttribute(k_pr_units<kComp, T, sizeof(T) == 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)units_smem));
+  int units_per_sm = 0;
+  BYO_CU(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&units_per_sm, k_pr_units<kComp, T, sizeof(T) == 8>,
+                                                            kPrBlock, units_smem));
+  const int grid_u = grid_for(ctx, (ntiles + max_chunks) * 32, kPrBlock, units_per_sm > 0 ? units_per_sm : 1);
   // The iterations run as one CUDA graph: a WHILE node whose body holds two
   // iterations (pa -> pb, then under an IF node pb -> pa), each ending in
   // k_pr_check, which sets the conditions from the L1 norm on the device.
@@ -723,7 +830,31 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   uint32_t it = 0;
   double L1 = 0.0;
   const T *last = pa;
-  if (max_iters > 0) {
+  if (max_iters > 0 && !ctx->pr_graphs) {
+    // one stream launch per kernel and a host check of the residual after
+    // each iteration (the same kernels in the same order: the same results)
+    PrLoop *hs = nullptr;
+    BYO_TRY(pinned(ctx, 4096, (void **)&hs));
+    const T *pdiv_in[2] = {da, db}, *pcur[2] = {pa, pb};
+    T *pnext[2] = {pb, pa}, *pdiv_out[2] = {db, da};
+    for (int hh = 0;; hh ^= 1) {
+      launch_t(ctx, "pr_pull", k_pr_units<kComp, T, sizeof(T) == 8>, dim3(grid_u), dim3(kPrBlock), units_smem,
+               (const uint64_t *)g->d_off, (const uint32_t *)g->d_slots, (const uint32_t *)g->d_deg,
+               (const PrDesc *)desc, (const uint64_t *)counts, pdiv_in[hh], pcur[hh], pnext[hh], pdiv_out[hh], part,
+               damping, added, d_l1);
+      if (nheavy)
+        launch_t(ctx, "pr_pull", k_pr_combine<kComp, T>, dim3(grid_c), dim3(256), 0, (const uint32_t *)heavy,
+                 (const uint64_t *)cbase, nheavy, (const T *)part, (const uint32_t *)g->d_deg, pcur[hh], pnext[hh],
+                 pdiv_out[hh], damping, added, d_l1);
+      launch(ctx, k_pr_check_plain, dim3(1), dim3(32), 0, d_l1, loop, hh);
+      BYO_CU(ctx, cudaMemcpyAsync(hs, loop, sizeof(PrLoop), cudaMemcpyDeviceToHost, ctx->stream));
+      BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+      if (hs->l1 < eps || hs->iters >= max_iters) break;
+    }
+    it = hs->iters;
+    L1 = hs->l1;
+    last = hs->last == 0 ? pb : pa;
+  } else if (max_iters > 0) {
     cudaGraph_t graph = nullptr, body = nullptr, second = nullptr;
     cudaGraphExec_t exec = nullptr;
     int rc = BYO_OK;
@@ -775,8 +906,10 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
       kp.func = (void *)k_pr_units<kComp, T, sizeof(T) == 8>;
       kp.gridDim = dim3(grid_u);
       kp.blockDim = dim3(kPrBlock);
+      kp.sharedMemBytes = (unsigned)units_smem;
       kp.kernelParams = ua;
       cudaError_t x = cudaGraphAddKernelNode(&nu, gr, dep ? &dep : nullptr, dep ? 1 : 0, &kp);
+      kp.sharedMemBytes = 0;
       if (x != cudaSuccess) return fail("pagerank units node", x);
       cudaGraphNode_t prev = nu;
       if (nheavy_) {

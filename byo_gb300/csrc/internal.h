@@ -59,6 +59,9 @@ struct byo_ctx {
   // grid-barrier test hook (byo_ctx_set_barrier_test): limit in ms (0 = the
   // default) and arrivals awaited beyond the launched blocks
   uint32_t bar_limit_ms = 0, bar_extra = 0;
+  // PageRank iterations as one CUDA graph (default) or one stream launch per
+  // kernel with a host check per iteration (byo_ctx_set_pagerank_graphs)
+  bool pr_graphs = true;
 };
 
 // What the last batch update did (PMA): batch keys, keys changed, leaves the
@@ -256,6 +259,7 @@ int bytepd_write_file(byo_graph *g, const char *path, uint32_t P);
 int bytepd_encode_host(byo_graph *g, uint32_t P, uint64_t *h_bo, uint32_t *h_deg, unsigned char *h_bytes,
                        uint64_t *nbytes);
 uint64_t map_remote_bytes(uint64_t n, uint32_t width);
+int gather_roof(byo_ctx *ctx, uint64_t table_bytes, double *gathers_per_s);
 
 // ---------------------------------------------------------------- PMA (pma.cu)
 int pma_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);

@@ -57,6 +57,77 @@ __global__ void __launch_bounds__(256) k_map_sum(const uint32_t *__restrict__ sl
   if (threadIdx.x == 0 && acc) atomicAdd(out, acc);
 }
 
+// Random 4-byte gathers from a table of `words` uint32: each thread draws
+// kGatherBatch independent indices per round from a counter-based hash and
+// keeps every loaded value in its sum, so all loads are live.  The rate this
+// sustains is the ceiling of a kernel whose time goes to one-word random
+// gathers from an L2-resident array (PageRank's pull).
+constexpr int kGatherBatch = 16;
+__device__ __forceinline__ uint32_t gather_hash(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return (uint32_t)x;
+}
+
+__global__ void __launch_bounds__(256) k_gather_roof(const uint32_t *__restrict__ table, uint64_t words,
+                                                     uint32_t rounds, unsigned long long *out) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  unsigned long long acc = 0;
+  for (uint32_t r = 0; r < rounds; r++) {
+    uint32_t v[kGatherBatch];
+#pragma unroll
+    for (int q = 0; q < kGatherBatch; q++)
+      v[q] = __ldg(table + gather_hash((tid * rounds + r) * kGatherBatch + q) % words);
+#pragma unroll
+    for (int q = 0; q < kGatherBatch; q++) acc += v[q];
+  }
+  if (acc == 0x5eedull) out[0] = acc;  // keeps the loads alive
+}
+
+int gather_roof(byo_ctx *ctx, uint64_t table_bytes, double *gathers_per_s) {
+  const uint64_t words = table_bytes / 4;
+  if (words < 1024) return set_error(ctx, BYO_EINVAL, "gather roof: table of at least 4 KiB");
+  uint32_t *table = nullptr;
+  unsigned long long *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = BYO_OK;
+  if (cudaMalloc(&table, words * 4) != cudaSuccess || cudaMalloc(&out, 8) != cudaSuccess) {
+    cudaGetLastError();
+    rc = set_error(ctx, BYO_ENOMEM, "gather roof: table");
+  }
+  if (rc == BYO_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+    rc = set_error(ctx, BYO_EDEVICE, "gather roof: events");
+  if (rc == BYO_OK && cudaMemsetAsync(table, 1, words * 4, ctx->stream) != cudaSuccess)
+    rc = set_error(ctx, BYO_EDEVICE, "gather roof: table fill");
+  if (rc == BYO_OK) {
+    const dim3 grid(ctx->num_sms * 8), block(256);
+    const uint32_t rounds = 64;
+    const double gathers = (double)grid.x * block.x * rounds * kGatherBatch;
+    launch(ctx, k_gather_roof, grid, block, 0, (const uint32_t *)table, words, rounds, out);  // warm
+    float best = 1e30f;
+    for (int rep = 0; rep < 5 && rc == BYO_OK; rep++) {
+      cudaEventRecord(e0, ctx->stream);
+      launch(ctx, k_gather_roof, grid, block, 0, (const uint32_t *)table, words, rounds, out);
+      cudaEventRecord(e1, ctx->stream);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        rc = set_error(ctx, BYO_EDEVICE, "gather roof: timing");
+      else if (ms < best)
+        best = ms;
+    }
+    if (rc == BYO_OK) *gathers_per_s = gathers / (best / 1e3);
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(ctx->stream);
+  if (table) cudaFree(table);
+  if (out) cudaFree(out);
+  return rc == BYO_OK ? check_launch(ctx, "gather roof") : rc;
+}
+
 uint64_t map_remote_bytes(uint64_t n, uint32_t width) {
   return width == 0 ? (n + 63) / 64 * 8 : n * width;
 }

@@ -448,6 +448,19 @@ typedef struct byo_round_log {
 int byo_last_rounds(byo_ctx *ctx, byo_round_log *out, uint64_t cap, uint64_t *count);
 /* Times every round with CUDA events (adds one host wait per round). */
 int byo_ctx_set_round_timing(byo_ctx *ctx, int on);
+/* PageRank's iterations run as one CUDA graph whose conditional nodes test
+ * the residual on the device (on = 1, the default), or as one stream launch
+ * per kernel with the residual checked on the host after each iteration
+ * (on = 0; the same kernels in the same order, so the same results; for
+ * profilers that cannot look inside conditional graphs).  No reference
+ * counterpart. */
+int byo_ctx_set_pagerank_graphs(byo_ctx *ctx, int on);
+/* The device's rate of random 4-byte gathers from a table of table_bytes
+ * (allocated and freed by the call): uniform indices from a counter-based
+ * hash, 16 independent loads per thread in flight, best of 5 timed launches.
+ * The second roof of kernels bound by one-word random gathers from an
+ * L2-resident array (PageRank's pull).  No reference counterpart. */
+int byo_gather_roof(byo_ctx *ctx, uint64_t table_bytes, double *gathers_per_s);
 /* Test hook for the bounded device waits: the grid barriers of the persistent
  * kernels (small BFS rounds, 64-source BFS, the update stream) give up after
  * limit_ms (<= 4000; 0 = the default 4 s) and wait for extra_blocks (0 or 1)
