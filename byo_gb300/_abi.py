@@ -78,6 +78,7 @@ class RoundLog(ctypes.Structure):
 
 
 F_BFS, F_BFS_LABEL, F_PR, F_PR_DELTA = 0, 1, 2, 3
+OP_REMOVE, OP_INSERT, OP_QUERY = 0, 1, 2
 VOP_PR_UPDATE, VOP_ZERO, VOP_PR_DELTA_FIRST, VOP_PR_DELTA = 0, 1, 2, 3
 
 
@@ -150,6 +151,8 @@ SIGNATURES = {
     "byo_graph_create": (_int, [_vp, _int, _u64, _u64, _vp, _vp, _P(_vp)]),
     "byo_graph_update_stream": (_int, [_vp, _vp, _vp, _vp, _u64, _vp]),
     "byo_graph_update_stream_device": (_int, [_vp, _vp, _vp, _vp, _u64, _vp]),
+    "byo_graph_mixed_stream": (_int, [_vp, _vp, _vp, _vp, _u64, _vp, _u32, _vp, _vp, _vp]),
+    "byo_graph_mixed_stream_device": (_int, [_vp, _vp, _vp, _vp, _u64, _vp, _u32, _vp, _vp, _vp]),
     "byo_graph_from_bytepd": (_int, [_vp, _u64, _vp, _vp, _vp, _u64, _u32, _int, _P(_vp)]),
     "byo_graph_read_bytepd": (_int, [_vp, ctypes.c_char_p, _u32, _int, _P(_vp)]),
     "byo_graph_write_bytepd": (_int, [_vp, ctypes.c_char_p, _u32]),

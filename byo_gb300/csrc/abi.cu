@@ -285,8 +285,9 @@ static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int
 }
 
 static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, const uint64_t *h_offsets,
-                                const uint8_t *h_ops, uint64_t nbatch, uint64_t *changed) {
-  if (!g || (nbatch && (!keys || !h_offsets || !h_ops))) return BYO_EINVAL;
+                                const uint8_t *h_ops, uint64_t nbatch, uint64_t *changed,
+                                const StreamQueries *qs = nullptr) {
+  if (!g || (nbatch && (!h_offsets || !h_ops))) return BYO_EINVAL;
   byo_ctx *ctx = g->ctx;
   if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS)
     return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA or VOS container");
@@ -294,7 +295,27 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
   if (h_offsets[0] != 0) return set_error(ctx, BYO_EINVAL, "update stream: offsets[0] != 0");
   for (uint64_t b = 0; b < nbatch; b++)
     if (h_offsets[b + 1] < h_offsets[b]) return set_error(ctx, BYO_EINVAL, "update stream: offsets decrease");
+  // the update stream inserts on any nonzero op; the mixed stream reads
+  // 0 remove, 1 insert, 2 query
+  uint64_t nq = 0;
+  for (uint64_t b = 0; qs && b < nbatch; b++) {
+    if (h_ops[b] > BYO_OP_QUERY) return set_error(ctx, BYO_EINVAL, "mixed stream: unknown op");
+    if (h_ops[b] == BYO_OP_QUERY) {
+      if (h_offsets[b + 1] != h_offsets[b]) return set_error(ctx, BYO_EINVAL, "mixed stream: a query op holds keys");
+      nq++;
+    }
+  }
+  if (nq) {
+    if (g->container != BYO_CONTAINER_PMA)
+      return set_error(ctx, BYO_ENOTSUP, "mixed stream: queries need the PMA container");
+    if (qs->k == 0 || qs->k > 64) return set_error(ctx, BYO_EINVAL, "mixed stream: 1 <= k <= 64 sources");
+    if (!qs->h_srcs || !qs->d_levels) return set_error(ctx, BYO_EINVAL, "mixed stream: null sources or levels");
+    if (g->n >= (1ull << 32) - 1) return set_error(ctx, BYO_EINVAL, "mixed stream: n too large");
+    for (uint64_t i = 0; i < nq * qs->k; i++)
+      if (qs->h_srcs[i] >= g->n) return set_error(ctx, BYO_EINVAL, "mixed stream: source >= n");
+  }
   const uint64_t total = h_offsets[nbatch];
+  if (total && !keys) return set_error(ctx, BYO_EINVAL, "update stream: null keys");
   const uint64_t *d = keys;
   if (host) {
     uint64_t *buf = nullptr;
@@ -307,7 +328,7 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
   BYO_CU(ctx, cudaMemcpyAsync(sb, h_offsets, (nbatch + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
   unsigned char *d_ops = reinterpret_cast<unsigned char *>(sb + nbatch + 1);
   std::vector<unsigned char> ops(nbatch);
-  for (uint64_t b = 0; b < nbatch; b++) ops[b] = h_ops[b] ? 1 : 0;
+  for (uint64_t b = 0; b < nbatch; b++) ops[b] = qs && h_ops[b] == BYO_OP_QUERY ? BYO_OP_QUERY : (h_ops[b] ? 1 : 0);
   BYO_CU(ctx, cudaMemcpyAsync(d_ops, ops.data(), nbatch, cudaMemcpyHostToDevice, ctx->stream));
   std::vector<long long> ch(nbatch);
   int rc = BYO_OK;
@@ -319,11 +340,33 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
       ch[b] = (long long)c;
     }
   } else {
-    rc = pma_update_stream(g, d, sb, h_offsets, d_ops, ops.data(), nbatch, ch.data());
+    rc = pma_update_stream(g, d, sb, h_offsets, d_ops, ops.data(), nbatch, ch.data(), qs);
   }
   if (changed)
     for (uint64_t b = 0; b < nbatch; b++) changed[b] = (uint64_t)ch[b];
   return rc;
+}
+
+static int mixed_common(byo_graph *g, const uint64_t *keys, int host, const uint64_t *offsets, const uint8_t *ops,
+                        uint64_t nops, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint64_t *changed,
+                        uint64_t *op_ns) {
+  if (!g) return BYO_EINVAL;
+  if (op_ns)
+    for (uint64_t b = 0; b < 2 * nops; b++) op_ns[b] = 0;
+  StreamQueries qs{h_srcs, k, d_levels, op_ns};
+  return update_stream_common(g, keys, host, offsets, ops, nops, changed, &qs);
+}
+
+int byo_graph_mixed_stream(byo_graph *g, const uint64_t *h_keys, const uint64_t *offsets, const uint8_t *ops,
+                           uint64_t nops, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint64_t *changed,
+                           uint64_t *op_ns) {
+  return mixed_common(g, h_keys, 1, offsets, ops, nops, h_srcs, k, d_levels, changed, op_ns);
+}
+
+int byo_graph_mixed_stream_device(byo_graph *g, const uint64_t *d_keys, const uint64_t *offsets, const uint8_t *ops,
+                                  uint64_t nops, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels,
+                                  uint64_t *changed, uint64_t *op_ns) {
+  return mixed_common(g, d_keys, 0, offsets, ops, nops, h_srcs, k, d_levels, changed, op_ns);
 }
 
 int byo_graph_update_stream(byo_graph *g, const uint64_t *h_keys, const uint64_t *offsets, const uint8_t *ops,

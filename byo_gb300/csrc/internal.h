@@ -118,8 +118,10 @@ enum Ws {
   WS_MISC,
   WS_STREAM,        // update stream: batch offsets and operations
   WS_MS_LEVELS,     // uint64[16][n] 64-source BFS: bit b of each pair's level
+  WS_STREAM_Q,      // mixed stream: query numbering, sources, descriptors, op times
   WS_COUNT
 };
+static_assert(WS_COUNT <= 24, "byo_graph::ws holds 24 workspaces");
 
 // ---------------------------------------------------------------- errors
 int set_error(byo_ctx *ctx, int code, const char *what, cudaError_t e = cudaSuccess);
@@ -267,8 +269,18 @@ int vos_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);
 int vos_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert, uint64_t *changed);
 int vos_compact(byo_graph *g, const uint64_t *offc, uint32_t *out);
 void vos_destroy(Vos *v);
+// Query ops of a mixed stream (ops[b] == 2): k sources per query, taken in
+// order from h_srcs; query q writes its levels to d_levels + q * k * n;
+// h_op_ns (may be null) receives each op's device start and end times.
+struct StreamQueries {
+  const uint32_t *h_srcs;
+  uint32_t k;
+  uint32_t *d_levels;
+  uint64_t *h_op_ns;
+};
 int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_boff, const uint64_t *h_boff,
-                      const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed);
+                      const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed,
+                      const StreamQueries *qs = nullptr);
 uint64_t pma_leaf_slots();
 int pma_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert,
                uint64_t *changed);

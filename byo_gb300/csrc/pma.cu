@@ -40,6 +40,7 @@
 #include "device.cuh"
 #include "gridsync.cuh"
 #include "internal.h"
+#include "msbfs.cuh"
 #include "scan.cuh"
 
 namespace byo {
@@ -1480,6 +1481,11 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
 // whose merge overflows a leaf or shrinks the array stops the kernel after its
 // merge; the host finishes that batch with the windowed path and relaunches
 // from the next one.  A batch with a key >= n stops it before its merge.
+// Query ops (the mixed stream) run a 64-source bit-lane BFS over the
+// container's own slots between the batches, inside the same kernel and under
+// the same barrier: the query state is cleared, the traversal runs
+// (ms_bfs_body), the levels are written to the query's output, and CTA 0
+// sorts the next batch.
 constexpr int kStreamThreads = 1024, kStreamWarps = kStreamThreads / 32;
 constexpr size_t kStreamSmem = (size_t)kStreamWarps * (kLeaf + kOptSeg) * 8;
 
@@ -1489,8 +1495,12 @@ struct StreamCtl {
   unsigned long long ctr[2][6];  // per buffer: [0] overflow cursor [1] overflowing leaves [2] delta [3] segments
                                  // [4] view chunks
   long long m;                   // keys in the container
-  unsigned int stop, reason;     // batch index + 1 where the kernel stopped; 1 overflow or shrink, 2 invalid keys
+  unsigned int stop, reason;     // batch index + 1 where the kernel stopped; 1 overflow or shrink, 2 invalid keys,
+                                 // 3 a query's hub chunk list overflowed
+  unsigned long long t_prev;     // globaltimer at the end of the previous op (or the kernel's start)
 };
+
+constexpr unsigned char kOpQuery = 2;  // ops[b]: 0 remove, 1 insert, 2 query
 
 // Batch b uses buffer b & 1 of the sorted keys, segment list, offset ranges
 // and chunk list, so that the next batch can be sorted and its segments found
@@ -1509,6 +1519,13 @@ struct StreamArgs {
   double shrink_below;   // a remove that leaves fewer keys rebuilds the array
   long long *changed;
   StreamCtl *ctl;
+  // queries (ops[b] == kOpQuery): op b runs the query described by
+  // qargs[qnum[b]] (device memory: its sources, its levels output and the
+  // shared work arrays and control block); op_ns[2b], op_ns[2b + 1]: op b's
+  // start and end (globaltimer)
+  const MsArgs *qargs;
+  const uint32_t *qnum;
+  unsigned long long *op_ns;
 };
 
 // One chunk of a long offset range, by the whole CTA (Y: the leaf's src list).
@@ -1559,12 +1576,14 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
   // warps that merge: those of CTAs 1.. (all of them on a one-CTA grid)
   const bool solo = nb == 1;
   const uint64_t mw0 = solo ? 0 : 32, nmw = (nthr >> 5) - mw0, gw = (tid >> 5) - (solo ? 0 : 32);
-  if (blockIdx.x == 0) stream_sort(a, a.first, As);
+  if (tid == 0) c->t_prev = globaltimer_ns();
+  if (blockIdx.x == 0 && a.ops[a.first] != kOpQuery) stream_sort(a, a.first, As);
   if (!grid_sync(&c->bar, nb)) return;
   for (uint64_t bi = a.first;; bi++) {
     const int cur = (int)(bi & 1), prv = cur ^ 1;
     const bool has = bi < a.nbatch;
-    const bool valid = has && c->bounds[cur][0] < a.n && c->bounds[cur][1] < a.n;
+    const bool query = has && a.ops[bi] == kOpQuery;
+    const bool valid = has && (query || (c->bounds[cur][0] < a.n && c->bounds[cur][1] < a.n));
     // phase 1
     if (bi > a.first) {
       const uint64_t nch = *(volatile unsigned long long *)&c->ctr[prv][4];
@@ -1579,7 +1598,7 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
       }
     }
     const uint64_t count = has ? a.boff[bi + 1] - a.boff[bi] : 0;
-    if (valid)
+    if (valid && !query)
       segments_range(a.sep, a.NL, a.sorted + (size_t)cur * kSmallSort, count,
                      a.seg + (size_t)cur * 2 * kSmallSort, &c->ctr[cur][3], tid, nthr);
     if (!grid_sync(&c->bar, nb)) return;
@@ -1591,10 +1610,41 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
       }
       return;
     }
+    const bool next_update = bi + 1 < a.nbatch && a.ops[bi + 1] != kOpQuery;
+    if (query) {
+      // a 64-source BFS over the current contents
+      const MsArgs &qa = a.qargs[a.qnum[bi]];
+      MsCtl *qc = qa.ctl;
+      if (blockIdx.x == 0)
+        for (uint32_t i = threadIdx.x; i < sizeof(MsCtl) / 8; i += blockDim.x)
+          reinterpret_cast<unsigned long long *>(qc)[i] = 0;
+      if (!grid_sync(&c->bar, nb)) return;
+      ms_bfs_body(qa, &c->bar);
+      if (!grid_sync(&c->bar, nb)) return;  // the round count is visible to all
+      ms_levels_body(qa, tid, nthr);
+      if (blockIdx.x == 0 && next_update) stream_sort(a, bi + 1, As);
+      if (tid == 0) {
+        c->ctr[cur][2] = 0;  // a query changes nothing and leaves no ranges to fill
+        c->ctr[cur][4] = 0;
+        if (qc->bar.err & 2u) {
+          c->stop = (unsigned int)bi + 1;
+          c->reason = 3;
+        }
+      }
+      if (!grid_sync(&c->bar, nb)) return;
+      if (tid == 0 && a.op_ns) {
+        const unsigned long long t = globaltimer_ns();
+        a.op_ns[2 * bi] = c->t_prev;
+        a.op_ns[2 * bi + 1] = t;
+        c->t_prev = t;
+      }
+      if (*(volatile unsigned int *)&c->stop) return;
+      continue;
+    }
     // phase 2
     const int insert = a.ops[bi];
     if (!solo && blockIdx.x == 0) {
-      if (bi + 1 < a.nbatch) stream_sort(a, bi + 1, As);
+      if (next_update) stream_sort(a, bi + 1, As);
     } else {
       const ViewOut view{a.sep, a.n, a.off, a.vrange + (size_t)cur * 2 * kSmallSort,
                          a.chunks + (size_t)cur * a.chunk_words, &c->ctr[cur][4]};
@@ -1608,10 +1658,16 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
       if (lane_id() == 0 && dsum) atomicAdd(&c->ctr[cur][2], (unsigned long long)dsum);
       if (solo) {
         __syncthreads();
-        if (bi + 1 < a.nbatch) stream_sort(a, bi + 1, As);
+        if (next_update) stream_sort(a, bi + 1, As);
       }
     }
     if (!grid_sync(&c->bar, nb)) return;
+    if (tid == 0 && a.op_ns) {
+      const unsigned long long t = globaltimer_ns();
+      a.op_ns[2 * bi] = c->t_prev;
+      a.op_ns[2 * bi + 1] = t;
+      c->t_prev = t;
+    }
     const long long total = c->m + (long long)*(volatile unsigned long long *)&c->ctr[cur][2];
     if (*(volatile unsigned long long *)&c->ctr[cur][1] || (!insert && (double)total < a.shrink_below)) {
       if (tid == 0) {
@@ -1624,13 +1680,42 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
 }
 
 int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_boff, const uint64_t *h_boff,
-                      const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed) {
+                      const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed,
+                      const StreamQueries *qs) {
   byo_ctx *ctx = g->ctx;
   Pma *p = g->pma;
   if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PMA container");
   for (uint64_t bi = 0; bi < nbatch; bi++) h_changed[bi] = 0;
   if (!nbatch) return BYO_OK;
   g->version++;
+  // queries: their numbering, sources, descriptors, shared control block and
+  // per-op times, in one workspace
+  std::vector<uint32_t> qnum(nbatch, 0);
+  uint64_t nq = 0;
+  for (uint64_t b = 0; b < nbatch; b++)
+    if (h_ops[b] == kOpQuery) qnum[b] = (uint32_t)nq++;
+  if (nq && !qs) return set_error(ctx, BYO_EINVAL, "update stream: query ops need sources");
+  uint32_t *d_qnum = nullptr, *d_qsrcs = nullptr;
+  MsArgs *d_qargs = nullptr;
+  MsCtl *d_qctl = nullptr;
+  unsigned long long *d_op_ns = nullptr;
+  if (qs) {
+    const size_t b_qnum = nbatch * 4, b_srcs = nq * qs->k * 4, b_args = nq * sizeof(MsArgs);
+    const size_t o_srcs = (b_qnum + 15) & ~15ull, o_args = (o_srcs + b_srcs + 15) & ~15ull;
+    const size_t o_ctl = (o_args + b_args + 15) & ~15ull, o_ns = (o_ctl + sizeof(MsCtl) + 15) & ~15ull;
+    unsigned char *wsp = nullptr;
+    BYO_TRY(ws(g, WS_STREAM_Q, o_ns + 16 * nbatch + 16, &wsp));
+    d_qnum = reinterpret_cast<uint32_t *>(wsp);
+    d_qsrcs = reinterpret_cast<uint32_t *>(wsp + o_srcs);
+    d_qargs = reinterpret_cast<MsArgs *>(wsp + o_args);
+    d_qctl = reinterpret_cast<MsCtl *>(wsp + o_ctl);
+    d_op_ns = reinterpret_cast<unsigned long long *>(wsp + o_ns);
+    BYO_CU(ctx, cudaMemcpyAsync(d_qnum, qnum.data(), b_qnum, cudaMemcpyHostToDevice, ctx->stream));
+    if (nq) BYO_CU(ctx, cudaMemcpyAsync(d_qsrcs, qs->h_srcs, b_srcs, cudaMemcpyHostToDevice, ctx->stream));
+    BYO_CU(ctx, cudaMemsetAsync(d_op_ns, 0, 16 * nbatch, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));  // qnum is read from host memory above
+  }
+  std::vector<MsArgs> qargs(nq);
   StreamCtl *c = nullptr;
   long long *d_changed = nullptr;
   BYO_TRY(ensure(ctx, p->misc, 128 + sizeof(StreamCtl) + 8 * nbatch));
@@ -1646,20 +1731,34 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
   while (bi < nbatch) {
     const uint64_t NL = p->NL;
     const uint64_t cnt_b = h_boff[bi + 1] - h_boff[bi];
-    if (cnt_b == 0) {
+    const bool query = h_ops[bi] == kOpQuery;
+    if (cnt_b == 0 && !query) {
       bi++;
       continue;
     }
-    if (cnt_b > kSmallSort || 2 * cnt_b > NL) {  // not a small batch: the ordinary update
+    if (!query && (cnt_b > kSmallSort || 2 * cnt_b > NL)) {  // not a small batch: the ordinary update
       uint64_t ch = 0;
       BYO_TRY(pma_update(g, d_keys + h_boff[bi], cnt_b, 0, h_ops[bi], &ch));
       h_changed[bi] = (long long)ch;
       bi++;
       continue;
     }
-    // the run of small batches from bi
+    // the run of small batches (and queries) from bi
     uint64_t be = bi;
-    while (be < nbatch && h_boff[be + 1] - h_boff[be] <= kSmallSort && 2 * (h_boff[be + 1] - h_boff[be]) <= NL) be++;
+    while (be < nbatch && (h_ops[be] == kOpQuery || (h_boff[be + 1] - h_boff[be] <= kSmallSort &&
+                                                     2 * (h_boff[be + 1] - h_boff[be]) <= NL)))
+      be++;
+    if (nq) {  // the queries read the container's current slots
+      MsArgs base = {};
+      BYO_TRY(ms_args_setup(g, qs->k, &base));
+      base.ctl = d_qctl;
+      for (uint64_t q = 0; q < nq; q++) {
+        qargs[q] = base;
+        qargs[q].srcs = d_qsrcs + q * qs->k;
+        qargs[q].levels = qs->d_levels + q * qs->k * g->n;
+      }
+      BYO_CU(ctx, cudaMemcpyAsync(d_qargs, qargs.data(), nq * sizeof(MsArgs), cudaMemcpyHostToDevice, ctx->stream));
+    }
     const uint64_t chunk_words = (g->n + 1) / kViewChunk + kSmallSort + 64;
     BYO_TRY(ensure(ctx, p->keys_a, 2 * kSmallSort * 8));
     BYO_TRY(ensure(ctx, p->bstart, std::max<uint64_t>(NL + 1, 4 * kSmallSort) * 8));
@@ -1696,6 +1795,9 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
     a.shrink_below = NL > 1 ? kRootMin * (double)NL * kLeaf : -1.0;
     a.changed = d_changed;
     a.ctl = c;
+    a.qargs = d_qargs;
+    a.qnum = d_qnum;
+    a.op_ns = d_op_ns;
     void *args[] = {(void *)&a};
     BYO_CU(ctx, cudaLaunchCooperativeKernel((const void *)k_pma_stream, dim3(ctx->num_sms * per_sm),
                                             dim3(kStreamThreads), args, kStreamSmem, ctx->stream));
@@ -1717,6 +1819,7 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
       for (uint64_t k = done_to; k < nbatch; k++) h_changed[k] = 0;
       return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
     }
+    if (hc->reason == 3) return set_error(ctx, BYO_EDEVICE, "mixed stream: a query's hub chunk list overflowed");
     // batch done_to merged with overflowing leaves (or shrinking): finish it
     const int buf = (int)(done_to & 1);
     const long long delta = (long long)hc->ctr[buf][2];
@@ -1727,6 +1830,10 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
     BYO_TRY(pma_finish_windowed(g, true, a.seg + (size_t)buf * 2 * kSmallSort, d_nseg,
                                 h_boff[done_to + 1] - h_boff[done_to], total, shrink));
     bi = done_to + 1;
+  }
+  if (qs && qs->h_op_ns) {
+    BYO_CU(ctx, cudaMemcpyAsync(qs->h_op_ns, d_op_ns, 16 * nbatch, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   }
   return BYO_OK;
 }

@@ -297,6 +297,38 @@ class Graph:
                                             ch.ctypes.data), self.ctx.h)
         return ch[:len(ks)].astype(np.int64)
 
+    def mixed_stream(self, ops, k, levels, device_keys=False):
+        """A stream of update batches and k-source BFS queries, in order
+        (byo_graph_mixed_stream).  ops: ("insert", keys), ("remove", keys)
+        or ("query", sources) with k sources each; `levels` is a device array
+        (anything with data_ptr(), e.g. a CUDA tensor) of nq * k * n uint32
+        that receives query q's levels at [q * k * n, (q + 1) * k * n).
+        Returns (changed per op, op times [nops, 2] in ns: device start and end
+        of the ops run inside the persistent kernel, 0 for the others)."""
+        codes = {"remove": _abi.OP_REMOVE, "insert": _abi.OP_INSERT, "query": _abi.OP_QUERY}
+        ks, srcs, o = [], [], []
+        for kind, x in ops:
+            o.append(codes[kind])
+            if kind == "query":
+                sv = np.ascontiguousarray(x, np.uint32)
+                if len(sv) != k:
+                    raise ValueError("a query takes exactly k sources")
+                srcs.append(sv)
+                ks.append(np.zeros(0, np.uint64))
+            else:
+                ks.append(self._keys(x))
+        off = np.zeros(len(ks) + 1, np.uint64)
+        off[1:] = np.cumsum([len(a) for a in ks])
+        keys = np.ascontiguousarray(np.concatenate(ks) if ks else np.zeros(0, np.uint64), np.uint64)
+        sv = np.ascontiguousarray(np.concatenate(srcs) if srcs else np.zeros(1, np.uint32), np.uint32)
+        oc = np.ascontiguousarray(o, np.uint8)
+        ch = np.zeros(max(len(o), 1), np.uint64)
+        t = np.zeros(2 * max(len(o), 1), np.uint64)
+        check(lib().byo_graph_mixed_stream(self.h, keys.ctypes.data if len(keys) else None, off.ctypes.data,
+                                           oc.ctypes.data, len(o), sv.ctypes.data, k, levels.data_ptr(),
+                                           ch.ctypes.data, t.ctypes.data), self.ctx.h)
+        return ch[:len(o)].astype(np.int64), t[:2 * len(o)].reshape(-1, 2)
+
     def insert_batch(self, batch, sorted=False):
         k = self._keys(batch)
         ch = ctypes.c_uint64(0)

@@ -308,6 +308,33 @@ int byo_graph_update_stream(byo_graph *g, const uint64_t *h_keys, const uint64_t
 int byo_graph_update_stream_device(byo_graph *g, const uint64_t *d_keys, const uint64_t *offsets, const uint8_t *ops,
                                    uint64_t nbatch, uint64_t *changed);
 
+/* A mixed stream of update batches and 64-source BFS queries, in order
+ * (the serving pattern of a dynamic graph: batches arrive between queries);
+ * PMA container.  ops[i]: BYO_OP_REMOVE / BYO_OP_INSERT (keys
+ * [offsets[i], offsets[i+1]) as in byo_graph_update_stream) or BYO_OP_QUERY
+ * (an empty key range): the q-th query op runs a k-source bit-lane BFS
+ * (k <= 64, sources h_srcs[q*k .. q*k+k)) over the contents at that point of
+ * the stream and writes levels as byo_bfs_multi does to
+ * d_levels + q*k*n (device memory of nq*k*n entries).  Runs of queries and
+ * small batches (as for byo_graph_update_stream) are drained by one
+ * persistent kernel under one bounded grid barrier: per query its state is
+ * cleared, the traversal runs over the container's own slots and the levels
+ * are written, with no host round trip; a larger batch, or one whose merge
+ * overflows a leaf, is finished by the host and the kernel resumes after it.
+ * changed[i] (may be NULL): keys inserted or removed by op i.  op_ns (may be
+ * NULL, 2*nops entries): device start and end time of each op run inside the
+ * kernel, in ns of one clock (0 for ops finished on the host path).  No
+ * reference counterpart: the reference runs queries and batches as separate
+ * calls (benchmarks/run_unweighted.h:781-893 for batches, BFS.h:47-64 for a
+ * query). */
+enum byo_stream_op { BYO_OP_REMOVE = 0, BYO_OP_INSERT = 1, BYO_OP_QUERY = 2 };
+int byo_graph_mixed_stream(byo_graph *g, const uint64_t *h_keys, const uint64_t *offsets, const uint8_t *ops,
+                           uint64_t nops, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels, uint64_t *changed,
+                           uint64_t *op_ns);
+int byo_graph_mixed_stream_device(byo_graph *g, const uint64_t *d_keys, const uint64_t *offsets, const uint8_t *ops,
+                                  uint64_t nops, const uint32_t *h_srcs, uint32_t k, uint32_t *d_levels,
+                                  uint64_t *changed, uint64_t *op_ns);
+
 /* ------------------------------------------------------------------ byte-PD graphs
  * The reference's compressed graphs: neighbour lists in the bytepd_amortized
  * encoding (gbbs/encodings/byte_pd_amortized.h:1100-1155,
