@@ -810,6 +810,11 @@ def run_mixed(args, rank, world, local_rank):
                      "kernel_ms_share": round(ms_kernel / max(elapsed_ms, 1e-9), 4)},
         "gpu_launches": launches, "clocks": clk,
     }
+    # the same step as one mixed stream (byo_graph_mixed_stream_device): runs
+    # of queries and batches of up to 4096 keys drained by one persistent
+    # kernel; larger batches finished on the host between launches
+    res["components"]["one_launch"] = mixed_one_launch(args, L, _abi, ctx, G, torch, stream, dev, n, order,
+                                                       sizes, bkeys, qsrc, units)
     # end to end: batches from pinned host memory, every query's levels back to the host
     hk = []
     for k in bkeys:
@@ -840,6 +845,59 @@ def run_mixed(args, rank, world, local_rank):
                   "h2d_bytes_per_step": int(upd_keys * 8),
                   "d2h_bytes_per_step": 4 * 64 * n * MIXED_QUERIES, "ms_per_step": dt * 1e3}
     return res, ctx, G
+
+
+def mixed_one_launch(args, L, _abi, ctx, G, torch, stream, dev, n, order, sizes, bkeys, qsrc, units):
+    ops, offs, srcs, kparts = [], [0], [], []
+    for kind, i in order:
+        if kind == "Q":
+            ops.append(_abi.OP_QUERY)
+            srcs.append(qsrc[i])
+        else:
+            ops.append(_abi.OP_INSERT if kind == "I" else _abi.OP_REMOVE)
+            kparts.append(bkeys[i])
+        offs.append(offs[-1] + (0 if kind == "Q" else bkeys[i].numel()))
+    keys = torch.cat(kparts)
+    offs = np.ascontiguousarray(offs, np.uint64)
+    opc = np.ascontiguousarray(ops, np.uint8)
+    srcv = np.ascontiguousarray(np.concatenate(srcs), np.uint32)
+    nq = len(srcs)
+    levels = torch.empty(nq * 64 * n, dtype=torch.int32, device=dev)
+    ch = np.zeros(len(ops), np.uint64)
+    t = np.zeros(2 * len(ops), np.uint64)
+    torch.cuda.synchronize()
+
+    def step():
+        _abi.check(L.byo_graph_mixed_stream_device(G.h, keys.data_ptr(), offs.ctypes.data, opc.ctypes.data, len(ops),
+                                                   srcv.ctypes.data, 64, levels.data_ptr(), ch.ctypes.data,
+                                                   t.ctypes.data), ctx.h)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.launches
+    qlat = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        tt = t.reshape(-1, 2)
+        qlat += [(tt[i, 1] - tt[i, 0]) / 1e6 for i in range(len(ops)) if ops[i] == _abi.OP_QUERY]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    tt = t.reshape(-1, 2)
+    in_kernel = [i for i in range(len(ops)) if tt[i, 1] > 0]
+    qlat = np.array(qlat)
+    del levels
+    return {"value": units / (ms / 1e3) / 1e9, "unit": MIXED_UNIT, "ms_per_step": ms,
+            "query_latency_ms": {"p50": float(np.percentile(qlat, 50)), "p99": float(np.percentile(qlat, 99)),
+                                 "mean": float(qlat.mean())},
+            "ops_in_kernel": len(in_kernel), "ops": len(ops),
+            "launches_per_step": (ctx.launches - launches0) / args.steps,
+            "how": "the step's %d ops through byo_graph_mixed_stream_device: queries and batches of <= 4096 keys "
+                   "run inside one persistent kernel (query latency = its device start/end times); larger "
+                   "batches on the host path between launches" % len(ops)}
 
 
 def run_multi(args, rank, world, local_rank):
