@@ -103,6 +103,11 @@ SIGNATURES = {
     "byo_ctx_stream": (_vp, [_vp]),
     "byo_ctx_launches": (_u64, [_vp]),
     "byo_ctx_synchronize": (_int, [_vp]),
+    "byo_buffer_alloc": (_int, [_vp, _u64, _P(_vp)]),
+    "byo_buffer_free": (None, [_vp, _vp]),
+    "byo_buffer_write": (_int, [_vp, _vp, _u64, _vp, _u64]),
+    "byo_buffer_read": (_int, [_vp, _vp, _u64, _vp, _u64]),
+    "byo_buffer_fill32": (_int, [_vp, _vp, _u64, _u64, _u32]),
     "byo_ctx_set_round_timing": (_int, [_vp, _int]),
     "byo_ctx_set_barrier_test": (_int, [_vp, _u32, _u32]),
     "byo_ctx_set_pagerank_graphs": (_int, [_vp, _int]),

@@ -32,6 +32,11 @@ int copy_to_host(byo_ctx *ctx, void *h, const void *d, size_t bytes) {
   return BYO_OK;
 }
 
+__global__ void k_fill32(uint32_t *d, uint64_t count, uint32_t value) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x)
+    d[i] = value;
+}
+
 }  // namespace
 
 struct byo_functor {
@@ -88,6 +93,44 @@ void byo_gpu_shutdown(byo_ctx *ctx) {
 const char *byo_last_error(const byo_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 void *byo_ctx_stream(byo_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 uint64_t byo_ctx_launches(const byo_ctx *ctx) { return ctx ? ctx->launches : 0; }
+int byo_buffer_alloc(byo_ctx *ctx, uint64_t bytes, void **d_out) {
+  if (!ctx || !d_out) return BYO_EINVAL;
+  *d_out = nullptr;
+  if (cudaMalloc(d_out, bytes ? bytes : 1) != cudaSuccess) {
+    cudaGetLastError();
+    *d_out = nullptr;
+    return set_error(ctx, BYO_ENOMEM, "buffer: device allocation");
+  }
+  return BYO_OK;
+}
+
+void byo_buffer_free(byo_ctx *ctx, void *d) {
+  if (!ctx || !d) return;
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+}
+
+int byo_buffer_write(byo_ctx *ctx, void *d, uint64_t offset, const void *h, uint64_t bytes) {
+  if (!ctx || !d || (bytes && !h)) return BYO_EINVAL;
+  if (!bytes) return BYO_OK;
+  BYO_CU(ctx, cudaMemcpyAsync(static_cast<char *>(d) + offset, h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  return BYO_OK;
+}
+
+int byo_buffer_read(byo_ctx *ctx, const void *d, uint64_t offset, void *h, uint64_t bytes) {
+  if (!ctx || !d || (bytes && !h)) return BYO_EINVAL;
+  return copy_to_host(ctx, h, static_cast<const char *>(d) + offset, bytes);
+}
+
+int byo_buffer_fill32(byo_ctx *ctx, void *d, uint64_t offset, uint64_t count, uint32_t value) {
+  if (!ctx || !d || (offset & 3)) return BYO_EINVAL;
+  if (!count) return BYO_OK;
+  launch(ctx, k_fill32, dim3(grid_for(ctx, count, 256)), dim3(256), 0,
+         reinterpret_cast<uint32_t *>(static_cast<char *>(d) + offset), count, value);
+  return check_launch(ctx, "buffer fill");
+}
+
 int byo_ctx_synchronize(byo_ctx *ctx) {
   if (!ctx) return BYO_EINVAL;
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));

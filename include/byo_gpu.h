@@ -62,6 +62,19 @@ int byo_ctx_synchronize(byo_ctx *ctx);
 /* Library version string. */
 const char *byo_version(void);
 
+/* Device buffers for callers without CUDA bindings (a C++ adapter, a cgo or
+ * JNI host): the arrays the edgeMap functors and the mixed stream read and
+ * write.  byo_buffer_alloc allocates `bytes` on the context's device;
+ * byo_buffer_write / byo_buffer_read copy `bytes` between host memory and the
+ * buffer at byte `offset` and return when the copy is done; byo_buffer_fill32
+ * sets `count` 32-bit words from byte `offset` to `value`.  No reference
+ * counterpart (the reference's arrays are host memory). */
+int byo_buffer_alloc(byo_ctx *ctx, uint64_t bytes, void **d_out);
+void byo_buffer_free(byo_ctx *ctx, void *d);
+int byo_buffer_write(byo_ctx *ctx, void *d, uint64_t offset, const void *h, uint64_t bytes);
+int byo_buffer_read(byo_ctx *ctx, const void *d, uint64_t offset, void *h, uint64_t bytes);
+int byo_buffer_fill32(byo_ctx *ctx, void *d, uint64_t offset, uint64_t count, uint32_t value);
+
 /* ------------------------------------------------------------------ containers
  * Replaces the container adapters of benchmarks/run_structures: CSR
  * (run_csr.cc:28-175, static) and PMA_graph (run_single_pma.cc:39-141, a

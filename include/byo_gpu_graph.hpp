@@ -17,6 +17,11 @@
 // gpu_cc, gpu_bfs_cc, gpu_pagerank, gpu_pagerank_delta, gpu_triangle_count,
 // gpu_map and gpu_map_remote.
 //
+// The edgeMap / vertexSubset API (gbbs/edge_map_data.h:254-315,
+// gbbs/vertex_subset.h:202-485) runs on the device: vertexSubset, the
+// functors BFS_F, BFS_ComponentLabel_F, PR_F and PR_Delta_F over
+// DeviceVector arrays, edgeMap, vertexMap and vertexFilter.
+//
 // Errors from the C ABI throw byo::Error (the reference aborts instead).
 #pragma once
 
@@ -304,6 +309,151 @@ inline std::vector<uint32_t> gpu_bfs_cc(const detail::DeviceGraph &G) {
   std::vector<uint32_t> label(G.num_vertices());
   Context::get().check(byo_bfs_cc(G.handle(), label.data()), "bfs_cc");
   return label;
+}
+
+// ---------------------------------------------------------------- edgeMap API
+// A device array of T on the context's device (the arrays the functors read
+// and write).
+template <class T>
+class DeviceVector {
+ public:
+  explicit DeviceVector(size_t n, T init = T()) : n_(n) {
+    Context &c = Context::get();
+    c.check(byo_buffer_alloc(c.h(), n * sizeof(T), &d_), "device vector");
+    std::vector<T> h(n, init);
+    c.check(byo_buffer_write(c.h(), d_, 0, h.data(), n * sizeof(T)), "device vector fill");
+  }
+  DeviceVector(const DeviceVector &) = delete;
+  DeviceVector &operator=(const DeviceVector &) = delete;
+  ~DeviceVector() { byo_buffer_free(Context::get().h(), d_); }
+  T *data() const { return static_cast<T *>(d_); }
+  size_t size() const { return n_; }
+  std::vector<T> to_host() const {
+    std::vector<T> h(n_);
+    Context::get().check(byo_buffer_read(Context::get().h(), d_, 0, h.data(), n_ * sizeof(T)), "device vector read");
+    return h;
+  }
+  void swap(DeviceVector &o) noexcept {
+    std::swap(d_, o.d_);
+    std::swap(n_, o.n_);
+  }
+  void assign(const std::vector<T> &h) {
+    Context::get().check(byo_buffer_write(Context::get().h(), d_, 0, h.data(), n_ * sizeof(T)), "device vector write");
+  }
+
+ private:
+  void *d_ = nullptr;
+  size_t n_;
+};
+
+// vertexSubset (vertex_subset.h:240-270): one vertex, a list, every vertex
+// (BitArray(n, true)) or the set bits of a device bitmap.
+class vertexSubset {
+ public:
+  vertexSubset(const detail::DeviceGraph &G, uint32_t v) { check(byo_vs_create_single(G.handle(), v, &h_)); }
+  vertexSubset(const detail::DeviceGraph &G, const std::vector<uint32_t> &ids) {
+    check(byo_vs_create_list(G.handle(), ids.data(), ids.size(), &h_));
+  }
+  static vertexSubset all(const detail::DeviceGraph &G) {
+    vertexSubset s;
+    s.check(byo_vs_create_all(G.handle(), &s.h_));
+    return s;
+  }
+  static vertexSubset from_bitmap(const detail::DeviceGraph &G, const DeviceVector<uint32_t> &bits) {
+    vertexSubset s;
+    s.check(byo_vs_create_bitmap(G.handle(), bits.data(), &s.h_));
+    return s;
+  }
+  explicit vertexSubset(byo_vertex_subset *h) : h_(h) {}
+  vertexSubset(vertexSubset &&o) noexcept : h_(o.h_) { o.h_ = nullptr; }
+  vertexSubset &operator=(vertexSubset &&o) noexcept {
+    std::swap(h_, o.h_);
+    return *this;
+  }
+  vertexSubset(const vertexSubset &) = delete;
+  ~vertexSubset() {
+    if (h_) byo_vs_destroy(h_);
+  }
+  size_t size() const { return byo_vs_size(h_); }
+  bool isEmpty() const { return size() == 0; }
+  bool isDense() const { return byo_vs_is_dense(h_) == 1; }
+  std::vector<uint32_t> toSparse() const {
+    std::vector<uint32_t> ids(size());
+    check(byo_vs_to_list(h_, ids.data(), ids.size()));
+    return ids;
+  }
+  byo_vertex_subset *handle() const { return h_; }
+
+ private:
+  vertexSubset() = default;
+  void check(int rc) const { Context::get().check(rc, "vertexSubset"); }
+  byo_vertex_subset *h_ = nullptr;
+};
+
+// The device functors (a GBBS functor struct's update / updateAtomic / cond).
+class Functor {
+ public:
+  Functor(Functor &&o) noexcept : h_(o.h_) { o.h_ = nullptr; }
+  Functor(const Functor &) = delete;
+  ~Functor() {
+    if (h_) byo_functor_destroy(h_);
+  }
+  byo_functor *handle() const { return h_; }
+
+ protected:
+  Functor() = default;
+  byo_functor *h_ = nullptr;
+};
+// BFS_F (BFS.h:30-45) over its own Parents array.
+class BFS_F : public Functor {
+ public:
+  BFS_F(const detail::DeviceGraph &G, uint32_t src) {
+    Context::get().check(byo_functor_bfs_create(G.handle(), src, &h_), "BFS_F");
+  }
+  std::vector<uint32_t> parents(size_t n) const {
+    std::vector<uint32_t> p(n);
+    Context::get().check(byo_functor_bfs_parents(h_, p.data()), "BFS_F parents");
+    return p;
+  }
+};
+// BFS_ComponentLabel_F (benchmarks/Connectivity/BFSCC/Connectivity.h:31-50).
+class BFS_ComponentLabel_F : public Functor {
+ public:
+  BFS_ComponentLabel_F(const detail::DeviceGraph &G, DeviceVector<uint32_t> &parents, uint32_t src) {
+    Context::get().check(byo_functor_bfs_label_create(G.handle(), src, parents.data(), &h_), "BFS_ComponentLabel_F");
+  }
+};
+// PR_F (benchmarks/PageRank/PageRank.h:33-50).
+class PR_F : public Functor {
+ public:
+  PR_F(const detail::DeviceGraph &G, const DeviceVector<double> &p_curr, DeviceVector<double> &p_next) {
+    Context::get().check(byo_functor_pr_create(G.handle(), p_curr.data(), p_next.data(), &h_), "PR_F");
+  }
+};
+// delta::PR_Delta_F (PageRank.h:200-226): delta holds n {delta, delta/degree} pairs.
+class PR_Delta_F : public Functor {
+ public:
+  PR_Delta_F(const detail::DeviceGraph &G, const DeviceVector<double> &delta, DeviceVector<double> &ngh_sum) {
+    Context::get().check(byo_functor_pr_delta_create(G.handle(), delta.data(), ngh_sum.data(), &h_), "PR_Delta_F");
+  }
+};
+
+// edgeMap (edge_map_data.h:312-315); flags as gbbs/flags.h (BYO_FL_*).
+inline vertexSubset edgeMap(const detail::DeviceGraph &G, const vertexSubset &vs, const Functor &f,
+                            int64_t threshold = -1, uint32_t flags = 0) {
+  byo_vertex_subset *out = nullptr;
+  Context::get().check(byo_edge_map(G.handle(), vs.handle(), f.handle(), threshold, flags, &out), "edgeMap");
+  return vertexSubset(out);
+}
+// vertexMap / vertexFilter (vertex_subset.h:382-485) with the reference's
+// vertex functions (BYO_VOP_*, arrays as byo_vertex_op describes).
+inline void vertexMap(const vertexSubset &vs, const byo_vertex_op &op) {
+  Context::get().check(byo_vertex_map(vs.handle(), &op), "vertexMap");
+}
+inline vertexSubset vertexFilter(const vertexSubset &vs, const byo_vertex_op &op) {
+  byo_vertex_subset *out = nullptr;
+  Context::get().check(byo_vertex_filter(vs.handle(), &op, &out), "vertexFilter");
+  return vertexSubset(out);
 }
 
 }  // namespace byo

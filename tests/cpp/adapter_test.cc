@@ -92,6 +92,43 @@ int main() {
   byo::GPU_PCSR_graph<int> pcsr(vd.data(), n, edges.size(), nullptr, edges.data());
   pcsr.insert_batch(batch.data(), batch.size());
   CHECK(pcsr.num_edges() == 16 && pcsr.degree(1) == 2 && pcsr.degree(6) == 2);
+
+  // the reference's own edgeMap loops through the adapter: bfs_cc::CC with
+  // BFS_ComponentLabel_F (BFSCC/Connectivity.h:52-88) and PageRank_edgeMap
+  // (PageRank.h:80-123), on the CSR of test_bfs.cc's graph
+  {
+    byo::DeviceVector<uint32_t> parents(n, BYO_NONE);
+    std::vector<uint32_t> host(n, BYO_NONE);
+    for (uint32_t i = 0; i < n; i++) {
+      if (host[i] != BYO_NONE || csr.degree(i) == 0) continue;
+      host[i] = i;
+      parents.assign(host);
+      byo::vertexSubset F(csr, i);
+      byo::BFS_ComponentLabel_F f(csr, parents, i);
+      while (!F.isEmpty()) F = byo::edgeMap(csr, F, f, -1, BYO_FL_SPARSE_BLOCKED | BYO_FL_DENSE_PARALLEL);
+      host = parents.to_host();
+    }
+    CHECK((host == std::vector<uint32_t>{0, 0, 2, 2, 2, 2, 2}));
+    byo::DeviceVector<double> pc(n, 1.0 / n), pn(n, 0.0);
+    byo::vertexSubset all = byo::vertexSubset::all(csr);
+    CHECK(all.size() == n && all.isDense());
+    for (int it = 0; it < 200; it++) {
+      byo::PR_F f(csr, pc, pn);
+      byo::vertexSubset none = byo::edgeMap(csr, all, f, 0, BYO_FL_NO_OUTPUT);
+      CHECK(none.isEmpty());
+      byo::vertexMap(all, byo_vertex_op{BYO_VOP_PR_UPDATE, pn.data(), nullptr, nullptr, 0.85, 0.0});
+      std::vector<double> a = pc.to_host(), b = pn.to_host();
+      double l1 = 0;
+      for (size_t v = 0; v < n; v++) l1 += a[v] > b[v] ? a[v] - b[v] : b[v] - a[v];
+      if (l1 < 1e-9) break;
+      byo::vertexMap(all, byo_vertex_op{BYO_VOP_ZERO, pc.data(), nullptr, nullptr, 0.0, 0.0});
+      pc.swap(pn);
+    }
+    std::vector<double> got = pn.to_host();
+    double diff = 0;
+    for (size_t v = 0; v < n; v++) diff += got[v] > pr[v] ? got[v] - pr[v] : pr[v] - got[v];
+    CHECK(diff < 1e-8);
+  }
   std::printf("adapter ok\n");
   return 0;
 }
