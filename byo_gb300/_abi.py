@@ -23,6 +23,7 @@ NONE = 0xFFFFFFFF
 CONTAINER_CSR = 0
 CONTAINER_PMA = 1
 CONTAINER_VOS = 2
+CONTAINER_PCSR = 3
 
 GEN_RMAT, GEN_ER, GEN_GRID, GEN_CHUNG_LU = 0, 1, 2, 3
 

@@ -153,11 +153,15 @@ int byo_graph_create_pma(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h
   return graph_from_host_csr(ctx, BYO_CONTAINER_PMA, n, m, h_offsets, h_nbrs, out);
 }
 
+static bool known_container(int c) {
+  return c == BYO_CONTAINER_CSR || c == BYO_CONTAINER_PMA || c == BYO_CONTAINER_VOS || c == BYO_CONTAINER_PCSR;
+}
+
 int byo_graph_create(byo_ctx *ctx, int container, uint64_t n, uint64_t m, const uint64_t *h_offsets,
                      const uint32_t *h_nbrs, byo_graph **out) {
   if (!ctx || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
+  if (!known_container(container))
     return set_error(ctx, BYO_EINVAL, "unknown container");
   return graph_from_host_csr(ctx, container, n, m, h_offsets, h_nbrs, out);
 }
@@ -170,7 +174,7 @@ int byo_adj_read(const char *path, int binary, uint64_t *n, uint64_t *m, uint64_
 int byo_graph_read_adj(byo_ctx *ctx, const char *path, int binary, int container, byo_graph **out) {
   if (!ctx || !path || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
+  if (!known_container(container))
     return set_error(ctx, BYO_EINVAL, "unknown container");
   uint64_t n = 0, m = 0;
   BYO_TRY(adj_read_host(ctx, path, binary, &n, &m, nullptr, nullptr));
@@ -184,7 +188,7 @@ int byo_graph_from_bytepd(byo_ctx *ctx, uint64_t n, const uint64_t *byte_offsets
                           const uint8_t *bytes, uint64_t nbytes, uint32_t block, int container, byo_graph **out) {
   if (!ctx || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
+  if (!known_container(container))
     return set_error(ctx, BYO_EINVAL, "unknown container");
   return graph_from_bytepd_host(ctx, n, byte_offsets, degrees, bytes, nbytes, block ? block : 1000, container, out);
 }
@@ -192,7 +196,7 @@ int byo_graph_from_bytepd(byo_ctx *ctx, uint64_t n, const uint64_t *byte_offsets
 int byo_graph_read_bytepd(byo_ctx *ctx, const char *path, uint32_t block, int container, byo_graph **out) {
   if (!ctx || !path || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
+  if (!known_container(container))
     return set_error(ctx, BYO_EINVAL, "unknown container");
   return bytepd_read_file(ctx, path, block ? block : 1000, container, out);
 }
@@ -219,7 +223,7 @@ int byo_graph_write_adj(byo_graph *g, const char *path, int binary) {
 int byo_graph_generate(byo_ctx *ctx, int container, const byo_gen_spec *spec, byo_graph **out) {
   if (!ctx || !out) return BYO_EINVAL;
   *out = nullptr;
-  if (container != BYO_CONTAINER_CSR && container != BYO_CONTAINER_PMA && container != BYO_CONTAINER_VOS)
+  if (!known_container(container))
     return set_error(ctx, BYO_EINVAL, "unknown container");
   return graph_generate(ctx, container, spec, out);
 }
@@ -234,6 +238,7 @@ void byo_graph_destroy(byo_graph *g) {
   }
   for (auto &b : g->ws) free_buf(b);
   if (g->pma) pma_destroy(g->pma);
+  else if (g->pcsr) pcsr_destroy(g->pcsr);  // owns d_slots
   else if (g->d_slots) cudaFree(g->d_slots);
   if (g->vos) vos_destroy(g->vos);
   if (g->d_off) cudaFree(g->d_off);
@@ -311,8 +316,8 @@ static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int
   if (!g) return BYO_EINVAL;
   byo_ctx *ctx = g->ctx;
   if (changed) *changed = 0;
-  if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS)
-    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA or VOS container");
+  if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS && g->container != BYO_CONTAINER_PCSR)
+    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA, VOS or PCSR container");
   g->upd = UpdateStats{};
   if (count == 0) return BYO_OK;
   if (!keys) return set_error(ctx, BYO_EINVAL, "null keys");
@@ -324,6 +329,7 @@ static int update_common(byo_graph *g, const uint64_t *keys, uint64_t count, int
     d = buf;
   }
   if (g->container == BYO_CONTAINER_VOS) return vos_update(g, d, count, sorted, insert, changed);
+  if (g->container == BYO_CONTAINER_PCSR) return pcsr_update(g, d, count, sorted, insert, changed);
   return pma_update(g, d, count, sorted, insert, changed);
 }
 
@@ -332,8 +338,8 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
                                 const StreamQueries *qs = nullptr) {
   if (!g || (nbatch && (!h_offsets || !h_ops))) return BYO_EINVAL;
   byo_ctx *ctx = g->ctx;
-  if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS)
-    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA or VOS container");
+  if (g->container != BYO_CONTAINER_PMA && g->container != BYO_CONTAINER_VOS && g->container != BYO_CONTAINER_PCSR)
+    return set_error(ctx, BYO_ENOTSUP, "batch updates need the PMA, VOS or PCSR container");
   if (!nbatch) return BYO_OK;
   if (h_offsets[0] != 0) return set_error(ctx, BYO_EINVAL, "update stream: offsets[0] != 0");
   for (uint64_t b = 0; b < nbatch; b++)
@@ -375,11 +381,12 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
   BYO_CU(ctx, cudaMemcpyAsync(d_ops, ops.data(), nbatch, cudaMemcpyHostToDevice, ctx->stream));
   std::vector<long long> ch(nbatch);
   int rc = BYO_OK;
-  if (g->container == BYO_CONTAINER_VOS) {  // one update per batch
+  if (g->container != BYO_CONTAINER_PMA) {  // VOS, PCSR: one update per batch
     for (uint64_t b = 0; b < nbatch && rc == BYO_OK; b++) {
       uint64_t c = 0;
-      if (h_offsets[b + 1] > h_offsets[b])
-        rc = vos_update(g, d + h_offsets[b], h_offsets[b + 1] - h_offsets[b], 0, ops[b], &c);
+      const uint64_t len = h_offsets[b + 1] - h_offsets[b];
+      if (len && g->container == BYO_CONTAINER_VOS) rc = vos_update(g, d + h_offsets[b], len, 0, ops[b], &c);
+      else if (len) rc = pcsr_update(g, d + h_offsets[b], len, 0, ops[b], &c);
       ch[b] = (long long)c;
     }
   } else {
@@ -428,7 +435,9 @@ int byo_graph_last_update_stats(const byo_graph *g, byo_update_stats *out) {
   out->changed = g->upd.changed;
   out->touched_leaves = g->upd.leaves;
   out->touched_entries = g->upd.entries;
-  out->leaf_slots = g->container == BYO_CONTAINER_PMA ? pma_leaf_slots() : 0;
+  out->leaf_slots = g->container == BYO_CONTAINER_PMA    ? pma_leaf_slots()
+                    : g->container == BYO_CONTAINER_PCSR ? pcsr_leaf_slots()
+                                                         : 0;
   out->path = g->upd.path;
   return BYO_OK;
 }

@@ -213,6 +213,8 @@ int graph_from_sorted_keys(byo_ctx *ctx, int container, uint64_t n, const uint64
       rc = pma_build(g, d_keys, m);
     } else if (container == BYO_CONTAINER_VOS) {
       rc = vos_build(g, d_keys, m);
+    } else if (container == BYO_CONTAINER_PCSR) {
+      rc = pcsr_build(g, d_keys, m);
     } else {
       // 16 ids of padding: bulk copies of a slot run round its end up to 16 bytes
       cudaError_t e = cudaMalloc(&g->d_slots, (m + 16) * sizeof(uint32_t));

@@ -31,6 +31,7 @@ struct DevBuf {
 
 struct Pma;  // pma.cu
 struct Vos;  // vos.cu
+struct Pcsr; // pcsr.cu
 struct Mlp;  // mlp.cu
 
 }  // namespace byo
@@ -82,6 +83,7 @@ struct byo_graph {
   uint32_t *d_deg = nullptr;
   byo::Pma *pma = nullptr;
   byo::Vos *vos = nullptr;  // vector of per-vertex runs (BYO_CONTAINER_VOS)
+  byo::Pcsr *pcsr = nullptr;  // packed CSR (BYO_CONTAINER_PCSR); d_off is its vertex index
   byo::DevBuf ws[24];  // per-graph workspaces, indexed by the Ws enum
   byo_tuning tune = {};  // launch shapes set by the caller or the autotuner (0 = automatic)
   // A PMA keeps a compact CSR snapshot of its contents for the read-only
@@ -269,6 +271,11 @@ int vos_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);
 int vos_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert, uint64_t *changed);
 int vos_compact(byo_graph *g, const uint64_t *offc, uint32_t *out);
 void vos_destroy(Vos *v);
+int pcsr_build(byo_graph *g, const uint64_t *d_keys, uint64_t m);
+int pcsr_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert, uint64_t *changed);
+int pcsr_compact(byo_graph *g, uint32_t *out);
+uint64_t pcsr_leaf_slots();
+void pcsr_destroy(Pcsr *p);
 // Query ops of a mixed stream (ops[b] == 2): k sources per query, taken in
 // order from h_srcs; query q writes its levels to d_levels + q * k * n;
 // h_op_ns (may be null) receives each op's device start and end times.

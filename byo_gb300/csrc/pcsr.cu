@@ -1,0 +1,631 @@
+// pcsr.cu -- the Packed CSR container (BYO_CONTAINER_PCSR): the layout of
+// the reference's PCSR target (benchmarks/run_structures/run_pcsr.cc:24-99;
+// its PCSR class lives in the un-vendored Packed-Memory-Array submodule and
+// follows the published Packed CSR of Wheatman & Xu, HPEC 2018).
+//
+// One packed array holds, in vertex order, a sentinel for every vertex
+// followed by its sorted neighbours.  The array is cut into leaves of kPL
+// slots, each left-packed with its slack at the end, and kept within density
+// bounds the way a packed-memory array is: a leaf that would overflow has the
+// smallest aligned window of leaves around it redistributed evenly, and the
+// whole array is laid out again when even the root is too dense (or, after a
+// remove, too sparse).  A slot holds a neighbour id or kSentinel: a vertex's
+// sentinel slot reads kSentinel too, and one bit per slot (head) marks the
+// sentinels.  vbeg[v] is the slot of v's sentinel and is the container's
+// d_off: v's slot range [vbeg[v], vbeg[v+1]) is its sentinel, its neighbours
+// and gaps, so the gapped view needs no rebuild after an update.  4 bytes per
+// slot and a bit, against the PMA container's 8 (src and dst per slot).
+//
+// Elements are ordered by a composite key: (v << 33) for v's sentinel and
+// (v << 33) | (w + 1) for the edge (v, w).  Every leaf keeps the vertex that
+// owns its first element (lv) and a routing separator (sep): every element of
+// leaf j lies in [sep[j], sep[j+1]).  The owner of any element is lv plus the
+// sentinels before it in the leaf, so leaves decode independently.
+//
+// A batch is validated, sorted and deduplicated on the device, turned into
+// composite keys and routed to leaves by sep; a warp per touched leaf decodes
+// it into shared memory, ranks each batch key in it and scatters the merged
+// sequence back in place when it fits, moving the sentinels' vbeg with them
+// and the degrees by atomics.  A leaf that would overflow leaves its merged
+// sequence in an overflow area for the windowed redistribution.
+#include <algorithm>
+#include <cmath>
+
+#include "device.cuh"
+#include "internal.h"
+
+namespace byo {
+
+constexpr uint32_t kPL = 512;       // slots per leaf
+constexpr uint32_t kPW = kPL / 32;  // head words per leaf
+constexpr double kPBuild = 0.70;    // density of a fresh layout
+constexpr double kPRootMax = 0.90;  // upper density bound at the root (1.0 at a leaf)
+constexpr double kPRootMin = 0.25;  // a remove below this lays the array out smaller
+constexpr uint64_t kCkMask = (1ull << 33) - 1;
+constexpr uint32_t kNoWindow = 0xFFFFFFFFu;
+constexpr int kPcsrWarps = 4;  // warps per CTA of the merge (40 KB of shared memory)
+
+struct Pcsr {
+  uint64_t NL = 0;
+  int H = 0;
+  uint32_t *slots = nullptr, *head = nullptr, *cnt = nullptr, *lv = nullptr;
+  uint64_t *sep = nullptr;
+  DevBuf keys_a, keys_b, ck, bstart, rcount, rpre, marks, win, staging, ovf, ovf_off, misc;
+  uint64_t rebuilds = 0, windows = 0;
+};
+
+__host__ __device__ __forceinline__ uint64_t ck_sent(uint64_t v) { return v << 33; }
+__host__ __device__ __forceinline__ uint64_t ck_edge(uint64_t v, uint64_t w) { return (v << 33) | (w + 1); }
+__device__ __forceinline__ bool ck_is_sent(uint64_t k) { return (k & kCkMask) == 0; }
+
+__host__ __device__ __forceinline__ double pcsr_bound(int h, int H) {
+  return H == 0 ? kPRootMax : 1.0 - (1.0 - kPRootMax) * (double)h / (double)H;
+}
+
+static int ceil_log2_u64(uint64_t x) {
+  int h = 0;
+  while ((1ull << h) < x) h++;
+  return h;
+}
+
+static uint64_t pcsr_leaves_for(uint64_t elems) {
+  const uint64_t nl = (uint64_t)std::ceil((double)elems / (kPBuild * kPL));
+  return nl ? nl : 1;
+}
+
+// ---------------------------------------------------------------- decode / encode
+
+// Sentinel counts of leaf j's head words, one word per lane (lanes >= kPW
+// hold 0): the word, its exclusive prefix and whether slot 0 is a sentinel.
+struct HeadScan {
+  uint32_t word, before, first;
+};
+
+__device__ __forceinline__ HeadScan head_scan(const uint32_t *__restrict__ head, uint64_t j) {
+  const unsigned lane = lane_id();
+  const uint32_t hw = lane < kPW ? head[j * kPW + lane] : 0u;
+  const uint32_t pc = __popc(hw);
+  const uint32_t incl = warp_inclusive_scan(pc);
+  return HeadScan{hw, incl - pc, __shfl_sync(kFull, hw, 0) & 1u};
+}
+
+// Owner and sentinel bit of slot i of a leaf from its head scan; every lane
+// of the warp calls it (the shuffles read word i / 32).
+__device__ __forceinline__ uint64_t slot_owner(const HeadScan &hs, uint32_t lv0, uint32_t i, bool &sent) {
+  const uint32_t w = (i >> 5) & 31u;
+  const uint32_t word = __shfl_sync(kFull, hs.word, w);
+  const uint32_t before = __shfl_sync(kFull, hs.before, w);
+  sent = (word >> (i & 31)) & 1u;
+  const uint32_t s_incl = before + __popc(word & (0xFFFFFFFFu >> (31 - (i & 31))));
+  return (uint64_t)lv0 + s_incl - hs.first;
+}
+
+// Composite keys of leaf j's c elements into A; a warp.
+__device__ __forceinline__ void pcsr_decode_leaf(const uint32_t *__restrict__ slots, const uint32_t *__restrict__ head,
+                                                 uint64_t j, uint32_t c, uint32_t lv0, uint64_t *A) {
+  const HeadScan hs = head_scan(head, j);
+  for (uint32_t base = 0; base < c; base += 32) {
+    const uint32_t i = base + lane_id();
+    bool sent;
+    const uint64_t owner = slot_owner(hs, lv0, i, sent);
+    if (i < c) A[i] = sent ? ck_sent(owner) : ck_edge(owner, slots[j * kPL + i]);
+  }
+}
+
+// Writes n_el composite keys E[0..) into leaf j (left-packed, the rest gaps):
+// slots, head words, cnt, lv and the vbeg of every sentinel; a warp.  The
+// separator is the caller's.
+__device__ __forceinline__ void pcsr_encode_leaf(uint32_t *slots, uint32_t *head, uint32_t *cnt, uint32_t *lv,
+                                                 uint64_t *vbeg, uint64_t j, const uint64_t *E, uint32_t n_el) {
+  const unsigned lane = lane_id();
+  for (uint32_t base = 0; base < kPL; base += 32) {
+    const uint32_t i = base + lane;
+    bool s = false;
+    uint32_t val = kSentinel;
+    if (i < n_el) {
+      const uint64_t k = E[i];
+      s = ck_is_sent(k);
+      if (s) vbeg[k >> 33] = j * kPL + i;
+      else val = (uint32_t)((k & kCkMask) - 1);
+    }
+    slots[j * kPL + i] = val;
+    const unsigned b = __ballot_sync(kFull, s);
+    if (lane == 0) head[j * kPW + (base >> 5)] = b;
+  }
+  if (lane == 0) {
+    cnt[j] = n_el;
+    lv[j] = n_el ? (uint32_t)(E[0] >> 33) : 0u;
+  }
+}
+
+// ---------------------------------------------------------------- build
+
+// Elements of a CSR (keys src << 32 | dst, sorted; off its offsets): v's
+// sentinel at off[v] + v, edge i of source u at i + u + 1.
+__global__ void k_pcsr_elems(const uint64_t *__restrict__ keys, uint64_t m, const uint64_t *__restrict__ off,
+                             uint64_t n, uint64_t *out) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nthr = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t v = tid; v < n; v += nthr) out[off[v] + v] = ck_sent(v);
+  for (uint64_t i = tid; i < m; i += nthr) {
+    const uint64_t k = keys[i], u = k >> 32;
+    out[i + u + 1] = ck_edge(u, k & 0xFFFFFFFFull);
+  }
+}
+
+// Each window's staged elements spread evenly over its leaves; a warp per
+// leaf.  Window mode (all = 0): leaf j with level h = lvl[j] belongs to the
+// aligned window [a, e) of 2^h leaves, whose elements are
+// stage[rpre[a] .. rpre[e]); its first leaf keeps its separator.  Layout mode
+// (all = 1): one window over all NL leaves holding stage[0 .. total).
+__global__ void __launch_bounds__(256) k_pcsr_spread(const uint64_t *__restrict__ stage, const uint64_t *__restrict__ rpre,
+                                                     const uint32_t *__restrict__ lvl, uint64_t NL, int all,
+                                                     uint64_t total, uint32_t *slots, uint32_t *head, uint32_t *cnt,
+                                                     uint32_t *lv, uint64_t *sep, uint64_t *vbeg) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    uint64_t a = 0, e = NL, s0 = 0, T = total;
+    if (!all) {
+      const uint32_t h = lvl[j];
+      if (h == kNoWindow) continue;
+      a = (j >> h) << h;
+      e = a + (1ull << h);
+      if (e > NL) e = NL;
+      s0 = rpre[a];
+      T = rpre[e] - s0;
+    }
+    const uint64_t k = j - a, width = e - a;
+    const uint64_t lo = T * k / width, hi = T * (k + 1) / width;
+    pcsr_encode_leaf(slots, head, cnt, lv, vbeg, j, stage + s0 + lo, (uint32_t)(hi - lo));
+    if (lane_id() == 0) {
+      if (all && k == 0) {
+        sep[j] = 0;
+      } else if (k > 0) {
+        uint64_t s = ~0ull;  // an empty leaf takes the next element's key
+        if (hi > lo) s = stage[s0 + lo];
+        else if (hi < T) s = stage[s0 + hi];
+        else if (!all && e < NL) s = sep[e];  // the next window's first leaf keeps its separator
+        sep[j] = s;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+static int pcsr_alloc(byo_ctx *ctx, Pcsr *p, uint64_t NL) {
+  uint32_t *slots = nullptr, *head = nullptr, *cnt = nullptr, *lv = nullptr;
+  uint64_t *sep = nullptr;
+  cudaError_t e = cudaMalloc(&slots, NL * kPL * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&head, NL * kPW * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&cnt, NL * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&lv, NL * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&sep, (NL + 1) * 8);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(slots);
+    cudaFree(head);
+    cudaFree(cnt);
+    cudaFree(lv);
+    cudaFree(sep);
+    return set_error(ctx, BYO_ENOMEM, "pcsr: leaves", e);
+  }
+  cudaFree(p->slots);
+  cudaFree(p->head);
+  cudaFree(p->cnt);
+  cudaFree(p->lv);
+  cudaFree(p->sep);
+  p->slots = slots;
+  p->head = head;
+  p->cnt = cnt;
+  p->lv = lv;
+  p->sep = sep;
+  p->NL = NL;
+  p->H = ceil_log2_u64(NL);
+  return BYO_OK;
+}
+
+// Lays the E sorted elements in `elems` out over NL new leaves.
+static int pcsr_layout(byo_graph *g, const uint64_t *elems, uint64_t E, uint64_t NL) {
+  byo_ctx *ctx = g->ctx;
+  Pcsr *p = g->pcsr;
+  BYO_TRY(pcsr_alloc(ctx, p, NL));
+  g->d_slots = p->slots;
+  g->nslots = NL * kPL;
+  launch(ctx, k_pcsr_spread, dim3(grid_for(ctx, NL * 32, 256)), dim3(256), 0, elems, (const uint64_t *)nullptr,
+         (const uint32_t *)nullptr, NL, 1, E, p->slots, p->head, p->cnt, p->lv, p->sep, g->d_off);
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  h[0] = NL * kPL;
+  BYO_CU(ctx, cudaMemcpyAsync(g->d_off + g->n, h, 8, cudaMemcpyHostToDevice, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));  // the pinned word is reused
+  return check_launch(ctx, "pcsr_layout");
+}
+
+int pcsr_build(byo_graph *g, const uint64_t *d_keys, uint64_t m) {
+  byo_ctx *ctx = g->ctx;
+  if (g->n >= (1ull << 31)) return set_error(ctx, BYO_EINVAL, "pcsr: n must be below 2^31");
+  g->pcsr = new Pcsr();
+  Pcsr *p = g->pcsr;
+  const uint64_t n = g->n, E = n + m;
+  BYO_TRY(offsets_from_keys(ctx, d_keys, m, n, g->d_off));  // the CSR's offsets give the element ranks
+  BYO_TRY(degrees_from_offsets(ctx, g->d_off, n, g->d_deg));
+  BYO_TRY(ensure(ctx, p->staging, (E ? E : 1) * 8));
+  uint64_t *el = (uint64_t *)p->staging.p;
+  launch(ctx, k_pcsr_elems, dim3(grid_for(ctx, std::max(n, m), 256)), dim3(256), 0, d_keys, m,
+         (const uint64_t *)g->d_off, n, el);
+  return pcsr_layout(g, el, E, pcsr_leaves_for(E));
+}
+
+void pcsr_destroy(Pcsr *p) {
+  if (!p) return;
+  cudaFree(p->slots);
+  cudaFree(p->head);
+  cudaFree(p->cnt);
+  cudaFree(p->lv);
+  cudaFree(p->sep);
+  for (DevBuf *b : {&p->keys_a, &p->keys_b, &p->ck, &p->bstart, &p->rcount, &p->rpre, &p->marks, &p->win,
+                    &p->staging, &p->ovf, &p->ovf_off, &p->misc})
+    free_buf(*b);
+  delete p;
+}
+
+uint64_t pcsr_leaf_slots() { return kPL; }
+
+// ---------------------------------------------------------------- snapshot
+
+// The compact CSR of the contents: the edge element of global rank e
+// (epre[j] + its index in leaf j) owned by u goes to out[e - u - 1], since
+// u's sentinel has rank u + offc[u] and its k-th edge rank u + offc[u] + 1 + k.
+__global__ void __launch_bounds__(256) k_pcsr_compact(const uint32_t *__restrict__ slots,
+                                                      const uint32_t *__restrict__ head,
+                                                      const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ lv,
+                                                      const uint64_t *__restrict__ epre, uint64_t NL, uint64_t m,
+                                                      uint32_t *out) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    const uint32_t c = cnt[j];
+    if (!c) continue;
+    const HeadScan hs = head_scan(head, j);
+    const uint64_t e0 = epre[j];
+    const uint32_t l0 = lv[j];
+    for (uint32_t base = 0; base < c; base += 32) {
+      const uint32_t i = base + lane_id();
+      bool sent;
+      const uint64_t owner = slot_owner(hs, l0, i, sent);
+      const uint64_t at = e0 + i - owner - 1;
+      if (i < c && !sent && at < m) out[at] = slots[j * kPL + i];
+    }
+  }
+}
+
+int pcsr_compact(byo_graph *g, uint32_t *out) {
+  byo_ctx *ctx = g->ctx;
+  Pcsr *p = g->pcsr;
+  BYO_TRY(ensure(ctx, p->rpre, (p->NL + 1) * 8));
+  uint64_t *epre = (uint64_t *)p->rpre.p;
+  BYO_TRY(scan_u32_to_u64(ctx, p->cnt, p->NL, epre));
+  launch_t(ctx, "pcsr_compact", k_pcsr_compact, dim3(grid_for(ctx, p->NL * 32, 256, 16)), dim3(256), 0,
+           (const uint32_t *)p->slots, (const uint32_t *)p->head, (const uint32_t *)p->cnt, (const uint32_t *)p->lv,
+           (const uint64_t *)epre, p->NL, g->m, out);
+  return check_launch(ctx, "pcsr_compact");
+}
+
+// ---------------------------------------------------------------- update
+
+// flags[0]: a key with src or dst >= n; flags[1]: `sorted` input not
+// strictly increasing.
+__global__ void k_pcsr_check(const uint64_t *__restrict__ keys, uint64_t b, uint64_t n, int sorted,
+                             unsigned int *flags) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < b; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[i];
+    if ((k >> 32) >= n || (k & 0xFFFFFFFFull) >= n) atomicOr(flags, 1u);
+    if (sorted && i > 0 && keys[i - 1] >= k) atomicOr(flags + 1, 1u);
+  }
+}
+
+__global__ void k_pcsr_keys(const uint64_t *__restrict__ keys, uint64_t b, uint64_t *ck) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < b; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[i];
+    ck[i] = ck_edge(k >> 32, k & 0xFFFFFFFFull);
+  }
+}
+
+// bstart[j] = first batch key >= sep[j]; bstart[0] = 0, bstart[NL] = b.
+__global__ void k_pcsr_route(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ ck, uint64_t b,
+                             uint64_t *bstart) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j <= NL; j += (uint64_t)gridDim.x * blockDim.x) {
+    if (j == 0 || j == NL) {
+      bstart[j] = j ? b : 0;
+      continue;
+    }
+    const uint64_t s = sep[j];
+    uint64_t lo = 0, hi = b;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (ck[mid] < s) lo = mid + 1;
+      else hi = mid;
+    }
+    bstart[j] = lo;
+  }
+}
+
+// Rank of x in A[0..c) (lower bound).
+__device__ __forceinline__ uint32_t rank_in(const uint64_t *A, uint32_t c, uint64_t x) {
+  uint32_t l = 0, hi = c;
+  while (l < hi) {
+    const uint32_t mid = (l + hi) >> 1;
+    if (A[mid] < x) l = mid + 1;
+    else hi = mid;
+  }
+  return l;
+}
+
+// A warp per leaf with batch keys: the leaf decoded into A, each batch key
+// ranked in A, the merged sequence scattered to O (shared) and written back
+// in place or, when it does not fit the leaf, to the overflow area.
+// Every output position comes from ranks:
+//   insert: A[i] moves by the kept batch keys of rank <= i (a scan of D, the
+//           kept keys per rank); kept key x of rank l lands at l + the kept
+//           keys before it
+//   remove: A[i] moves back by the removed keys before it.
+// ctr: [0] overflow cursor, [1] overflowing leaves, [2] change of the edge
+// count, [3] leaves merged, [4] elements they held.
+__global__ void __launch_bounds__(32 * kPcsrWarps) k_pcsr_merge(
+    uint32_t *slots, uint32_t *head, uint32_t *cnt, uint32_t *lv, uint64_t NL, const uint64_t *__restrict__ ck,
+    const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
+    unsigned long long *ctr, uint32_t *deg, uint64_t *vbeg) {
+  __shared__ uint64_t As[kPcsrWarps][kPL];
+  __shared__ uint64_t Os[kPcsrWarps][kPL];
+  __shared__ uint32_t Ds[kPcsrWarps][kPL + 1];
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  uint64_t *A = As[w], *O = Os[w];
+  uint32_t *D = Ds[w];
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  long long dsum = 0;
+  unsigned long long nleaves = 0, nentries = 0;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
+    const uint32_t c = min(cnt[j], kPL);
+    if (b0 == b1) {
+      if (lane == 0) rcount[j] = c;
+      continue;
+    }
+    nleaves++;
+    nentries += c;
+    pcsr_decode_leaf(slots, head, j, c, lv[j], A);
+    for (uint32_t i = lane; i <= c; i += 32) D[i] = 0;
+    __syncwarp();
+    uint32_t changed = 0;
+    for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
+      const uint64_t t = t0 + lane;
+      bool act = false;
+      if (t < b1) {
+        const uint64_t x = ck[t];
+        const uint32_t l = rank_in(A, c, x);
+        const bool present = l < c && A[l] == x;
+        act = insert ? !present : present;
+        if (act) {
+          if (insert) atomicAdd(D + l, 1u);
+          else D[l] = 1u;
+          atomicAdd(deg + (x >> 33), insert ? 1u : 0xFFFFFFFFu);
+        }
+      }
+      changed += __popc(__ballot_sync(kFull, act));
+    }
+    __syncwarp();
+    const uint32_t r = insert ? c + changed : c - changed;
+    dsum += insert ? (long long)changed : -(long long)changed;
+    uint64_t *dstp = O;
+    if (r > kPL) {
+      unsigned long long at = 0;
+      if (lane == 0) {
+        at = atomicAdd(&ctr[0], (unsigned long long)r);
+        atomicAdd(&ctr[1], 1ull);
+        ovf_off[j] = at;
+      }
+      at = __shfl_sync(kFull, at, 0);
+      dstp = ovf + at;
+    }
+    if (insert) {
+      uint32_t carry = 0;
+      for (uint32_t i0 = 0; i0 <= c; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const uint32_t inc = warp_inclusive_scan(i <= c ? D[i] : 0u) + carry;
+        if (i < c) dstp[i + inc] = A[i];
+        carry = __shfl_sync(kFull, inc, 31);
+      }
+      uint32_t kept_before = 0;
+      for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
+        const uint64_t t = t0 + lane;
+        bool keep = false;
+        uint32_t l = 0;
+        uint64_t x = 0;
+        if (t < b1) {
+          x = ck[t];
+          l = rank_in(A, c, x);
+          keep = !(l < c && A[l] == x);
+        }
+        const unsigned mk = __ballot_sync(kFull, keep);
+        if (keep) dstp[l + kept_before + __popc(mk & lanemask_lt())] = x;
+        kept_before += __popc(mk);
+      }
+    } else {
+      uint32_t removed = 0;
+      for (uint32_t i0 = 0; i0 < c; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const bool gone = i < c && D[i];
+        const unsigned mg = __ballot_sync(kFull, gone);
+        if (i < c && !gone) dstp[i - removed - __popc(mg & lanemask_lt())] = A[i];
+        removed += __popc(mg);
+      }
+    }
+    __syncwarp();
+    // in place: the separator stays, every key routed here is >= it
+    if (r <= kPL) pcsr_encode_leaf(slots, head, cnt, lv, vbeg, j, O, r);
+    if (lane == 0) rcount[j] = r;
+    __syncwarp();
+  }
+  if (lane == 0) {
+    if (dsum) atomicAdd(&ctr[2], (unsigned long long)dsum);
+    if (nleaves) {
+      atomicAdd(&ctr[3], nleaves);
+      atomicAdd(&ctr[4], nentries);
+    }
+  }
+}
+
+// For each overflowing leaf the smallest aligned window within its density
+// bound: marks[h * NL + index] = 1; *grow when even the root is too dense.
+__global__ void k_pcsr_windows(const uint32_t *__restrict__ rcount, const uint64_t *__restrict__ rpre, uint64_t NL,
+                               int H, uint8_t *marks, unsigned int *grow) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < NL; j += (uint64_t)gridDim.x * blockDim.x) {
+    if (rcount[j] <= kPL) continue;
+    bool found = false;
+    for (int h = 1; h <= H && !found; h++) {
+      const uint64_t a = (j >> h) << h;
+      uint64_t e = a + (1ull << h);
+      if (e > NL) e = NL;
+      if ((double)(rpre[e] - rpre[a]) <= pcsr_bound(h, H) * (double)(e - a) * kPL) {
+        marks[(uint64_t)h * NL + (j >> h)] = 1;
+        found = true;
+      }
+    }
+    if (!found) atomicOr(grow, 1u);
+  }
+}
+
+// Level of every leaf's window: the highest marked ancestor (kNoWindow if none).
+__global__ void k_pcsr_cover(const uint8_t *__restrict__ marks, uint64_t NL, int H, uint32_t *lvl) {
+  for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < NL; j += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t code = kNoWindow;
+    for (int h = H; h >= 1; h--)
+      if (marks[(uint64_t)h * NL + (j >> h)]) {
+        code = (uint32_t)h;
+        break;
+      }
+    lvl[j] = code;
+  }
+}
+
+// The elements of every leaf in a window (every leaf when lvl is null) as
+// composite keys at stage[rpre[j] ...]: from the overflow area for a leaf
+// that overflowed, decoded from the leaf otherwise.  A warp per leaf.
+__global__ void __launch_bounds__(256) k_pcsr_gather(const uint32_t *__restrict__ slots,
+                                                     const uint32_t *__restrict__ head,
+                                                     const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ lv,
+                                                     const uint32_t *__restrict__ rcount,
+                                                     const uint64_t *__restrict__ rpre, const uint64_t *__restrict__ ovf,
+                                                     const uint64_t *__restrict__ ovf_off,
+                                                     const uint32_t *__restrict__ lvl, uint64_t NL, uint64_t *stage) {
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    if (lvl && lvl[j] == kNoWindow) continue;
+    const uint32_t r = rcount[j];
+    uint64_t *out = stage + rpre[j];
+    if (r > kPL) {
+      const uint64_t *src = ovf + ovf_off[j];
+      for (uint32_t i = lane_id(); i < r; i += 32) out[i] = src[i];
+    } else {
+      pcsr_decode_leaf(slots, head, j, r, lv[j], out);
+    }
+  }
+}
+
+int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sorted, int insert,
+                uint64_t *changed) {
+  byo_ctx *ctx = g->ctx;
+  Pcsr *p = g->pcsr;
+  if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PCSR container");
+  g->version++;  // any snapshot of the contents is stale from here on
+  const uint64_t n = g->n, m_before = g->m;
+  // 1. validate, then sort and deduplicate
+  BYO_TRY(ensure(ctx, p->keys_a, count * 8));
+  BYO_TRY(ensure(ctx, p->keys_b, count * 8));
+  BYO_TRY(ensure(ctx, p->ck, count * 8));
+  BYO_TRY(ensure(ctx, p->misc, 128));
+  uint64_t *ka = (uint64_t *)p->keys_a.p, *kb = (uint64_t *)p->keys_b.p, *ck = (uint64_t *)p->ck.p;
+  unsigned long long *ctr = (unsigned long long *)p->misc.p;  // [0..4] merge counters
+  unsigned int *flags = (unsigned int *)(ctr + 8);            // [0] range, [1] order, [2] grow
+  BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 128, ctx->stream));
+  launch(ctx, k_pcsr_check, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, n, sorted, flags);
+  uint64_t *h = nullptr;
+  BYO_TRY(pinned(ctx, 4096, (void **)&h));
+  BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const unsigned int *hf = (const unsigned int *)h;
+  if (hf[0]) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+  if (hf[1]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  const uint64_t *batch = d_keys_in;
+  uint64_t b = count;
+  if (!sorted) {
+    BYO_TRY(sort_bucketed(ctx, d_keys_in, count, n, ka, kb));
+    BYO_TRY(unique_u64(ctx, ka, count, 0, kb, &b));
+    batch = kb;
+  }
+  launch(ctx, k_pcsr_keys, dim3(grid_for(ctx, b, 256)), dim3(256), 0, batch, b, ck);
+  // 2. route and merge
+  const uint64_t NL = p->NL;
+  BYO_TRY(ensure(ctx, p->bstart, (NL + 1) * 8));
+  BYO_TRY(ensure(ctx, p->rcount, NL * 4));
+  BYO_TRY(ensure(ctx, p->rpre, (NL + 1) * 8));
+  BYO_TRY(ensure(ctx, p->ovf, (n + m_before + b + 1) * 8));  // the merged leaves hold at most every element
+  BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
+  uint64_t *bstart = (uint64_t *)p->bstart.p, *rpre = (uint64_t *)p->rpre.p;
+  uint32_t *rcount = (uint32_t *)p->rcount.p;
+  launch(ctx, k_pcsr_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
+         (const uint64_t *)ck, b, bstart);
+  launch_t(ctx, "pcsr_merge", k_pcsr_merge, dim3(grid_for(ctx, NL * 32, 32 * kPcsrWarps, 5)),
+           dim3(32 * kPcsrWarps), 0, p->slots, p->head, p->cnt, p->lv, NL, (const uint64_t *)ck,
+           (const uint64_t *)bstart, insert, rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, g->d_deg,
+           g->d_off);
+  BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 40, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  const uint64_t novf = h[1], merged_leaves = h[3], merged_entries = h[4];
+  const uint64_t m_after = (uint64_t)((long long)m_before + (long long)h[2]);
+  g->m = m_after;
+  const uint64_t ch = insert ? m_after - m_before : m_before - m_after;
+  if (changed) *changed = ch;
+  const uint64_t total = n + m_after;
+  const bool shrink = !insert && NL > 1 && (double)total < kPRootMin * (double)NL * kPL;
+  g->upd = UpdateStats{b, ch, merged_leaves, merged_entries, (novf || shrink) ? 2u : 0u};
+  if (novf == 0 && !shrink) return check_launch(ctx, "pcsr_update");
+  // 3. redistribution: windows over the counts after the merge, or a new
+  // layout when the root is out of bounds
+  BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
+  BYO_TRY(ensure(ctx, p->staging, (total ? total : 1) * 8));
+  BYO_TRY(ensure(ctx, p->win, NL * 4));
+  uint64_t *stg = (uint64_t *)p->staging.p;
+  uint32_t *lvl = (uint32_t *)p->win.p;
+  bool rebuild = shrink || (double)total > kPRootMax * (double)NL * kPL;
+  if (!rebuild) {
+    BYO_TRY(ensure(ctx, p->marks, (uint64_t)(p->H + 1) * NL));
+    uint8_t *marks = (uint8_t *)p->marks.p;
+    BYO_CU(ctx, cudaMemsetAsync(marks, 0, (uint64_t)(p->H + 1) * NL, ctx->stream));
+    launch(ctx, k_pcsr_windows, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint32_t *)rcount,
+           (const uint64_t *)rpre, NL, p->H, marks, flags + 2);
+    BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+    rebuild = hf[2] != 0;
+    if (!rebuild)
+      launch(ctx, k_pcsr_cover, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint8_t *)marks, NL, p->H, lvl);
+  }
+  launch(ctx, k_pcsr_gather, dim3(grid_for(ctx, NL * 32, 256, 16)), dim3(256), 0, (const uint32_t *)p->slots,
+         (const uint32_t *)p->head, (const uint32_t *)p->cnt, (const uint32_t *)p->lv, (const uint32_t *)rcount,
+         (const uint64_t *)rpre, (const uint64_t *)p->ovf.p, (const uint64_t *)p->ovf_off.p,
+         rebuild ? (const uint32_t *)nullptr : (const uint32_t *)lvl, NL, stg);
+  BYO_TRY(check_launch(ctx, "pcsr_gather"));
+  if (rebuild) {
+    p->rebuilds++;
+    return pcsr_layout(g, stg, total, pcsr_leaves_for(total));
+  }
+  p->windows++;
+  launch_t(ctx, "pcsr_redistribute", k_pcsr_spread, dim3(grid_for(ctx, NL * 32, 256, 16)), dim3(256), 0,
+           (const uint64_t *)stg, (const uint64_t *)rpre, (const uint32_t *)lvl, NL, 0, total, p->slots, p->head,
+           p->cnt, p->lv, p->sep, g->d_off);
+  return check_launch(ctx, "pcsr_update");
+}
+
+}  // namespace byo

@@ -1216,7 +1216,9 @@ int pma_compact(byo_graph *g, uint32_t *out) {
 
 int traversal_view(byo_graph *g, byo_graph **out) {
   *out = g;
-  if (!(g->container == BYO_CONTAINER_PMA && g->pma) && !(g->container == BYO_CONTAINER_VOS && g->vos)) return BYO_OK;
+  if (!(g->container == BYO_CONTAINER_PMA && g->pma) && !(g->container == BYO_CONTAINER_VOS && g->vos) &&
+      !(g->container == BYO_CONTAINER_PCSR && g->pcsr))
+    return BYO_OK;
   byo_ctx *ctx = g->ctx;
   byo_graph *s = g->snap;
   if (!s) {
@@ -1249,6 +1251,7 @@ int traversal_view(byo_graph *g, byo_graph **out) {
   s->d_deg = g->d_deg;
   BYO_TRY(scan_u32_to_u64(ctx, g->d_deg, g->n, s->d_off));
   if (g->pma) BYO_TRY(pma_compact(g, s->d_slots));
+  else if (g->pcsr) BYO_TRY(pcsr_compact(g, s->d_slots));
   else BYO_TRY(vos_compact(g, s->d_off, s->d_slots));
   g->snap_version = g->version;
   *out = s;

@@ -107,11 +107,13 @@ class Context:
 
 
 def _container(name):
-    """csr (static), pma (packed-memory array, CPMA / PMA_graph) or vos (vector
-    of per-vertex sorted runs, the vector-of-sets containers)."""
-    table = {"csr": _abi.CONTAINER_CSR, "pma": _abi.CONTAINER_PMA, "vos": _abi.CONTAINER_VOS}
+    """csr (static), pma (packed-memory array, CPMA / PMA_graph), vos (vector
+    of per-vertex sorted runs, the vector-of-sets containers) or pcsr (Packed
+    CSR: per-vertex sentinels and neighbour ids in one packed array)."""
+    table = {"csr": _abi.CONTAINER_CSR, "pma": _abi.CONTAINER_PMA, "vos": _abi.CONTAINER_VOS,
+             "pcsr": _abi.CONTAINER_PCSR}
     if name not in table:
-        raise ValueError("container must be csr, pma or vos")
+        raise ValueError("container must be csr, pma, vos or pcsr")
     return table[name]
 
 
@@ -191,7 +193,8 @@ class Graph:
 
     @property
     def container(self):
-        return {_abi.CONTAINER_PMA: "pma", _abi.CONTAINER_VOS: "vos"}.get(lib().byo_graph_container(self.h), "csr")
+        names = {_abi.CONTAINER_PMA: "pma", _abi.CONTAINER_VOS: "vos", _abi.CONTAINER_PCSR: "pcsr"}
+        return names.get(lib().byo_graph_container(self.h), "csr")
 
     def degrees(self):
         out = np.empty(self.N(), np.uint32)

@@ -83,10 +83,18 @@ int byo_buffer_fill32(byo_ctx *ctx, void *d, uint64_t offset, uint64_t count, ui
  * run_single_pma.cc:75-89 consume it): offsets[n+1] and nbrs[m], sorted and
  * duplicate-free per vertex.  The arrays are copied; the caller keeps them. */
 /* CSR (static), PMA (one packed-memory array of src << 32 | dst keys, the
- * CPMA / PMA_graph counterpart) and VOS (a vector of per-vertex sorted runs
+ * CPMA / PMA_graph counterpart), VOS (a vector of per-vertex sorted runs
  * with slack, the counterpart of the vector-of-sets containers,
- * run_vector_pma.cc / run_vector_vector.cc).  PMA and VOS take updates. */
-enum byo_container { BYO_CONTAINER_CSR = 0, BYO_CONTAINER_PMA = 1, BYO_CONTAINER_VOS = 2 };
+ * run_vector_pma.cc / run_vector_vector.cc) and PCSR (the Packed CSR of
+ * run_pcsr.cc:24-99: one packed array of per-vertex sentinels and neighbour
+ * ids, 4 bytes a slot, with the vertex index kept up to date by the updates;
+ * n below 2^31).  PMA, VOS and PCSR take updates. */
+enum byo_container {
+  BYO_CONTAINER_CSR = 0,
+  BYO_CONTAINER_PMA = 1,
+  BYO_CONTAINER_VOS = 2,
+  BYO_CONTAINER_PCSR = 3
+};
 
 int byo_graph_create_csr(byo_ctx *ctx, uint64_t n, uint64_t m, const uint64_t *h_offsets,
                          const uint32_t *h_nbrs, byo_graph **out);
@@ -119,7 +127,7 @@ int byo_graph_neighbors(byo_graph *g, uint32_t v, uint32_t *h_out, uint64_t cap,
  * must be strictly increasing).  Inserting a present key and removing an
  * absent key are no-ops.  Keys with src or dst >= n are rejected (BYO_EINVAL).
  * *changed (may be NULL) receives the number of keys actually inserted or
- * removed.  Only BYO_CONTAINER_PMA supports updates (CSR: BYO_ENOTSUP). */
+ * removed.  The PMA, VOS and PCSR containers take updates (CSR: BYO_ENOTSUP). */
 int byo_graph_insert_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
                            uint64_t *changed);
 int byo_graph_remove_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,

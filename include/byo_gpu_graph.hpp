@@ -240,13 +240,22 @@ class GPU_VOS_graph : public GPU_PMA_graph<W> {
       : GPU_PMA_graph<W>(BYO_CONTAINER_VOS, v_data, n, m, deletion_fn, e0, w) {}
 };
 
-// The PCSR target (run_pcsr.cc:24-99, symmetric_PCSR_graph): one packed
-// array of a graph's edges in (source, destination) order with gaps, and a
-// per-vertex index into it -- the layout the PMA container keeps (leaves of
-// sorted keys with slack, the view's per-vertex offsets).  The target takes
-// the PMA container under its own name.
+// The PCSR target (run_pcsr.cc:24-99, symmetric_PCSR_graph) over
+// BYO_CONTAINER_PCSR: one packed array of per-vertex sentinels and sorted
+// neighbour ids with gaps, and a per-vertex index into it that the batch
+// updates keep current; the same interface as GPU_PMA_graph.
 template <class W>
-using GPU_PCSR_graph = GPU_PMA_graph<W>;
+class GPU_PCSR_graph : public GPU_PMA_graph<W> {
+ public:
+  using typename GPU_PMA_graph<W>::vertex_weight_type;
+  GPU_PCSR_graph() = default;
+  GPU_PCSR_graph(const uint64_t *off, const uint32_t *nbrs, uint64_t n, uint64_t m)
+      : GPU_PMA_graph<W>(BYO_CONTAINER_PCSR, off, nbrs, n, m) {}
+  template <class VData, class Edge>
+  GPU_PCSR_graph(VData *v_data, size_t n, size_t m, std::function<void()> deletion_fn, Edge *e0,
+                 vertex_weight_type *w = nullptr)
+      : GPU_PMA_graph<W>(BYO_CONTAINER_PCSR, v_data, n, m, deletion_fn, e0, w) {}
+};
 
 // ---------------------------------------------------------------- GPU algorithms
 // BFS (BFS.h:47-64): Parents with UINT_E_MAX for unreached, parent[src] = src.
