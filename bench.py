@@ -3,7 +3,7 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload dynamic|static|mixed|multi|scale|families|map|bytepd|stream|tc]
-                    [--container pma|vos] [--policy m20|learned|...]
+                    [--container pma|vos|pcsr] [--policy m20|learned|...]
 
 Workloads (synthetic: seeded RMAT a=.57 b=.19 c=.19 d=.05, symmetrised,
 deduplicated, no self loops; the reference publishes no dataset for them):
@@ -28,7 +28,8 @@ deduplicated, no self loops; the reference publishes no dataset for them):
            per batch.
   tc       triangle counting (degree ordered) on RMAT n=2^22, average degree
            32, CSR: one count per step.
---container vos runs the dynamic step on the vector of per-vertex runs.
+--container vos runs the dynamic step on the vector of per-vertex runs,
+--container pcsr on the packed CSR (sentinels and neighbour ids in one array).
 
 The metric is the composite of BFS, CC, PageRank and update rates; `value` is the step's edge operations per
 second in G/s: BFS traversed edges (undirected, Graph500 convention) + CC
@@ -202,10 +203,16 @@ def cc_bytes(n, m):
     return 4 * m + 8 * (n + 1) + 8 * n
 
 
-def update_bytes(B, touched_entries):
-    # 8-byte keys read + written once for the sort, and the 4-byte entries of
+# bytes a merge reads and writes per element of a touched leaf: the PMA's
+# 4-byte src and dst read and written; the PCSR's 4-byte slot read and written
+# (its sentinel bits add 1/4 B); the vector of runs reports no touched leaves
+ENTRY_BYTES = {"pma": 16, "pcsr": 8.25, "vos": 8}
+
+
+def update_bytes(B, touched_entries, container="pma"):
+    # 8-byte keys read + written once for the sort, and every element of
     # every leaf the merge touches read + written once
-    return 16 * B + 8 * touched_entries
+    return 16 * B + ENTRY_BYTES[container] * touched_entries
 
 
 def dynamic_config(dynamic, container, n, m):
@@ -303,7 +310,7 @@ def batch_sweep(byo, L, _abi, ctx, G, torch, stream, dev, n, policy, O, st):
                 ms = e0.elapsed_time(e1)
                 if r > 0:
                     (ins_ms if phase else rem_ms).append(ms)
-                    upd_bytes[1 - phase] += update_bytes(2 * b, G.last_update_stats()["touched_entries"])
+                    upd_bytes[1 - phase] += update_bytes(2 * b, G.last_update_stats()["touched_entries"], G.container)
                 # verification, outside the timing
                 tv = time.perf_counter()
                 ok = int(ch.value) == (st.insert_batch(okeys) if phase else st.remove_batch(okeys))
@@ -542,8 +549,8 @@ def run_ours(args, rank, world, local_rank):
            "cc": frac(cc_bytes(n, m_trav), comp[2]),
            "pr": frac(pr_iteration_bytes(n, m_trav, nslots) * pr_iters, comp[3])}
     if dynamic:
-        per["insert"] = frac(update_bytes(B, upd_stats["insert"]["touched_entries"]), comp[0])
-        per["remove"] = frac(update_bytes(B, upd_stats["remove"]["touched_entries"]), comp[4])
+        per["insert"] = frac(update_bytes(B, upd_stats["insert"]["touched_entries"], container), comp[0])
+        per["remove"] = frac(update_bytes(B, upd_stats["remove"]["touched_entries"], container), comp[4])
         per["insert"]["touched_leaves"] = upd_stats["insert"]["touched_leaves"]
         per["insert"]["touched_entries"] = upd_stats["insert"]["touched_entries"]
         per["remove"]["touched_leaves"] = upd_stats["remove"]["touched_leaves"]
@@ -551,7 +558,8 @@ def run_ours(args, rank, world, local_rank):
     roof["per_component"] = per
     roof["per_component_bytes"] = ("bfs 4*sum(deg of reached) + 8(n+1) + 8*reached + 4n (includes the PMA snapshot "
                                    "rebuild in its time); cc one pass 4m + 8(n+1) + 8n; pr per iteration 4m + 4m + "
-                                   "8(n+1) + 16n; insert/remove 16 B per key + 8 B per entry of every touched leaf")
+                                   "8(n+1) + 16n; insert/remove 16 B per key + per element of every touched leaf "
+                                   "16 B (PMA) or 8.25 B (PCSR)")
 
     # the learned policy against the m/20 rule (and in-place merge) on the
     # same state, same GPU: BFS and the update pair, median of 5
@@ -1735,8 +1743,9 @@ def main():
                     choices=["dynamic", "static", "mixed", "multi", "scale", "families", "map", "bytepd",
                              "stream", "tc"])
     ap.add_argument("--lg", type=int, default=0, help="multi: log2 vertices (default 24)")
-    ap.add_argument("--container", default="pma", choices=["pma", "vos"],
-                    help="dynamic: the container updated (pma: packed-memory array; vos: vector of per-vertex runs)")
+    ap.add_argument("--container", default="pma", choices=["pma", "vos", "pcsr"],
+                    help="dynamic: the container updated (pma: packed-memory array; vos: vector of per-vertex runs; "
+                         "pcsr: packed CSR)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--policy", default="auto", choices=sorted(POLICIES) + ["auto"],
                     help="auto: the committed learned network if present, else m20")
