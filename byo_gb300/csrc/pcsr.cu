@@ -22,12 +22,13 @@
 // leaf j lies in [sep[j], sep[j+1]).  The owner of any element is lv plus the
 // sentinels before it in the leaf, so leaves decode independently.
 //
-// A batch is validated, sorted and deduplicated on the device, turned into
-// composite keys and routed to leaves by sep; a warp per touched leaf decodes
-// it into shared memory, ranks each batch key in it and scatters the merged
-// sequence back in place when it fits, moving the sentinels' vbeg with them
-// and the degrees by atomics.  A leaf that would overflow leaves its merged
-// sequence in an overflow area for the windowed redistribution.
+// A batch is validated and sorted on the device and routed to leaves by sep
+// (batch keys compared as composite keys, duplicates skipped by the merge); a
+// warp per touched leaf decodes it into shared memory, ranks each batch key in
+// it and scatters the merged sequence back in place when it fits, moving the
+// sentinels' vbeg with them and the degrees by atomics.  A leaf that would
+// overflow leaves its merged sequence in an overflow area for the windowed
+// redistribution.
 #include <algorithm>
 #include <cmath>
 
@@ -43,20 +44,22 @@ constexpr double kPRootMax = 0.90;  // upper density bound at the root (1.0 at a
 constexpr double kPRootMin = 0.25;  // a remove below this lays the array out smaller
 constexpr uint64_t kCkMask = (1ull << 33) - 1;
 constexpr uint32_t kNoWindow = 0xFFFFFFFFu;
-constexpr int kPcsrWarps = 4;  // warps per CTA of the merge (40 KB of shared memory)
+constexpr int kPcsrWarps = 4;  // warps per CTA of the merge (24.6 KB of shared memory, 8 CTAs per SM)
 
 struct Pcsr {
   uint64_t NL = 0;
   int H = 0;
   uint32_t *slots = nullptr, *head = nullptr, *cnt = nullptr, *lv = nullptr;
   uint64_t *sep = nullptr;
-  DevBuf keys_a, keys_b, ck, bstart, rcount, rpre, marks, win, staging, ovf, ovf_off, misc;
+  DevBuf keys_a, keys_b, bstart, rcount, rpre, marks, win, staging, ovf, ovf_off, misc;
   uint64_t rebuilds = 0, windows = 0;
 };
 
 __host__ __device__ __forceinline__ uint64_t ck_sent(uint64_t v) { return v << 33; }
 __host__ __device__ __forceinline__ uint64_t ck_edge(uint64_t v, uint64_t w) { return (v << 33) | (w + 1); }
 __device__ __forceinline__ bool ck_is_sent(uint64_t k) { return (k & kCkMask) == 0; }
+// composite key of a batch key src << 32 | dst (order preserving)
+__device__ __forceinline__ uint64_t ck_of(uint64_t k) { return ck_edge(k >> 32, k & 0xFFFFFFFFull); }
 
 __host__ __device__ __forceinline__ double pcsr_bound(int h, int H) {
   return H == 0 ? kPRootMax : 1.0 - (1.0 - kPRootMax) * (double)h / (double)H;
@@ -104,11 +107,20 @@ __device__ __forceinline__ uint64_t slot_owner(const HeadScan &hs, uint32_t lv0,
 __device__ __forceinline__ void pcsr_decode_leaf(const uint32_t *__restrict__ slots, const uint32_t *__restrict__ head,
                                                  uint64_t j, uint32_t c, uint32_t lv0, uint64_t *A) {
   const HeadScan hs = head_scan(head, j);
-  for (uint32_t base = 0; base < c; base += 32) {
-    const uint32_t i = base + lane_id();
-    bool sent;
-    const uint64_t owner = slot_owner(hs, lv0, i, sent);
-    if (i < c) A[i] = sent ? ck_sent(owner) : ck_edge(owner, slots[j * kPL + i]);
+  for (uint32_t base = 0; base < c; base += 256) {
+    uint32_t x[8];  // eight loads per lane in flight
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const uint32_t i = base + 32 * q + lane_id();
+      x[q] = i < c ? slots[j * kPL + i] : kSentinel;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const uint32_t i = base + 32 * q + lane_id();
+      bool sent;
+      const uint64_t owner = slot_owner(hs, lv0, i, sent);
+      if (i < c) A[i] = sent ? ck_sent(owner) : ck_edge(owner, x[q]);
+    }
   }
 }
 
@@ -263,7 +275,7 @@ void pcsr_destroy(Pcsr *p) {
   cudaFree(p->cnt);
   cudaFree(p->lv);
   cudaFree(p->sep);
-  for (DevBuf *b : {&p->keys_a, &p->keys_b, &p->ck, &p->bstart, &p->rcount, &p->rpre, &p->marks, &p->win,
+  for (DevBuf *b : {&p->keys_a, &p->keys_b, &p->bstart, &p->rcount, &p->rpre, &p->marks, &p->win,
                     &p->staging, &p->ovf, &p->ovf_off, &p->misc})
     free_buf(*b);
   delete p;
@@ -289,12 +301,22 @@ __global__ void __launch_bounds__(256) k_pcsr_compact(const uint32_t *__restrict
     const HeadScan hs = head_scan(head, j);
     const uint64_t e0 = epre[j];
     const uint32_t l0 = lv[j];
-    for (uint32_t base = 0; base < c; base += 32) {
-      const uint32_t i = base + lane_id();
-      bool sent;
-      const uint64_t owner = slot_owner(hs, l0, i, sent);
-      const uint64_t at = e0 + i - owner - 1;
-      if (i < c && !sent && at < m) out[at] = slots[j * kPL + i];
+    // eight streaming loads per lane in flight before the stores
+    for (uint32_t base = 0; base < c; base += 256) {
+      uint32_t x[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const uint32_t i = base + 32 * q + lane_id();
+        x[q] = i < c ? __ldcs(slots + j * kPL + i) : kSentinel;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const uint32_t i = base + 32 * q + lane_id();
+        bool sent;
+        const uint64_t owner = slot_owner(hs, l0, i, sent);
+        const uint64_t at = e0 + i - owner - 1;
+        if (i < c && !sent && at < m) out[at] = x[q];
+      }
     }
   }
 }
@@ -324,16 +346,10 @@ __global__ void k_pcsr_check(const uint64_t *__restrict__ keys, uint64_t b, uint
   }
 }
 
-__global__ void k_pcsr_keys(const uint64_t *__restrict__ keys, uint64_t b, uint64_t *ck) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < b; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t k = keys[i];
-    ck[i] = ck_edge(k >> 32, k & 0xFFFFFFFFull);
-  }
-}
-
-// bstart[j] = first batch key >= sep[j]; bstart[0] = 0, bstart[NL] = b.
-__global__ void k_pcsr_route(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ ck, uint64_t b,
-                             uint64_t *bstart) {
+// bstart[j] = first batch key (sorted src << 32 | dst) whose composite key is
+// >= sep[j]; bstart[0] = 0, bstart[NL] = b.
+__global__ void k_pcsr_route(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
+                             uint64_t b, uint64_t *bstart) {
   for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j <= NL; j += (uint64_t)gridDim.x * blockDim.x) {
     if (j == 0 || j == NL) {
       bstart[j] = j ? b : 0;
@@ -343,7 +359,7 @@ __global__ void k_pcsr_route(const uint64_t *__restrict__ sep, uint64_t NL, cons
     uint64_t lo = 0, hi = b;
     while (lo < hi) {
       const uint64_t mid = (lo + hi) >> 1;
-      if (ck[mid] < s) lo = mid + 1;
+      if (ck_of(keys[mid]) < s) lo = mid + 1;
       else hi = mid;
     }
     bstart[j] = lo;
@@ -361,25 +377,58 @@ __device__ __forceinline__ uint32_t rank_in(const uint64_t *A, uint32_t c, uint6
   return l;
 }
 
-// A warp per leaf with batch keys: the leaf decoded into A, each batch key
-// ranked in A, the merged sequence scattered to O (shared) and written back
-// in place or, when it does not fit the leaf, to the overflow area.
-// Every output position comes from ranks:
+// Where one merged element goes: in place (its slot, the sentinel bit in the
+// warp's head words H, vbeg for a sentinel, lv for position 0) or, for a leaf
+// that overflows, its composite key in the overflow area.
+struct MergeOut {
+  uint32_t *slots;
+  uint64_t *vbeg;
+  uint32_t *lv;
+  uint32_t *H;
+  uint64_t j;
+  uint64_t *ovf;  // non-null: the leaf overflows
+};
+
+__device__ __forceinline__ void merge_put(const MergeOut &o, uint32_t pos, uint64_t k) {
+  if (o.ovf) {
+    o.ovf[pos] = k;
+    return;
+  }
+  const uint64_t at = o.j * kPL + pos;
+  if (ck_is_sent(k)) {
+    o.slots[at] = kSentinel;
+    o.vbeg[k >> 33] = at;
+    atomicOr(o.H + (pos >> 5), 1u << (pos & 31));
+  } else {
+    o.slots[at] = (uint32_t)((k & kCkMask) - 1);
+  }
+  if (pos == 0) o.lv[o.j] = (uint32_t)(k >> 33);
+}
+
+// A warp per leaf with batch keys (sorted src << 32 | dst; a key equal to its
+// predecessor is skipped, so the batch needs no separate deduplication): the
+// leaf is decoded into A (shared), each batch key ranked in A, and every
+// merged element written straight to its position -- in place, the leaf's
+// own slots, when the result fits, else to the overflow area.  Positions come
+// from ranks:
 //   insert: A[i] moves by the kept batch keys of rank <= i (a scan of D, the
 //           kept keys per rank); kept key x of rank l lands at l + the kept
-//           keys before it
-//   remove: A[i] moves back by the removed keys before it.
+//           keys before it, written while ranking when the leaf cannot
+//           overflow (c + batch keys <= kPL)
+//   remove: A[i] moves back by the removed keys before it, and the slots a
+//           remove frees at the end become gaps.
+// Slots and sentinel bits past max(old, new count) are gaps already.
 // ctr: [0] overflow cursor, [1] overflowing leaves, [2] change of the edge
 // count, [3] leaves merged, [4] elements they held.
-__global__ void __launch_bounds__(32 * kPcsrWarps) k_pcsr_merge(
-    uint32_t *slots, uint32_t *head, uint32_t *cnt, uint32_t *lv, uint64_t NL, const uint64_t *__restrict__ ck,
+__global__ void __launch_bounds__(32 * kPcsrWarps, 8) k_pcsr_merge(
+    uint32_t *slots, uint32_t *head, uint32_t *cnt, uint32_t *lv, uint64_t NL, const uint64_t *__restrict__ keys,
     const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
     unsigned long long *ctr, uint32_t *deg, uint64_t *vbeg) {
   __shared__ uint64_t As[kPcsrWarps][kPL];
-  __shared__ uint64_t Os[kPcsrWarps][kPL];
   __shared__ uint32_t Ds[kPcsrWarps][kPL + 1];
+  __shared__ uint32_t Hs[kPcsrWarps][kPW];
   const unsigned w = threadIdx.x >> 5, lane = lane_id();
-  uint64_t *A = As[w], *O = Os[w];
+  uint64_t *A = As[w];
   uint32_t *D = Ds[w];
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -396,14 +445,19 @@ __global__ void __launch_bounds__(32 * kPcsrWarps) k_pcsr_merge(
     nentries += c;
     pcsr_decode_leaf(slots, head, j, c, lv[j], A);
     for (uint32_t i = lane; i <= c; i += 32) D[i] = 0;
+    if (lane < kPW) Hs[w][lane] = 0;
     __syncwarp();
+    MergeOut o{slots, vbeg, lv, Hs[w], j, nullptr};
+    const bool direct = insert && c + (b1 - b0) <= kPL;
     uint32_t changed = 0;
     for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
       const uint64_t t = t0 + lane;
       bool act = false;
-      if (t < b1) {
-        const uint64_t x = ck[t];
-        const uint32_t l = rank_in(A, c, x);
+      uint32_t l = 0;
+      uint64_t x = 0;
+      if (t < b1 && !(t > b0 && keys[t - 1] == keys[t])) {
+        x = ck_of(keys[t]);
+        l = rank_in(A, c, x);
         const bool present = l < c && A[l] == x;
         act = insert ? !present : present;
         if (act) {
@@ -412,12 +466,13 @@ __global__ void __launch_bounds__(32 * kPcsrWarps) k_pcsr_merge(
           atomicAdd(deg + (x >> 33), insert ? 1u : 0xFFFFFFFFu);
         }
       }
-      changed += __popc(__ballot_sync(kFull, act));
+      const unsigned ma = __ballot_sync(kFull, act);
+      if (direct && act) merge_put(o, l + changed + __popc(ma & lanemask_lt()), x);
+      changed += __popc(ma);
     }
     __syncwarp();
     const uint32_t r = insert ? c + changed : c - changed;
     dsum += insert ? (long long)changed : -(long long)changed;
-    uint64_t *dstp = O;
     if (r > kPL) {
       unsigned long long at = 0;
       if (lane == 0) {
@@ -426,30 +481,32 @@ __global__ void __launch_bounds__(32 * kPcsrWarps) k_pcsr_merge(
         ovf_off[j] = at;
       }
       at = __shfl_sync(kFull, at, 0);
-      dstp = ovf + at;
+      o.ovf = ovf + at;
     }
     if (insert) {
       uint32_t carry = 0;
       for (uint32_t i0 = 0; i0 <= c; i0 += 32) {
         const uint32_t i = i0 + lane;
         const uint32_t inc = warp_inclusive_scan(i <= c ? D[i] : 0u) + carry;
-        if (i < c) dstp[i + inc] = A[i];
+        if (i < c) merge_put(o, i + inc, A[i]);
         carry = __shfl_sync(kFull, inc, 31);
       }
-      uint32_t kept_before = 0;
-      for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
-        const uint64_t t = t0 + lane;
-        bool keep = false;
-        uint32_t l = 0;
-        uint64_t x = 0;
-        if (t < b1) {
-          x = ck[t];
-          l = rank_in(A, c, x);
-          keep = !(l < c && A[l] == x);
+      if (!direct) {
+        uint32_t kept_before = 0;
+        for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
+          const uint64_t t = t0 + lane;
+          bool keep = false;
+          uint32_t l = 0;
+          uint64_t x = 0;
+          if (t < b1 && !(t > b0 && keys[t - 1] == keys[t])) {
+            x = ck_of(keys[t]);
+            l = rank_in(A, c, x);
+            keep = !(l < c && A[l] == x);
+          }
+          const unsigned mk = __ballot_sync(kFull, keep);
+          if (keep) merge_put(o, l + kept_before + __popc(mk & lanemask_lt()), x);
+          kept_before += __popc(mk);
         }
-        const unsigned mk = __ballot_sync(kFull, keep);
-        if (keep) dstp[l + kept_before + __popc(mk & lanemask_lt())] = x;
-        kept_before += __popc(mk);
       }
     } else {
       uint32_t removed = 0;
@@ -457,13 +514,20 @@ __global__ void __launch_bounds__(32 * kPcsrWarps) k_pcsr_merge(
         const uint32_t i = i0 + lane;
         const bool gone = i < c && D[i];
         const unsigned mg = __ballot_sync(kFull, gone);
-        if (i < c && !gone) dstp[i - removed - __popc(mg & lanemask_lt())] = A[i];
+        if (i < c && !gone) merge_put(o, i - removed - __popc(mg & lanemask_lt()), A[i]);
         removed += __popc(mg);
       }
     }
     __syncwarp();
-    // in place: the separator stays, every key routed here is >= it
-    if (r <= kPL) pcsr_encode_leaf(slots, head, cnt, lv, vbeg, j, O, r);
+    if (!o.ovf) {
+      // in place; the separator stays (every key routed here is >= it)
+      for (uint32_t i = r + lane; i < c; i += 32) slots[j * kPL + i] = kSentinel;
+      if (lane < (max(c, r) + 31) / 32) head[j * kPW + lane] = Hs[w][lane];
+      if (lane == 0) {
+        cnt[j] = r;
+        if (r == 0) lv[j] = 0;
+      }
+    }
     if (lane == 0) rcount[j] = r;
     __syncwarp();
   }
@@ -541,12 +605,11 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PCSR container");
   g->version++;  // any snapshot of the contents is stale from here on
   const uint64_t n = g->n, m_before = g->m;
-  // 1. validate, then sort and deduplicate
+  // 1. validate, then sort (duplicates stay: the merge skips them)
   BYO_TRY(ensure(ctx, p->keys_a, count * 8));
   BYO_TRY(ensure(ctx, p->keys_b, count * 8));
-  BYO_TRY(ensure(ctx, p->ck, count * 8));
   BYO_TRY(ensure(ctx, p->misc, 128));
-  uint64_t *ka = (uint64_t *)p->keys_a.p, *kb = (uint64_t *)p->keys_b.p, *ck = (uint64_t *)p->ck.p;
+  uint64_t *ka = (uint64_t *)p->keys_a.p, *kb = (uint64_t *)p->keys_b.p;
   unsigned long long *ctr = (unsigned long long *)p->misc.p;  // [0..4] merge counters
   unsigned int *flags = (unsigned int *)(ctr + 8);            // [0] range, [1] order, [2] grow
   BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 128, ctx->stream));
@@ -562,10 +625,8 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   uint64_t b = count;
   if (!sorted) {
     BYO_TRY(sort_bucketed(ctx, d_keys_in, count, n, ka, kb));
-    BYO_TRY(unique_u64(ctx, ka, count, 0, kb, &b));
-    batch = kb;
+    batch = ka;
   }
-  launch(ctx, k_pcsr_keys, dim3(grid_for(ctx, b, 256)), dim3(256), 0, batch, b, ck);
   // 2. route and merge
   const uint64_t NL = p->NL;
   BYO_TRY(ensure(ctx, p->bstart, (NL + 1) * 8));
@@ -576,9 +637,9 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   uint64_t *bstart = (uint64_t *)p->bstart.p, *rpre = (uint64_t *)p->rpre.p;
   uint32_t *rcount = (uint32_t *)p->rcount.p;
   launch(ctx, k_pcsr_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
-         (const uint64_t *)ck, b, bstart);
-  launch_t(ctx, "pcsr_merge", k_pcsr_merge, dim3(grid_for(ctx, NL * 32, 32 * kPcsrWarps, 5)),
-           dim3(32 * kPcsrWarps), 0, p->slots, p->head, p->cnt, p->lv, NL, (const uint64_t *)ck,
+         batch, b, bstart);
+  launch_t(ctx, "pcsr_merge", k_pcsr_merge, dim3(grid_for(ctx, NL * 32, 32 * kPcsrWarps, 8)),
+           dim3(32 * kPcsrWarps), 0, p->slots, p->head, p->cnt, p->lv, NL, batch,
            (const uint64_t *)bstart, insert, rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, g->d_deg,
            g->d_off);
   BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 40, cudaMemcpyDeviceToHost, ctx->stream));
