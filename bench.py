@@ -488,7 +488,7 @@ def run_ours(args, rank, world, local_rank):
 
     # per-kernel shares over the timed region
     tags = ["bfs_push", "bfs_pull", "bfs_blocked", "cc_finish", "pr_pull", "tc_intersect", "sort_scatter",
-            "pma_merge", "pma_redistribute"]
+            "pma_merge", "pma_redistribute", "pcsr_merge", "pcsr_redistribute", "pcsr_compact"]
     ktimes = {t: ctx.kernel_time(t) for t in tags}
     ctx.kernel_timing(None)
     dom = max(tags, key=lambda t: ktimes[t][1])
@@ -569,6 +569,13 @@ def run_ours(args, rank, world, local_rank):
     # end to end through the public host API
     e2e = run_e2e(args, byo, G, ctx, torch, dynamic, keys, B, n, policy, total_units, world, dev)
 
+    # the same step on the packed CSR container
+    if dynamic and container == "pma" and rank == 0 and not args.no_pcsr:
+        t0 = time.time()
+        components["pcsr"] = pcsr_compare(args, byo, L, _abi, ctx, torch, stream, keys, B, policy, G, parent, label,
+                                          pr, total_units, peak)
+        log("pcsr arm: %.1f s" % (time.time() - t0))
+
     # BASELINE's batch-size sweep with verification after every batch
     if dynamic and ostore is not None and not args.no_sweep:
         t0 = time.time()
@@ -587,6 +594,94 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
     }
     return res, ctx, G
+
+
+def pcsr_compare(args, byo, L, _abi, ctx, torch, stream, keys, B, policy, G, parent, label, pr, total_units,
+                 peak):
+    """The dynamic step on the packed CSR container (run_pcsr.cc's layout:
+    per-vertex sentinels and neighbour ids in one packed array) built from the
+    same RMAT draws: its contents after the insert must equal the headline
+    container's (whose contents the oracle checked), then W warm-up and K timed
+    steps of the same insert, BFS, CC, PageRank, remove with CUDA events per
+    phase on the library's stream."""
+    P = byo.Graph.generate(ctx, "rmat", seed=SEED, lg_n=LG_N, draws=DRAWS, container="pcsr")
+    ch = ctypes.c_uint64(0)
+    rounds, it, l1 = ctypes.c_uint32(0), ctypes.c_uint32(0), ctypes.c_double(0)
+
+    def ins(g):
+        _abi.check(L.byo_graph_insert_batch_device(g.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+
+    def rem(g):
+        _abi.check(L.byo_graph_remove_batch_device(g.h, keys.data_ptr(), B, 0, ctypes.byref(ch)), ctx.h)
+
+    ins(P)
+    ins(G)
+    po, pn = P.export_csr()
+    go, gn = G.export_csr()
+    same = bool(np.array_equal(po, go) and np.array_equal(pn, gn))
+    del po, pn, go, gn
+    nslots_after_insert = P.nslots()
+    rem(P)
+    rem(G)
+    ins(P)
+    st_ins = P.last_update_stats()
+    rem(P)
+    st_rem = P.last_update_stats()
+    ctx.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+
+    def step(record):
+        with torch.cuda.stream(stream):
+            if record:
+                ev[0].record(stream)
+            ins(P)
+            if record:
+                ev[1].record(stream)
+            _abi.check(L.byo_bfs_device(P.h, SRC, parent.data_ptr(), None, policy, ctypes.byref(rounds)), ctx.h)
+            if record:
+                ev[2].record(stream)
+            _abi.check(L.byo_cc_device(P.h, label.data_ptr()), ctx.h)
+            if record:
+                ev[3].record(stream)
+            _abi.check(L.byo_pagerank_device(P.h, PR_EPS, PR_ITERS, 0, pr.data_ptr(), ctypes.byref(it),
+                                             ctypes.byref(l1)), ctx.h)
+            if record:
+                ev[4].record(stream)
+            rem(P)
+            if record:
+                ev[5].record(stream)
+
+    for _ in range(args.warmup):
+        step(False)
+    ctx.synchronize()
+    comp = np.zeros(5)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        step(True)
+        stream.synchronize()
+        for i in range(5):
+            comp[i] += ev[i].elapsed_time(ev[i + 1])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    step_ms = t0.elapsed_time(t1) / args.steps
+    comp /= args.steps
+
+    def frac(byts, ms):
+        gbs = byts / (ms / 1e3) / 1e9
+        return {"achieved_gbs": gbs, "frac": gbs / peak, "algorithmic_bytes": byts, "ms": ms}
+
+    out = {"same_contents_as_pma": same, "value": total_units / (step_ms / 1e3) / 1e9, "ms_per_step": step_ms,
+           "insert_ms": comp[0], "bfs_ms": comp[1], "cc_ms": comp[2], "pr_ms": comp[3], "remove_ms": comp[4],
+           "insert_edges_per_s": B / (comp[0] / 1e3), "remove_edges_per_s": B / (comp[4] / 1e3),
+           "insert_roofline": frac(update_bytes(B, st_ins["touched_entries"], "pcsr"), comp[0]),
+           "remove_roofline": frac(update_bytes(B, st_rem["touched_entries"], "pcsr"), comp[4]),
+           "slots": nslots_after_insert, "container_bytes": int(nslots_after_insert * 4.125),
+           "pma_container_bytes": int(G.nslots() * 8),
+           "how": "same step and units as the headline; value = the headline's edge operations per step / this "
+                  "step's device time; BFS includes the snapshot rebuild (k_pcsr_compact)"}
+    P.close()
+    return out
 
 
 def compare_policies(L, _abi, ctx, G, keys, B, parent, dynamic, torch, stream):
@@ -1752,6 +1847,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="dynamic/static: skip the oracle check before timing")
     ap.add_argument("--no-sweep", action="store_true", help="dynamic: skip the 1e3/1e5/1e7 batch-size sweep")
+    ap.add_argument("--no-pcsr", action="store_true", help="dynamic PMA: skip the same step on the packed CSR")
     ap.add_argument("--pr-launches", default="graph", choices=["graph", "stream"],
                     help="PageRank iterations as one CUDA graph (default) or one stream launch per kernel "
                          "(for per-kernel profiles)")
