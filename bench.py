@@ -340,8 +340,8 @@ def batch_sweep(byo, L, _abi, ctx, G, torch, stream, dev, n, policy, O, st):
                   "insert then remove; edges/s = directed keys (2 x pairs) / device time of the call (sort + merge + "
                   "view upkeep, as the reference times insert_batch, run_unweighted.h:832-835); every batch, timed "
                   "and untimed, verified against the oracle outside the timing: contents, changed count, BFS(%d) "
-                  "parents, CC labels (%.1f s of checking); hbm_gbs = (16 B per key + 8 B per entry of every "
-                  "touched leaf) / time" % (SWEEP_ROUNDS, SRC, t_verify))
+                  "parents, CC labels (%.1f s of checking); hbm_gbs = (16 B per key + 16 B (PMA) or 8.25 B "
+                  "(PCSR) per element of every touched leaf) / time" % (SWEEP_ROUNDS, SRC, t_verify))
     return out
 
 
