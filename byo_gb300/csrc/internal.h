@@ -289,6 +289,11 @@ int pma_update_stream(byo_graph *g, const uint64_t *d_keys, const uint64_t *d_bo
                       const unsigned char *d_ops, const unsigned char *h_ops, uint64_t nbatch, long long *h_changed,
                       const StreamQueries *qs = nullptr);
 uint64_t pma_leaf_slots();
+// One CTA sorts up to sort_small_max() (4096) keys in registers; bounds[0],
+// bounds[1] receive the largest src and dst.  It does not index by key, so it
+// may run before the batch is validated.
+uint64_t sort_small_max();
+int sort_small_keys(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t *out, unsigned long long *bounds);
 int pma_update(byo_graph *g, const uint64_t *d_keys, uint64_t count, int sorted, int insert,
                uint64_t *changed);
 int pma_export_keys(byo_graph *g, uint64_t *d_keys_out);

@@ -377,6 +377,59 @@ __device__ __forceinline__ uint32_t rank_in(const uint64_t *A, uint32_t c, uint6
   return l;
 }
 
+// Leaf of every key of a sorted batch: the last leaf whose separator is <= its
+// composite key (as k_pcsr_route assigns them).  Nothing when the batch
+// failed validation (flags[0] | flags[1]).
+__global__ void k_pcsr_leafof(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
+                              uint64_t b, const unsigned int *flags, uint32_t *leaf) {
+  if (flags[0] | flags[1]) return;
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < b; q += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t x = ck_of(keys[q]);
+    uint64_t lo = 0, len = NL;
+    while (len > 1) {
+      const uint64_t half = len >> 1;
+      if (sep[lo + half] <= x) lo += half;
+      len -= half;
+    }
+    leaf[q] = (uint32_t)lo;
+  }
+}
+
+// The segment list of a sorted batch from its keys' leaves: one entry per
+// leaf with keys, (leaf, b0 << 32 | b1), in any order.
+__global__ void k_pcsr_segs(const uint32_t *__restrict__ leaf, uint64_t b, const unsigned int *flags, uint64_t *seg,
+                            unsigned long long *nseg) {
+  if (flags[0] | flags[1]) return;
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, nthr = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = tid & ~31ull; base < b; base += nthr) {
+    const uint64_t q = base + lane_id();
+    const uint32_t j = q < b ? leaf[q] : 0u;
+    const bool start = q < b && (q == 0 || leaf[q - 1] != j);
+    uint64_t b1 = b;
+    if (start) {  // the first key past q on a later leaf
+      uint64_t l = q + 1, h = b;
+      while (l < h) {
+        const uint64_t mid = (l + h) >> 1;
+        if (leaf[mid] <= j) l = mid + 1;
+        else h = mid;
+      }
+      b1 = l;
+    }
+    const uint64_t at = warp_append(start, nseg);
+    if (start) {
+      seg[2 * at] = j;
+      seg[2 * at + 1] = q << 32 | b1;
+    }
+  }
+}
+
+// rcount of the listed leaves from the merge's segment list.
+__global__ void k_pcsr_seg_counts(const uint64_t *__restrict__ seg, const unsigned long long *nseg, uint32_t *rcount) {
+  const uint64_t ns = *nseg;
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < ns; q += (uint64_t)gridDim.x * blockDim.x)
+    rcount[seg[2 * q] & 0xFFFFFFFFull] = (uint32_t)(seg[2 * q] >> 32);
+}
+
 // Where one merged element goes: in place (its slot, the sentinel bit in the
 // warp's head words H, vbeg for a sentinel, lv for position 0) or, for a leaf
 // that overflows, its composite key in the overflow area.
@@ -418,12 +471,17 @@ __device__ __forceinline__ void merge_put(const MergeOut &o, uint32_t pos, uint6
 //   remove: A[i] moves back by the removed keys before it, and the slots a
 //           remove frees at the end become gaps.
 // Slots and sentinel bits past max(old, new count) are gaps already.
+// kList: the leaves with keys come from a segment list (seg[2q] = leaf,
+// seg[2q + 1] = b0 << 32 | b1, *nseg entries) instead of bstart over every
+// leaf, and a leaf's count after the merge goes to the high half of seg[2q]
+// instead of rcount.
 // ctr: [0] overflow cursor, [1] overflowing leaves, [2] change of the edge
 // count, [3] leaves merged, [4] elements they held.
+template <bool kList>
 __global__ void __launch_bounds__(32 * kPcsrWarps, 8) k_pcsr_merge(
     uint32_t *slots, uint32_t *head, uint32_t *cnt, uint32_t *lv, uint64_t NL, const uint64_t *__restrict__ keys,
-    const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
-    unsigned long long *ctr, uint32_t *deg, uint64_t *vbeg) {
+    const uint64_t *__restrict__ bstart, uint64_t *seg, const unsigned long long *nseg, int insert, uint32_t *rcount,
+    uint64_t *ovf, uint64_t *ovf_off, unsigned long long *ctr, uint32_t *deg, uint64_t *vbeg) {
   __shared__ uint64_t As[kPcsrWarps][kPL];
   __shared__ uint32_t Ds[kPcsrWarps][kPL + 1];
   __shared__ uint32_t Hs[kPcsrWarps][kPW];
@@ -434,8 +492,18 @@ __global__ void __launch_bounds__(32 * kPcsrWarps, 8) k_pcsr_merge(
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   long long dsum = 0;
   unsigned long long nleaves = 0, nentries = 0;
-  for (uint64_t j = gw; j < NL; j += nw) {
-    const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
+  const uint64_t nwork = kList ? *nseg : NL;
+  for (uint64_t q = gw; q < nwork; q += nw) {
+    uint64_t j, b0, b1;
+    if (kList) {
+      j = seg[2 * q];
+      b0 = seg[2 * q + 1] >> 32;
+      b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
+    } else {
+      j = q;
+      b0 = bstart[j];
+      b1 = bstart[j + 1];
+    }
     const uint32_t c = min(cnt[j], kPL);
     if (b0 == b1) {
       if (lane == 0) rcount[j] = c;
@@ -528,7 +596,10 @@ __global__ void __launch_bounds__(32 * kPcsrWarps, 8) k_pcsr_merge(
         if (r == 0) lv[j] = 0;
       }
     }
-    if (lane == 0) rcount[j] = r;
+    if (lane == 0) {
+      if (kList) seg[2 * q] = j | (uint64_t)r << 32;
+      else rcount[j] = r;
+    }
     __syncwarp();
   }
   if (lane == 0) {
@@ -605,45 +676,75 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PCSR container");
   g->version++;  // any snapshot of the contents is stale from here on
   const uint64_t n = g->n, m_before = g->m;
-  // 1. validate, then sort (duplicates stay: the merge skips them)
+  // 1. validate, then sort (duplicates stay: the merge skips them).  A batch
+  // of at most one key per leaf takes the segment list (only its own leaves
+  // are visited); when it also needs no bucketed sort (sorted input, or at
+  // most 4096 keys for the one-CTA register sort, which does not index by
+  // key) its validation is read after the single synchronisation of the
+  // update, and the segment kernels drop an invalid batch.
+  const uint64_t NL = p->NL;
+  const bool small = !sorted && count <= sort_small_max();
+  const bool list = count <= NL && count < (1ull << 32);
+  const bool defer = list && (sorted || small);
   BYO_TRY(ensure(ctx, p->keys_a, count * 8));
   BYO_TRY(ensure(ctx, p->keys_b, count * 8));
   BYO_TRY(ensure(ctx, p->misc, 128));
   uint64_t *ka = (uint64_t *)p->keys_a.p, *kb = (uint64_t *)p->keys_b.p;
-  unsigned long long *ctr = (unsigned long long *)p->misc.p;  // [0..4] merge counters
-  unsigned int *flags = (unsigned int *)(ctr + 8);            // [0] range, [1] order, [2] grow
+  // misc: [0..4] merge counters, [5] segments, [6..7] the small sort's bounds,
+  // then flags [0] range, [1] order, [2] grow
+  unsigned long long *ctr = (unsigned long long *)p->misc.p;
+  unsigned int *flags = (unsigned int *)(ctr + 8);
   BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 128, ctx->stream));
   launch(ctx, k_pcsr_check, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, n, sorted, flags);
   uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
-  BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  const unsigned int *hf = (const unsigned int *)h;
-  if (hf[0]) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
-  if (hf[1]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  const unsigned int *hf = (const unsigned int *)(h + 8);
+  if (!defer) {
+    BYO_CU(ctx, cudaMemcpyAsync(h + 8, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hf[0]) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+    if (hf[1]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  }
   const uint64_t *batch = d_keys_in;
   uint64_t b = count;
-  if (!sorted) {
+  if (small) {
+    BYO_TRY(sort_small_keys(ctx, d_keys_in, count, ka, ctr + 6));
+    batch = ka;
+  } else if (!sorted) {
     BYO_TRY(sort_bucketed(ctx, d_keys_in, count, n, ka, kb));
     batch = ka;
   }
-  // 2. route and merge
-  const uint64_t NL = p->NL;
-  BYO_TRY(ensure(ctx, p->bstart, (NL + 1) * 8));
+  // 2. route and merge (bstart doubles as the segment list)
+  const uint64_t list_words = list ? 2 * std::min<uint64_t>(count, NL) + 2 : 0;
+  BYO_TRY(ensure(ctx, p->bstart, std::max<uint64_t>(NL + 1, list_words) * 8));
   BYO_TRY(ensure(ctx, p->rcount, NL * 4));
   BYO_TRY(ensure(ctx, p->rpre, (NL + 1) * 8));
   BYO_TRY(ensure(ctx, p->ovf, (n + m_before + b + 1) * 8));  // the merged leaves hold at most every element
   BYO_TRY(ensure(ctx, p->ovf_off, NL * 8));
   uint64_t *bstart = (uint64_t *)p->bstart.p, *rpre = (uint64_t *)p->rpre.p;
   uint32_t *rcount = (uint32_t *)p->rcount.p;
-  launch(ctx, k_pcsr_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
-         batch, b, bstart);
-  launch_t(ctx, "pcsr_merge", k_pcsr_merge, dim3(grid_for(ctx, NL * 32, 32 * kPcsrWarps, 8)),
-           dim3(32 * kPcsrWarps), 0, p->slots, p->head, p->cnt, p->lv, NL, batch,
-           (const uint64_t *)bstart, insert, rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, g->d_deg,
-           g->d_off);
-  BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 40, cudaMemcpyDeviceToHost, ctx->stream));
+  if (list) {
+    uint32_t *leaf = reinterpret_cast<uint32_t *>(kb);  // free once the batch is sorted
+    launch(ctx, k_pcsr_leafof, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL, batch, b,
+           (const unsigned int *)flags, leaf);
+    launch(ctx, k_pcsr_segs, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint32_t *)leaf, b,
+           (const unsigned int *)flags, bstart, ctr + 5);
+    launch_t(ctx, "pcsr_merge", k_pcsr_merge<true>, dim3(grid_for(ctx, b * 32, 32 * kPcsrWarps, 8)),
+             dim3(32 * kPcsrWarps), 0, p->slots, p->head, p->cnt, p->lv, NL, batch, (const uint64_t *)nullptr,
+             bstart, (const unsigned long long *)(ctr + 5), insert, rcount, (uint64_t *)p->ovf.p,
+             (uint64_t *)p->ovf_off.p, ctr, g->d_deg, g->d_off);
+  } else {
+    launch(ctx, k_pcsr_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL, batch,
+           b, bstart);
+    launch_t(ctx, "pcsr_merge", k_pcsr_merge<false>, dim3(grid_for(ctx, NL * 32, 32 * kPcsrWarps, 8)),
+             dim3(32 * kPcsrWarps), 0, p->slots, p->head, p->cnt, p->lv, NL, batch, (const uint64_t *)bstart,
+             (uint64_t *)nullptr, (const unsigned long long *)nullptr, insert, rcount, (uint64_t *)p->ovf.p,
+             (uint64_t *)p->ovf_off.p, ctr, g->d_deg, g->d_off);
+  }
+  BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 80, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
+  if (defer && hf[0]) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+  if (defer && hf[1]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
   const uint64_t novf = h[1], merged_leaves = h[3], merged_entries = h[4];
   const uint64_t m_after = (uint64_t)((long long)m_before + (long long)h[2]);
   g->m = m_after;
@@ -655,6 +756,11 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   if (novf == 0 && !shrink) return check_launch(ctx, "pcsr_update");
   // 3. redistribution: windows over the counts after the merge, or a new
   // layout when the root is out of bounds
+  if (list) {  // counts of every leaf: unlisted ones keep theirs
+    BYO_CU(ctx, cudaMemcpyAsync(rcount, p->cnt, NL * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    launch(ctx, k_pcsr_seg_counts, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)bstart,
+           (const unsigned long long *)(ctr + 5), rcount);
+  }
   BYO_TRY(scan_u32_to_u64(ctx, rcount, NL, rpre));
   BYO_TRY(ensure(ctx, p->staging, (total ? total : 1) * 8));
   BYO_TRY(ensure(ctx, p->win, NL * 4));
@@ -667,7 +773,7 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
     BYO_CU(ctx, cudaMemsetAsync(marks, 0, (uint64_t)(p->H + 1) * NL, ctx->stream));
     launch(ctx, k_pcsr_windows, dim3(grid_for(ctx, NL, 256)), dim3(256), 0, (const uint32_t *)rcount,
            (const uint64_t *)rpre, NL, p->H, marks, flags + 2);
-    BYO_CU(ctx, cudaMemcpyAsync(h, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    BYO_CU(ctx, cudaMemcpyAsync(h + 8, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
     BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
     rebuild = hf[2] != 0;
     if (!rebuild)

@@ -942,6 +942,19 @@ __global__ void __launch_bounds__(1024) k_sort_small(const uint64_t *__restrict_
   sort_small_block<K>(in, count, out, bounds, s, red);
 }
 
+uint64_t sort_small_max() { return kSmallSort; }
+
+int sort_small_keys(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t *out, unsigned long long *bounds) {
+  if (count > kSmallSort) return set_error(ctx, BYO_EINVAL, "small sort: more than 4096 keys");
+  if (count <= 1024)
+    launch(ctx, k_sort_small<1>, dim3(1), dim3(1024), 0, in, (uint32_t)count, out, bounds);
+  else if (count <= 2048)
+    launch(ctx, k_sort_small<2>, dim3(1), dim3(1024), 0, in, (uint32_t)count, out, bounds);
+  else
+    launch(ctx, k_sort_small<4>, dim3(1), dim3(1024), 0, in, (uint32_t)count, out, bounds);
+  return BYO_OK;
+}
+
 
 // A block per chunk of a long range; the leaf's src list is staged in shared
 // memory and each thread fills kViewChunk / kViewThreads vertices a block
@@ -1350,12 +1363,21 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   }
   uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
-  // A batch small enough for the segment-list merge that needs no bucketed
-  // sort is validated on the device (the segment kernel drops an invalid
-  // batch) and checked here after the single synchronisation of the update.
-  const bool list = 2 * count <= p->NL && count < (1ull << 32);
-  const bool defer = list && (sorted || small_sort) && ctx->update_policy != BYO_UPDATE_REBUILD &&
-                     ctx->update_policy != BYO_UPDATE_LEARNED;
+  // 2. strategy: in-place merge (default), rebuild when asked for or chosen by
+  // the learned policy from the host-side features (batch size, m, slots,
+  // sortedness, direction); capacity may still force a rebuild below.
+  int strategy = 0;
+  if (ctx->update_policy == BYO_UPDATE_REBUILD) strategy = 1;
+  else if (ctx->update_policy == BYO_UPDATE_LEARNED)
+    strategy = update_strategy(ctx, count, m_before, p->NL * kLeaf, sorted, insert);
+  ctx->last_update_strategy = strategy;
+  // A batch of at most one key per leaf takes the segment-list merge, which
+  // visits only its own leaves and keeps the view current around them.  When
+  // it also needs no bucketed sort it is validated on the device (the segment
+  // kernel drops an invalid batch) and checked here after the single
+  // synchronisation of the update.
+  const bool list = count <= p->NL && count < (1ull << 32);
+  const bool defer = list && (sorted || small_sort) && strategy == 0;
   if (!defer) {
     BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
     BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1373,19 +1395,15 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     BYO_TRY(sort_bucketed(ctx, d_keys_in, count, g->n, ka, kb));
     batch = ka;
   }
-  // 2. strategy: in-place merge (default), rebuild when asked for or chosen by
-  // the learned policy; capacity may still force a rebuild below
+  // bstart doubles as the segment list (two words per touched leaf) and rpre
+  // as the merged leaves' view ranges (two words each)
   const uint64_t NL = p->NL;
-  BYO_TRY(ensure(ctx, p->bstart, (NL + 1) * 8));
+  const uint64_t list_words = list ? 2 * std::min<uint64_t>(count, NL) + 2 : 0;
+  BYO_TRY(ensure(ctx, p->bstart, std::max<uint64_t>(NL + 1, list_words) * 8));
   BYO_TRY(ensure(ctx, p->rcount, NL * 4));
-  BYO_TRY(ensure(ctx, p->rpre, (NL + 1) * 8));
+  BYO_TRY(ensure(ctx, p->rpre, std::max<uint64_t>(NL + 1, list_words) * 8));
   uint64_t *bstart = (uint64_t *)p->bstart.p, *rpre = (uint64_t *)p->rpre.p;
   uint32_t *rcount = (uint32_t *)p->rcount.p;
-  int strategy = 0;
-  if (ctx->update_policy == BYO_UPDATE_REBUILD) strategy = 1;
-  else if (ctx->update_policy == BYO_UPDATE_LEARNED)
-    strategy = update_strategy(ctx, b, m_before, NL * kLeaf, sorted, insert);
-  ctx->last_update_strategy = strategy;
   if (strategy == 1) {
     launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
            (const uint64_t *)batch, b, bstart);
@@ -1420,7 +1438,7 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   const double cap = (double)NL * kLeaf;
   const double shrink_below = !insert && NL > 1 ? kRootMin * cap : -1.0;
   if (list) {
-    uint64_t *seg = bstart;  // 2 * b <= NL words
+    uint64_t *seg = bstart;  // 2 * min(b, NL) + 2 words
     launch(ctx, k_pma_segments, dim3(grid_for(ctx, b, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
            (const uint64_t *)batch, b, seg, ctr + 3, defer ? (const unsigned long long *)bounds : nullptr, g->n,
            (const unsigned int *)flags);

@@ -178,3 +178,43 @@ def test_pcsr_large_batch_generate(ctx, oracle_mod):
     _check(byo, O, G, ro, rn, (10,))
     G.close()
     P.close()
+
+
+def test_pcsr_segment_list_overflow(ctx, oracle_mod):
+    """Batches of at most one key per leaf take the segment-list merge; one
+    that overflows a leaf goes on to the windowed redistribution from it, and
+    small unsorted, sorted and invalid batches take the deferred validation."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 100000
+    s, d = O.uniform_pairs(95, n, 30000)
+    off, nb = O.build_csr(n, s, d)
+    G = byo.Graph.from_csr(ctx, off, nb, container="pcsr")
+    st = O.Store(off, nb)
+    leaves = G.nslots() // 512
+    rng = np.random.default_rng(96)
+    # 200 new neighbours of vertex 5 (400 keys, fewer than the leaves): its
+    # leaf overflows inside a segment-list merge
+    pairs = np.stack([np.full(200, 5), rng.choice(n, 200, replace=False)], 1)
+    keys = O.keys_from_pairs(pairs[:, 0], pairs[:, 1])
+    assert len(keys) <= leaves
+    assert G.insert_batch(keys) == st.insert_batch(keys)
+    assert G.last_update_stats()["path"] == 2
+    ro, rn = st.export_csr()
+    _check(byo, O, G, ro, rn, (5, 0))
+    # small batches: unsorted with duplicates, sorted, removed again
+    for size in (1, 7, 300):
+        p = rng.integers(0, n, size=(size, 2))
+        k = O.keys_from_pairs(p[:, 0], p[:, 1])
+        k = np.concatenate([k, k[: size // 2]])
+        assert G.insert_batch(k) == st.insert_batch(k)
+        ks = np.unique(k)
+        assert G.remove_batch(ks, sorted=True) == st.remove_batch(ks)
+        assert G.insert_batch(ks, sorted=True) == st.insert_batch(ks)
+    ro, rn = st.export_csr()
+    _check(byo, O, G, ro, rn, (5,))
+    with pytest.raises(byo.ByoError) as e:
+        G.remove_batch(np.array([(2 << 32) | 3, (n << 32) | 3], np.uint64))
+    assert e.value.code == byo._abi.BYO_EINVAL
+    _check(byo, O, G, ro, rn)
+    G.close()
