@@ -89,9 +89,21 @@ int main() {
   vos.remove_sorted_batch(sorted.data(), sorted.size());
   CHECK(vos.num_edges() == 14 && vos.degree(6) == 1);
   CHECK((vos.offsets() == pma.offsets()) && (vos.edges() == pma.edges()));
+  // the packed CSR: the same calls, its own layout
   byo::GPU_PCSR_graph<int> pcsr(vd.data(), n, edges.size(), nullptr, edges.data());
+  CHECK(pcsr.num_edges() == 12);
   pcsr.insert_batch(batch.data(), batch.size());
   CHECK(pcsr.num_edges() == 16 && pcsr.degree(1) == 2 && pcsr.degree(6) == 2);
+  CHECK((byo::gpu_bfs(pcsr, 0) == std::vector<uint32_t>{0, 0, 1, 2, 5, 6, 0}));
+  {
+    std::vector<uint32_t> nb6;
+    pcsr.map_neighbors(6, [&](size_t, uint32_t v, auto) { nb6.push_back(v); });
+    CHECK((nb6 == std::vector<uint32_t>{0, 5}));
+  }
+  pcsr.remove_sorted_batch(sorted.data(), sorted.size());
+  CHECK(pcsr.num_edges() == 14 && pcsr.degree(6) == 1);
+  CHECK((pcsr.offsets() == pma.offsets()) && (pcsr.edges() == pma.edges()));
+  CHECK((byo::gpu_cc(pcsr) == std::vector<uint32_t>{0, 0, 0, 0, 0, 0, 0}));
 
   // the reference's own edgeMap loops through the adapter: bfs_cc::CC with
   // BFS_ComponentLabel_F (BFSCC/Connectivity.h:52-88) and PageRank_edgeMap

@@ -26,7 +26,7 @@ def test_encode_matches_oracle_and_decodes(ctx, oracle_mod):
             bo, dg, data = G.to_bytepd(P)
             obo, odg, odata = O.bytepd_encode(off, nb, P)
             assert np.array_equal(bo, obo) and np.array_equal(dg, odg) and bytes(data) == bytes(odata), P
-            for cont in ("csr", "pma"):
+            for cont in ("csr", "pma", "pcsr"):
                 H = byo.Graph.from_bytepd(ctx, obo, odg, odata, block=P, container=cont)
                 o2, n2 = H.export_csr()
                 assert np.array_equal(o2, off) and np.array_equal(n2, nb), (P, cont)
@@ -68,7 +68,7 @@ def test_file_round_trip(ctx, oracle_mod, tmp_path):
     assert (n, m, total) == (len(off) - 1, len(nb), len(data))
     assert raw[24:24 + 8 * (n + 1)] == bo.tobytes() and raw[24 + 8 * (n + 1):24 + 8 * (n + 1) + 4 * n] == dg.tobytes()
     assert raw[24 + 12 * n + 8:] == bytes(data)
-    for cont in ("csr", "pma"):
+    for cont in ("csr", "pma", "pcsr"):
         H = byo.Graph.read_bytepd(ctx, path, container=cont)
         o2, n2 = H.export_csr()
         assert np.array_equal(o2, off) and np.array_equal(n2, nb)

@@ -27,7 +27,7 @@ def _on(ctx):
     return torch.cuda.stream(torch.cuda.ExternalStream(ctx.stream))
 
 
-def _graph(ctx, O):
+def _graph(ctx, O, container="csr"):
     """Three RMAT components of different sizes plus isolated vertices."""
     import byo_gb300 as byo
     parts, base = [], 0
@@ -39,7 +39,7 @@ def _graph(ctx, O):
     s = np.concatenate([p[0] for p in parts]).astype(np.uint32)
     d = np.concatenate([p[1] for p in parts]).astype(np.uint32)
     off, nb = O.build_csr(n, s, d)
-    return byo.Graph.from_csr(ctx, off, nb), off, nb
+    return byo.Graph.from_csr(ctx, off, nb, container=container), off, nb
 
 
 def _bfs_cc_via_edgemap(byo, G, torch, flags):
@@ -70,13 +70,16 @@ def _bfs_cc_via_edgemap(byo, G, torch, flags):
     return lab
 
 
-def test_bfs_cc_as_reference_loop(ctx, oracle_mod):
+@pytest.mark.parametrize("container", ["csr", "pma", "pcsr"])
+def test_bfs_cc_as_reference_loop(ctx, oracle_mod, container):
+    """On every container: edgeMap reads the container's own view (the PMA's
+    and the packed CSR's gaps, the packed CSR's vertex sentinels)."""
     import torch
 
     import byo_gb300 as byo
     from byo_gb300 import _abi
     O = oracle_mod
-    G, off, nb = _graph(ctx, O)
+    G, off, nb = _graph(ctx, O, container)
     exp = O.cc(off, nb)
     with _on(ctx):
         _bfs_cc_flags(byo, G, torch, exp)
@@ -92,7 +95,8 @@ def _bfs_cc_flags(byo, G, torch, exp):
         assert np.array_equal(lab, exp), flags
 
 
-def test_pagerank_edgemap_as_reference_loop(ctx, oracle_mod):
+@pytest.mark.parametrize("container", ["csr", "pma", "pcsr"])
+def test_pagerank_edgemap_as_reference_loop(ctx, oracle_mod, container):
     import torch
 
     import byo_gb300 as byo
@@ -100,7 +104,7 @@ def test_pagerank_edgemap_as_reference_loop(ctx, oracle_mod):
     O = oracle_mod
     s, d = O.rmat_edges(9, 14, 1 << 18)
     off, nb = O.build_csr(1 << 14, s, d)
-    G = byo.Graph.from_csr(ctx, off, nb)
+    G = byo.Graph.from_csr(ctx, off, nb, container=container)
     with _on(ctx):
         _pr_edgemap_loop(byo, G, torch, O, off, nb)
     # the library's own PageRank_edgeMap runs the same loop, with the stop rule

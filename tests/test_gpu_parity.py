@@ -319,7 +319,7 @@ def test_pagerank_delta_and_edgemap(ctx, oracle_mod):
 
 @pytest.mark.gpu
 def test_graph_files_round_trip(ctx, oracle_mod, tmp_path):
-    """write_adj then read_adj, both layouts, into both containers."""
+    """write_adj then read_adj, both layouts, into every container."""
     import byo_gb300 as byo
     G = byo.Graph.generate(ctx, "rmat", seed=17, lg_n=12, draws=1 << 15, container="pma")
     G.insert_batch(np.array([(1 << 32) | 2, (2 << 32) | 1], np.uint64))
@@ -327,7 +327,7 @@ def test_graph_files_round_trip(ctx, oracle_mod, tmp_path):
     for binary in (False, True):
         p = str(tmp_path / ("g.bin" if binary else "g.adj"))
         G.write_adj(p, binary)
-        for cont in ("csr", "pma"):
+        for cont in ("csr", "pma", "pcsr"):
             H = byo.Graph.read_adj(ctx, p, binary, container=cont)
             o2, n2 = H.export_csr()
             assert np.array_equal(o2, off) and np.array_equal(n2, nb)
@@ -350,7 +350,7 @@ def test_triangle_count_paths(ctx, oracle_mod):
     dst = np.concatenate([d.astype(np.int64), cd[mask]])
     off, nb = O.build_csr(1 << 12, src.astype(np.uint32), dst.astype(np.uint32))
     want = O.triangle_count(off, nb)
-    for cont in ("csr", "pma"):
+    for cont in ("csr", "pma", "pcsr"):
         G = byo.Graph.from_csr(ctx, off, nb, container=cont)
         for stage in (0, 512):
             G.set_tuning(tc_stage=stage)
