@@ -479,12 +479,12 @@ constexpr uint32_t kOptSeg = 256;
 
 __device__ __forceinline__ uint64_t bval(const uint64_t *B, uint64_t j) { return B[j]; }
 
-// kList: the leaves with work come from a segment list (seg[2q] = leaf,
-// seg[2q + 1] = b0 << 32 | b1, *nseg entries) instead of bstart over every
-// leaf.  Then rcount is not written: the count after the merge goes to the
-// high half of seg[2q] instead.  When deg is given, every key that enters or
-// leaves adjusts deg[src].  When off is given (list mode), a leaf merged in
-// place also refreshes the view offsets around it (view_refresh_warp).
+// The leaves with work come from a segment list (seg[2q] = leaf,
+// seg[2q + 1] = b0 << 32 | b1, *nseg entries); the count after the merge goes
+// to the high half of seg[2q].  When deg is given, every key that enters or
+// leaves adjusts deg[src].  When off is given, a leaf merged in place also
+// refreshes the view offsets around it (view_refresh_warp).  Batches of more
+// keys than leaves take k_pma_merge_rank instead.
 struct ViewOut {
   const uint64_t *sep;
   uint64_t n;
@@ -495,34 +495,22 @@ struct ViewOut {
 // One leaf (work item q) merged by the calling warp, with Aw / Bw its staging
 // in shared memory (kLeaf and kOptSeg keys); returns the change of the leaf's
 // key count.
-template <bool kList>
 __device__ __forceinline__ long long merge_leaf(uint64_t q, uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL,
-                                                const uint64_t *__restrict__ keys, const uint64_t *__restrict__ bstart,
-                                                uint64_t *seg, int insert, uint32_t *rcount, uint64_t *ovf,
+                                                const uint64_t *__restrict__ keys, uint64_t *seg, int insert,
+                                                uint64_t *ovf,
                                                 uint64_t *ovf_off, unsigned long long *ctr, uint32_t *deg,
                                                 const ViewOut &view, uint64_t *Aw, uint64_t *Bw, uint64_t &tleaves,
                                                 uint64_t &tentries) {
   const unsigned lane = lane_id();
   const uint64_t *A = Aw;
   {
-    uint64_t j, b0, b1;
-    if (kList) {
-      j = seg[2 * q] & 0xFFFFFFFFull;
-      b0 = seg[2 * q + 1] >> 32;
-      b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
-    } else {
-      j = q;
-      b0 = bstart[j];
-      b1 = bstart[j + 1];
-    }
+    const uint64_t j = seg[2 * q] & 0xFFFFFFFFull;
+    const uint64_t b0 = seg[2 * q + 1] >> 32, b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
     const uint32_t c = cnt[j];
     // the leaf's last src before the merge, for the view refresh
-    const uint32_t old_last = kList && view.off && c ? src[j * kLeaf + c - 1] : 0xFFFFFFFFu;
+    const uint32_t old_last = view.off && c ? src[j * kLeaf + c - 1] : 0xFFFFFFFFu;
     if (b0 == b1) {
-      if (lane == 0) {
-        if (kList) seg[2 * q] = j | (uint64_t)c << 32;
-        else rcount[j] = c;
-      }
+      if (lane == 0) seg[2 * q] = j | (uint64_t)c << 32;
       return 0;
     }
     const uint64_t nb = b1 - b0;
@@ -634,12 +622,9 @@ __device__ __forceinline__ long long merge_leaf(uint64_t q, uint32_t *src, uint3
       }
       if (lane == 0) cnt[j] = r;
     }
-    if (lane == 0) {
-      if (kList) seg[2 * q] = j | (uint64_t)r << 32;
-      else rcount[j] = r;
-    }
+    if (lane == 0) seg[2 * q] = j | (uint64_t)r << 32;
     __syncwarp();  // the leaf's new contents (and A's last reads) are done warp-wide
-    if (kList && view.off && !ostage)
+    if (view.off && !ostage)
       view_refresh_warp(src, view.sep, NL, view.n, j, r, old_last, keys[b0] >> 32, keys[b1 - 1] >> 32,
                         reinterpret_cast<uint32_t *>(Aw), view.off, q, view.range, view.chunks, view.nchunks);
     __syncwarp();
@@ -647,11 +632,9 @@ __device__ __forceinline__ long long merge_leaf(uint64_t q, uint32_t *src, uint3
   }
 }
 
-template <bool kList>
 __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
-    uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
-    const uint64_t *__restrict__ bstart, uint64_t *seg, const unsigned long long *nseg,
-    int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
+    uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys, uint64_t *seg,
+    const unsigned long long *nseg, int insert, uint64_t *ovf, uint64_t *ovf_off,
     unsigned long long *ctr /* [0] overflow cursor, [1] leaves overflowed */, long long *delta, uint32_t *deg,
     ViewOut view) {
   __shared__ uint64_t As[kOptWarps][kLeaf];
@@ -661,14 +644,187 @@ __global__ void __launch_bounds__(32 * kOptWarps) k_pma_merge_opt(
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   long long dsum = 0;
   uint64_t tleaves = 0, tentries = 0;
-  const uint64_t nwork = kList ? *nseg : NL;
+  const uint64_t nwork = *nseg;
   for (uint64_t q = gw; q < nwork; q += nw)
-    dsum += merge_leaf<kList>(q, src, dst, cnt, NL, keys, bstart, seg, insert, rcount, ovf, ovf_off, ctr, deg, view,
-                              As[w], Bsh[w], tleaves, tentries);
+    dsum += merge_leaf(q, src, dst, cnt, NL, keys, seg, insert, ovf, ovf_off, ctr, deg, view, As[w], Bsh[w], tleaves,
+                       tentries);
   if (lane_id() == 0 && dsum) atomicAdd((unsigned long long *)delta, (unsigned long long)dsum);
   if (lane_id() == 0 && tleaves) {  // ctr[5], ctr[6]: touched leaves and the keys they held
     atomicAdd(&ctr[5], (unsigned long long)tleaves);
     atomicAdd(&ctr[6], (unsigned long long)tentries);
+  }
+}
+
+// ---------------------------------------------------------------- rank merge (large batches)
+// A warp per leaf with batch keys, every output position from ranks instead
+// of the merge path: the leaf's keys staged in shared memory (A), each batch
+// key ranked in A by a binary search (a key equal to its predecessor in the
+// batch is skipped), and every element written straight to its slot:
+//   insert: A[i] moves by the kept batch keys of rank <= i (a warp scan of D,
+//           the kept keys per rank); kept key x of rank l lands at l + the
+//           kept keys before it, written while ranking when the leaf cannot
+//           overflow (c + batch keys <= kLeaf)
+//   remove: A[i] moves back by the removed keys before it; the slots freed
+//           at the end become gaps.
+// A leaf whose result does not fit goes whole to the overflow area.
+// ctr: [0] overflow cursor, [1] overflowing leaves, [5] leaves merged, [6]
+// the keys they held; *delta the change of the key count.
+constexpr int kRankWarps = 4;
+
+struct RankOut {
+  uint32_t *src, *dst;
+  uint64_t base;
+  uint64_t *ovf;  // non-null: the leaf overflows
+};
+
+__device__ __forceinline__ void rank_put(const RankOut &o, uint32_t pos, uint64_t k) {
+  if (o.ovf) {
+    o.ovf[pos] = k;
+  } else {
+    o.src[o.base + pos] = (uint32_t)(k >> 32);
+    o.dst[o.base + pos] = (uint32_t)k;
+  }
+}
+
+__device__ __forceinline__ uint32_t rank_of(const uint64_t *A, uint32_t c, uint64_t x) {
+  uint32_t l = 0, hi = c;
+  while (l < hi) {
+    const uint32_t mid = (l + hi) >> 1;
+    if (A[mid] < x) l = mid + 1;
+    else hi = mid;
+  }
+  return l;
+}
+
+__global__ void __launch_bounds__(32 * kRankWarps, 8) k_pma_merge_rank(
+    uint32_t *src, uint32_t *dst, uint32_t *cnt, uint64_t NL, const uint64_t *__restrict__ keys,
+    const uint64_t *__restrict__ bstart, int insert, uint32_t *rcount, uint64_t *ovf, uint64_t *ovf_off,
+    unsigned long long *ctr, long long *delta) {
+  __shared__ uint64_t As[kRankWarps][kLeaf];
+  __shared__ uint32_t Ds[kRankWarps][kLeaf + 1];
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  uint64_t *A = As[w];
+  uint32_t *D = Ds[w];
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  long long dsum = 0;
+  unsigned long long nleaves = 0, nentries = 0;
+  for (uint64_t j = gw; j < NL; j += nw) {
+    const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
+    const uint32_t c = min(cnt[j], kLeaf);
+    if (b0 == b1) {
+      if (lane == 0) rcount[j] = c;
+      continue;
+    }
+    nleaves++;
+    nentries += c;
+    const uint64_t base = j * kLeaf;
+    for (uint32_t e0 = 0; e0 < c; e0 += 256) {  // eight loads of each array per lane in flight
+      uint32_t hs[8], ds[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const uint32_t e = e0 + 32 * u + lane;
+        hs[u] = e < c ? src[base + e] : 0u;
+        ds[u] = e < c ? dst[base + e] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const uint32_t e = e0 + 32 * u + lane;
+        if (e < c) A[e] = (uint64_t)hs[u] << 32 | ds[u];
+      }
+    }
+    for (uint32_t i = lane; i <= c; i += 32) D[i] = 0;
+    __syncwarp();
+    RankOut o{src, dst, base, nullptr};
+    const bool direct = insert && c + (b1 - b0) <= kLeaf;
+    uint32_t changed = 0;
+    for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
+      const uint64_t t = t0 + lane;
+      bool act = false;
+      uint32_t l = 0;
+      uint64_t x = 0;
+      if (t < b1) {
+        x = keys[t];
+        if (!(t > b0 && keys[t - 1] == x)) {
+          l = rank_of(A, c, x);
+          const bool present = l < c && A[l] == x;
+          act = insert ? !present : present;
+          if (act) {
+            if (insert) atomicAdd(D + l, 1u);
+            else D[l] = 1u;
+          }
+        }
+      }
+      const unsigned ma = __ballot_sync(kFull, act);
+      if (direct && act) rank_put(o, l + changed + __popc(ma & lanemask_lt()), x);
+      changed += __popc(ma);
+    }
+    __syncwarp();
+    const uint32_t r = insert ? c + changed : c - changed;
+    dsum += insert ? (long long)changed : -(long long)changed;
+    if (r > kLeaf) {
+      unsigned long long at = 0;
+      if (lane == 0) {
+        at = atomicAdd(&ctr[0], (unsigned long long)r);
+        atomicAdd(&ctr[1], 1ull);
+        ovf_off[j] = at;
+      }
+      at = __shfl_sync(kFull, at, 0);
+      o.ovf = ovf + at;
+    }
+    if (insert) {
+      uint32_t carry = 0;
+      for (uint32_t i0 = 0; i0 <= c; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const uint32_t inc = warp_inclusive_scan(i <= c ? D[i] : 0u) + carry;
+        if (i < c) rank_put(o, i + inc, A[i]);
+        carry = __shfl_sync(kFull, inc, 31);
+      }
+      if (!direct) {
+        uint32_t kept_before = 0;
+        for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
+          const uint64_t t = t0 + lane;
+          bool keep = false;
+          uint32_t l = 0;
+          uint64_t x = 0;
+          if (t < b1) {
+            x = keys[t];
+            if (!(t > b0 && keys[t - 1] == x)) {
+              l = rank_of(A, c, x);
+              keep = !(l < c && A[l] == x);
+            }
+          }
+          const unsigned mk = __ballot_sync(kFull, keep);
+          if (keep) rank_put(o, l + kept_before + __popc(mk & lanemask_lt()), x);
+          kept_before += __popc(mk);
+        }
+      }
+    } else {
+      uint32_t removed = 0;
+      for (uint32_t i0 = 0; i0 < c; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const bool gone = i < c && D[i];
+        const unsigned mg = __ballot_sync(kFull, gone);
+        if (i < c && !gone) rank_put(o, i - removed - __popc(mg & lanemask_lt()), A[i]);
+        removed += __popc(mg);
+      }
+    }
+    if (!o.ovf) {
+      for (uint32_t i = r + lane; i < c; i += 32) {
+        src[base + i] = kSentinel;
+        dst[base + i] = kSentinel;
+      }
+      if (lane == 0) cnt[j] = r;
+    }
+    if (lane == 0) rcount[j] = r;
+    __syncwarp();
+  }
+  if (lane == 0) {
+    if (dsum) atomicAdd((unsigned long long *)delta, (unsigned long long)dsum);
+    if (nleaves) {
+      atomicAdd(&ctr[5], nleaves);
+      atomicAdd(&ctr[6], nentries);
+    }
   }
 }
 
@@ -1446,18 +1602,17 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     // ranges in rpre, chunks of long ranges in win (both free here)
     BYO_TRY(ensure(ctx, p->win, ((g->n + 1) / kViewChunk + b + 64) * 8));
     ViewOut view{(const uint64_t *)p->sep, g->n, g->d_off, rpre, (uint64_t *)p->win.p, ctr + 4};
-    launch_t(ctx, "pma_merge", k_pma_merge_opt<true>, dim3(grid_for(ctx, b * 32, 32 * kOptWarps, 6)),
-             dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
-             (const uint64_t *)nullptr, seg, (const unsigned long long *)(ctr + 3), insert, rcount,
-             (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2), g->d_deg, view);
+    launch_t(ctx, "pma_merge", k_pma_merge_opt, dim3(grid_for(ctx, b * 32, 32 * kOptWarps, 6)),
+             dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch, seg,
+             (const unsigned long long *)(ctr + 3), insert, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr,
+             (long long *)(ctr + 2), g->d_deg, view);
   } else {
     launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
            (const uint64_t *)batch, b, bstart);
-    launch_t(ctx, "pma_merge", k_pma_merge_opt<false>, dim3(grid_for(ctx, NL * 32, 32 * kOptWarps, 6)),
-             dim3(32 * kOptWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
-             (const uint64_t *)bstart, (uint64_t *)nullptr, (const unsigned long long *)nullptr, insert,
-             rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr, (long long *)(ctr + 2),
-             (uint32_t *)nullptr, ViewOut{});
+    launch_t(ctx, "pma_merge", k_pma_merge_rank, dim3(grid_for(ctx, NL * 32, 32 * kRankWarps, 8)),
+             dim3(32 * kRankWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
+             (const uint64_t *)bstart, insert, rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr,
+             (long long *)(ctr + 2));
   }
   BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 88, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1673,9 +1828,9 @@ __global__ void __launch_bounds__(kStreamThreads) k_pma_stream(StreamArgs a) {
       long long dsum = 0;
       uint64_t tleaves = 0, tentries = 0;  // not reported by the stream
       for (uint64_t q = gw; q < ns; q += nmw)
-        dsum += merge_leaf<true>(q, a.src, a.dst, a.cnt, a.NL, a.sorted + (size_t)cur * kSmallSort, nullptr,
-                                 a.seg + (size_t)cur * 2 * kSmallSort, insert, nullptr, a.ovf, a.ovf_off, c->ctr[cur],
-                                 a.deg, view, As + (size_t)w * kLeaf, Bs + (size_t)w * kOptSeg, tleaves, tentries);
+        dsum += merge_leaf(q, a.src, a.dst, a.cnt, a.NL, a.sorted + (size_t)cur * kSmallSort,
+                           a.seg + (size_t)cur * 2 * kSmallSort, insert, a.ovf, a.ovf_off, c->ctr[cur], a.deg, view,
+                           As + (size_t)w * kLeaf, Bs + (size_t)w * kOptSeg, tleaves, tentries);
       if (lane_id() == 0 && dsum) atomicAdd(&c->ctr[cur][2], (unsigned long long)dsum);
       if (solo) {
         __syncthreads();
