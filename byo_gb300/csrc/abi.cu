@@ -355,8 +355,6 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
     }
   }
   if (nq) {
-    if (g->container != BYO_CONTAINER_PMA)
-      return set_error(ctx, BYO_ENOTSUP, "mixed stream: queries need the PMA container");
     if (qs->k == 0 || qs->k > 64) return set_error(ctx, BYO_EINVAL, "mixed stream: 1 <= k <= 64 sources");
     if (!qs->h_srcs || !qs->d_levels) return set_error(ctx, BYO_EINVAL, "mixed stream: null sources or levels");
     if (g->n >= (1ull << 32) - 1) return set_error(ctx, BYO_EINVAL, "mixed stream: n too large");
@@ -381,12 +379,23 @@ static int update_stream_common(byo_graph *g, const uint64_t *keys, int host, co
   BYO_CU(ctx, cudaMemcpyAsync(d_ops, ops.data(), nbatch, cudaMemcpyHostToDevice, ctx->stream));
   std::vector<long long> ch(nbatch);
   int rc = BYO_OK;
-  if (g->container != BYO_CONTAINER_PMA) {  // VOS, PCSR: one update per batch
+  if (g->container != BYO_CONTAINER_PMA) {  // VOS, PCSR: one op at a time
+    uint64_t q = 0;
     for (uint64_t b = 0; b < nbatch && rc == BYO_OK; b++) {
       uint64_t c = 0;
       const uint64_t len = h_offsets[b + 1] - h_offsets[b];
-      if (len && g->container == BYO_CONTAINER_VOS) rc = vos_update(g, d + h_offsets[b], len, 0, ops[b], &c);
-      else if (len) rc = pcsr_update(g, d + h_offsets[b], len, 0, ops[b], &c);
+      if (ops[b] == BYO_OP_QUERY) {
+        byo_graph *t = nullptr;
+        uint32_t rounds = 0;
+        rc = traversal_view(g, &t);
+        if (rc == BYO_OK)
+          rc = bfs_multi_run(t, qs->h_srcs + q * qs->k, qs->k, qs->d_levels + q * qs->k * g->n, &rounds);
+        q++;
+      } else if (len && g->container == BYO_CONTAINER_VOS) {
+        rc = vos_update(g, d + h_offsets[b], len, 0, ops[b], &c);
+      } else if (len) {
+        rc = pcsr_update(g, d + h_offsets[b], len, 0, ops[b], &c);
+      }
       ch[b] = (long long)c;
     }
   } else {

@@ -309,7 +309,8 @@ __device__ __forceinline__ uint64_t seg_of(const uint64_t *pre, uint64_t nseg, u
 // The old keys of the touched runs, in chunks over their concatenation
 // (abase): each key moves to its place in the staging copy of its run,
 // shifted by the kept batch keys of its run that go before it (insert:
-// rank <= i; remove: rank < i, and a kept batch key of rank i removes it).
+// rank <= i; remove: rank < i, and a kept batch key among those of rank i
+// removes it).
 // The ranks and kept-key prefix of a window's batch keys are staged in shared
 // memory when they fit; each lane walks a pointer forward through its run's
 // batch keys as its keys rise.
@@ -393,7 +394,11 @@ __global__ void __launch_bounds__(kVosBlock)
           if (insert) {
             temp[stb[w][j] + i + before] = xq[q];
           } else {
-            const bool gone = l < e && (staged ? srk[w][l] : rk[g0 + l]) == i && kflag[g0 + l];
+            // the batch keys of rank i: absent ones (below A[i]) first, then
+            // A[i] itself and its duplicates; A[i] goes if any is kept
+            bool gone = false;
+            for (uint32_t t = l; t < e && !gone && (staged ? srk[w][t] : rk[g0 + t]) == i; t++)
+              gone = kflag[g0 + t] != 0;
             if (!gone) temp[stb[w][j] + i - before] = xq[q];
           }
         }

@@ -307,7 +307,8 @@ class Graph:
         (anything with data_ptr(), e.g. a CUDA tensor) of nq * k * n uint32
         that receives query q's levels at [q * k * n, (q + 1) * k * n).
         Returns (changed per op, op times [nops, 2] in ns: device start and end
-        of the ops run inside the persistent kernel, 0 for the others)."""
+        of the ops run inside the PMA's persistent kernel, 0 for the others
+        and on the other containers, which run the ops one by one)."""
         codes = {"remove": _abi.OP_REMOVE, "insert": _abi.OP_INSERT, "query": _abi.OP_QUERY}
         ks, srcs, o = [], [], []
         for kind, x in ops:

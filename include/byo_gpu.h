@@ -331,20 +331,23 @@ int byo_graph_update_stream_device(byo_graph *g, const uint64_t *d_keys, const u
 
 /* A mixed stream of update batches and 64-source BFS queries, in order
  * (the serving pattern of a dynamic graph: batches arrive between queries);
- * PMA container.  ops[i]: BYO_OP_REMOVE / BYO_OP_INSERT (keys
+ * PMA, packed CSR or vector-of-runs container.  ops[i]: BYO_OP_REMOVE /
+ * BYO_OP_INSERT (keys
  * [offsets[i], offsets[i+1]) as in byo_graph_update_stream) or BYO_OP_QUERY
  * (an empty key range): the q-th query op runs a k-source bit-lane BFS
  * (k <= 64, sources h_srcs[q*k .. q*k+k)) over the contents at that point of
  * the stream and writes levels as byo_bfs_multi does to
- * d_levels + q*k*n (device memory of nq*k*n entries).  Runs of queries and
- * small batches (as for byo_graph_update_stream) are drained by one
- * persistent kernel under one bounded grid barrier: per query its state is
+ * d_levels + q*k*n (device memory of nq*k*n entries).  On the PMA, runs of
+ * queries and small batches (as for byo_graph_update_stream) are drained by
+ * one persistent kernel under one bounded grid barrier: per query its state is
  * cleared, the traversal runs over the container's own slots and the levels
  * are written, with no host round trip; a larger batch, or one whose merge
  * overflows a leaf, is finished by the host and the kernel resumes after it.
+ * The other containers run the ops one by one (each batch through its own
+ * update, each query as byo_bfs_multi on the contents at that point).
  * changed[i] (may be NULL): keys inserted or removed by op i.  op_ns (may be
  * NULL, 2*nops entries): device start and end time of each op run inside the
- * kernel, in ns of one clock (0 for ops finished on the host path).  No
+ * PMA's kernel, in ns of one clock (0 for ops run otherwise).  No
  * reference counterpart: the reference runs queries and batches as separate
  * calls (benchmarks/run_unweighted.h:781-893 for batches, BFS.h:47-64 for a
  * query). */

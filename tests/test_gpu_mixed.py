@@ -71,3 +71,53 @@ def test_mixed_stream_matches_oracle_after_every_op(ctx, oracle_mod):
     assert np.array_equal(go, so) and np.array_equal(gn, sn)
     assert times[4].tolist() == [0, 0]  # the large batch ran on the host path
     G.close()
+
+
+@pytest.mark.parametrize("container", ["pcsr", "vos"])
+def test_mixed_stream_other_containers(ctx, oracle_mod, container):
+    """The same stream API on the packed CSR and the vector of runs, which run
+    it op by op: every query's levels and every batch's count against the
+    oracle at its point of the stream; op times stay 0 there."""
+    import torch
+
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 14
+    n = 1 << lg
+    s, d = O.rmat_edges(18, lg, 1 << 17)
+    off, nb = O.build_csr(n, s, d)
+    G = byo.Graph.from_csr(ctx, off, nb, container=container)
+    st = O.Store(off, nb)
+    rng = np.random.default_rng(6)
+    deg = np.diff(off.astype(np.int64))
+
+    def batch(seed, pairs):
+        us, ud = O.uniform_pairs(seed, n, pairs)
+        return O.keys_from_pairs(us, ud)
+
+    def query():
+        return rng.choice(np.nonzero(deg)[0], 16).astype(np.uint32)
+
+    b1, b2 = batch(71, 500), batch(72, 20000)
+    ops = [("query", query()), ("insert", b1), ("insert", b2), ("query", query()), ("remove", b1),
+           ("query", query()), ("remove", b2)]
+    nq = 3
+    levels = torch.full((nq * 16 * n,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    changed, times = G.mixed_stream(ops, 16, levels)
+    lev = levels.cpu().numpy().view(np.uint32).reshape(nq, 16, n)
+    q = 0
+    for i, (kind, x) in enumerate(ops):
+        if kind == "query":
+            so, sn = st.export_csr()
+            for j, src in enumerate(x):
+                assert np.array_equal(lev[q, j], O.bfs(so, sn, int(src))[1]), "query %d source %d" % (q, j)
+            q += 1
+        else:
+            exp = st.insert_batch(x) if kind == "insert" else st.remove_batch(x)
+            assert changed[i] == exp, "op %d" % i
+    assert not times.any()
+    so, sn = st.export_csr()
+    go, gn = G.export_csr()
+    assert np.array_equal(go, so) and np.array_equal(gn, sn)
+    G.close()

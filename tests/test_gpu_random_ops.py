@@ -1,0 +1,87 @@
+"""Seeded random sequences of batch updates on every updatable container
+(PMA, packed CSR, vector of runs) against the oracle's sorted-set store: the
+changed count after every operation, the contents and degrees every few
+operations, BFS and CC at the end.  Sizes are log-uniform from 1 to 2*10^4
+pairs, so every update path runs (segment list and full-leaf merges, the
+register, bucketed and unsorted sorts, leaf overflow, growth and shrinking);
+batches come unsorted with duplicates or sorted and deduplicated, and removes
+draw half their pairs from the edges present."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(byo, O, G, st):
+    ro, rn = st.export_csr()
+    go, gn = G.export_csr()
+    assert np.array_equal(go, ro) and np.array_equal(gn, rn)
+    assert np.array_equal(G.degrees(), np.diff(ro).astype(np.uint32))
+    return ro, rn
+
+
+@pytest.mark.parametrize("container", ["pma", "pcsr", "vos"])
+def test_random_update_sequence(ctx, oracle_mod, container):
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 14
+    n = 1 << lg
+    s, d = O.rmat_edges(101, lg, 1 << 16)
+    off, nb = O.build_csr(n, s, d)
+    G = byo.Graph.from_csr(ctx, off, nb, container=container)
+    st = O.Store(off, nb)
+    rng = np.random.default_rng(102)
+    for op in range(40):
+        size = int(np.round(10.0 ** rng.uniform(0, np.log10(2e4))))
+        insert = bool(rng.integers(0, 2))
+        if insert:
+            p = rng.integers(0, n, size=(size, 2))
+        else:
+            # half the pairs from the edges present, half random
+            ro, rn = st.export_csr()
+            src = np.repeat(np.arange(n), np.diff(ro).astype(np.int64))
+            pick = rng.integers(0, max(len(rn), 1), size=size // 2 + 1) if len(rn) else np.zeros(0, np.int64)
+            p = np.concatenate([np.stack([src[pick], rn[pick]], 1) if len(rn) else np.zeros((0, 2), np.int64),
+                                rng.integers(0, n, size=(size - size // 2, 2))])
+        keys = O.keys_from_pairs(p[:, 0], p[:, 1])
+        sorted_ = bool(rng.integers(0, 3) == 0)
+        if sorted_:
+            keys = np.unique(keys)
+        else:
+            keys = np.concatenate([keys, keys[: len(keys) // 5]])  # duplicates
+            rng.shuffle(keys)
+        if insert:
+            assert G.insert_batch(keys, sorted=sorted_) == st.insert_batch(keys), (op, size)
+        else:
+            assert G.remove_batch(keys, sorted=sorted_) == st.remove_batch(keys), (op, size)
+        assert G.M() == st.num_edges
+        if op % 5 == 4:
+            _check(byo, O, G, st)
+    ro, rn = _check(byo, O, G, st)
+    for src in (0, 7):
+        opar, olev = O.bfs(ro, rn, src)
+        par, lev = byo.BFS(G, src, levels=True)
+        assert np.array_equal(lev, olev) and np.array_equal(par, opar)
+    assert np.array_equal(byo.SimpleUnionAsync(G), O.cc(ro, rn))
+    G.close()
+
+
+@pytest.mark.parametrize("container", ["pma", "pcsr", "vos"])
+def test_remove_with_absent_key_of_equal_rank(ctx, oracle_mod, container):
+    """A remove batch whose absent key sorts just below a present one of the
+    same vertex (both rank 1 in the vertex's run): the present one goes, the
+    next vertex's neighbours are untouched."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n = 64
+    pairs = np.array([(3, 10), (3, 20), (3, 30), (4, 11), (4, 12), (5, 40), (9, 1)])
+    off, nb = O.build_csr(n, pairs[:, 0].astype(np.uint32), pairs[:, 1].astype(np.uint32))
+    G = byo.Graph.from_csr(ctx, off, nb, container=container)
+    st = O.Store(off, nb)
+    for batch, sorted_ in (([(3, 15), (3, 20), (3, 20)], False), ([(4, 10), (4, 11), (5, 39)], True),
+                           ([(3, 29), (3, 30), (4, 12), (5, 41)], False)):
+        k = np.array([(a << 32) | b for a, b in batch], np.uint64)
+        k = np.unique(k) if sorted_ else k
+        assert G.remove_batch(k, sorted=sorted_) == st.remove_batch(k)
+        _check(byo, O, G, st)
+    G.close()
