@@ -85,3 +85,44 @@ def test_remove_with_absent_key_of_equal_rank(ctx, oracle_mod, container):
         assert G.remove_batch(k, sorted=sorted_) == st.remove_batch(k)
         _check(byo, O, G, st)
     G.close()
+
+
+@pytest.mark.parametrize("container", ["pma", "pcsr", "vos"])
+def test_random_update_stream(ctx, oracle_mod, container):
+    """60 seeded batches through byo_graph_update_stream (on the PMA drained by
+    the persistent kernel, larger batches by the host between its launches):
+    sizes log-uniform 1-3000 pairs, unsorted with duplicates, removes half of
+    present edges; every batch's count and the final contents against the
+    oracle."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 15
+    n = 1 << lg
+    s, d = O.rmat_edges(111, lg, 1 << 17)
+    off, nb = O.build_csr(n, s, d)
+    G = byo.Graph.from_csr(ctx, off, nb, container=container)
+    st = O.Store(off, nb)
+    rng = np.random.default_rng(112)
+    batches, ops = [], []
+    shadow = O.Store(off, nb)  # to draw removes from edges present at that point
+    for b in range(60):
+        size = int(np.round(10.0 ** rng.uniform(0, np.log10(3000))))
+        insert = bool(rng.integers(0, 2))
+        if insert:
+            p = rng.integers(0, n, size=(size, 2))
+        else:
+            ro, rn = shadow.export_csr()
+            src = np.repeat(np.arange(n), np.diff(ro).astype(np.int64))
+            pick = rng.integers(0, len(rn), size=size // 2 + 1)
+            p = np.concatenate([np.stack([src[pick], rn[pick]], 1), rng.integers(0, n, size=(size - size // 2, 2))])
+        keys = O.keys_from_pairs(p[:, 0], p[:, 1])
+        keys = np.concatenate([keys, keys[: len(keys) // 4]])
+        rng.shuffle(keys)
+        (shadow.insert_batch if insert else shadow.remove_batch)(keys)
+        batches.append(keys)
+        ops.append(insert)
+    got = G.update_stream(batches, ops)
+    exp = [st.insert_batch(k) if ins else st.remove_batch(k) for k, ins in zip(batches, ops)]
+    assert got.tolist() == exp
+    _check(byo, O, G, st)
+    G.close()
