@@ -126,3 +126,59 @@ def test_random_update_stream(ctx, oracle_mod, container):
     assert got.tolist() == exp
     _check(byo, O, G, st)
     G.close()
+
+
+@pytest.mark.parametrize("container", ["pma", "pcsr", "vos"])
+def test_random_mixed_stream(ctx, oracle_mod, container):
+    """30 seeded ops through byo_graph_mixed_stream: 16-source queries between
+    batches of 1-3000 pairs (unsorted with duplicates, removes half of present
+    edges); every query's levels, every batch's count and the final contents
+    against the oracle at that point of the stream."""
+    import torch
+
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 14
+    n = 1 << lg
+    s, d = O.rmat_edges(121, lg, 1 << 16)
+    off, nb = O.build_csr(n, s, d)
+    G = byo.Graph.from_csr(ctx, off, nb, container=container)
+    st = O.Store(off, nb)
+    shadow = O.Store(off, nb)
+    rng = np.random.default_rng(122)
+    ops = []
+    for i in range(30):
+        if rng.integers(0, 3) == 0:
+            ops.append(("query", rng.integers(0, n, 16).astype(np.uint32)))
+            continue
+        size = int(np.round(10.0 ** rng.uniform(0, np.log10(3000))))
+        insert = bool(rng.integers(0, 2))
+        if insert:
+            p = rng.integers(0, n, size=(size, 2))
+        else:
+            ro, rn = shadow.export_csr()
+            src = np.repeat(np.arange(n), np.diff(ro).astype(np.int64))
+            pick = rng.integers(0, len(rn), size=size // 2 + 1)
+            p = np.concatenate([np.stack([src[pick], rn[pick]], 1), rng.integers(0, n, size=(size - size // 2, 2))])
+        keys = O.keys_from_pairs(p[:, 0], p[:, 1])
+        keys = np.concatenate([keys, keys[: len(keys) // 4]])
+        rng.shuffle(keys)
+        (shadow.insert_batch if insert else shadow.remove_batch)(keys)
+        ops.append(("insert" if insert else "remove", keys))
+    nq = sum(1 for kind, _ in ops if kind == "query")
+    levels = torch.full((max(nq, 1) * 16 * n,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    changed, _ = G.mixed_stream(ops, 16, levels)
+    lev = levels.cpu().numpy().view(np.uint32).reshape(-1, 16, n)
+    q = 0
+    for i, (kind, x) in enumerate(ops):
+        if kind == "query":
+            so, sn = st.export_csr()
+            for j, src in enumerate(x):
+                assert np.array_equal(lev[q, j], O.bfs(so, sn, int(src))[1]), "op %d source %d" % (i, j)
+            q += 1
+        else:
+            exp = st.insert_batch(x) if kind == "insert" else st.remove_batch(x)
+            assert changed[i] == exp, "op %d" % i
+    _check(byo, O, G, st)
+    G.close()
