@@ -675,7 +675,13 @@ __global__ void __launch_bounds__(kPrBlock, 5) k_pr_units(const uint64_t *__rest
   if (threadIdx.x == 0 && l1loc != 0.0) atomicAdd(l1, l1loc);
 }
 
-// One warp per heavy vertex: its chunk partials in chunk order.
+// A group of kCombineLanes lanes per heavy vertex (32 / kCombineLanes
+// vertices per warp; most heavy vertices have a few chunks): its chunk
+// partials, lane l of the group taking chunks l, l + G, ... in order, summed
+// by a fixed tree over the group; then the vertex is finished by the group's
+// first lane.  Measured at RMAT 2^22 (ms per iteration of units + combine):
+// groups of 32 / 8 / 4 lanes 0.563 / 0.543 / 0.549.
+constexpr int kCombineLanes = 8;
 template <bool kComp, typename T>
 __global__ void __launch_bounds__(256) k_pr_combine(const uint32_t *__restrict__ heavy,
                                                     const uint64_t *__restrict__ cbase, uint64_t nheavy,
@@ -683,19 +689,24 @@ __global__ void __launch_bounds__(256) k_pr_combine(const uint32_t *__restrict__
                                                     const T *__restrict__ p_curr, T *__restrict__ p_next,
                                                     T *__restrict__ pdiv_out, T damping, T added, double *l1) {
   __shared__ double sm[9];
-  const unsigned lane = lane_id();
+  constexpr int kPer = 32 / kCombineLanes;
+  const unsigned lane = lane_id(), gl = lane % kCombineLanes;
   const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   double l1loc = 0.0;
-  for (uint64_t h = gw; h < nheavy; h += nw) {
-    const uint64_t c0 = cbase[h], c1 = cbase[h + 1];
+  for (uint64_t base = gw * kPer; base < nheavy; base += nw * kPer) {
+    const uint64_t h = base + lane / kCombineLanes;
     T s = T(0), c = T(0);
-    for (uint64_t k = c0 + lane; k < c1; k += 32) {
-      acc_add<kComp>(s, c, part[2 * k]);
-      if (kComp) c += part[2 * k + 1];
+    if (h < nheavy) {
+      const uint64_t c0 = cbase[h], c1 = cbase[h + 1];
+      for (uint64_t k = c0 + gl; k < c1; k += kCombineLanes) {
+        acc_add<kComp>(s, c, part[2 * k]);
+        if (kComp) c += part[2 * k + 1];
+      }
     }
-    T tot = group_total<kComp, T, 32>(s, c);
-    if (lane == 0) pr_finish<kComp, T>(heavy[h], tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+    const T tot = group_total<kComp, T, kCombineLanes>(s, c);
+    if (h < nheavy && gl == 0)
+      pr_finish<kComp, T>(heavy[h], tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
   }
   l1loc = block_sum(l1loc, sm);
   if (threadIdx.x == 0 && l1loc != 0.0) atomicAdd(l1, l1loc);
@@ -809,7 +820,7 @@ static int pagerank_impl(byo_graph *g, double eps, uint32_t max_iters, double *d
   BYO_TRY(ws(g, WS_TC_CNT, 2 * max_chunks + 2, &part));
   const T damping = (T)0.85;
   const T added = (T)((1 - 0.85) * (1 / (double)n));
-  const int grid_c = grid_for(ctx, nheavy * 32, 256, 8);
+  const int grid_c = grid_for(ctx, nheavy * kCombineLanes, 256, 8);
   const size_t units_smem = (size_t)(kPrBlock / 32) * pr_warp_smem<T>();
   BYO_CU(ctx, cudaFuncSetAttribute(k_pr_units<kComp, T, sizeof(T) == 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)units_smem));
