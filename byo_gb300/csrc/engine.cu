@@ -264,7 +264,7 @@ __device__ __forceinline__ bool in_frontier(const uint32_t *s_bits, int stage_wo
   return (word >> (u & 31)) & 1u;
 }
 
-__global__ void __launch_bounds__(1024) k_pull(const uint64_t *__restrict__ off,
+__global__ void __launch_bounds__(1024, 2) k_pull(const uint64_t *__restrict__ off,
                                                const uint32_t *__restrict__ slots,
                                                const uint32_t *__restrict__ deg,
                                                const uint32_t *__restrict__ Fbits, uint64_t n,
