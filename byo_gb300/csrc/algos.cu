@@ -36,13 +36,15 @@ constexpr int kSample = 2;
 
 __device__ __forceinline__ uint32_t ld_parent(const uint32_t *p, uint32_t v) { return __ldcg(p + v); }
 
-// Root of v with path halving; parents only ever point to smaller ids.
+// Root of v, with path halving when kHalve; parents only ever point to
+// smaller ids.
+template <bool kHalve = true>
 __device__ __forceinline__ uint32_t cc_find(uint32_t *p, uint32_t v) {
   uint32_t cur = ld_parent(p, v);
   if (cur == v) return v;
   uint32_t prev = v, next;
   while (cur > (next = ld_parent(p, cur))) {
-    p[prev] = next;
+    if (kHalve) p[prev] = next;
     prev = cur;
     cur = next;
   }
@@ -88,10 +90,13 @@ __global__ void k_cc_sample(const uint64_t *__restrict__ off, const uint32_t *__
   }
 }
 
+// Every vertex to its root.  The finds do not halve: a halving store into
+// p[w] by a thread passing through w could land after w's own thread wrote
+// its root there, and leave a stale ancestor behind the last pass.
 __global__ void k_cc_compress(uint32_t *p, uint64_t n) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x)
-    p[v] = cc_find(p, (uint32_t)v);
+    p[v] = cc_find<false>(p, (uint32_t)v);
 }
 
 // The vertices whose remaining edges must be linked: more than kSample

@@ -86,3 +86,22 @@ def test_structured_graphs(ctx, oracle_mod, name):
         p64, it64, _ = byo.PageRank(G, 1e-6, 60, precision=1, info=True)
         assert it64 == oit and float(np.abs(p64 - op).sum()) <= 1e-12, container
         G.close()
+
+
+def test_cc_labels_stable_over_repeats(ctx, oracle_mod):
+    """Connectivity on a graph of thousands of small components, repeated:
+    the labels must be the component minima on every run (a compress pass
+    whose finds halved paths once left one vertex pointing at a non-root
+    ancestor in about one run of 40)."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n, s, d = _graphs(O)["sparse"]
+    off, nb = O.build_csr(n, np.asarray(s, np.uint32), np.asarray(d, np.uint32))
+    olab = O.cc(off, nb)
+    for container in ("csr", "pcsr"):
+        G = byo.Graph.from_csr(ctx, off, nb, container=container)
+        for _ in range(150):
+            assert np.array_equal(byo.SimpleUnionAsync(G), olab), container
+        for _ in range(20):
+            assert np.array_equal(byo.bfs_cc(G), olab), container
+        G.close()
