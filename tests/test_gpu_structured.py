@@ -105,3 +105,38 @@ def test_cc_labels_stable_over_repeats(ctx, oracle_mod):
         for _ in range(20):
             assert np.array_equal(byo.bfs_cc(G), olab), container
         G.close()
+
+
+@pytest.mark.parametrize("name", ["sparse", "star", "rmat"])
+def test_traversals_repeat_identically(ctx, oracle_mod, name):
+    """Races show up as rare differences between runs: BFS under every
+    policy, 64-source BFS and PageRank repeated on the same graph must give
+    the oracle's levels and min-id parents every time, and PageRank the same
+    bits every time (its sums have a fixed order)."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    if name == "rmat":
+        s, d = O.rmat_edges(141, 15, 1 << 19)
+        n = 1 << 15
+    else:
+        n, s, d = _graphs(O)[name]
+    off, nb = O.build_csr(n, np.asarray(s, np.uint32), np.asarray(d, np.uint32))
+    deg = np.diff(off.astype(np.int64))
+    src = int(np.argmax(deg))
+    opar, olev = O.bfs(off, nb, src)
+    multi = np.random.default_rng(142).integers(0, n, 64).astype(np.uint32)
+    exp_multi = [O.bfs(off, nb, int(x))[1] for x in multi[:8]]
+    for container in ("csr", "pma"):
+        G = byo.Graph.from_csr(ctx, off, nb, container=container)
+        for _ in range(12):
+            for pol in (0, 1, 2, 3, 4, 5):
+                par, lev = byo.BFS(G, src, policy=pol, levels=True)
+                assert np.array_equal(lev, olev) and np.array_equal(par, opar), (container, pol)
+        for _ in range(6):
+            lv = byo.BFS_multi(G, multi)
+            for j in range(8):
+                assert np.array_equal(lv[j], exp_multi[j]), (container, j)
+        p0 = byo.PageRank(G, 1e-6, 20)
+        for _ in range(5):
+            assert np.array_equal(byo.PageRank(G, 1e-6, 20), p0), container
+        G.close()
