@@ -78,15 +78,28 @@ __global__ void k_cc_sample(const uint64_t *__restrict__ off, const uint32_t *__
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t b = off[v], e = off[v + 1];
-    int taken = 0;
-    for (uint64_t j = b; j < e; j++) {
-      const uint32_t u = slots[j];
-      if (u == kSentinel) continue;
-      if (taken++ == round) {
-        cc_link(p, (uint32_t)v, u);
-        break;
+    if (b + round >= e) continue;  // fewer than round + 1 slots
+    // slots b .. b + round: the sampled neighbour is the last when none is a
+    // gap (always, on a compact CSR)
+    uint32_t x = kSentinel;
+    bool gap = false;
+    for (int r = 0; r <= round; r++) {
+      x = slots[b + r];
+      gap |= x == kSentinel;
+    }
+    if (gap) {  // a gapped view: the round-th neighbour past the gaps
+      x = kSentinel;
+      int taken = 0;
+      for (uint64_t j = b; j < e; j++) {
+        const uint32_t y = slots[j];
+        if (y == kSentinel) continue;
+        if (taken++ == round) {
+          x = y;
+          break;
+        }
       }
     }
+    if (x != kSentinel) cc_link(p, (uint32_t)v, x);
   }
 }
 
