@@ -58,3 +58,14 @@ def test_pagerank_iteration_bytes():
     assert bench.pr_iteration_bytes(n, m, m) == 4 * m + 4 * m + 8 * (n + 1) + 4 * n + 4 * n + 4 * n + 4 * n
     # a gapped view reads its gaps too, but gathers only for edges
     assert bench.pr_iteration_bytes(n, m, m + 500) - bench.pr_iteration_bytes(n, m, m) == 4 * 500
+
+
+def test_update_bytes_per_container():
+    """Batch update bytes: 16 B per key (sort read + write) plus each element
+    of a touched leaf read and written: the PMA's 8-byte (src, dst) entries,
+    the packed CSR's 4-byte slots and sentinel bits."""
+    import bench
+    B, E = 2 * 10 ** 7, 96_645_293
+    assert bench.update_bytes(B, E, "pma") == 16 * B + 16 * E
+    assert bench.update_bytes(B, E, "pcsr") == 16 * B + 8.25 * E
+    assert bench.update_bytes(B, 0) == 16 * B
