@@ -490,7 +490,7 @@ __global__ void k_pr_desc_chunks(const uint64_t *__restrict__ off, const uint32_
       d.v0 = v;
       d.v1 = kNoVertex;
       d.chunk = (uint32_t)(cbase[h] + k);
-      d.pad = 0;
+      d.pad = cbase[h + 1] - cbase[h] == 1;  // the vertex's only chunk: its unit finishes it
       desc[base + cbase[h] + k] = d;
     }
   }
@@ -662,8 +662,12 @@ __global__ void __launch_bounds__(kPrBlock, 5) k_pr_units(const uint64_t *__rest
       }
       T tot = group_total<kComp, T, 32>(s, c);
       if (lane == 0) {
-        part[2 * (uint64_t)d.chunk] = tot;
-        part[2 * (uint64_t)d.chunk + 1] = T(0);
+        if (d.pad) {
+          pr_finish<kComp, T>(d.v0, tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+        } else {
+          part[2 * (uint64_t)d.chunk] = tot;
+          part[2 * (uint64_t)d.chunk + 1] = T(0);
+        }
       }
       continue;
     }
@@ -683,8 +687,12 @@ __global__ void __launch_bounds__(kPrBlock, 5) k_pr_units(const uint64_t *__rest
       for (uint32_t r = lane; r < len; r += 32) acc_add<kComp>(s, c, buf[r]);
       T tot = group_total<kComp, T, 32>(s, c);
       if (lane == 0) {
-        part[2 * (uint64_t)d.chunk] = tot;
-        part[2 * (uint64_t)d.chunk + 1] = T(0);
+        if (d.pad) {
+          pr_finish<kComp, T>(d.v0, tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
+        } else {
+          part[2 * (uint64_t)d.chunk] = tot;
+          part[2 * (uint64_t)d.chunk + 1] = T(0);
+        }
       }
     }
     __syncwarp();
@@ -715,15 +723,18 @@ __global__ void __launch_bounds__(256) k_pr_combine(const uint32_t *__restrict__
   for (uint64_t base = gw * kPer; base < nheavy; base += nw * kPer) {
     const uint64_t h = base + lane / kCombineLanes;
     T s = T(0), c = T(0);
+    bool mine = false;  // a vertex of several chunks (one chunk: finished by its unit)
     if (h < nheavy) {
       const uint64_t c0 = cbase[h], c1 = cbase[h + 1];
-      for (uint64_t k = c0 + gl; k < c1; k += kCombineLanes) {
-        acc_add<kComp>(s, c, part[2 * k]);
-        if (kComp) c += part[2 * k + 1];
-      }
+      mine = c1 - c0 > 1;
+      if (mine)
+        for (uint64_t k = c0 + gl; k < c1; k += kCombineLanes) {
+          acc_add<kComp>(s, c, part[2 * k]);
+          if (kComp) c += part[2 * k + 1];
+        }
     }
     const T tot = group_total<kComp, T, kCombineLanes>(s, c);
-    if (h < nheavy && gl == 0)
+    if (mine && gl == 0)
       pr_finish<kComp, T>(heavy[h], tot, deg, p_curr, p_next, pdiv_out, damping, added, l1loc);
   }
   l1loc = block_sum(l1loc, sm);
