@@ -3,8 +3,9 @@
 C1 (the reference's run_csr case): CSR on RMAT(.57, .19, .19) with 2^20
 vertices and 2^24 draws, symmetrised and deduplicated: BFS from 10 (levels and
 min-id parents), CC labels (minimum vertex id), PageRank with eps 1e-6.
-C2 (the dynamic packed-memory-array case): RMAT with 2^22 vertices and 2^26
-draws in the PMA container; a batch of 10^7 uniform pairs (2*10^7 directed
+C2 (the dynamic case): RMAT with 2^22 vertices and 2^26 draws in each
+updatable container (the packed-memory array, the packed CSR, the vector of
+sorted runs); a batch of 10^7 uniform pairs (2*10^7 directed
 keys, unsorted) inserted and then removed, plus 10^3 and 10^5 pair batches:
 after every batch the sorted adjacency and the changed-key count equal the
 oracle's sorted-set store (gbbs/graph.h:3071-3124 semantics), and BFS(10) and
@@ -55,14 +56,15 @@ def test_c1_csr_rmat20(ctx, oracle_mod):
     G.close()
 
 
-def test_c2_pma_rmat22_batches(ctx, oracle_mod):
+@pytest.mark.parametrize("container", ["pma", "pcsr", "vos"])
+def test_c2_rmat22_batches(ctx, oracle_mod, container):
     import byo_gb300 as byo
     O = oracle_mod
     s, d = O.rmat_edges(1, 22, 1 << 26)
     off, nb = O.build_csr(1 << 22, s, d)
     del s, d
     n = 1 << 22
-    G = byo.Graph.generate(ctx, "rmat", seed=1, lg_n=22, draws=1 << 26, container="pma")
+    G = byo.Graph.generate(ctx, "rmat", seed=1, lg_n=22, draws=1 << 26, container=container)
     go, gn = G.export_csr()
     assert np.array_equal(go, off) and np.array_equal(gn, nb), "generated C2 graph differs from the oracle's"
     del go, gn

@@ -140,3 +140,108 @@ def test_traversals_repeat_identically(ctx, oracle_mod, name):
         for _ in range(5):
             assert np.array_equal(byo.PageRank(G, 1e-6, 20), p0), container
         G.close()
+
+
+def _remote(n, rng):
+    """Test_Map_Remote arrays of widths 0 (a bit vector), 4 and 16 bytes."""
+    bits = rng.integers(0, 2, size=n).astype(bool)
+    packed = np.concatenate([np.packbits(bits, bitorder="little"),
+                             np.zeros((-((n + 7) // 8)) % 8, np.uint8)]).view(np.uint64)
+    wide = np.full((n, 2), 5, np.uint64)  # the padding word is not read
+    wide[:, 0] = rng.integers(0, 1 << 40, size=n)
+    return {0: packed, 4: rng.integers(0, 1 << 31, size=n).astype(np.uint32), 16: wide}
+
+
+@pytest.mark.parametrize("name", ["path", "star", "cliques", "tree", "lollipop", "sparse"])
+def test_structured_delta_map_bytepd(ctx, oracle_mod, name):
+    """PageRankDelta (the oracle's round count, L1 <= 1e-6), Test_Map and
+    Test_Map_Remote on every container (the PMA's gaps, the packed CSR's
+    sentinel slots and the vector of runs' slack all read as no edge), and
+    the byte-PD encoder (byte-identical) and decoder at block sizes 1000, 7
+    and 1 on the structured graphs."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    n, s, d = _graphs(O)[name]
+    off, nb = O.build_csr(n, np.asarray(s, np.uint32), np.asarray(d, np.uint32))
+    rng = np.random.default_rng(134)
+    od, orr, _ = O.pagerank_delta(off, nb, 1e-7, 1e-3, 100)
+    remote = _remote(n, rng)
+    exp_remote = {w: O.map_remote(off, nb, a, w) for w, a in remote.items()}
+    exp_map = O.map_sum(off, nb)
+    for container in ("csr", "pma", "pcsr", "vos"):
+        G = byo.Graph.from_csr(ctx, off, nb, container=container)
+        p, r, _ = byo.PageRankDelta(G, 1e-7, 1e-3, 100, info=True)
+        assert r == orr and float(np.abs(p - od).sum()) <= 1e-6, container
+        assert byo.Test_Map(G) == exp_map, container
+        for w, a in remote.items():
+            assert byo.Test_Map_Remote(G, a, w) == exp_remote[w], (container, w)
+        G.close()
+    G = byo.Graph.from_csr(ctx, off, nb)
+    for P in (1000, 7, 1):
+        obo, odg, odata = O.bytepd_encode(off, nb, P)
+        bo, dg, data = G.to_bytepd(P)
+        assert np.array_equal(bo, obo) and np.array_equal(dg, odg) and bytes(data) == bytes(odata), P
+        H = byo.Graph.from_bytepd(ctx, obo, odg, odata, block=P, container="pcsr")
+        o2, n2 = H.export_csr()
+        assert np.array_equal(o2, off) and np.array_equal(n2, nb), P
+        H.close()
+    G.close()
+
+
+def _bulk_ops(O, gs):
+    """(graph, [(insert?, keys)]) pairs of whole-structure updates; each
+    sequence ends on a symmetric graph (BFS and CC follow out-edges)."""
+    out = []
+    n, _, _ = gs["star"]
+    hub = O.keys_from_pairs(np.zeros(n - 1, np.int64), np.arange(1, n))
+    out.append(("star", [(False, hub), (True, hub[: n // 2]), (True, hub)]))
+    cut = np.arange(0, 2999, 10)
+    cuts = O.keys_from_pairs(cut, cut + 1)
+    out.append(("path", [(False, cuts), (True, cuts[::2]), (True, cuts)]))
+    a, b = np.triu_indices(90, 1)
+    big = O.keys_from_pairs(a + 500, b + 500)  # overlaps cliques from id 500 on
+    out.append(("cliques", [(True, big), (False, big), (True, O.keys_from_pairs(a[::3] + 500, b[::3] + 500))]))
+    a, b = np.triu_indices(150, 1)
+    fresh = O.keys_from_pairs(a + 95000, b + 95000)  # ids past every edge so far
+    out.append(("sparse", [(True, fresh), (False, fresh[: len(fresh) // 2]), (False, fresh)]))
+    tail = np.arange(200, 2200)
+    out.append(("lollipop", [(False, O.keys_from_pairs(tail - 1, tail)),
+                             (True, O.keys_from_pairs(np.zeros(2000, np.int64), tail))]))
+    return out
+
+
+@pytest.mark.parametrize("container", ["pma", "pcsr", "vos"])
+def test_structured_bulk_updates(ctx, oracle_mod, container):
+    """Whole-structure updates: the star's hub loses every edge (one vertex's
+    run across many leaves), regains half, then all; every tenth edge of the
+    path is cut and rejoined; a 90-clique is laid over the cliques and taken
+    off; a 150-clique appears among ids that had no edges and goes in two
+    steps; the lollipop's tail becomes a second star.  The changed count,
+    contents and degrees after every batch, BFS and CC after each graph, all
+    against the oracle."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    gs = _graphs(O)
+    for name, ops in _bulk_ops(O, gs):
+        n, s, d = gs[name]
+        off, nb = O.build_csr(n, np.asarray(s, np.uint32), np.asarray(d, np.uint32))
+        G = byo.Graph.from_csr(ctx, off, nb, container=container)
+        st = O.Store(off, nb)
+        rng = np.random.default_rng(135)
+        for i, (ins, keys) in enumerate(ops):
+            k = keys.copy()
+            rng.shuffle(k)
+            if ins:
+                assert G.insert_batch(k) == st.insert_batch(k), (name, i)
+            else:
+                assert G.remove_batch(k) == st.remove_batch(k), (name, i)
+            ro, rn = st.export_csr()
+            go, gn = G.export_csr()
+            assert np.array_equal(go, ro) and np.array_equal(gn, rn), (name, i)
+            assert np.array_equal(G.degrees(), np.diff(ro).astype(np.uint32)), (name, i)
+        for src in (0, int(np.argmax(np.diff(ro)))):
+            opar, olev = O.bfs(ro, rn, src)
+            par, lev = byo.BFS(G, src, levels=True)
+            assert np.array_equal(lev, olev) and np.array_equal(par, opar), (name, src)
+        assert np.array_equal(byo.SimpleUnionAsync(G), O.cc(ro, rn)), name
+        G.close()
