@@ -194,7 +194,9 @@ int sort_u64(byo_ctx *ctx, uint64_t *keys, uint64_t *tmp, uint64_t count, uint64
              uint64_t **sorted);
 // Sorts an update batch (keys src<<32|dst, src,dst < n) from `in` into `out`
 // by a bucket partition on src and per-bucket shared-memory sorts; `tmp`
-// (count keys) is used only by buckets too large for shared memory.
+// (count keys) is used only by buckets too large for shared memory.  A key
+// with src or dst >= n is placed without an out-of-bounds access (in an
+// unspecified order), so the sort may run before the batch is validated.
 int sort_bucketed(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t n, uint64_t *out, uint64_t *tmp);
 // Removes adjacent duplicates of a sorted array (and src==dst keys if
 // drop_loops) into out; *out_count on the host.  Scratch slots 3.

@@ -347,10 +347,17 @@ __global__ void k_pcsr_check(const uint64_t *__restrict__ keys, uint64_t b, uint
 }
 
 // bstart[j] = first batch key (sorted src << 32 | dst) whose composite key is
-// >= sep[j]; bstart[0] = 0, bstart[NL] = b.
+// >= sep[j]; bstart[0] = 0, bstart[NL] = b.  A batch the check flagged (a key
+// >= n, or a "sorted" batch that is not) is routed to no leaf, so the merge
+// changes nothing; the host rejects it after the merge.
 __global__ void k_pcsr_route(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
-                             uint64_t b, uint64_t *bstart) {
+                             uint64_t b, const unsigned int *bad, uint64_t *bstart) {
+  const bool drop = bad[0] || bad[1];
   for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j <= NL; j += (uint64_t)gridDim.x * blockDim.x) {
+    if (drop) {
+      bstart[j] = 0;
+      continue;
+    }
     if (j == 0 || j == NL) {
       bstart[j] = j ? b : 0;
       continue;
@@ -493,38 +500,59 @@ __global__ void __launch_bounds__(32 * kPcsrWarps, 8) k_pcsr_merge(
   long long dsum = 0;
   unsigned long long nleaves = 0, nentries = 0;
   const uint64_t nwork = kList ? *nseg : NL;
-  for (uint64_t q = gw; q < nwork; q += nw) {
-    uint64_t j, b0, b1;
+  // the next work item's leaf, batch range, count and first owner are loaded
+  // while this one merges (a leaf is listed once, and only the warp merging
+  // it writes its cnt and lv)
+  uint64_t nj = 0, nb0 = 0, nb1 = 0;
+  uint32_t ncnt = 0, nlv = 0;
+  auto fetch = [&](uint64_t q) {
     if (kList) {
-      j = seg[2 * q];
-      b0 = seg[2 * q + 1] >> 32;
-      b1 = seg[2 * q + 1] & 0xFFFFFFFFull;
+      nj = seg[2 * q];
+      const uint64_t r = seg[2 * q + 1];
+      nb0 = r >> 32;
+      nb1 = r & 0xFFFFFFFFull;
     } else {
-      j = q;
-      b0 = bstart[j];
-      b1 = bstart[j + 1];
+      nj = q;
+      nb0 = bstart[q];
+      nb1 = bstart[q + 1];
     }
-    const uint32_t c = min(cnt[j], kPL);
+    ncnt = cnt[nj];
+    nlv = lv[nj];
+  };
+  if (gw < nwork) fetch(gw);
+  for (uint64_t q = gw; q < nwork; q += nw) {
+    const uint64_t j = nj, b0 = nb0, b1 = nb1;
+    const uint32_t c = min(ncnt, kPL), lv0 = nlv;
+    if (q + nw < nwork) fetch(q + nw);
     if (b0 == b1) {
       if (lane == 0) rcount[j] = c;
       continue;
     }
     nleaves++;
     nentries += c;
-    pcsr_decode_leaf(slots, head, j, c, lv[j], A);
+    // the first round of batch keys is in flight with the leaf's loads
+    uint64_t xn = b0 + lane < b1 ? keys[b0 + lane] : 0;
+    pcsr_decode_leaf(slots, head, j, c, lv0, A);
     for (uint32_t i = lane; i <= c; i += 32) D[i] = 0;
     if (lane < kPW) Hs[w][lane] = 0;
     __syncwarp();
     MergeOut o{slots, vbeg, lv, Hs[w], j, nullptr};
     const bool direct = insert && c + (b1 - b0) <= kPL;
     uint32_t changed = 0;
+    uint64_t prev_last = 0;  // the previous round's last key
     for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
       const uint64_t t = t0 + lane;
       bool act = false;
       uint32_t l = 0;
       uint64_t x = 0;
-      if (t < b1 && !(t > b0 && keys[t - 1] == keys[t])) {
-        x = ck_of(keys[t]);
+      const uint64_t k = xn;
+      // the next round's key loads while this round ranks
+      xn = t + 32 < b1 ? keys[t + 32] : 0;
+      uint64_t before = __shfl_up_sync(kFull, k, 1);
+      if (lane == 0) before = prev_last;
+      prev_last = __shfl_sync(kFull, k, 31);
+      if (t < b1 && !(t > b0 && before == k)) {
+        x = ck_of(k);
         l = rank_in(A, c, x);
         const bool present = l < c && A[l] == x;
         act = insert ? !present : present;
@@ -676,16 +704,14 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PCSR container");
   g->version++;  // any snapshot of the contents is stale from here on
   const uint64_t n = g->n, m_before = g->m;
-  // 1. validate, then sort (duplicates stay: the merge skips them).  A batch
-  // of at most one key per leaf takes the segment list (only its own leaves
-  // are visited); when it also needs no bucketed sort (sorted input, or at
-  // most 4096 keys for the one-CTA register sort, which does not index by
-  // key) its validation is read after the single synchronisation of the
-  // update, and the segment kernels drop an invalid batch.
+  // 1. validate on the device, sort (duplicates stay: the merge skips them).
+  // No sort indexes out of bounds by key, and the segment kernels or the
+  // routing drop an invalid batch (the merge then has no work), so the
+  // validation is read after the single synchronisation of the update.  A batch of at most one key per leaf takes
+  // the segment list (only its own leaves are visited).
   const uint64_t NL = p->NL;
   const bool small = !sorted && count <= sort_small_max();
   const bool list = count <= NL && count < (1ull << 32);
-  const bool defer = list && (sorted || small);
   BYO_TRY(ensure(ctx, p->keys_a, count * 8));
   BYO_TRY(ensure(ctx, p->keys_b, count * 8));
   BYO_TRY(ensure(ctx, p->misc, 128));
@@ -699,12 +725,6 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   uint64_t *h = nullptr;
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
   const unsigned int *hf = (const unsigned int *)(h + 8);
-  if (!defer) {
-    BYO_CU(ctx, cudaMemcpyAsync(h + 8, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
-    BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-    if (hf[0]) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
-    if (hf[1]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
-  }
   const uint64_t *batch = d_keys_in;
   uint64_t b = count;
   if (small) {
@@ -735,16 +755,17 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
              (uint64_t *)p->ovf_off.p, ctr, g->d_deg, g->d_off);
   } else {
     launch(ctx, k_pcsr_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL, batch,
-           b, bstart);
+           b, (const unsigned int *)flags, bstart);
     launch_t(ctx, "pcsr_merge", k_pcsr_merge<false>, dim3(grid_for(ctx, NL * 32, 32 * kPcsrWarps, 8)),
              dim3(32 * kPcsrWarps), 0, p->slots, p->head, p->cnt, p->lv, NL, batch, (const uint64_t *)bstart,
              (uint64_t *)nullptr, (const unsigned long long *)nullptr, insert, rcount, (uint64_t *)p->ovf.p,
              (uint64_t *)p->ovf_off.p, ctr, g->d_deg, g->d_off);
   }
   BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 80, cudaMemcpyDeviceToHost, ctx->stream));
+  BYO_CU(ctx, cudaMemcpyAsync(h + 8, flags, 16, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  if (defer && hf[0]) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
-  if (defer && hf[1]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
+  if (hf[0]) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+  if (hf[1]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
   const uint64_t novf = h[1], merged_leaves = h[3], merged_entries = h[4];
   const uint64_t m_after = (uint64_t)((long long)m_before + (long long)h[2]);
   g->m = m_after;

@@ -129,10 +129,19 @@ __global__ void k_check_sorted(const uint64_t *__restrict__ keys, uint64_t cnt, 
 
 // ---------------------------------------------------------------- routing / counting
 
+// bounds (optional): the batch's largest src and dst, and *unsorted; a batch
+// with a key >= n, or a "sorted" batch that is not, is routed to no leaf (the
+// merge then changes nothing and the host rejects it after the merge).
 __global__ void k_pma_route(const uint64_t *__restrict__ sep, uint64_t NL, const uint64_t *__restrict__ keys,
-                            uint64_t b, uint64_t *bstart) {
+                            uint64_t b, uint64_t *bstart, const unsigned long long *bounds, uint64_t n,
+                            const unsigned int *unsorted) {
+  const bool drop = bounds && (bounds[0] >= n || bounds[1] >= n || *unsorted);
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= NL;
        i += (uint64_t)gridDim.x * blockDim.x) {
+    if (drop) {
+      bstart[i] = 0;
+      continue;
+    }
     if (i == NL) {
       bstart[NL] = b;
       continue;
@@ -709,9 +718,23 @@ __global__ void __launch_bounds__(32 * kRankWarps, 8) k_pma_merge_rank(
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   long long dsum = 0;
   unsigned long long nleaves = 0, nentries = 0;
+  // the next leaf's batch range and count are loaded while this one merges
+  // (cnt[j] is written only by the warp that merges leaf j)
+  uint64_t nb0 = 0, nb1 = 0;
+  uint32_t ncnt = 0;
+  if (gw < NL) {
+    nb0 = bstart[gw];
+    nb1 = bstart[gw + 1];
+    ncnt = cnt[gw];
+  }
   for (uint64_t j = gw; j < NL; j += nw) {
-    const uint64_t b0 = bstart[j], b1 = bstart[j + 1];
-    const uint32_t c = min(cnt[j], kLeaf);
+    const uint64_t b0 = nb0, b1 = nb1;
+    const uint32_t c = min(ncnt, kLeaf);
+    if (j + nw < NL) {
+      nb0 = bstart[j + nw];
+      nb1 = bstart[j + nw + 1];
+      ncnt = cnt[j + nw];
+    }
     if (b0 == b1) {
       if (lane == 0) rcount[j] = c;
       continue;
@@ -719,6 +742,8 @@ __global__ void __launch_bounds__(32 * kRankWarps, 8) k_pma_merge_rank(
     nleaves++;
     nentries += c;
     const uint64_t base = j * kLeaf;
+    // the first round of batch keys is in flight with the leaf's loads
+    uint64_t xn = b0 + lane < b1 ? keys[b0 + lane] : 0;
     for (uint32_t e0 = 0; e0 < c; e0 += 256) {  // eight loads of each array per lane in flight
       uint32_t hs[8], ds[8];
 #pragma unroll
@@ -738,14 +763,19 @@ __global__ void __launch_bounds__(32 * kRankWarps, 8) k_pma_merge_rank(
     RankOut o{src, dst, base, nullptr};
     const bool direct = insert && c + (b1 - b0) <= kLeaf;
     uint32_t changed = 0;
+    uint64_t prev_last = 0;  // the previous round's last key
     for (uint64_t t0 = b0; t0 < b1; t0 += 32) {
       const uint64_t t = t0 + lane;
       bool act = false;
       uint32_t l = 0;
-      uint64_t x = 0;
+      const uint64_t x = xn;
+      // the next round's key loads while this round ranks
+      xn = t + 32 < b1 ? keys[t + 32] : 0;
+      uint64_t before = __shfl_up_sync(kFull, x, 1);
+      if (lane == 0) before = prev_last;
+      prev_last = __shfl_sync(kFull, x, 31);
       if (t < b1) {
-        x = keys[t];
-        if (!(t > b0 && keys[t - 1] == x)) {
+        if (!(t > b0 && before == x)) {
           l = rank_of(A, c, x);
           const bool present = l < c && A[l] == x;
           act = insert ? !present : present;
@@ -1272,8 +1302,11 @@ static uint64_t leaves_for(uint64_t m) {
   return NL < 1 ? 1 : NL;
 }
 
-// Recomputes the traversal view (off, deg, nslots, m) from the leaves.
-static int pma_view(byo_graph *g) {
+// Recomputes the traversal view (off, deg, nslots) from the leaves, with no
+// host synchronisation: m, the element count the leaves hold, is known to the
+// caller, and the pass over long vertex ranges reads its chunk count on the
+// device (it exits at once when there are none).
+static int pma_view(byo_graph *g, uint64_t m) {
   byo_ctx *ctx = g->ctx;
   Pma *p = g->pma;
   uint64_t *epre = nullptr, *elem = nullptr;
@@ -1289,17 +1322,11 @@ static int pma_view(byo_graph *g) {
   launch_t(ctx, "pma_view", k_pma_view_leaves, dim3(grid_for(ctx, p->NL * 32, 32 * kViewWarps, 8)), dim3(32 * kViewWarps), 0,
          (const uint32_t *)p->src, (const uint32_t *)p->cnt, (const uint64_t *)p->sep, (const uint64_t *)epre, p->NL,
          g->n, g->d_off, elem, (uint64_t *)p->vrange.p, chunks, nch);
-  uint64_t *h = nullptr;
-  BYO_TRY(pinned(ctx, 4096, (void **)&h));
-  BYO_CU(ctx, cudaMemcpyAsync(h, epre + p->NL, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaMemcpyAsync(h + 1, nch, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
-  g->m = h[0];
-  if (h[1])
-    launch_t(ctx, "pma_view", k_pma_view_chunks, dim3(grid_for(ctx, h[1], 1, 8)), dim3(kViewThreads), 0, (const uint32_t *)p->src,
-           (const uint32_t *)p->cnt, (const uint64_t *)nullptr, (const uint64_t *)p->vrange.p,
-           (const uint64_t *)chunks, (const unsigned long long *)nch, g->d_off, (const unsigned long long *)nullptr,
-           (uint64_t)0, 0.0, (const uint64_t *)epre, elem);
+  g->m = m;
+  launch_t(ctx, "pma_view", k_pma_view_chunks, dim3(grid_for(ctx, (g->n + 1) / kViewChunk + 1, 1, 8)),
+           dim3(kViewThreads), 0, (const uint32_t *)p->src, (const uint32_t *)p->cnt, (const uint64_t *)nullptr,
+           (const uint64_t *)p->vrange.p, (const uint64_t *)chunks, (const unsigned long long *)nch, g->d_off,
+           (const unsigned long long *)nullptr, (uint64_t)0, 0.0, (const uint64_t *)epre, elem);
   launch(ctx, k_pma_deg, dim3(grid_for(ctx, g->n, 256)), dim3(256), 0, (const uint64_t *)elem, g->n, g->d_deg);
   g->d_slots = p->dst;
   g->nslots = p->NL * kLeaf;
@@ -1328,7 +1355,7 @@ static int pma_layout(byo_graph *g, const uint64_t *d_keys, uint64_t m, uint64_t
   p->sep = sp;
   p->NL = NL;
   p->H = ceil_log2(NL);
-  return pma_view(g);
+  return pma_view(g, m);
 }
 
 int pma_build(byo_graph *g, const uint64_t *d_keys, uint64_t m) {
@@ -1482,7 +1509,7 @@ static int pma_finish_windowed(byo_graph *g, bool list, const uint64_t *bstart, 
            (const uint64_t *)stg, (const uint64_t *)rpre, (const uint32_t *)win, NL, p->src, p->dst, p->cnt, p->sep,
            NL, 0, (const uint64_t *)p->sep);
   BYO_TRY(check_launch(ctx, "pma_update"));
-  return pma_view(g);
+  return pma_view(g, total);
 }
 
 uint64_t pma_leaf_slots() { return kLeaf; }
@@ -1528,12 +1555,13 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
     strategy = update_strategy(ctx, count, m_before, p->NL * kLeaf, sorted, insert);
   ctx->last_update_strategy = strategy;
   // A batch of at most one key per leaf takes the segment-list merge, which
-  // visits only its own leaves and keeps the view current around them.  When
-  // it also needs no bucketed sort it is validated on the device (the segment
-  // kernel drops an invalid batch) and checked here after the single
-  // synchronisation of the update.
+  // visits only its own leaves and keeps the view current around them.  An
+  // in-place merge (either kind) validates the batch on the device -- the
+  // segment kernel, or the routing for the rank merge, drops an invalid batch,
+  // and no sort indexes out of bounds by key -- and the result is checked
+  // after the merge's synchronisation; the rebuild strategy checks it first.
   const bool list = count <= p->NL && count < (1ull << 32);
-  const bool defer = list && (sorted || small_sort) && strategy == 0;
+  const bool defer = strategy == 0;
   if (!defer) {
     BYO_CU(ctx, cudaMemcpyAsync(h, p->misc.p, 32, cudaMemcpyDeviceToHost, ctx->stream));
     BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1562,12 +1590,14 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   uint32_t *rcount = (uint32_t *)p->rcount.p;
   if (strategy == 1) {
     launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
-           (const uint64_t *)batch, b, bstart);
+           (const uint64_t *)batch, b, bstart, (const unsigned long long *)nullptr, (uint64_t)0,
+           (const unsigned int *)nullptr);
     if (!sorted) {  // the counting merge wants unique keys
       BYO_TRY(unique_u64(ctx, ka, count, 0, kb, &b));
       batch = kb;
       launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
-             (const uint64_t *)batch, b, bstart);
+             (const uint64_t *)batch, b, bstart, (const unsigned long long *)nullptr, (uint64_t)0,
+             (const unsigned int *)nullptr);
     }
     launch(ctx, k_pma_count, dim3(grid_for(ctx, NL * 32, 32 * kPmaWarps, 4)), dim3(32 * kPmaWarps), 0,
            (const uint32_t *)p->src, (const uint32_t *)p->dst, (const uint32_t *)p->cnt, NL,
@@ -1608,7 +1638,8 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
              (long long *)(ctr + 2), g->d_deg, view);
   } else {
     launch(ctx, k_pma_route, dim3(grid_for(ctx, NL + 1, 256)), dim3(256), 0, (const uint64_t *)p->sep, NL,
-           (const uint64_t *)batch, b, bstart);
+           (const uint64_t *)batch, b, bstart, defer ? (const unsigned long long *)bounds : nullptr, g->n,
+           (const unsigned int *)flags);
     launch_t(ctx, "pma_merge", k_pma_merge_rank, dim3(grid_for(ctx, NL * 32, 32 * kRankWarps, 8)),
              dim3(32 * kRankWarps), 0, p->src, p->dst, p->cnt, NL, (const uint64_t *)batch,
              (const uint64_t *)bstart, insert, rcount, (uint64_t *)p->ovf.p, (uint64_t *)p->ovf_off.p, ctr,
@@ -1642,7 +1673,7 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
       return check_launch(ctx, "pma_update");
     }
     BYO_TRY(check_launch(ctx, "pma_update"));
-    return pma_view(g);
+    return pma_view(g, total);
   }
   // 4. overflow (or shrink): windows over the counts after the merge
   return pma_finish_windowed(g, list, bstart, (const unsigned long long *)(ctr + 3), b, total, shrink);

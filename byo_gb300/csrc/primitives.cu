@@ -274,19 +274,26 @@ int sort_u64(byo_ctx *ctx, uint64_t *keys, uint64_t *tmp, uint64_t count, uint64
 // Traffic: read, read + write, read + write = 40 bytes per key (LSD over 44
 // significant bits needs 6 passes of 24 bytes).
 
-__global__ void k_bucket_count(const uint64_t *__restrict__ keys, uint64_t count, int shift,
+// The bucket of a key; a src >= n (a batch that validation will reject after
+// the sort) goes to the last bucket, so no key indexes out of bounds.
+__device__ __forceinline__ uint64_t key_bucket(uint64_t k, int shift, uint64_t nb) {
+  const uint64_t b = (k >> 32) >> shift;
+  return b < nb ? b : nb - 1;
+}
+
+__global__ void k_bucket_count(const uint64_t *__restrict__ keys, uint64_t count, int shift, uint64_t nb,
                                unsigned int *cnt) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
        i += (uint64_t)gridDim.x * blockDim.x)
-    atomicAdd(cnt + ((keys[i] >> 32) >> shift), 1u);
+    atomicAdd(cnt + key_bucket(keys[i], shift, nb), 1u);
 }
 
-__global__ void k_bucket_scatter(const uint64_t *__restrict__ keys, uint64_t count, int shift,
+__global__ void k_bucket_scatter(const uint64_t *__restrict__ keys, uint64_t count, int shift, uint64_t nb,
                                  const uint64_t *__restrict__ boff, unsigned int *cursor, uint64_t *out) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t k = keys[i];
-    const uint64_t b = (k >> 32) >> shift;
+    const uint64_t b = key_bucket(k, shift, nb);
     out[boff[b] + atomicAdd(cursor + b, 1u)] = k;
   }
 }
@@ -650,9 +657,9 @@ int sort_bucketed(byo_ctx *ctx, const uint64_t *in, uint64_t count, uint64_t n, 
   BYO_TRY(scratch(ctx, 5, nb + 1, &boff));
   unsigned int *cursor = cnt + nb, *nlarge = cnt + 2 * nb;
   BYO_CU(ctx, cudaMemsetAsync(cnt, 0, (2 * nb + 8) * 4, ctx->stream));
-  launch(ctx, k_bucket_count, dim3(grid_for(ctx, count, 256, 16)), dim3(256), 0, in, count, shift, cnt);
+  launch(ctx, k_bucket_count, dim3(grid_for(ctx, count, 256, 16)), dim3(256), 0, in, count, shift, nb, cnt);
   BYO_TRY(scan_u32_to_u64(ctx, cnt, nb, boff));
-  launch(ctx, k_bucket_scatter, dim3(grid_for(ctx, count, 256, 16)), dim3(256), 0, in, count, shift,
+  launch(ctx, k_bucket_scatter, dim3(grid_for(ctx, count, 256, 16)), dim3(256), 0, in, count, shift, nb,
          (const uint64_t *)boff, cursor, tmp);
   // the large-bucket list reuses the count array (the counts live in boff now)
   launch_t(ctx, "sort_scatter", k_bucket_sort, dim3(grid_for(ctx, nb * 32, 256, 8)), dim3(256), 0,

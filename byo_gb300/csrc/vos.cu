@@ -220,12 +220,15 @@ int vos_compact(byo_graph *g, const uint64_t *offc, uint32_t *out) {
 
 // ---------------------------------------------------------------- update
 
-__global__ void k_vos_bounds(const uint64_t *__restrict__ keys, uint64_t cnt, unsigned long long *out) {
+// out[0], out[1]: the largest src and dst; out[4] set when `sorted` and the
+// batch is not strictly increasing.
+__global__ void k_vos_bounds(const uint64_t *__restrict__ keys, uint64_t cnt, int sorted, unsigned long long *out) {
   unsigned long long ms = 0, md = 0;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t k = keys[i];
     ms = ms > (k >> 32) ? ms : (k >> 32);
     md = md > (k & 0xFFFFFFFFull) ? md : (k & 0xFFFFFFFFull);
+    if (sorted && i > 0 && keys[i - 1] >= k) out[4] = 1;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -558,12 +561,14 @@ int vos_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   BYO_TRY(pinned(ctx, 4096, (void **)&h));
   // 1. validate, sort (duplicates kept)
   BYO_TRY(ensure(ctx, V->misc, 64));
-  unsigned long long *ctr = (unsigned long long *)V->misc.p;  // [0,1] bounds, [2] outgrown, [3] delta
+  // [0,1] bounds, [2] outgrown, [3] delta, [4] a "sorted" batch out of order
+  unsigned long long *ctr = (unsigned long long *)V->misc.p;
   BYO_CU(ctx, cudaMemsetAsync(ctr, 0, 64, ctx->stream));
-  launch(ctx, k_vos_bounds, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, ctr);
-  BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  launch(ctx, k_vos_bounds, dim3(grid_for(ctx, count, 256)), dim3(256), 0, d_keys_in, count, sorted, ctr);
+  BYO_CU(ctx, cudaMemcpyAsync(h, ctr, 40, cudaMemcpyDeviceToHost, ctx->stream));
   BYO_CU(ctx, cudaStreamSynchronize(ctx->stream));
   if (h[0] >= g->n || h[1] >= g->n) return set_error(ctx, BYO_EINVAL, "update key with src or dst >= n");
+  if (h[4]) return set_error(ctx, BYO_EINVAL, "sorted batch not increasing");
   BYO_TRY(ensure(ctx, V->keys_a, count * 8));
   BYO_TRY(ensure(ctx, V->keys_b, count * 8));
   const uint64_t *keys = d_keys_in;

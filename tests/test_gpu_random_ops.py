@@ -182,3 +182,55 @@ def test_random_mixed_stream(ctx, oracle_mod, container):
             assert changed[i] == exp, "op %d" % i
     _check(byo, O, G, st)
     G.close()
+
+
+@pytest.mark.parametrize("container", ["pma", "pcsr", "vos"])
+def test_rejected_batches_every_size(ctx, oracle_mod, container):
+    """A batch with one key out of range (src = n, dst = n, or both 2^32 - 1),
+    or a batch passed as sorted that is not, is rejected with BYO_EINVAL at
+    every size -- the one-CTA register sort (<= 4096 keys), the bucketed and
+    two-level sorts (2^21 keys and more), the segment-list and full-leaf
+    merges -- and leaves the contents, degrees and edge count unchanged; the
+    same batch without the bad key then applies as the oracle's store says."""
+    import byo_gb300 as byo
+    O = oracle_mod
+    lg = 14
+    n = 1 << lg
+    s, d = O.rmat_edges(151, lg, 1 << 17)
+    off, nb = O.build_csr(n, s, d)
+    G = byo.Graph.from_csr(ctx, off, nb, container=container)
+    st = O.Store(off, nb)
+    rng = np.random.default_rng(152)
+    bads = ((n << 32) | 1, (3 << 32) | n, (0xFFFFFFFF << 32) | 0xFFFFFFFF)
+    # 3000 pairs again at the end: by then the graph has more leaves than
+    # keys, so the segment list meets the bucketed sort
+    for size in (1, 100, 3000, 20000, 300000, 1 << 21, 3000, 100):
+        p = rng.integers(0, n, size=(size, 2))
+        keys = O.keys_from_pairs(p[:, 0], p[:, 1])
+        m_before = G.M()
+        for bad in bads:
+            k = keys.copy()
+            k[int(rng.integers(0, len(k)))] = bad
+            for op in (G.insert_batch, G.remove_batch):
+                with pytest.raises(byo.ByoError) as e:
+                    op(k)
+                assert e.value.code == byo._abi.BYO_EINVAL, (size, hex(bad))
+                assert G.M() == m_before, (size, hex(bad))
+        u = np.unique(keys)
+        if len(u) > 1:
+            j = int(rng.integers(0, len(u) - 1))
+            u[j], u[j + 1] = u[j + 1], u[j]
+            for op in (G.insert_batch, G.remove_batch):
+                with pytest.raises(byo.ByoError) as e:
+                    op(u, sorted=True)
+                assert e.value.code == byo._abi.BYO_EINVAL, (size, "order")
+        ro, rn = st.export_csr()
+        go, gn = G.export_csr()
+        assert np.array_equal(go, ro) and np.array_equal(gn, rn), (size, "changed by a rejected batch")
+        assert np.array_equal(G.degrees(), np.diff(ro).astype(np.uint32)), size
+        assert G.insert_batch(keys) == st.insert_batch(keys), size
+        half = keys[: len(keys) // 2]
+        assert G.remove_batch(half) == st.remove_batch(half), size
+        assert G.M() == st.num_edges, size
+    _check(byo, O, G, st)
+    G.close()
