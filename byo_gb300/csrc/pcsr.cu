@@ -707,8 +707,9 @@ int pcsr_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sor
   // 1. validate on the device, sort (duplicates stay: the merge skips them).
   // No sort indexes out of bounds by key, and the segment kernels or the
   // routing drop an invalid batch (the merge then has no work), so the
-  // validation is read after the single synchronisation of the update.  A batch of at most one key per leaf takes
-  // the segment list (only its own leaves are visited).
+  // validation is read after the single synchronisation of the update.  A
+  // batch of at most one key per leaf takes the segment list (only its own
+  // leaves are visited).
   const uint64_t NL = p->NL;
   const bool small = !sorted && count <= sort_small_max();
   const bool list = count <= NL && count < (1ull << 32);

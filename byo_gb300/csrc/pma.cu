@@ -1521,7 +1521,7 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   if (!p) return set_error(ctx, BYO_ENOTSUP, "not a PMA container");
   g->version++;  // any snapshot of the contents is stale from here on
   const uint64_t m_before = g->m;
-  // 1. validate, copy, sort, unique
+  // 1. bounds and order checks, sort (duplicates kept: the merges skip them)
   BYO_TRY(ensure(ctx, p->keys_a, count * 8));
   BYO_TRY(ensure(ctx, p->keys_b, count * 8));
   BYO_TRY(ensure(ctx, p->misc, 128));
@@ -1529,8 +1529,9 @@ int pma_update(byo_graph *g, const uint64_t *d_keys_in, uint64_t count, int sort
   unsigned long long *bounds = (unsigned long long *)p->misc.p;
   unsigned int *flags = (unsigned int *)(bounds + 2);  // [0] unsorted, [1] grow, [2] any overflow, [4..] counters
   BYO_CU(ctx, cudaMemsetAsync(p->misc.p, 0, 128, ctx->stream));
-  // a batch that fits one block is sorted there (with the bounds) before it is
-  // validated: that sort does not index by key
+  // the largest src and dst come from the one-block sort for a batch that
+  // fits it, else from k_key_bounds; no sort indexes out of bounds by key, so
+  // the checks can be read after the sort (or after the merge)
   const bool small_sort = !sorted && count <= kSmallSort;
   if (small_sort) {
     if (count <= 1024)
