@@ -89,13 +89,6 @@ __device__ __forceinline__ bool test_bit_cg(const uint32_t *bits, uint32_t v) {
   return (__ldcg(bits + (v >> 5)) >> (v & 31)) & 1u;
 }
 
-// Error-free transform (Knuth TwoSum) for the compensated PageRank sums.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = __fadd_rn(a, b);
-  float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
 // Bitonic sort of R*32 keys held by a warp in registers: element r*32 + lane
 // lives in register r of that lane; strides below 32 exchange through
 // shuffles, larger strides swap registers inside a lane.

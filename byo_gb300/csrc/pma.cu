@@ -156,16 +156,6 @@ __global__ void k_pma_route(const uint64_t *__restrict__ sep, uint64_t NL, const
   }
 }
 
-__device__ __forceinline__ bool leaf_contains(const uint32_t *src, const uint32_t *dst, uint64_t base, uint32_t c,
-                                              uint64_t key) {
-  uint32_t lo = 0, hi = c;
-  while (lo < hi) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (slot_key(src, dst, base + mid) < key) lo = mid + 1; else hi = mid;
-  }
-  return lo < c && slot_key(src, dst, base + lo) == key;
-}
-
 // rcount[i] = elements of leaf i after the update.  One warp per leaf; the
 // leaf's keys are staged in the warp's shared memory, then every batch key of
 // the leaf's segment is looked up there.

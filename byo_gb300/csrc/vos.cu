@@ -300,15 +300,6 @@ struct InSegOld {
   __device__ uint64_t operator()(uint64_t s) const { return deg[keys[segs[s]] >> 32]; }
 };
 
-__device__ __forceinline__ uint64_t seg_of(const uint64_t *pre, uint64_t nseg, uint64_t t) {
-  uint64_t lo = 0, hi = nseg;  // last s with pre[s] <= t
-  while (hi - lo > 1) {
-    const uint64_t mid = (lo + hi) >> 1;
-    if (pre[mid] <= t) lo = mid; else hi = mid;
-  }
-  return lo;
-}
-
 // The old keys of the touched runs, in chunks over their concatenation
 // (abase): each key moves to its place in the staging copy of its run,
 // shifted by the kept batch keys of its run that go before it (insert:
