@@ -125,7 +125,9 @@ int byo_graph_neighbors(byo_graph *g, uint32_t v, uint32_t *h_out, uint64_t cap,
  * PMA_graph::insert_sorted_batch / remove_sorted_batch (run_single_pma.cc:63-70).
  * keys may be unsorted and contain duplicates unless `sorted` is 1 (then they
  * must be strictly increasing).  Inserting a present key and removing an
- * absent key are no-ops.  Keys with src or dst >= n are rejected (BYO_EINVAL).
+ * absent key are no-ops.  A batch with a key whose src or dst is >= n, or one
+ * passed as sorted that is not strictly increasing, is rejected whole
+ * (BYO_EINVAL) and leaves the container unchanged.
  * *changed (may be NULL) receives the number of keys actually inserted or
  * removed.  The PMA, VOS and PCSR containers take updates (CSR: BYO_ENOTSUP). */
 int byo_graph_insert_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
