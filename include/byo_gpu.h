@@ -127,7 +127,10 @@ int byo_graph_neighbors(byo_graph *g, uint32_t v, uint32_t *h_out, uint64_t cap,
  * must be strictly increasing).  Inserting a present key and removing an
  * absent key are no-ops.  A batch with a key whose src or dst is >= n, or one
  * passed as sorted that is not strictly increasing, is rejected whole
- * (BYO_EINVAL) and leaves the container unchanged.
+ * (BYO_EINVAL) and leaves the container unchanged.  BYO_ENOMEM or
+ * BYO_EDEVICE from an update (a grow or rebuild that could not allocate, after
+ * the merge had started) leaves the contents unspecified: destroy the graph.
+ * (The reference aborts on a failed allocation.)
  * *changed (may be NULL) receives the number of keys actually inserted or
  * removed.  The PMA, VOS and PCSR containers take updates (CSR: BYO_ENOTSUP). */
 int byo_graph_insert_batch(byo_graph *g, const uint64_t *h_keys, uint64_t count, int sorted,
