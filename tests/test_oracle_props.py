@@ -218,3 +218,31 @@ def test_bytepd_golden_and_round_trip(oracle_mod):
         bo, deg, data = O.bytepd_encode(o, n_, P)
         o2, n2 = O.bytepd_decode(bo, deg, data, P)
         assert np.array_equal(o2, o) and np.array_equal(n2, n_)
+
+
+def test_mlp_ref_gradient_matches_finite_differences():
+    """The FP64 restatement of the policy network's loss gradient (the checker
+    of the device training kernels) against central differences of its own
+    loss, on up to 10 random parameters of every weight and bias block."""
+    from oracle import mlp_ref
+    rng = np.random.default_rng(71)
+    p = rng.normal(0, 0.3, mlp_ref.NPARAMS)
+    X = rng.normal(0, 1, (24, mlp_ref.NIN))
+    Y = rng.normal(0, 1, (24, mlp_ref.NOUT))
+    mask = rng.integers(1, 1 << mlp_ref.NOUT, 24).astype(np.uint8)
+    loss, g = mlp_ref.loss_grad(p, X, Y, mask)
+    assert g.shape == (mlp_ref.NPARAMS,) and loss > 0
+    h = 1e-6
+    picks, o = [], 0
+    for _, shape in mlp_ref.SIZES:
+        k = int(np.prod(shape))
+        picks += list(o + rng.choice(k, min(k, 10), replace=False))
+        o += k
+    for i in picks:
+        q = p.copy()
+        q[i] += h
+        lp, _ = mlp_ref.loss_grad(q, X, Y, mask)
+        q[i] -= 2 * h
+        lm, _ = mlp_ref.loss_grad(q, X, Y, mask)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])), (int(i), fd, g[i])
